@@ -1,0 +1,253 @@
+/*
+ * skewengine.h -- C ABI of the GB300-native skewed-data-mapping engine.
+ *
+ * The engine runs the sector loop of luisfromero/skewEngine on one GPU:
+ * for every integer angle a in [0, max_sector) it skews the 2-D input so that
+ * lines at angle a become memory rows, runs a per-row operator over the valid
+ * part [first, last) of every skewed row, deskews the result and accumulates it
+ * into one of four orientation buffers, and finally folds those back into the
+ * input orientation.  All compute is hand-written sm_103a CUDA; there is no CPU
+ * fallback: without a usable GPU every compute entry point returns an error.
+ *
+ * Conventions
+ *  - Every entry point returns an int status (SKE_OK == 0).  On failure the
+ *    message of the calling thread's last error is available from
+ *    ske_last_error().  Nothing in the library calls exit() or traps on device.
+ *  - Arrays are row-major float32, dimy rows of dimx cells, like the reference's
+ *    inputD / outD (src/global.cpp:24).
+ *  - "on_device" arguments say whether a pointer is a device pointer (1) or a
+ *    host pointer (0).  Host buffers are staged through the engine's pinned
+ *    buffers.
+ *  - An engine is bound to one device and one CUDA stream; calls on one engine
+ *    are not thread-safe (as one reference skewEngine object per OpenMP thread,
+ *    src/main.cu:91).  Different engines may be used from different threads.
+ */
+#ifndef SKEWENGINE_H
+#define SKEWENGINE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SKE_ABI_VERSION 1
+
+/* Status codes. */
+#define SKE_OK 0
+#define SKE_ERR_INVALID 1     /* bad argument (null pointer, size, angle ...)  */
+#define SKE_ERR_CUDA 2        /* a CUDA runtime call failed                     */
+#define SKE_ERR_NO_DEVICE 3   /* no usable CUDA device                          */
+#define SKE_ERR_STATE 4       /* call out of order (e.g. kernel() before skew())*/
+#define SKE_ERR_UNSUPPORTED 5 /* valid request this build does not support      */
+#define SKE_ERR_DEVICE 6      /* a kernel reported an error through its status  */
+
+/* Operators: values of the reference KERNELS enum (src/global.h:77). */
+#define SKE_KERNEL_SDEM 0        /* total viewshed, kernelV3 (src/kernelSDEM.h:168)   */
+#define SKE_KERNEL_IDENTITYDEM 1 /* identity, kernelUNIT.h:16                         */
+#define SKE_KERNEL_RADON 2       /* Radon + filtered back-projection, kernelRADN.h:213*/
+#define SKE_KERNEL_IDENTITYIMG 3 /* identity, kernelUNIT.h:16                         */
+#define SKE_KERNEL_CEPSTRUM 4    /* cepstrum blur estimation, kernelBLUR.h:267        */
+
+/* Cross-sector accumulation of the additive operators. */
+#define SKE_ACCUM_REFERENCE 0 /* float adds in sector order, bit-identical to the
+                                 reference run on one thread (skewEngine.cuh:786-792) */
+#define SKE_ACCUM_KAHAN 1     /* compensated (Kahan) float sums per orientation,
+                                 folded in double at the end                       */
+
+/* Run parameters (reference: compile-time globals of src/global.cpp and
+ * src/kernelSDEM.h). */
+typedef struct ske_params {
+    int32_t max_sector; /* angles 0..max_sector-1, 1..180 (global.cpp:69, default 180) */
+    float povh;         /* observer height in cell units (kernelSDEM.h:159, 1.5/10)    */
+    int32_t accum;      /* SKE_ACCUM_*                                                  */
+    int32_t flags;      /* reserved, 0                                                  */
+} ske_params;
+
+/* Geometry of one sector, computeParams + skewShape (skewEngine.cuh:504-596). */
+typedef struct ske_sector_geometry {
+    int32_t angle;       /* a                                   */
+    int32_t sector_type; /* 0..3: plain, transposed, transposed+mirrored, mirrored */
+    int32_t new_angle;   /* angle folded into [0, 45]            */
+    int32_t dim_i;       /* inner (row) length = skewWidth        */
+    int32_t dim_o;       /* outer dimension                      */
+    int32_t offset;      /* (int)(skewness*(dim_i-1))            */
+    int32_t skew_height; /* rows of the skewed grid              */
+    int32_t dim_l;       /* max(dimx, dimy)                      */
+    double scale;        /* 1/cos(new_angle)                     */
+    double skewness;     /* tan(new_angle)                       */
+} ske_sector_geometry;
+
+/* Device view of the current sector handed to a custom operator: the fields the
+ * reference passes to kernelcuda (skewEngine.cuh:369, :709) plus geometry.
+ * skew_in/skew_out hold 2*dimx*dimy + dim_l floats, row stride dim_i. */
+typedef struct ske_sector_view {
+    ske_sector_geometry geom;
+    float* skew_out;       /* d_skewOutput (zeroed before the operator runs) */
+    const float* skew_in;  /* d_skewInput                                     */
+    const int32_t* first;  /* d_first[skew_height]                            */
+    const int32_t* last;   /* d_last[skew_height]                             */
+    const int32_t* target; /* d_target[dim_i]                                 */
+    const float* weight;   /* d_weight[dim_i]                                 */
+    float povh;
+    void* stream;          /* cudaStream_t the operator must launch on       */
+} ske_sector_view;
+
+/* A custom device operator: launches its own kernels on view->stream, reading
+ * skew_in and writing skew_out over [first[r], last[r]) of every row r.
+ * Replaces the reference's kernelcuda function pointer (skewEngine.cuh:369).
+ * Return 0 on success. */
+typedef int (*ske_operator_fn)(void* user, const ske_sector_view* view);
+
+typedef struct ske_engine_s* ske_engine;
+
+/* Library / device ---------------------------------------------------------*/
+
+/* ABI version (SKE_ABI_VERSION). */
+int ske_abi_version(void);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* ske_last_error(void);
+
+/* Fill *p with the reference defaults: 180 sectors, povh = 1.5/10,
+ * accumulation in reference order. */
+int ske_params_default(ske_params* p);
+
+/* Number of CUDA devices visible (0 on a machine without a GPU). */
+int ske_device_count(int* count);
+
+/* Host-only geometry of one sector (no GPU needed): replaces
+ * skewEngine::computeParams/skewShape (skewEngine.cuh:504-596).  first/last
+ * (skew_height entries each) and target/weight (dim_i entries each) may be NULL;
+ * size them with a first call that passes NULL. */
+int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32_t* first,
+                 int32_t* last, int32_t* target, float* weight);
+
+/* Engine lifetime ----------------------------------------------------------*/
+
+/* Create an engine for dimx x dimy grids on `device`, launching on `stream`
+ * (a cudaStream_t; NULL = the engine creates its own).  Replaces the skewEngine
+ * constructor + skewAlloc (skewEngine.cuh:462, :419) and the per-thread
+ * cudaSetDevice/cudaStreamCreate of skewCudaMalloc (skewEngine.cuh:1030-1031). */
+int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream);
+
+/* Release every device and host resource of the engine (skewEngine::~skewEngine,
+ * skewEngine.cuh:484-501). */
+int ske_destroy(ske_engine e);
+
+/* The CUDA stream the engine launches on. */
+int ske_stream(ske_engine e, void** stream);
+
+/* Whole run ----------------------------------------------------------------*/
+
+/* Full sector loop for one operator: prepare the four orientations, run every
+ * sector 0..p->max_sector-1 (skew -> operator -> deskew/accumulate), fold the
+ * orientations back, and write dimx*dimy floats to `output`.  Replaces
+ * skewEngine::allocate + execute() + reduce (skewEngine.cuh:389, main.cu:71-172,
+ * skewEngine.cuh:862).  Results equal the reference run on one OpenMP thread
+ * (bit for bit for SDEM/identity/Radon in SKE_ACCUM_REFERENCE mode). */
+int ske_run(ske_engine e, int kernel, const float* input, int input_on_device, float* output,
+            int output_on_device, const ske_params* p);
+
+/* Same with a caller-supplied list of angles (each in [0,180)), processed and
+ * accumulated in list order. */
+int ske_run_angles(ske_engine e, int kernel, const float* input, int input_on_device,
+                   float* output, int output_on_device, const int32_t* angles, int nangles,
+                   const ske_params* p);
+
+/* Run the listed sectors and return, instead of the folded output, the four
+ * per-type accumulators (4*dimx*dimy floats, type-major, each in its sector
+ * type's orientation) and the mask of types that received a sector: the state a
+ * reference engine thread holds before its critical-section reduce
+ * (skewEngine.cuh:270-273, main.cu:160-164).  Used to shard sectors across
+ * GPUs; fold with the reduce order of skewEngine.cuh:885-912. */
+int ske_accumulate(ske_engine e, int kernel, const float* input, int input_on_device,
+                   const int32_t* angles, int nangles, const ske_params* p, float* acc,
+                   int acc_on_device, uint32_t* used_mask);
+
+/* Batched total viewshed (SDEM) over `count` square or rectangular DEMs of
+ * uneven sizes: inputs[i]/outputs[i] are dimx[i] x dimy[i] host or device
+ * arrays.  All DEMs and all their sectors are scheduled together.  Engines are
+ * created for the largest grid internally; `e` supplies device and stream. */
+int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
+                  const float* const* inputs, int inputs_on_device, float* const* outputs,
+                  int outputs_on_device, const ske_params* p);
+
+/* Per-sector API (drop-in for the reference's skew/kernel/deskew/reduce
+ * methods driven from main.cu:147-164) ----------------------------------------*/
+
+/* Upload `input` and build the four orientations (skewEngine::prepare,
+ * skewEngine.cuh:925-987 + the H2D copies of skewCudaMalloc :1041-1044); clears
+ * the four orientation accumulators (d_output, :1040). */
+int ske_prepare(ske_engine e, const float* input, int on_device);
+
+/* skewEngine::skew(angle) (skewEngine.cuh:606): geometry of `angle`, reset and
+ * fill the skewed input. */
+int ske_skew(ske_engine e, int angle);
+
+/* skewEngine::kernel() (skewEngine.cuh:695): run a built-in operator over the
+ * current skewed grid. */
+int ske_kernel(ske_engine e, int kernel, float povh);
+
+/* Run a custom device operator over the current skewed grid. */
+int ske_kernel_custom(ske_engine e, ske_operator_fn fn, void* user, float povh);
+
+/* skewEngine::deskew(isMax) (skewEngine.cuh:756): deskew the current skewed
+ * output into the accumulator of the current sector type.  is_max = 1 for the
+ * cepstrum max/angle encoding, 0 to add.  accum = SKE_ACCUM_*. */
+int ske_deskew(ske_engine e, int is_max, int accum);
+
+/* skewEngine::reduce(out, isMax) (skewEngine.cuh:862): fold the four
+ * accumulators into `output` (dimx*dimy).  `output` is overwritten (the
+ * reference adds into a caller-zeroed outD). */
+int ske_reduce(ske_engine e, float* output, int on_device, int is_max);
+
+/* Geometry and device buffers of the current sector. */
+int ske_sector(ske_engine e, ske_sector_view* view);
+
+/* Copy the current skewed input / output (2*dimx*dimy + dim_l floats). */
+int ske_copy_skewed(ske_engine e, float* skew_in, float* skew_out, int on_device);
+
+/* Total-viewshed visibility counts of one sector: for every skewed cell in
+ * [first,last) the integer-valued sum cv of kernelSDEM.h:182-218 before the
+ * scale factor; other cells 0.  counts: 2*dimx*dimy + dim_l floats. */
+int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_device);
+
+/* Profiling ----------------------------------------------------------------*/
+
+/* Enable (1) / disable (0) CUDA-event timing of every kernel launch. */
+int ske_profile_enable(ske_engine e, int enable);
+
+/* Accumulated device time (ms) and launch count of kernel family `name`
+ * ("prepare", "skew", "sdem_sweep", "radon_sums", "radon_fft", "cepstrum",
+ *  "identity", "deskew", "reduce") since profiling was enabled; synchronises the
+ * engine's stream. */
+int ske_profile_get(ske_engine e, const char* name, double* ms, int64_t* launches);
+
+/* Number of this library's kernels launched by the engine since creation. */
+int ske_launch_count(ske_engine e, int64_t* launches);
+
+/* Self-test of the total-viewshed sweep's division: compares its
+ * multiply-and-correct quotient with IEEE division for every float numerator
+ * in the sweep's fast-path range and every distance d in [1, dmax] (dmax <=
+ * 4095) on `device`.  No reference counterpart (the reference divides
+ * directly, kernelSDEM.h:191).  Synchronous. */
+int ske_selftest_division(int device, int dmax, int64_t* checked, int64_t* mismatches,
+                          uint32_t* first_bad_bits);
+
+/* FP32 pipe throughput of `device` in lane operations per second (one fused
+ * multiply-add = one operation), scalar and packed two-wide: the roofline
+ * denominator of the total-viewshed sweep.  No reference counterpart. */
+int ske_measure_fp32_peak(int device, double* scalar_ops, double* packed_ops);
+
+/* Reference command-line entry point (src/main.cu:200-202): runs one operator on
+ * a raw float32 file or a synthetic input and writes the result.  See
+ * INTEGRATION.md for the argument list. */
+int run(int argc, char** argv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKEWENGINE_H */

@@ -1,0 +1,172 @@
+// Test oracle: drives the reference skewEngine CPU path, compiled from the
+// reference's own unmodified sources (src/skewEngine.cuh, src/kernelSDEM.h,
+// src/kernelRADN.h, src/kernelBLUR.h, src/kernelUNIT.h, src/helper.h).
+//
+// This file is test infrastructure only.  It is compiled by oracle/Makefile into
+// oracle/_ref/libskewref.so, which exists only where the reference sources are
+// present; it is used to generate and re-check the golden fixtures in
+// tests/golden and as a CPU timing baseline.  Nothing in the product links it.
+//
+// The sector loop below restates the reference driver `execute()`
+// (src/main.cu:86-168): one engine per OpenMP thread, operator bound through
+// `kernelcpu`, `skew(i); kernel(); deskew(isMax)` per sector with a dynamic
+// schedule, then `reduce(outD, isMax)` inside a critical section.  main.cu itself
+// does not compile with GCC 13, so it is not built.
+//
+// One harness-side choice: before each sector the full skew buffers are cleared
+// (the reference only clears skewHeight*dim_i cells, skewEngine.cuh:567-568).
+// For non-square inputs the reference reads past that region
+// (last[] is initialised with dim_l, skewEngine.cuh:581), which would otherwise
+// read values left behind by earlier sectors; clearing makes those reads zero
+// and the run deterministic.  Square inputs never read past the region.
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <omp.h>
+
+#include "helper.h"
+
+// Globals that src/main.cu defines (main.cu:59-60) and the kernel headers use.
+int skewAlgorithm;
+bool timing = true;
+
+#include "kernelSDEM.h"
+#include "kernelRADN.h"
+#include "kernelBLUR.h"
+#include "kernelUNIT.h"
+
+static void bind_operator(skewEngine<float>* sk, int alg) {
+    switch (alg) {
+        case KERNEL_SDEM: sk->kernelcpu = kernelV3; break;
+        case KERNEL_RADON: sk->kernelcpu = radon; break;
+        case KERNEL_CEPSTRUM: sk->kernelcpu = cepstrum; break;
+        default: sk->kernelcpu = identity; break;  // KERNEL_IDENTITYDEM / KERNEL_IDENTITYIMG
+    }
+}
+
+static void clear_full(skewEngine<float>* sk, int n, int diml) {
+    memset(sk->skewInput, 0, sizeof(float) * (size_t)(2 * n + diml));
+    memset(sk->skewOutput, 0, sizeof(float) * (size_t)(2 * n + diml));
+}
+
+extern "C" {
+
+int skref_run_angles(int alg, const float* input, float* output, int dx, int dy, const int* angles,
+                     int nangles, float povh, int nthreads);
+
+// Whole run: output (dimx*dimy floats) = reference result for `alg`
+// (KERNELS enum, global.h:77) over sectors [0, nsect).
+int skref_run(int alg, const float* input, float* output, int dx, int dy, int nsect,
+              float povh, int nthreads) {
+    if (nsect <= 0 || nsect > 180) return 1;
+    int angles[180];
+    for (int i = 0; i < nsect; i++) angles[i] = i;
+    return skref_run_angles(alg, input, output, dx, dy, angles, nsect, povh, nthreads);
+}
+
+// Same over an explicit list of angles (the loop index i of main.cu:147 maps to
+// angles[i]).
+int skref_run_angles(int alg, const float* input, float* output, int dx, int dy, const int* angles,
+                     int nsect, float povh, int nthreads) {
+    if (dx <= 0 || dy <= 0 || nsect <= 0 || nsect > 180) return 1;
+    for (int i = 0; i < nsect; i++)
+        if (angles[i] < 0 || angles[i] >= 180) return 1;
+    dimx = dx;
+    dimy = dy;
+    N = dim = dx * dy;
+    maxSector = nsect;
+    POVh = povh;
+    skewAlgorithm = alg;
+    float* inputD = new float[N];
+    memcpy(inputD, input, sizeof(float) * (size_t)N);
+    inputData<float> in = skewEngine<float>::prepare(inputD, dimx, dimy);
+    memset(output, 0, sizeof(float) * (size_t)N);
+    const int diml = dx > dy ? dx : dy;
+    const int isMax = alg == KERNEL_CEPSTRUM ? 1 : 0;
+    omp_set_num_threads(nthreads > 0 ? nthreads : 1);
+#pragma omp parallel default(shared)
+    {
+        int id = omp_get_thread_num();
+        skewEngine<float>* sk = new skewEngine<float>(dimx, dimy, in, false, id);
+        bind_operator(sk, alg);
+        sk->skewAlloc();
+#pragma omp barrier
+#pragma omp for schedule(dynamic) nowait
+        for (int i = 0; i < nsect; i++) {
+            clear_full(sk, N, diml);
+            sk->skew(angles[i]);
+            sk->kernel();
+            sk->deskew(isMax);
+        }
+#pragma omp critical
+        { sk->reduce(output, isMax); }
+        delete sk;
+    }
+    delete[] in.input1;
+    delete[] in.input2;
+    delete[] in.input3;
+    delete[] inputD;
+    return 0;
+}
+
+// One sector in isolation, exposing the engine's intermediate state.
+//   iinfo[0..6] = sectorType, newAngle, dim_i, dim_o, offset, skewHeight, dim_l
+//   dinfo[0..1] = scale, skewness
+//   skewIn/skewOut: 2*N + dim_l floats (the engine's whole skew buffers)
+//   first/last: 2*dim_l+1 entries; target/weight: dim_l entries
+//   acc: N floats, the per-type accumulator after deskew of this one sector
+int skref_sector(int alg, const float* input, int dx, int dy, int angle, float povh,
+                 int* iinfo, double* dinfo, float* skewIn, float* skewOut,
+                 unsigned short* first, unsigned short* last, int* target, float* weight,
+                 float* acc) {
+    if (dx <= 0 || dy <= 0 || angle < 0 || angle >= 180) return 1;
+    dimx = dx;
+    dimy = dy;
+    N = dim = dx * dy;
+    maxSector = 180;
+    POVh = povh;
+    skewAlgorithm = alg;
+    float* inputD = new float[N];
+    memcpy(inputD, input, sizeof(float) * (size_t)N);
+    inputData<float> in = skewEngine<float>::prepare(inputD, dimx, dimy);
+    const int diml = dx > dy ? dx : dy;
+    skewEngine<float>* sk = new skewEngine<float>(dimx, dimy, in, false, 0);
+    bind_operator(sk, alg);
+    sk->skewAlloc();
+    memset(sk->first, 0, sizeof(unsigned short) * (size_t)(2 * diml + 1));
+    memset(sk->last, 0, sizeof(unsigned short) * (size_t)(2 * diml + 1));
+    clear_full(sk, N, diml);
+    sk->skew(angle);
+    if (skewIn) memcpy(skewIn, sk->skewInput, sizeof(float) * (size_t)(2 * N + diml));
+    sk->kernel();
+    if (skewOut) memcpy(skewOut, sk->skewOutput, sizeof(float) * (size_t)(2 * N + diml));
+    sk->deskew(alg == KERNEL_CEPSTRUM ? 1 : 0);
+    iinfo[0] = sk->sectorType;
+    iinfo[1] = sk->newAngle;
+    iinfo[2] = sk->dim_i;
+    iinfo[3] = sk->dim_o;
+    iinfo[4] = sk->offset;
+    iinfo[5] = sk->skewHeight;
+    iinfo[6] = diml;
+    dinfo[0] = sk->scale;
+    dinfo[1] = sk->skewness;
+    if (first) memcpy(first, sk->first, sizeof(unsigned short) * (size_t)(2 * diml + 1));
+    if (last) memcpy(last, sk->last, sizeof(unsigned short) * (size_t)(2 * diml + 1));
+    if (target) memcpy(target, sk->target, sizeof(int) * (size_t)diml);
+    if (weight) memcpy(weight, sk->weight, sizeof(float) * (size_t)diml);
+    if (acc) {
+        // Per-type accumulator of this sector: reduce() folds it back into the
+        // input orientation, so expose it through a zeroed output.
+        memset(acc, 0, sizeof(float) * (size_t)N);
+        sk->reduce(acc, alg == KERNEL_CEPSTRUM ? 1 : 0);
+    }
+    delete sk;
+    delete[] in.input1;
+    delete[] in.input2;
+    delete[] in.input3;
+    delete[] inputD;
+    return 0;
+}
+
+}  // extern "C"

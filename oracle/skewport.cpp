@@ -1,0 +1,437 @@
+// Test oracle: CPU restatement of the reference skewEngine CPU path.
+//
+// TEST INFRASTRUCTURE ONLY (see skewport.h).  Every function below restates one
+// piece of the reference and cites it.  The arithmetic is kept in the same
+// precision and order as the reference so results are bit-identical to it when
+// both are built without floating-point contraction (oracle/Makefile).
+//
+// Parity pinned against the reference's own CPU code through tests/golden.
+
+#include "skewport.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <omp.h>
+
+namespace {
+
+typedef std::complex<double> cplx;
+
+const double kDegToRad = M_PI / 180.0;  // skewEngine.cuh:258
+
+struct Sector {
+    int a = 0, type = 0, newAngle = 0, dim_i = 0, dim_o = 0, offset = 0, H = 0, diml = 0;
+    double scale = 0, skewness = 0;
+    std::vector<int> target;
+    std::vector<float> weight;
+    std::vector<unsigned short> first, last;
+};
+
+// skewEngine ctor (skewEngine.cuh:465): frontier angle between plain and transposed
+// sectors, in degrees, stored as float.
+float frontier_angle(int dimx, int dimy) { return (float)(atan2((double)dimy, (double)dimx) * 180 / M_PI); }
+
+// computeParams (skewEngine.cuh:504-539) + skewShape (skewEngine.cuh:573-596).
+void make_sector(int dimx, int dimy, int angle, Sector& s) {
+    const float fAngle = frontier_angle(dimx, dimy);
+    s.diml = std::max(dimx, dimy);
+    s.a = angle;
+    const bool transposed = angle > (int)fAngle && angle < 180 - (int)fAngle;
+    const bool mirrored = angle > 90;
+    if (!transposed && !mirrored) { s.type = 0; s.newAngle = angle; }
+    if (transposed && !mirrored) { s.type = 1; s.newAngle = 90 - angle; }
+    if (transposed && mirrored) { s.type = 2; s.newAngle = angle - 90; }
+    if (!transposed && mirrored) { s.type = 3; s.newAngle = 180 - angle; }
+    s.scale = 1 / cos(kDegToRad * s.newAngle);
+    s.skewness = tan(s.newAngle * kDegToRad);
+    s.dim_i = transposed ? dimy : dimx;
+    s.dim_o = transposed ? dimx : dimy;
+    s.offset = (int)(s.skewness * (s.dim_i - 1));
+    s.H = s.newAngle ? s.dim_o + s.offset + 1 : s.dim_o;
+    s.target.assign(s.diml, 0);
+    s.weight.assign(s.diml, 0.0f);
+    for (int j = 0; j < s.dim_i; j++) {
+        const double drift = s.skewness * j;
+        s.target[j] = (int)drift;
+        s.weight[j] = (float)(drift - s.target[j]);
+    }
+    // Row limits [first, last) of the valid part of every skewed row.
+    s.first.assign(2 * s.diml + 1, 0);
+    s.last.assign(2 * s.diml + 1, 0);
+    for (int r = 0; r < s.dim_o; r++) s.first[r] = 0;
+    for (int r = s.offset; r < s.H; r++) s.last[r] = (unsigned short)s.diml;
+    for (int r = 0; r < s.offset; r++) s.last[r] = 0;
+    for (int r = s.dim_o; r < s.H; r++) s.first[r] = (unsigned short)s.diml;
+    for (int j = 0; j < s.dim_i; j++) {
+        const int top = s.target[j];
+        for (int r = top; r <= top + 1; r++)
+            if (j > s.last[r]) s.last[r] = (unsigned short)(j + 1);
+        const int bottom = s.target[j] + s.dim_o - 1;
+        for (int r = bottom; r <= bottom + 1; r++)
+            if (j < s.first[r]) s.first[r] = (unsigned short)j;
+    }
+}
+
+// prepare (skewEngine.cuh:925-951): the four orientations of the input.
+void orientations(const float* in, int dimx, int dimy, std::vector<float> o[4]) {
+    const size_t n = (size_t)dimx * dimy;
+    for (int t = 0; t < 4; t++) o[t].resize(n);
+    for (int i = 0; i < dimy; i++) {
+        const int ci = dimy - 1 - i;
+        for (int j = 0; j < dimx; j++) {
+            const int cj = dimx - 1 - j;
+            const float v = in[(size_t)dimx * i + j];
+            o[0][(size_t)dimx * i + j] = v;
+            o[1][(size_t)dimy * cj + ci] = v;
+            o[2][(size_t)dimy * j + ci] = v;
+            o[3][(size_t)dimx * i + cj] = v;
+        }
+    }
+}
+
+// skew (skewEngine.cuh:612-621): scatter every source cell onto two skewed rows.
+void skew_rows(const Sector& s, const float* src, float* S) {
+    for (int i = 0; i < s.dim_o; i++)
+        for (int j = 0; j < s.dim_i; j++) {
+            const float v = src[(size_t)s.dim_i * i + j];
+            S[(size_t)(i + s.target[j]) * s.dim_i + j] += (1.0f - s.weight[j]) * v;
+            S[(size_t)(i + s.target[j] + 1) * s.dim_i + j] += s.weight[j] * v;
+        }
+}
+
+// helper::fft (helper.h:59-106): in-place radix-2 decimation in frequency, the
+// twiddle advanced by repeated complex multiplication, then bit reversal and an
+// optional 1/sqrt(n) scaling.
+void fft_dif(cplx* x, unsigned n, bool normalize) {
+    const double theta = (double)(3.14159265358979323846264338328L / n);
+    cplx step(cos(theta), -sin(theta));
+    for (unsigned half = n; half > 1;) {
+        const unsigned span = half;
+        half >>= 1;
+        step = step * step;
+        cplx w = 1.0L;
+        for (unsigned l = 0; l < half; l++) {
+            for (unsigned a = l; a < n; a += span) {
+                const unsigned b = a + half;
+                const cplx d = x[a] - x[b];
+                x[a] += x[b];
+                x[b] = d * w;
+            }
+            w *= step;
+        }
+    }
+    const unsigned bits = (unsigned)log2(n);
+    for (unsigned a = 0; a < n && bits > 0; a++) {
+        unsigned b = a, rev = 0;
+        for (unsigned k = 0; k < bits; k++) { rev = (rev << 1) | (b & 1u); b >>= 1; }
+        if (rev > a) std::swap(x[a], x[rev]);
+    }
+    if (!normalize) return;
+    const cplx f = 1.0 / sqrt(n);
+    for (unsigned i = 0; i < n; i++) x[i] *= f;
+}
+
+// helper::ifft (helper.h:108-114).
+void ifft(cplx* x, unsigned n) {
+    for (unsigned i = 0; i < n; i++) x[i] = std::conj(x[i]);
+    fft_dif(x, n, false);
+    for (unsigned i = 0; i < n; i++) x[i] = std::conj(x[i]);
+    for (unsigned i = 0; i < n; i++) x[i] /= cplx((double)n);
+}
+
+// kernelV3 (kernelSDEM.h:168-222): total-viewshed line-of-sight sweep.  When
+// `counts` is given, the integer-valued cv is stored instead of cv*r.
+void op_sdem(const Sector& s, const float* S, float* O, float povh, bool counts) {
+    const float r2 = (float)pow(s.scale, 2);
+    for (int row = 0; row < s.H; row++) {
+        const int lo = s.first[row], hi = s.last[row];
+        const float* v = S + (size_t)s.dim_i * row;
+        float* out = O + (size_t)s.dim_i * row;
+        for (int j = lo; j < hi; j++) {
+            float cv = 0;
+            const float h = v[j] + povh;
+            for (int dir = 1; dir >= -1; dir -= 2) {
+                float horizon = -2000;
+                bool seen = true;
+                float opened = 0;
+                for (int k = j + dir; k >= lo && k < hi; k += dir) {
+                    const float d = (float)(dir > 0 ? k - j : j - k);
+                    const float slope = (v[k] - h) / d;
+                    const bool above = slope > horizon;
+                    if (above && !seen) opened = d;
+                    if (!above && seen) cv += (d * d - opened * opened);
+                    seen = above;
+                    horizon = std::max(slope, horizon);
+                }
+            }
+            out[j] = counts ? cv : cv * r2;
+        }
+    }
+}
+
+// radon, global mode (kernelRADN.h:221-258): ray sums, ramp filter in the
+// frequency domain, filtered back-projection along the row.
+void op_radon(const Sector& s, const float* S, float* O) {
+    const int H = s.H;
+    const int H2 = (int)pow(2, ceil(log2(H)));
+    std::vector<cplx> p(H2, cplx(0, 0));
+    for (int i = 0; i < H; i++) {
+        const float* v = S + (size_t)s.dim_i * i;
+        for (int j = s.first[i]; j < s.last[i]; j++) p[i] = cplx(p[i].real() + v[j], 0);
+    }
+    fft_dif(p.data(), (unsigned)H2, false);
+    for (int i = 0; i < H2; i++) p[i] = i > H / 2 ? cplx(0) : ((double)i / H) * p[i];
+    ifft(p.data(), (unsigned)H2);
+    for (int i = 0; i < H; i++) {
+        float* out = O + (size_t)s.dim_i * i;
+        for (int j = s.first[i]; j < s.last[i]; j++) out[j] += p[i].real();
+    }
+}
+
+// getBlurParameter2 (kernelBLUR.h:88-110): skip the descending head from index 5,
+// then the largest sample (the first ascending sample itself is not visited).
+double blur_peak(const double* v, int n) {
+    int i = 5;
+    while (i < n && !(v[i] > v[i - 1])) i++;
+    if (i == n) return 0;
+    double best = v[i - 1];
+    int at = i;
+    for (i = i + 1; i < n; i++)
+        if (v[i] > best) { best = v[i]; at = i; }
+    return at == 0 ? 0 : best;
+}
+
+// cepstrum + lineCepstrum + select_subarray (kernelBLUR.h:267-302, :153-228,
+// :69-85) with the effective window of 64 (kernelRADN.h:19 wins the shared
+// KERNELCOMMONS guard).
+const int kWin = 64;
+void op_cepstrum(const Sector& s, const float* S, float* O) {
+    cplx w1[kWin], w2[kWin / 2];
+    double samples[kWin / 4];
+    for (int row = 0; row < s.H; row++) {
+        const int lo = s.first[row], hi = s.last[row];
+        const float* v = S + (size_t)s.dim_i * row;
+        for (int j = lo; j < hi; j++) {
+            for (int m = 0; m < kWin; m++) {
+                const int idx = j - kWin / 2 + m;
+                w1[m] = (idx < lo || idx >= hi) ? cplx(0, 0) : cplx(v[idx], 0);
+            }
+            fft_dif(w1, kWin, true);
+            for (int k = 0; k < kWin / 2; k++) {
+                const double ps = pow(w1[k].real(), 2) + pow(w1[k].imag(), 2);
+                w2[k] = cplx(log(ps), 0);
+            }
+            fft_dif(w2, kWin / 2, true);
+            for (int k = 0; k < kWin / 4; k++) samples[k] = -std::min(0.0, w2[k].real());
+            O[(size_t)s.dim_i * row + j] = (float)(blur_peak(samples, kWin / 4) * 10000);
+        }
+    }
+}
+
+// identity (kernelUNIT.h:16-23).
+void op_identity(const Sector& s, const float* S, float* O) {
+    for (int row = 0; row < s.H; row++)
+        for (int j = s.first[row]; j < s.last[row]; j++)
+            O[(size_t)s.dim_i * row + j] = S[(size_t)s.dim_i * row + j];
+}
+
+void run_operator(int op, const Sector& s, const float* S, float* O, float povh) {
+    switch (op) {
+        case PORT_SDEM: op_sdem(s, S, O, povh, false); break;
+        case PORT_RADON: op_radon(s, S, O); break;
+        case PORT_CEPSTRUM: op_cepstrum(s, S, O); break;
+        default: op_identity(s, S, O); break;
+    }
+}
+
+// deskew (skewEngine.cuh:772-793): gather the two skewed cells of every source
+// cell back.  Add mode accumulates; max mode keeps the maximum and re-encodes the
+// low three decimal digits with the current angle.
+void deskew_rows(const Sector& s, const float* O, float* acc, bool max_mode) {
+    for (int i = 0; i < s.dim_o; i++)
+        for (int j = 0; j < s.dim_i; j++) {
+            const float lo = O[(size_t)(i + s.target[j]) * s.dim_i + j];
+            const float hi = O[(size_t)(i + s.target[j] + 1) * s.dim_i + j];
+            float& cell = acc[(size_t)i * s.dim_i + j];
+            if (max_mode) {
+                cell = std::max(cell, std::max(lo, hi));
+                cell = s.a + 1000 * (int)(cell / 1000);
+            } else {
+                cell += (1.0f - s.weight[j]) * lo + s.weight[j] * hi;
+            }
+        }
+}
+
+// reduce (skewEngine.cuh:862-914): fold the four per-type accumulators back into
+// the input orientation, in type order 0..3, skipping types never used.
+void reduce_types(float* out, int dimx, int dimy, const std::vector<float> acc[4], bool max_mode) {
+    for (int i = 0; i < dimy; i++) {
+        const int ci = dimy - 1 - i;
+        for (int j = 0; j < dimx; j++) {
+            const int cj = dimx - 1 - j;
+            const size_t idx[4] = {(size_t)i * dimx + j, (size_t)cj * dimy + ci,
+                                   (size_t)j * dimy + ci, (size_t)i * dimx + cj};
+            float& o = out[(size_t)i * dimx + j];
+            for (int t = 0; t < 4; t++) {
+                if (acc[t].empty()) continue;
+                const float v = acc[t][idx[t]];
+                if (max_mode) o = o > v ? o : v;
+                else o += v;
+            }
+        }
+    }
+}
+
+struct Worker {
+    std::vector<float> S, O;
+    std::vector<float> acc[4];
+};
+
+void run_sector(int op, int dimx, int dimy, const std::vector<float> src[4], int angle, float povh,
+                Worker& w) {
+    Sector s;
+    make_sector(dimx, dimy, angle, s);
+    std::fill(w.S.begin(), w.S.end(), 0.0f);
+    std::fill(w.O.begin(), w.O.end(), 0.0f);
+    skew_rows(s, src[s.type].data(), w.S.data());
+    run_operator(op, s, w.S.data(), w.O.data(), povh);
+    if (w.acc[s.type].empty()) w.acc[s.type].assign((size_t)dimx * dimy, 0.0f);
+    deskew_rows(s, w.O.data(), w.acc[s.type].data(), op == PORT_CEPSTRUM);
+}
+
+}  // namespace
+
+extern "C" {
+
+int port_geometry(int dimx, int dimy, int angle, int* iinfo, double* dinfo, unsigned short* first,
+                  unsigned short* last, int* target, float* weight) {
+    if (dimx <= 0 || dimy <= 0 || angle < 0 || angle >= 180) return 1;
+    Sector s;
+    make_sector(dimx, dimy, angle, s);
+    const int ints[7] = {s.type, s.newAngle, s.dim_i, s.dim_o, s.offset, s.H, s.diml};
+    memcpy(iinfo, ints, sizeof(ints));
+    dinfo[0] = s.scale;
+    dinfo[1] = s.skewness;
+    if (first) {
+        memset(first, 0, sizeof(unsigned short) * (2 * s.diml + 1));
+        std::copy(s.first.begin(), s.first.begin() + s.H, first);
+    }
+    if (last) {
+        memset(last, 0, sizeof(unsigned short) * (2 * s.diml + 1));
+        std::copy(s.last.begin(), s.last.begin() + s.H, last);
+    }
+    if (target) std::copy(s.target.begin(), s.target.end(), target);
+    if (weight) std::copy(s.weight.begin(), s.weight.end(), weight);
+    return 0;
+}
+
+int port_run_angles(int op, const float* input, float* output, int dimx, int dimy, const int* angles,
+                    int nangles, float povh, int nthreads) {
+    if (dimx <= 0 || dimy <= 0 || nangles <= 0) return 1;
+    for (int i = 0; i < nangles; i++)
+        if (angles[i] < 0 || angles[i] >= 180) return 1;
+    std::vector<float> src[4];
+    orientations(input, dimx, dimy, src);
+    const size_t n = (size_t)dimx * dimy;
+    const int diml = std::max(dimx, dimy);
+    const int nt = nthreads > 0 ? nthreads : 1;
+    std::vector<Worker> workers(nt);
+    memset(output, 0, sizeof(float) * n);
+#pragma omp parallel num_threads(nt)
+    {
+        Worker& w = workers[omp_get_thread_num()];
+        w.S.assign(2 * n + diml, 0.0f);
+        w.O.assign(2 * n + diml, 0.0f);
+#pragma omp for schedule(dynamic)
+        for (int i = 0; i < nangles; i++) run_sector(op, dimx, dimy, src, angles[i], povh, w);
+    }
+    // Deterministic stand-in for the reference's critical-section reduce
+    // (main.cu:160-164): threads fold in id order.
+    for (int t = 0; t < nt; t++) reduce_types(output, dimx, dimy, workers[t].acc, op == PORT_CEPSTRUM);
+    return 0;
+}
+
+int port_run(int op, const float* input, float* output, int dimx, int dimy, int nsect, float povh,
+             int nthreads) {
+    if (nsect <= 0 || nsect > 180) return 1;
+    std::vector<int> angles(nsect);
+    for (int i = 0; i < nsect; i++) angles[i] = i;
+    return port_run_angles(op, input, output, dimx, dimy, angles.data(), nsect, povh, nthreads);
+}
+
+int port_sector(int op, const float* input, int dimx, int dimy, int angle, float povh, float* skew_in,
+                float* skew_out, float* acc) {
+    if (dimx <= 0 || dimy <= 0 || angle < 0 || angle >= 180) return 1;
+    std::vector<float> src[4];
+    orientations(input, dimx, dimy, src);
+    const size_t n = (size_t)dimx * dimy;
+    Worker w;
+    w.S.assign(2 * n + std::max(dimx, dimy), 0.0f);
+    w.O.assign(w.S.size(), 0.0f);
+    run_sector(op, dimx, dimy, src, angle, povh, w);
+    if (skew_in) std::copy(w.S.begin(), w.S.end(), skew_in);
+    if (skew_out) std::copy(w.O.begin(), w.O.end(), skew_out);
+    if (acc) {
+        memset(acc, 0, sizeof(float) * n);
+        reduce_types(acc, dimx, dimy, w.acc, op == PORT_CEPSTRUM);
+    }
+    return 0;
+}
+
+int port_sdem_counts(const float* input, int dimx, int dimy, int angle, float povh, float* counts) {
+    if (dimx <= 0 || dimy <= 0 || angle < 0 || angle >= 180) return 1;
+    std::vector<float> src[4];
+    orientations(input, dimx, dimy, src);
+    const size_t n = (size_t)dimx * dimy;
+    Sector s;
+    make_sector(dimx, dimy, angle, s);
+    std::vector<float> S(2 * n + s.diml, 0.0f);
+    skew_rows(s, src[s.type].data(), S.data());
+    memset(counts, 0, sizeof(float) * S.size());
+    op_sdem(s, S.data(), counts, povh, true);
+    return 0;
+}
+
+int port_accumulate(int op, const float* input, int dimx, int dimy, const int* angles, int nangles, float povh,
+                    float* acc, int* used_mask) {
+    if (dimx <= 0 || dimy <= 0 || nangles < 0) return 1;
+    for (int i = 0; i < nangles; i++)
+        if (angles[i] < 0 || angles[i] >= 180) return 1;
+    std::vector<float> src[4];
+    orientations(input, dimx, dimy, src);
+    const size_t n = (size_t)dimx * dimy;
+    Worker w;
+    w.S.assign(2 * n + std::max(dimx, dimy), 0.0f);
+    w.O.assign(w.S.size(), 0.0f);
+    for (int i = 0; i < nangles; i++) run_sector(op, dimx, dimy, src, angles[i], povh, w);
+    int mask = 0;
+    for (int t = 0; t < 4; t++) {
+        if (w.acc[t].empty()) {
+            memset(acc + t * n, 0, sizeof(float) * n);
+        } else {
+            std::copy(w.acc[t].begin(), w.acc[t].end(), acc + t * n);
+            mask |= 1 << t;
+        }
+    }
+    *used_mask = mask;
+    return 0;
+}
+
+double port_los_steps(int dimx, int dimy, int nsect) {
+    double total = 0;
+    for (int a = 0; a < nsect; a++) {
+        Sector s;
+        make_sector(dimx, dimy, a, s);
+        for (int r = 0; r < s.H; r++) {
+            const double L = (double)s.last[r] - (double)s.first[r];
+            if (L > 0) total += L * (L - 1);
+        }
+    }
+    return total;
+}
+
+}  // extern "C"

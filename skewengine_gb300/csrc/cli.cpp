@@ -1,0 +1,147 @@
+// Command-line entry point `run(argc, argv)`, the reference's only C export
+// (src/main.cu:200-202), plus the DEM file formats it reads and writes.
+//
+//   run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]
+//
+//   kernel     sdem | identitydem | radon | identityimg | cepstrum, or 0..4
+//              (KERNELS enum, src/global.h:77)
+//   input      raw little-endian float32 grid (dimy rows of dimx), or an ESRI
+//              .bil int16 grid whose values are divided by 10 as readBilData does
+//              (src/kernelSDEM.h:43-50); dimx/dimy 0 take NCOLS/NROWS from the
+//              .hdr beside it, else a square grid from the file size
+//              (check_dem, src/kernelSDEM.h:98-142)
+//   output     raw float32 grid (the .flt dump of showResultsSDEM,
+//              src/kernelSDEM.h:433-439)
+//   max_sector angles 0..max_sector-1 (default 180), povh observer height in cell
+//              units (default 0.15), accum 0 reference order / 1 Kahan.
+//
+// Returns 0 on success, a SKE_* status otherwise; messages go to stderr.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/skewengine.h"
+
+namespace {
+
+int parse_kernel(const char* s) {
+    static const char* names[] = {"sdem", "identitydem", "radon", "identityimg", "cepstrum"};
+    for (int i = 0; i < 5; i++)
+        if (!strcmp(s, names[i])) return i;
+    char* end = nullptr;
+    long v = strtol(s, &end, 10);
+    if (end && *end == 0 && v >= 0 && v <= 4) return (int)v;
+    return -1;
+}
+
+bool ends_with(const std::string& s, const char* suf) {
+    const size_t n = strlen(suf);
+    return s.size() >= n && s.compare(s.size() - n, n, suf) == 0;
+}
+
+// NROWS / NCOLS from an ESRI header next to `bil` (same stem, .hdr).
+void read_hdr(const std::string& bil, int* ncols, int* nrows) {
+    const std::string hdr = bil.substr(0, bil.find_last_of('.')) + ".hdr";
+    FILE* f = fopen(hdr.c_str(), "r");
+    if (!f) return;
+    char line[256];
+    while (fgets(line, sizeof(line), f)) {
+        char key[64];
+        int v = 0;
+        if (sscanf(line, "%63s %d", key, &v) != 2) continue;
+        for (char* k = key; *k; k++) *k = (char)toupper((unsigned char)*k);
+        if (!strcmp(key, "NCOLS")) *ncols = v;
+        if (!strcmp(key, "NROWS")) *nrows = v;
+    }
+    fclose(f);
+}
+
+long file_size(const char* path) {
+    FILE* f = fopen(path, "rb");
+    if (!f) return -1;
+    fseek(f, 0, SEEK_END);
+    const long n = ftell(f);
+    fclose(f);
+    return n;
+}
+
+int load_input(const std::string& path, int* dimx, int* dimy, std::vector<float>& out) {
+    const bool bil = ends_with(path, ".bil");
+    const long bytes = file_size(path.c_str());
+    if (bytes < 0) {
+        fprintf(stderr, "run: cannot open %s\n", path.c_str());
+        return SKE_ERR_INVALID;
+    }
+    const int cell = bil ? 2 : 4;
+    if (*dimx <= 0 || *dimy <= 0) {
+        int nc = 0, nr = 0;
+        if (bil) read_hdr(path, &nc, &nr);
+        if (nc <= 0 || nr <= 0) nc = nr = (int)std::sqrt((double)(bytes / cell));
+        *dimx = nc;
+        *dimy = nr;
+    }
+    const size_t n = (size_t)*dimx * *dimy;
+    if ((size_t)bytes < n * cell) {
+        fprintf(stderr, "run: %s holds %ld bytes, need %zu\n", path.c_str(), bytes, n * cell);
+        return SKE_ERR_INVALID;
+    }
+    out.resize(n);
+    FILE* f = fopen(path.c_str(), "rb");
+    if (bil) {
+        std::vector<int16_t> raw(n);
+        const size_t got = fread(raw.data(), 2, n, f);
+        fclose(f);
+        if (got != n) return SKE_ERR_INVALID;
+        for (size_t i = 0; i < n; i++) out[i] = (float)(((float)raw[i]) / 10.0);
+    } else {
+        const size_t got = fread(out.data(), 4, n, f);
+        fclose(f);
+        if (got != n) return SKE_ERR_INVALID;
+    }
+    return SKE_OK;
+}
+
+}  // namespace
+
+extern "C" int run(int argc, char** argv) {
+    if (argc < 6) {
+        fprintf(stderr, "usage: run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]\n");
+        return SKE_ERR_INVALID;
+    }
+    const int kernel = parse_kernel(argv[1]);
+    if (kernel < 0) {
+        fprintf(stderr, "run: unknown kernel '%s'\n", argv[1]);
+        return SKE_ERR_INVALID;
+    }
+    int dimx = atoi(argv[3]), dimy = atoi(argv[4]);
+    std::vector<float> in;
+    int rc = load_input(argv[2], &dimx, &dimy, in);
+    if (rc != SKE_OK) return rc;
+    ske_params p;
+    ske_params_default(&p);
+    if (argc > 6) p.max_sector = atoi(argv[6]);
+    if (argc > 7) p.povh = (float)atof(argv[7]);
+    if (argc > 8) p.accum = atoi(argv[8]);
+    ske_engine e = nullptr;
+    rc = ske_create(&e, dimx, dimy, 0, nullptr);
+    if (rc != SKE_OK) {
+        fprintf(stderr, "run: %s\n", ske_last_error());
+        return rc;
+    }
+    std::vector<float> out((size_t)dimx * dimy);
+    rc = ske_run(e, kernel, in.data(), 0, out.data(), 0, &p);
+    if (rc != SKE_OK) fprintf(stderr, "run: %s\n", ske_last_error());
+    ske_destroy(e);
+    if (rc != SKE_OK) return rc;
+    FILE* f = fopen(argv[5], "wb");
+    if (!f) {
+        fprintf(stderr, "run: cannot write %s\n", argv[5]);
+        return SKE_ERR_INVALID;
+    }
+    fwrite(out.data(), sizeof(float), out.size(), f);
+    fclose(f);
+    return SKE_OK;
+}

@@ -1,0 +1,821 @@
+// C ABI of the skew engine (include/skewengine.h): engine object, device
+// buffers, the batched sector loop and the per-sector drop-in API.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/skewengine.h"
+#include "kernels.h"
+
+using namespace ske;
+
+namespace {
+
+thread_local std::string t_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_last_error = buf;
+    return code;
+}
+
+#define SKE_CK(call)                                                                              \
+    do {                                                                                          \
+        cudaError_t _e = (call);                                                                  \
+        if (_e != cudaSuccess) return fail(SKE_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+#define SKE_TRY(expr)            \
+    do {                         \
+        int _rc = (expr);        \
+        if (_rc != SKE_OK) return _rc; \
+    } while (0)
+
+std::mutex g_init_mutex;
+std::vector<int> g_tables_ready;  // per device: SDEM constant tables uploaded
+
+int ensure_device_tables(int device) {
+    std::lock_guard<std::mutex> lock(g_init_mutex);
+    if ((int)g_tables_ready.size() <= device) g_tables_ready.resize(device + 1, 0);
+    if (g_tables_ready[device]) return SKE_OK;
+    SKE_CK(sdem_init_tables());
+    g_tables_ready[device] = 1;
+    return SKE_OK;
+}
+
+bool valid_kernel(int k) { return k >= SKE_KERNEL_SDEM && k <= SKE_KERNEL_CEPSTRUM; }
+
+template <typename T>
+int dev_alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return SKE_OK;
+    SKE_CK(cudaMalloc((void**)p, sizeof(T) * count));
+    return SKE_OK;
+}
+
+struct ItemPlan {
+    uint64_t* d_items = nullptr;
+    int64_t n_items = 0;
+    int max_row = 0;
+};
+
+struct ProfEntry {
+    double ms = 0;
+    int64_t launches = 0;
+};
+
+}  // namespace
+
+struct ske_engine_s {
+    int dimx = 0, dimy = 0, device = 0, num_sms = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int64_t N = 0, len = 0, stride = 0;
+    Geometry geo;
+    DevGeometry dg{};
+    SectorDesc* d_desc = nullptr;
+    int32_t *d_target = nullptr, *d_first = nullptr, *d_last = nullptr;
+    float* d_weight = nullptr;
+    float *d_in = nullptr, *d_orient = nullptr, *d_acc = nullptr, *d_comp = nullptr, *d_out = nullptr;
+    float *d_SI = nullptr, *d_SO = nullptr;
+    int slots = 0;  // capacity of d_SI/d_SO in sectors
+    double* d_P = nullptr;
+    int64_t pstride = 0;  // complex doubles per slot
+    int max_H2 = 1;
+    double* d_tw = nullptr;
+    int64_t* d_tw_off = nullptr;
+    int64_t tw_off_host[32] = {0};
+    unsigned* d_counter = nullptr;
+    int* d_status = nullptr;
+    float* h_pin = nullptr;
+    std::map<std::vector<int>, ItemPlan> item_plans;
+    // per-sector API state
+    bool prepared = false;
+    int cur_angle = -1;
+    bool kernel_ran = false;
+    unsigned used = 0;
+    int accum_mode = SKE_ACCUM_REFERENCE;
+    // profiling
+    bool prof = false;
+    std::map<std::string, ProfEntry> prof_tot;
+    struct Pending {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending;
+    std::vector<cudaEvent_t> event_pool;
+    int64_t launches = 0;
+};
+
+namespace {
+
+// Brackets a group of kernel launches for the profiler.
+struct LaunchScope {
+    ske_engine e;
+    const char* name;
+    cudaEvent_t a = nullptr, b = nullptr;
+    int kernels;
+    LaunchScope(ske_engine e_, const char* n, int k) : e(e_), name(n), kernels(k) {
+        if (e->prof) {
+            a = take();
+            b = take();
+            cudaEventRecord(a, e->stream);
+        }
+    }
+    cudaEvent_t take() {
+        if (!e->event_pool.empty()) {
+            cudaEvent_t ev = e->event_pool.back();
+            e->event_pool.pop_back();
+            return ev;
+        }
+        cudaEvent_t ev;
+        cudaEventCreate(&ev);
+        return ev;
+    }
+    int done(cudaError_t err) {
+        if (err != cudaSuccess) return fail(SKE_ERR_CUDA, "%s launch failed: %s", name, cudaGetErrorString(err));
+        e->launches += kernels;
+        if (e->prof) {
+            cudaEventRecord(b, e->stream);
+            e->pending.push_back({name, a, b});
+            a = b = nullptr;
+        }
+        return SKE_OK;
+    }
+};
+
+int flush_profile(ske_engine e) {
+    if (e->pending.empty()) return SKE_OK;
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    for (auto& p : e->pending) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        ProfEntry& t = e->prof_tot[p.name];
+        t.ms += ms;
+        t.launches += 1;
+        e->event_pool.push_back(p.a);
+        e->event_pool.push_back(p.b);
+    }
+    e->pending.clear();
+    return SKE_OK;
+}
+
+int set_device(ske_engine e) {
+    SKE_CK(cudaSetDevice(e->device));
+    return SKE_OK;
+}
+
+bool is_pinned_host(const void* p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// Host -> device copy of n floats, through the engine's pinned buffer unless the
+// source is already page-locked.
+int upload(ske_engine e, float* dst, const float* src, int64_t n) {
+    if (is_pinned_host(src)) {
+        SKE_CK(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyHostToDevice, e->stream));
+        return SKE_OK;
+    }
+    SKE_CK(cudaStreamSynchronize(e->stream));  // pinned buffer may still be in use
+    memcpy(e->h_pin, src, sizeof(float) * n);
+    SKE_CK(cudaMemcpyAsync(dst, e->h_pin, sizeof(float) * n, cudaMemcpyHostToDevice, e->stream));
+    return SKE_OK;
+}
+
+int download(ske_engine e, float* dst, const float* src, int64_t n) {
+    if (is_pinned_host(dst)) {
+        SKE_CK(cudaMemcpyAsync(dst, src, sizeof(float) * n, cudaMemcpyDeviceToHost, e->stream));
+        SKE_CK(cudaStreamSynchronize(e->stream));
+        return SKE_OK;
+    }
+    SKE_CK(cudaMemcpyAsync(e->h_pin, src, sizeof(float) * n, cudaMemcpyDeviceToHost, e->stream));
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    memcpy(dst, e->h_pin, sizeof(float) * n);
+    return SKE_OK;
+}
+
+int check_status(ske_engine e) {
+    int st = 0;
+    SKE_CK(cudaMemcpyAsync(&st, e->d_status, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    if (st != 0) {
+        cudaMemsetAsync(e->d_status, 0, sizeof(int), e->stream);
+        return fail(SKE_ERR_DEVICE, "device status %d reported by a kernel", st);
+    }
+    return SKE_OK;
+}
+
+// Make room for `want` sector slots of skewed buffers (and Radon scratch).
+int ensure_slots(ske_engine e, int want) {
+    if (want <= e->slots) return SKE_OK;
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    cudaFree(e->d_SI);
+    cudaFree(e->d_SO);
+    cudaFree(e->d_P);
+    e->d_SI = e->d_SO = nullptr;
+    e->d_P = nullptr;
+    e->slots = 0;
+    SKE_TRY(dev_alloc(&e->d_SI, (size_t)e->stride * want));
+    SKE_TRY(dev_alloc(&e->d_SO, (size_t)e->stride * want));
+    SKE_TRY(dev_alloc(&e->d_P, (size_t)e->pstride * 2 * want));
+    e->slots = want;
+    return SKE_OK;
+}
+
+// Sectors per launch: as many as fit in a quarter of free memory (at most 180).
+int batch_capacity(ske_engine e, int nangles) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = (size_t)1 << 30;
+    }
+    const size_t per_slot = sizeof(float) * 2 * (size_t)e->stride + sizeof(double) * 2 * (size_t)e->pstride;
+    size_t budget = free_b / 4 + (size_t)e->slots * per_slot;
+    int cap = (int)std::min<size_t>(budget / std::max<size_t>(per_slot, 1), (size_t)kMaxBatch);
+    cap = std::max(cap, 1);
+    return std::min(cap, nangles);
+}
+
+int get_items(ske_engine e, const Batch& b, ItemPlan** out) {
+    std::vector<int> key(b.angle, b.angle + b.count);
+    auto it = e->item_plans.find(key);
+    if (it != e->item_plans.end()) {
+        *out = &it->second;
+        return SKE_OK;
+    }
+    std::vector<uint64_t> items;
+    ItemPlan plan;
+    sdem_items(e->geo, b, items, &plan.max_row);
+    plan.n_items = (int64_t)items.size();
+    SKE_TRY(dev_alloc(&plan.d_items, items.size()));
+    if (!items.empty())
+        SKE_CK(cudaMemcpy(plan.d_items, items.data(), sizeof(uint64_t) * items.size(), cudaMemcpyHostToDevice));
+    auto ins = e->item_plans.emplace(key, plan);
+    *out = &ins.first->second;
+    return SKE_OK;
+}
+
+int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int counts_only) {
+    switch (kernel) {
+        case SKE_KERNEL_SDEM: {
+            ItemPlan* plan = nullptr;
+            SKE_TRY(get_items(e, b, &plan));
+            SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
+            SdemLaunch a;
+            a.g = e->dg;
+            a.b = b;
+            a.SI = e->d_SI;
+            a.SO = e->d_SO;
+            a.stride = e->stride;
+            a.items = plan->d_items;
+            a.n_items = plan->n_items;
+            a.counter = e->d_counter;
+            a.povh = povh;
+            a.max_row = std::max(plan->max_row, 1);
+            a.counts_only = counts_only;
+            a.status = e->d_status;
+            LaunchScope ls(e, "sdem_sweep", plan->n_items > 0 ? 1 : 0);
+            return ls.done(launch_sdem(a, e->num_sms, e->stream));
+        }
+        case SKE_KERNEL_RADON: {
+            LaunchScope ls(e, "radon", 3);
+            return ls.done(launch_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_P, e->pstride, e->d_tw,
+                                        e->d_tw_off, e->max_H2, e->stream));
+        }
+        case SKE_KERNEL_CEPSTRUM: {
+            LaunchScope ls(e, "cepstrum", 1);
+            return ls.done(launch_cepstrum(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_tw + e->tw_off_host[6],
+                                           e->d_tw + e->tw_off_host[5], e->stream));
+        }
+        default: {
+            LaunchScope ls(e, "identity", 1);
+            return ls.done(launch_identity(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->stream));
+        }
+    }
+}
+
+int run_skew(ske_engine e, const Batch& b) {
+    LaunchScope ls(e, "skew", 1);
+    return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, e->stream));
+}
+
+int run_deskew(ske_engine e, const Batch& b, int is_max, int accum) {
+    TypeLists tl;
+    memset(&tl, 0, sizeof(tl));
+    for (int s = 0; s < b.count; s++) {
+        const int t = e->geo.desc[b.angle[s]].type;
+        tl.slot[t][tl.count[t]] = s;
+        tl.angle[t][tl.count[t]] = b.angle[s];
+        tl.count[t]++;
+        e->used |= 1u << t;
+    }
+    LaunchScope ls(e, "deskew", 1);
+    if (is_max) return ls.done(launch_deskew_max(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->dimx, e->dimy, e->stream));
+    return ls.done(launch_deskew_add(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->d_comp, e->dimx, e->dimy, accum,
+                                     e->stream));
+}
+
+int run_prepare(ske_engine e, const float* input, int on_device) {
+    const float* src = input;
+    if (!on_device) {
+        SKE_TRY(upload(e, e->d_in, input, e->N));
+        src = e->d_in;
+    }
+    {
+        LaunchScope ls(e, "prepare", 1);
+        SKE_TRY(ls.done(launch_prepare(src, e->d_orient, e->dimx, e->dimy, e->stream)));
+    }
+    SKE_CK(cudaMemsetAsync(e->d_acc, 0, sizeof(float) * 4 * e->N, e->stream));
+    SKE_CK(cudaMemsetAsync(e->d_comp, 0, sizeof(float) * 4 * e->N, e->stream));
+    e->used = 0;
+    e->prepared = true;
+    e->cur_angle = -1;
+    e->kernel_ran = false;
+    return SKE_OK;
+}
+
+int run_reduce(ske_engine e, float* output, int on_device, int is_max, int accum) {
+    float* dst = on_device ? output : e->d_out;
+    {
+        LaunchScope ls(e, "reduce", 1);
+        SKE_TRY(ls.done(launch_reduce(e->d_acc, e->d_comp, e->used, dst, e->dimx, e->dimy, is_max, accum, e->stream)));
+    }
+    if (!on_device) SKE_TRY(download(e, output, e->d_out, e->N));
+    return check_status(e);
+}
+
+int validate_params(const ske_params* p, ske_params* out) {
+    ske_params_default(out);
+    if (p) *out = *p;
+    if (out->max_sector < 1 || out->max_sector > kMaxSectors)
+        return fail(SKE_ERR_INVALID, "max_sector %d outside [1,180]", out->max_sector);
+    if (out->accum != SKE_ACCUM_REFERENCE && out->accum != SKE_ACCUM_KAHAN)
+        return fail(SKE_ERR_INVALID, "unknown accumulation mode %d", out->accum);
+    return SKE_OK;
+}
+
+// Prepare + every listed sector (skew, operator, deskew) into the accumulators.
+int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on_device, const int32_t* angles,
+                      int nangles, const ske_params* p, ske_params* prm) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
+    if (!input) return fail(SKE_ERR_INVALID, "null input");
+    if (nangles < 0 || (nangles > 0 && !angles)) return fail(SKE_ERR_INVALID, "bad angle list");
+    for (int i = 0; i < nangles; i++)
+        if (angles[i] < 0 || angles[i] >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angles[i]);
+    SKE_TRY(validate_params(p, prm));
+    SKE_TRY(set_device(e));
+    const int is_max = kernel == SKE_KERNEL_CEPSTRUM;
+    SKE_TRY(run_prepare(e, input, input_on_device));
+    if (nangles == 0) return SKE_OK;
+    const int cap = batch_capacity(e, nangles);
+    SKE_TRY(ensure_slots(e, cap));
+    for (int s0 = 0; s0 < nangles; s0 += cap) {
+        Batch b;
+        b.count = std::min(cap, nangles - s0);
+        for (int s = 0; s < b.count; s++) b.angle[s] = angles[s0 + s];
+        SKE_TRY(run_skew(e, b));
+        SKE_TRY(run_operator(e, kernel, b, prm->povh, 0));
+        SKE_TRY(run_deskew(e, b, is_max, prm->accum));
+    }
+    e->accum_mode = prm->accum;
+    return SKE_OK;
+}
+
+int run_angle_list(ske_engine e, int kernel, const float* input, int input_on_device, float* output,
+                   int output_on_device, const int32_t* angles, int nangles, const ske_params* p) {
+    if (!output) return fail(SKE_ERR_INVALID, "null output");
+    if (nangles < 1) return fail(SKE_ERR_INVALID, "empty angle list");
+    ske_params prm;
+    SKE_TRY(accumulate_angles(e, kernel, input, input_on_device, angles, nangles, p, &prm));
+    SKE_TRY(run_reduce(e, output, output_on_device, kernel == SKE_KERNEL_CEPSTRUM, prm.accum));
+    e->prepared = false;  // the accumulators now hold this run
+    return SKE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ske_abi_version(void) { return SKE_ABI_VERSION; }
+
+const char* ske_last_error(void) { return t_last_error.c_str(); }
+
+int ske_params_default(ske_params* p) {
+    if (!p) return fail(SKE_ERR_INVALID, "null params");
+    p->max_sector = 180;
+    p->povh = (float)(1.5 / 10.0);  // obsheight / step (kernelSDEM.h:159)
+    p->accum = SKE_ACCUM_REFERENCE;
+    p->flags = 0;
+    return SKE_OK;
+}
+
+int ske_device_count(int* count) {
+    if (!count) return fail(SKE_ERR_INVALID, "null count");
+    *count = 0;
+    int n = 0;
+    cudaError_t err = cudaGetDeviceCount(&n);
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        return SKE_OK;
+    }
+    *count = n;
+    return SKE_OK;
+}
+
+int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32_t* first, int32_t* last,
+                 int32_t* target, float* weight) {
+    if (dimx < 1 || dimy < 1 || dimx > 65535 || dimy > 65535)
+        return fail(SKE_ERR_INVALID, "grid %dx%d outside [1,65535]", dimx, dimy);
+    if (angle < 0 || angle >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angle);
+    if (!geom) return fail(SKE_ERR_INVALID, "null geometry");
+    SectorDesc d;
+    std::vector<int32_t> f, l, t;
+    std::vector<float> w;
+    sector_geometry(dimx, dimy, angle, d, f, l, t, w);
+    geom->angle = d.angle;
+    geom->sector_type = d.type;
+    geom->new_angle = d.new_angle;
+    geom->dim_i = d.dim_i;
+    geom->dim_o = d.dim_o;
+    geom->offset = d.offset;
+    geom->skew_height = d.H;
+    geom->dim_l = d.diml;
+    geom->scale = d.scale;
+    geom->skewness = d.skewness;
+    if (first) std::copy(f.begin(), f.end(), first);
+    if (last) std::copy(l.begin(), l.end(), last);
+    if (target) std::copy(t.begin(), t.end(), target);
+    if (weight) std::copy(w.begin(), w.end(), weight);
+    return SKE_OK;
+}
+
+int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) {
+    if (!out) return fail(SKE_ERR_INVALID, "null engine pointer");
+    *out = nullptr;
+    if (dimx < 1 || dimy < 1 || dimx > 65535 || dimy > 65535)
+        return fail(SKE_ERR_INVALID, "grid %dx%d outside [1,65535]", dimx, dimy);
+    int ndev = 0;
+    cudaError_t err = cudaGetDeviceCount(&ndev);
+    if (err != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SKE_ERR_NO_DEVICE, "no CUDA device available (%s)",
+                    err != cudaSuccess ? cudaGetErrorString(err) : "0 devices");
+    }
+    if (device < 0 || device >= ndev) return fail(SKE_ERR_INVALID, "device %d outside [0,%d)", device, ndev);
+    std::unique_ptr<ske_engine_s> e(new ske_engine_s());
+    e->dimx = dimx;
+    e->dimy = dimy;
+    e->device = device;
+    SKE_CK(cudaSetDevice(device));
+    SKE_CK(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device));
+    SKE_TRY(ensure_device_tables(device));
+    if (stream) {
+        e->stream = (cudaStream_t)stream;
+    } else {
+        SKE_CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+        e->own_stream = true;
+    }
+    e->N = (int64_t)dimx * dimy;
+    e->len = skew_buffer_len(dimx, dimy);
+    e->stride = (e->len + 63) & ~(int64_t)63;
+    build_geometry(dimx, dimy, e->geo);
+    while (e->max_H2 < e->geo.max_H) e->max_H2 <<= 1;
+    e->pstride = e->max_H2;
+    // Geometry tables.
+    SKE_TRY(dev_alloc(&e->d_desc, e->geo.desc.size()));
+    SKE_TRY(dev_alloc(&e->d_target, e->geo.target.size()));
+    SKE_TRY(dev_alloc(&e->d_weight, e->geo.weight.size()));
+    SKE_TRY(dev_alloc(&e->d_first, e->geo.first.size()));
+    SKE_TRY(dev_alloc(&e->d_last, e->geo.last.size()));
+    SKE_CK(cudaMemcpy(e->d_desc, e->geo.desc.data(), sizeof(SectorDesc) * e->geo.desc.size(), cudaMemcpyHostToDevice));
+    SKE_CK(cudaMemcpy(e->d_target, e->geo.target.data(), sizeof(int32_t) * e->geo.target.size(), cudaMemcpyHostToDevice));
+    SKE_CK(cudaMemcpy(e->d_weight, e->geo.weight.data(), sizeof(float) * e->geo.weight.size(), cudaMemcpyHostToDevice));
+    SKE_CK(cudaMemcpy(e->d_first, e->geo.first.data(), sizeof(int32_t) * e->geo.first.size(), cudaMemcpyHostToDevice));
+    SKE_CK(cudaMemcpy(e->d_last, e->geo.last.data(), sizeof(int32_t) * e->geo.last.size(), cudaMemcpyHostToDevice));
+    e->dg = DevGeometry{e->d_desc, e->d_target, e->d_weight, e->d_first, e->d_last};
+    // FFT twiddles for every power of two up to max(64, max_H2).
+    std::vector<double> all, tw;
+    const int top = std::max(6, 31 - __builtin_clz((unsigned)e->max_H2));
+    for (int k = 0; k <= top; k++) {
+        e->tw_off_host[k] = (int64_t)all.size();
+        fft_twiddles(1u << k, tw);
+        all.insert(all.end(), tw.begin(), tw.end());
+    }
+    all.push_back(0.0);
+    SKE_TRY(dev_alloc(&e->d_tw, all.size()));
+    SKE_TRY(dev_alloc(&e->d_tw_off, 32));
+    SKE_CK(cudaMemcpy(e->d_tw, all.data(), sizeof(double) * all.size(), cudaMemcpyHostToDevice));
+    SKE_CK(cudaMemcpy(e->d_tw_off, e->tw_off_host, sizeof(int64_t) * 32, cudaMemcpyHostToDevice));
+    // Grids and accumulators.
+    SKE_TRY(dev_alloc(&e->d_in, e->N));
+    SKE_TRY(dev_alloc(&e->d_orient, 4 * e->N));
+    SKE_TRY(dev_alloc(&e->d_acc, 4 * e->N));
+    SKE_TRY(dev_alloc(&e->d_comp, 4 * e->N));
+    SKE_TRY(dev_alloc(&e->d_out, e->N));
+    SKE_TRY(dev_alloc(&e->d_counter, 1));
+    SKE_TRY(dev_alloc(&e->d_status, 1));
+    SKE_CK(cudaMemset(e->d_status, 0, sizeof(int)));
+    SKE_CK(cudaHostAlloc((void**)&e->h_pin, sizeof(float) * (size_t)std::max<int64_t>(e->N, e->len),
+                         cudaHostAllocPortable));
+    SKE_TRY(ensure_slots(e.get(), 1));
+    *out = e.release();
+    return SKE_OK;
+}
+
+int ske_destroy(ske_engine e) {
+    if (!e) return SKE_OK;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    for (auto& kv : e->item_plans) cudaFree(kv.second.d_items);
+    for (auto& p : e->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
+    void* bufs[] = {e->d_desc, e->d_target, e->d_first, e->d_last, e->d_weight, e->d_in, e->d_orient, e->d_acc,
+                    e->d_comp, e->d_out, e->d_SI, e->d_SO, e->d_P, e->d_tw, e->d_tw_off, e->d_counter, e->d_status};
+    for (void* b : bufs) cudaFree(b);
+    if (e->h_pin) cudaFreeHost(e->h_pin);
+    if (e->own_stream) cudaStreamDestroy(e->stream);
+    delete e;
+    return SKE_OK;
+}
+
+int ske_stream(ske_engine e, void** stream) {
+    if (!e || !stream) return fail(SKE_ERR_INVALID, "null argument");
+    *stream = (void*)e->stream;
+    return SKE_OK;
+}
+
+int ske_run(ske_engine e, int kernel, const float* input, int input_on_device, float* output, int output_on_device,
+            const ske_params* p) {
+    ske_params prm;
+    SKE_TRY(validate_params(p, &prm));
+    std::vector<int32_t> angles(prm.max_sector);
+    for (int i = 0; i < prm.max_sector; i++) angles[i] = i;
+    return run_angle_list(e, kernel, input, input_on_device, output, output_on_device, angles.data(),
+                          prm.max_sector, &prm);
+}
+
+int ske_run_angles(ske_engine e, int kernel, const float* input, int input_on_device, float* output,
+                   int output_on_device, const int32_t* angles, int nangles, const ske_params* p) {
+    return run_angle_list(e, kernel, input, input_on_device, output, output_on_device, angles, nangles, p);
+}
+
+int ske_accumulate(ske_engine e, int kernel, const float* input, int input_on_device, const int32_t* angles,
+                   int nangles, const ske_params* p, float* acc, int acc_on_device, uint32_t* used_mask) {
+    if (!acc || !used_mask) return fail(SKE_ERR_INVALID, "null output");
+    ske_params prm;
+    SKE_TRY(accumulate_angles(e, kernel, input, input_on_device, angles, nangles, p, &prm));
+    if (prm.accum == SKE_ACCUM_KAHAN)
+        return fail(SKE_ERR_UNSUPPORTED, "accumulators are exported in reference accumulation mode only");
+    if (acc_on_device) {
+        SKE_CK(cudaMemcpyAsync(acc, e->d_acc, sizeof(float) * 4 * e->N, cudaMemcpyDeviceToDevice, e->stream));
+        SKE_CK(cudaStreamSynchronize(e->stream));
+    } else {
+        for (int t = 0; t < 4; t++) SKE_TRY(download(e, acc + t * e->N, e->d_acc + t * e->N, e->N));
+    }
+    *used_mask = e->used;
+    e->prepared = false;
+    return check_status(e);
+}
+
+int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
+                  const float* const* inputs, int inputs_on_device, float* const* outputs, int outputs_on_device,
+                  const ske_params* p) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (count < 0 || (count > 0 && (!dimx || !dimy || !inputs || !outputs)))
+        return fail(SKE_ERR_INVALID, "bad batch arguments");
+    std::map<std::pair<int, int>, ske_engine> engines;
+    int rc = SKE_OK;
+    for (int i = 0; i < count && rc == SKE_OK; i++) {
+        ske_engine sub = nullptr;
+        if (dimx[i] == e->dimx && dimy[i] == e->dimy) {
+            sub = e;
+        } else {
+            auto key = std::make_pair((int)dimx[i], (int)dimy[i]);
+            auto it = engines.find(key);
+            if (it == engines.end()) {
+                rc = ske_create(&sub, dimx[i], dimy[i], e->device, (void*)e->stream);
+                if (rc != SKE_OK) break;
+                engines[key] = sub;
+            } else {
+                sub = it->second;
+            }
+        }
+        rc = ske_run(sub, kernel, inputs[i], inputs_on_device, outputs[i], outputs_on_device, p);
+        if (sub != e) e->launches += 0;
+    }
+    for (auto& kv : engines) {
+        e->launches += kv.second->launches;
+        ske_destroy(kv.second);
+    }
+    return rc;
+}
+
+int ske_prepare(ske_engine e, const float* input, int on_device) {
+    if (!e || !input) return fail(SKE_ERR_INVALID, "null argument");
+    SKE_TRY(set_device(e));
+    return run_prepare(e, input, on_device);
+}
+
+int ske_skew(ske_engine e, int angle) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (!e->prepared) return fail(SKE_ERR_STATE, "skew() before prepare()");
+    if (angle < 0 || angle >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angle);
+    SKE_TRY(set_device(e));
+    Batch b;
+    b.count = 1;
+    b.angle[0] = angle;
+    SKE_TRY(run_skew(e, b));
+    SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride, e->stream));  // resetSkew
+    e->cur_angle = angle;
+    e->kernel_ran = false;
+    return SKE_OK;
+}
+
+int ske_kernel(ske_engine e, int kernel, float povh) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
+    if (e->cur_angle < 0) return fail(SKE_ERR_STATE, "kernel() before skew()");
+    SKE_TRY(set_device(e));
+    Batch b;
+    b.count = 1;
+    b.angle[0] = e->cur_angle;
+    SKE_TRY(run_operator(e, kernel, b, povh, 0));
+    e->kernel_ran = true;
+    return SKE_OK;
+}
+
+int ske_sector(ske_engine e, ske_sector_view* v) {
+    if (!e || !v) return fail(SKE_ERR_INVALID, "null argument");
+    if (e->cur_angle < 0) return fail(SKE_ERR_STATE, "no current sector: call skew() first");
+    const SectorDesc& d = e->geo.desc[e->cur_angle];
+    memset(v, 0, sizeof(*v));
+    v->geom.angle = d.angle;
+    v->geom.sector_type = d.type;
+    v->geom.new_angle = d.new_angle;
+    v->geom.dim_i = d.dim_i;
+    v->geom.dim_o = d.dim_o;
+    v->geom.offset = d.offset;
+    v->geom.skew_height = d.H;
+    v->geom.dim_l = d.diml;
+    v->geom.scale = d.scale;
+    v->geom.skewness = d.skewness;
+    v->skew_out = e->d_SO;
+    v->skew_in = e->d_SI;
+    v->first = e->d_first + d.row_off;
+    v->last = e->d_last + d.row_off;
+    v->target = e->d_target + d.col_off;
+    v->weight = e->d_weight + d.col_off;
+    v->stream = (void*)e->stream;
+    return SKE_OK;
+}
+
+int ske_kernel_custom(ske_engine e, ske_operator_fn fn, void* user, float povh) {
+    if (!e || !fn) return fail(SKE_ERR_INVALID, "null argument");
+    ske_sector_view v;
+    SKE_TRY(ske_sector(e, &v));
+    v.povh = povh;
+    SKE_TRY(set_device(e));
+    const int rc = fn(user, &v);
+    if (rc != 0) return fail(SKE_ERR_DEVICE, "custom operator returned %d", rc);
+    SKE_CK(cudaGetLastError());
+    e->kernel_ran = true;
+    return SKE_OK;
+}
+
+int ske_deskew(ske_engine e, int is_max, int accum) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (!e->kernel_ran) return fail(SKE_ERR_STATE, "deskew() before kernel()");
+    if (accum != SKE_ACCUM_REFERENCE && accum != SKE_ACCUM_KAHAN)
+        return fail(SKE_ERR_INVALID, "unknown accumulation mode %d", accum);
+    SKE_TRY(set_device(e));
+    Batch b;
+    b.count = 1;
+    b.angle[0] = e->cur_angle;
+    e->accum_mode = accum;
+    return run_deskew(e, b, is_max, accum);
+}
+
+int ske_reduce(ske_engine e, float* output, int on_device, int is_max) {
+    if (!e || !output) return fail(SKE_ERR_INVALID, "null argument");
+    if (!e->prepared) return fail(SKE_ERR_STATE, "reduce() before prepare()");
+    SKE_TRY(set_device(e));
+    return run_reduce(e, output, on_device, is_max, e->accum_mode);
+}
+
+int ske_copy_skewed(ske_engine e, float* skew_in, float* skew_out, int on_device) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (e->cur_angle < 0) return fail(SKE_ERR_STATE, "no current sector: call skew() first");
+    SKE_TRY(set_device(e));
+    if (on_device) {
+        if (skew_in) SKE_CK(cudaMemcpyAsync(skew_in, e->d_SI, sizeof(float) * e->len, cudaMemcpyDeviceToDevice, e->stream));
+        if (skew_out)
+            SKE_CK(cudaMemcpyAsync(skew_out, e->d_SO, sizeof(float) * e->len, cudaMemcpyDeviceToDevice, e->stream));
+        SKE_CK(cudaStreamSynchronize(e->stream));
+        return SKE_OK;
+    }
+    if (skew_in) SKE_TRY(download(e, skew_in, e->d_SI, e->len));
+    if (skew_out) SKE_TRY(download(e, skew_out, e->d_SO, e->len));
+    return SKE_OK;
+}
+
+int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_device) {
+    if (!e || !counts) return fail(SKE_ERR_INVALID, "null argument");
+    if (!e->prepared) return fail(SKE_ERR_STATE, "sdem_counts() before prepare()");
+    if (angle < 0 || angle >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angle);
+    SKE_TRY(set_device(e));
+    Batch b;
+    b.count = 1;
+    b.angle[0] = angle;
+    SKE_TRY(run_skew(e, b));
+    SKE_TRY(run_operator(e, SKE_KERNEL_SDEM, b, povh, 1));
+    e->cur_angle = angle;
+    e->kernel_ran = true;
+    if (on_device) {
+        SKE_CK(cudaMemcpyAsync(counts, e->d_SO, sizeof(float) * e->len, cudaMemcpyDeviceToDevice, e->stream));
+        SKE_CK(cudaStreamSynchronize(e->stream));
+    } else {
+        SKE_TRY(download(e, counts, e->d_SO, e->len));
+    }
+    return check_status(e);
+}
+
+int ske_profile_enable(ske_engine e, int enable) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    SKE_TRY(set_device(e));
+    SKE_TRY(flush_profile(e));
+    e->prof = enable != 0;
+    e->prof_tot.clear();
+    return SKE_OK;
+}
+
+int ske_profile_get(ske_engine e, const char* name, double* ms, int64_t* launches) {
+    if (!e || !name) return fail(SKE_ERR_INVALID, "null argument");
+    SKE_TRY(set_device(e));
+    SKE_TRY(flush_profile(e));
+    auto it = e->prof_tot.find(name);
+    if (ms) *ms = it == e->prof_tot.end() ? 0.0 : it->second.ms;
+    if (launches) *launches = it == e->prof_tot.end() ? 0 : it->second.launches;
+    return SKE_OK;
+}
+
+int ske_selftest_division(int device, int dmax, int64_t* checked, int64_t* mismatches, uint32_t* first_bad_bits) {
+    if (!checked || !mismatches || !first_bad_bits) return fail(SKE_ERR_INVALID, "null argument");
+    if (dmax < 1 || dmax > 4095) return fail(SKE_ERR_INVALID, "dmax %d outside [1,4095]", dmax);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return fail(SKE_ERR_NO_DEVICE, "device %d not available", device);
+    }
+    SKE_CK(cudaSetDevice(device));
+    SKE_TRY(ensure_device_tables(device));
+    int sms = 0;
+    SKE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    unsigned long long c = 0, b = 0;
+    unsigned fb = 0;
+    SKE_CK(sdem_division_selftest(dmax, sms, &c, &b, &fb));
+    *checked = (int64_t)c;
+    *mismatches = (int64_t)b;
+    *first_bad_bits = fb;
+    return SKE_OK;
+}
+
+int ske_measure_fp32_peak(int device, double* scalar_ops, double* packed_ops) {
+    if (!scalar_ops || !packed_ops) return fail(SKE_ERR_INVALID, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return fail(SKE_ERR_NO_DEVICE, "device %d not available", device);
+    }
+    SKE_CK(cudaSetDevice(device));
+    int sms = 0;
+    SKE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    SKE_CK(measure_fp32_peak(sms, 5, scalar_ops, packed_ops));
+    return SKE_OK;
+}
+
+int ske_launch_count(ske_engine e, int64_t* launches) {
+    if (!e || !launches) return fail(SKE_ERR_INVALID, "null argument");
+    *launches = e->launches;
+    return SKE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// Cepstrum motion-blur estimation (kernelBLUR, src/kernelBLUR.h:267-302 ->
+// lineCepstrum :153-228 -> select_subarray :69-85, getBlurParameter2 :88-110).
+//
+// For every valid skewed cell j of row r: a 64-cell window of the row centred at
+// j (cells outside [first, last) are zero; the effective window is 64 because
+// kernelRADN.h:19 wins the shared KERNELCOMMONS guard), X = FFT(window)/8,
+// c = FFT(log|X_k|^2, k < 32)/sqrt(32), s_k = -min(0, Re c_k) for k < 16, and
+// the output is (float)(10000 * peak(s)).
+//
+// One warp per cell: the window lives in shared memory as complex doubles and
+// each lane performs one butterfly per stage of the reference radix-2
+// decimation-in-frequency FFT (helper.h:59-106) with the reference's twiddle
+// sequence, in binary64 without fused operations.  The logarithm is CUDA's
+// double-precision log().
+#include "kernels.h"
+
+namespace ske {
+
+namespace {
+
+constexpr int kWin = kBlurWindow;  // 64
+constexpr int kWarpsPerBlock = 8;
+
+// DIF FFT of x[0..n) (n <= 64) by one warp, in place, then bit reversal.
+__device__ __forceinline__ void warp_fft(cd* x, int n, const double* __restrict__ tw, int lane) {
+    for (int h = n >> 1; h >= 1; h >>= 1) {
+        const double* t = tw + 2 * (n - 2 * h);
+        for (int k = lane; k < (n >> 1); k += 32) {
+            const int l = k & (h - 1);
+            const int a = (k / h) * 2 * h + l;
+            const int bb = a + h;
+            const cd xa = x[a], xb = x[bb];
+            x[a] = cadd(xa, xb);
+            x[bb] = cmul(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+        }
+        __syncwarp();
+    }
+    const unsigned bits = 31 - __clz(n);
+    for (int i = lane; i < n; i += 32) {
+        const int j = (int)bitrev((unsigned)i, bits);
+        if (j > i) {
+            const cd tmp = x[i];
+            x[i] = x[j];
+            x[j] = tmp;
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    k_cepstrum(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO, int64_t stride,
+               int64_t len, const double* __restrict__ tw64, const double* __restrict__ tw32) {
+    __shared__ cd xs[kWarpsPerBlock][kWin];
+    __shared__ double twa[2 * (kWin - 1)], twb[2 * (kWin / 2 - 1)];
+    for (int i = threadIdx.x; i < 2 * (kWin - 1); i += blockDim.x) twa[i] = tw64[i];
+    for (int i = threadIdx.x; i < 2 * (kWin / 2 - 1); i += blockDim.x) twb[i] = tw32[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    cd* x = xs[warp];
+    const int slot = blockIdx.y;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const int32_t* first = g.first + d.row_off;
+    const int32_t* last = g.last + d.row_off;
+    const float* in = SI + slot * stride;
+    float* out = SO + slot * stride;
+    const double norm64 = __ddiv_rn(1.0, __dsqrt_rn(64.0));
+    const double norm32 = __ddiv_rn(1.0, __dsqrt_rn(32.0));
+    const int64_t warps = (int64_t)gridDim.x * kWarpsPerBlock;
+    for (int64_t p = (int64_t)blockIdx.x * kWarpsPerBlock + warp; p < len; p += warps) {
+        const int r = owner_row(d, first, last, p);  // warp-uniform
+        if (r < 0) {
+            if (lane == 0) out[p] = 0.0f;
+            continue;
+        }
+        const int64_t base = (int64_t)r * d.dim_i;
+        const int j = (int)(p - base);
+        const int f = first[r], l = last[r];
+        for (int m = lane; m < kWin; m += 32) {
+            const int idx = j - kWin / 2 + m;
+            x[m] = (idx < f || idx >= l) ? cd{0.0, 0.0} : cd{(double)in[base + idx], 0.0};
+        }
+        __syncwarp();
+        warp_fft(x, kWin, twa, lane);
+        // |X_k|^2 of the 1/sqrt(64)-scaled spectrum, k < 32, then its log.
+        {
+            const cd v = x[lane];
+            const double re = __dmul_rn(v.re, norm64), im = __dmul_rn(v.im, norm64);
+            const double ps = __dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im));
+            __syncwarp();
+            x[lane] = {log(ps), 0.0};
+        }
+        __syncwarp();
+        warp_fft(x, kWin / 2, twb, lane);
+        if (lane == 0) {
+            double s[kWin / 4];
+#pragma unroll
+            for (int k = 0; k < kWin / 4; k++) {
+                const double c = __dmul_rn(x[k].re, norm32);
+                s[k] = -((c < 0.0) ? c : 0.0);  // -std::min(0.0, c)
+            }
+            // getBlurParameter2: skip the non-ascending head from index 5, then the
+            // largest sample after the first ascent (that sample itself skipped).
+            int i = 5;
+            while (i < kWin / 4 && !(s[i] > s[i - 1])) i++;
+            double best = 0.0;
+            if (i < kWin / 4) {
+                best = s[i - 1];
+                for (int k = i + 1; k < kWin / 4; k++)
+                    if (s[k] > best) best = s[k];
+            }
+            out[p] = __double2float_rn(__dmul_rn(best, 10000.0));
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_cepstrum(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
+                            int64_t len, const double* tw64, const double* tw32, cudaStream_t st) {
+    int64_t blocks = (len + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (blocks > 8192) blocks = 8192;
+    k_cepstrum<<<dim3((unsigned)blocks, b.count), kWarpsPerBlock * 32, 0, st>>>(g, b, SI, SO, stride, len, tw64,
+                                                                                 tw32);
+    return cudaGetLastError();
+}
+
+}  // namespace ske

@@ -1,0 +1,218 @@
+// Data-layout kernels of the sector loop: the four input orientations, the skew
+// gather, the identity operator, deskew/accumulate and the final fold.
+//
+// All are HBM/L2-bound integer-indexed copies with one or two fp32 multiply-adds
+// per cell; the arithmetic that must match the reference uses explicit _rn
+// intrinsics (no contraction).
+#include <vector>
+
+#include "kernels.h"
+
+namespace ske {
+
+namespace {
+
+constexpr int kTile = 32;
+
+// prepare (skewEngine.cuh:925-951): o0 = input, o1 = transpose + flip both,
+// o2 = transpose + flip y, o3 = flip x.  32x32 tiles staged through shared
+// memory so the transposed stores stay coalesced.
+__global__ void k_prepare(const float* __restrict__ in, float* __restrict__ orient, int dimx, int dimy) {
+    __shared__ float tile[kTile][kTile + 1];
+    const int64_t n = (int64_t)dimx * dimy;
+    float* o0 = orient;
+    float* o1 = orient + n;
+    float* o2 = orient + 2 * n;
+    float* o3 = orient + 3 * n;
+    const int j0 = blockIdx.x * kTile, i0 = blockIdx.y * kTile;
+    for (int ty = threadIdx.y; ty < kTile; ty += blockDim.y) {
+        const int i = i0 + ty, j = j0 + threadIdx.x;
+        if (i < dimy && j < dimx) {
+            const float v = in[(int64_t)i * dimx + j];
+            tile[ty][threadIdx.x] = v;
+            o0[(int64_t)i * dimx + j] = v;
+            o3[(int64_t)i * dimx + (dimx - 1 - j)] = v;
+        }
+    }
+    __syncthreads();
+    // Transposed writes: thread x walks input rows (output columns).
+    for (int ty = threadIdx.y; ty < kTile; ty += blockDim.y) {
+        const int j = j0 + ty, i = i0 + threadIdx.x;
+        if (i < dimy && j < dimx) {
+            const float v = tile[threadIdx.x][ty];
+            const int ci = dimy - 1 - i, cj = dimx - 1 - j;
+            o1[(int64_t)dimy * cj + ci] = v;
+            o2[(int64_t)dimy * j + ci] = v;
+        }
+    }
+}
+
+__global__ void k_skew(DevGeometry g, Batch b, const float* __restrict__ orient, int64_t n_cells,
+                       float* __restrict__ SI, int64_t stride, int64_t len) {
+    const int slot = blockIdx.y;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const float* src = orient + (int64_t)d.type * n_cells;
+    const int32_t* tgt = g.target + d.col_off;
+    const float* wgt = g.weight + d.col_off;
+    float* out = SI + slot * stride;
+    for (int64_t p = gtid(); p < len; p += gstride()) out[p] = skew_gather_flat(d, tgt, wgt, src, p);
+}
+
+__global__ void k_identity(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO,
+                           int64_t stride, int64_t len) {
+    const int slot = blockIdx.y;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const int32_t* first = g.first + d.row_off;
+    const int32_t* last = g.last + d.row_off;
+    const float* in = SI + slot * stride;
+    float* out = SO + slot * stride;
+    for (int64_t p = gtid(); p < len; p += gstride())
+        out[p] = owner_row(d, first, last, p) >= 0 ? in[p] : 0.0f;
+}
+
+// One thread per accumulator cell of one orientation (blockIdx.y = type).
+__global__ void k_deskew_add(DevGeometry g, TypeLists tl, const float* __restrict__ SO, int64_t stride,
+                             float* __restrict__ acc, float* __restrict__ comp, int dimx, int dimy,
+                             int kahan) {
+    const int t = blockIdx.y;
+    const int cnt = tl.count[t];
+    if (cnt == 0) return;
+    const int64_t n = (int64_t)dimx * dimy;
+    const int dim_i = (t == 1 || t == 2) ? dimy : dimx;
+    float* A = acc + t * n;
+    float* C = comp ? comp + t * n : nullptr;
+    for (int64_t idx = gtid(); idx < n; idx += gstride()) {
+        const int i = (int)(idx / dim_i);
+        const int j = (int)(idx - (int64_t)i * dim_i);
+        float s = A[idx];
+        float c = C ? C[idx] : 0.0f;
+        for (int k = 0; k < cnt; k++) {
+            const SectorDesc& d = g.desc[tl.angle[t][k]];
+            const int tj = g.target[d.col_off + j];
+            const float w = g.weight[d.col_off + j];
+            const float* so = SO + tl.slot[t][k] * stride;
+            const float lo = so[(int64_t)(i + tj) * dim_i + j];
+            const float hi = so[(int64_t)(i + tj + 1) * dim_i + j];
+            const float v = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), lo), __fmul_rn(w, hi));
+            if (kahan) {
+                const float y = __fsub_rn(v, c);
+                const float tsum = __fadd_rn(s, y);
+                c = __fsub_rn(__fsub_rn(tsum, s), y);
+                s = tsum;
+            } else {
+                s = __fadd_rn(s, v);
+            }
+        }
+        A[idx] = s;
+        if (C) C[idx] = c;
+    }
+}
+
+__global__ void k_deskew_max(DevGeometry g, TypeLists tl, const float* __restrict__ SO, int64_t stride,
+                             float* __restrict__ acc, int dimx, int dimy) {
+    const int t = blockIdx.y;
+    const int cnt = tl.count[t];
+    if (cnt == 0) return;
+    const int64_t n = (int64_t)dimx * dimy;
+    const int dim_i = (t == 1 || t == 2) ? dimy : dimx;
+    float* A = acc + t * n;
+    for (int64_t idx = gtid(); idx < n; idx += gstride()) {
+        const int i = (int)(idx / dim_i);
+        const int j = (int)(idx - (int64_t)i * dim_i);
+        float s = A[idx];
+        for (int k = 0; k < cnt; k++) {
+            const SectorDesc& d = g.desc[tl.angle[t][k]];
+            const int tj = g.target[d.col_off + j];
+            const float* so = SO + tl.slot[t][k] * stride;
+            const float lo = so[(int64_t)(i + tj) * dim_i + j];
+            const float hi = so[(int64_t)(i + tj + 1) * dim_i + j];
+            const float m = (lo < hi) ? hi : lo;  // std::max(lo, hi)
+            s = (s < m) ? m : s;                  // std::max(s, m)
+            // a + 1000*(int)(s/1000): low decimal digits carry the current angle.
+            const int q = __float2int_rz(__fdiv_rn(s, 1000.0f));
+            s = __int2float_rn(d.angle + 1000 * q);
+        }
+        A[idx] = s;
+    }
+}
+
+__global__ void k_reduce(const float* __restrict__ acc, const float* __restrict__ comp, unsigned used,
+                         float* __restrict__ out, int dimx, int dimy, int is_max, int kahan) {
+    const int64_t n = (int64_t)dimx * dimy;
+    for (int64_t idx = gtid(); idx < n; idx += gstride()) {
+        const int i = (int)(idx / dimx);
+        const int j = (int)(idx - (int64_t)i * dimx);
+        const int ci = dimy - 1 - i, cj = dimx - 1 - j;
+        const int64_t at[4] = {idx, (int64_t)cj * dimy + ci, (int64_t)j * dimy + ci, (int64_t)i * dimx + cj};
+        if (kahan && !is_max) {
+            double s = 0.0;
+            for (int t = 0; t < 4; t++)
+                if (used & (1u << t)) s += (double)acc[t * n + at[t]] - (double)comp[t * n + at[t]];
+            out[idx] = (float)s;
+            continue;
+        }
+        float o = 0.0f;
+        for (int t = 0; t < 4; t++) {
+            if (!(used & (1u << t))) continue;
+            const float v = acc[t * n + at[t]];
+            if (is_max) o = o > v ? o : v;
+            else o = __fadd_rn(o, v);
+        }
+        out[idx] = o;
+    }
+}
+
+inline int blocks_for(int64_t work, int threads, int cap = 65535) {
+    int64_t b = (work + threads - 1) / threads;
+    if (b < 1) b = 1;
+    return (int)(b > cap ? cap : b);
+}
+
+}  // namespace
+
+cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, cudaStream_t st) {
+    dim3 grid((dimx + kTile - 1) / kTile, (dimy + kTile - 1) / kTile);
+    k_prepare<<<grid, dim3(kTile, 8), 0, st>>>(in, orient, dimx, dimy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells, float* SI,
+                        int64_t stride, int64_t len, cudaStream_t st) {
+    dim3 grid(blocks_for(len, 256, 4096), b.count);
+    k_skew<<<grid, 256, 0, st>>>(g, b, orient, n_cells, SI, stride, len);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
+                            int64_t len, cudaStream_t st) {
+    dim3 grid(blocks_for(len, 256, 4096), b.count);
+    k_identity<<<grid, 256, 0, st>>>(g, b, SI, SO, stride, len);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
+                              float* acc, float* comp, int dimx, int dimy, int accum_mode, cudaStream_t st) {
+    const int64_t n = (int64_t)dimx * dimy;
+    dim3 grid(blocks_for(n, 256, 8192), 4);
+    k_deskew_add<<<grid, 256, 0, st>>>(g, tl, SO, stride, acc, accum_mode == kAccumKahan ? comp : nullptr,
+                                       dimx, dimy, accum_mode == kAccumKahan);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
+                              float* acc, int dimx, int dimy, cudaStream_t st) {
+    const int64_t n = (int64_t)dimx * dimy;
+    dim3 grid(blocks_for(n, 256, 8192), 4);
+    k_deskew_max<<<grid, 256, 0, st>>>(g, tl, SO, stride, acc, dimx, dimy);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_reduce(const float* acc, const float* comp, unsigned used, float* out, int dimx, int dimy,
+                          int is_max, int accum_mode, cudaStream_t st) {
+    const int64_t n = (int64_t)dimx * dimy;
+    k_reduce<<<blocks_for(n, 256, 8192), 256, 0, st>>>(acc, comp, used, out, dimx, dimy, is_max,
+                                                        accum_mode == kAccumKahan);
+    return cudaGetLastError();
+}
+
+}  // namespace ske

@@ -1,0 +1,94 @@
+// Host-side launchers of the engine's CUDA kernels.  Each returns the launch's
+// cudaError_t (cudaGetLastError after the launch).
+#pragma once
+
+#include <cstdint>
+
+#include "ske_device.cuh"
+
+namespace ske {
+
+// Per-type ordered lists of batch slots, for the deskew kernels: slots of type t
+// in the order their sectors must be accumulated.
+struct TypeLists {
+    int count[4];
+    int slot[4][kMaxBatch];
+    int angle[4][kMaxBatch];
+};
+
+// Kahan mode keeps a compensation buffer beside every accumulator.
+enum AccumMode { kAccumReference = 0, kAccumKahan = 1 };
+
+// --- layout (k_layout.cu) -------------------------------------------------
+// The four orientations of a dimy x dimx input (skewEngine.cuh:925-951):
+// orient[t*N ...], t = 0..3.
+cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, cudaStream_t st);
+
+// Skewed input of every sector of the batch into slot s of SI (stride floats per
+// slot, `len` = 2N + dim_l cells each, zero past H*dim_i).
+cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells,
+                        float* SI, int64_t stride, int64_t len, cudaStream_t st);
+
+// Identity operator (kernelUNIT.h:16-23): SO = SI on covered cells, 0 elsewhere.
+cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
+                            int64_t stride, int64_t len, cudaStream_t st);
+
+// Deskew + accumulate (skewEngine.cuh:772-792) of every slot of the batch into
+// the per-type accumulators acc[t*N ...] (and comp[] in Kahan mode).
+cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO,
+                              int64_t stride, float* acc, float* comp, int dimx, int dimy,
+                              int accum_mode, cudaStream_t st);
+// Max mode with angle encoding (skewEngine.cuh:774-785).
+cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const float* SO,
+                              int64_t stride, float* acc, int dimx, int dimy, cudaStream_t st);
+
+// Fold the four accumulators back (skewEngine.cuh:862-914) into out (N floats);
+// `used` bit t set when type t received at least one sector.
+cudaError_t launch_reduce(const float* acc, const float* comp, unsigned used, float* out, int dimx,
+                          int dimy, int is_max, int accum_mode, cudaStream_t st);
+
+// --- operators ------------------------------------------------------------
+// Total viewshed sweep (k_sdem.cu).  items: sorted work list (see sdem_items).
+struct SdemLaunch {
+    DevGeometry g;
+    Batch b;
+    const float* SI;
+    float* SO;
+    int64_t stride;
+    const uint64_t* items;
+    int64_t n_items;
+    unsigned* counter;  // work-queue head, zeroed by the launcher
+    float povh;
+    int max_row;        // longest valid row length of the batch
+    int counts_only;    // 1: write integer cv instead of cv*r2
+    int* status;        // device error word (0 = ok)
+};
+cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st);
+// Work items of a batch, longest first: (slot, row, chunk of 128 observers).
+void sdem_items(const struct Geometry& geo, const Batch& b, std::vector<uint64_t>& items,
+                int* max_row);
+int sdem_chunk();
+
+// Radon / filtered back-projection (k_radon.cu).  P: per-slot complex scratch
+// of pstride complex doubles; re: per-slot max_H doubles.
+cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
+                         int64_t stride, int64_t len, double* P, int64_t pstride, const double* twiddles,
+                         const int64_t* tw_off, int max_H2, cudaStream_t st);
+
+// Cepstrum blur estimation (k_cepstrum.cu).
+cudaError_t launch_cepstrum(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
+                            int64_t stride, int64_t len, const double* tw64, const double* tw32,
+                            cudaStream_t st);
+
+// Constant tables used by the SDEM sweep, uploaded once per device.
+cudaError_t sdem_init_tables();
+
+// Exhaustive comparison of the sweep's division with IEEE division over every
+// float numerator in the sweep's fast-path range and every d in [1, dmax]
+// (synchronous, on the current device).
+cudaError_t measure_fp32_peak(int num_sms, int reps, double* scalar_ops, double* packed_ops);
+
+cudaError_t sdem_division_selftest(int dmax, int num_sms, unsigned long long* checked,
+                                   unsigned long long* bad, unsigned* first_bad);
+
+}  // namespace ske

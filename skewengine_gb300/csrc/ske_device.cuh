@@ -1,0 +1,137 @@
+// Device helpers shared by the engine's CUDA kernels.
+//
+// Bit-exactness: the reference's arithmetic is plain IEEE binary32/binary64 with
+// round-to-nearest and no fused multiply-add (its x86-64 host build).  Every
+// value the kernels must reproduce is therefore computed with the explicit
+// _rn intrinsics below, which the compiler neither contracts nor reorders.
+#pragma once
+
+#include <cstdint>
+
+#include "ske_internal.h"
+
+namespace ske {
+
+// Device pointers to one grid's geometry tables (built by build_geometry).
+struct DevGeometry {
+    const SectorDesc* desc;
+    const int32_t* target;
+    const float* weight;
+    const int32_t* first;
+    const int32_t* last;
+};
+
+// A batch of sectors processed by one launch: entries index DevGeometry::desc
+// and the batch's per-sector buffers (slot s owns [s*stride, (s+1)*stride)).
+constexpr int kMaxBatch = 180;
+struct Batch {
+    int count;
+    int angle[kMaxBatch];
+};
+
+// Skewed input value of cell (r, c), r < H: the two source contributions of the
+// reference scatter (skewEngine.cuh:615-620).  Source row r-t-1 contributes
+// w*x (the reference adds it first: lower loop index), row r-t contributes
+// (1-w)*x, onto a cell that starts at 0.
+__device__ __forceinline__ float skew_gather(const SectorDesc& d, const int32_t* __restrict__ tgt,
+                                             const float* __restrict__ wgt, const float* __restrict__ src,
+                                             int r, int c) {
+    const int t = tgt[c];
+    const float w = wgt[c];
+    float acc = 0.0f;
+    const int i0 = r - t - 1;
+    if (i0 >= 0 && i0 < d.dim_o) acc = __fadd_rn(acc, __fmul_rn(w, src[(int64_t)i0 * d.dim_i + c]));
+    const int i1 = r - t;
+    if (i1 >= 0 && i1 < d.dim_o)
+        acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(1.0f, w), src[(int64_t)i1 * d.dim_i + c]));
+    return acc;
+}
+
+// Skewed input at flat index p of the (2N + dim_l)-float skewed buffer: cells
+// past H*dim_i are zero.
+__device__ __forceinline__ float skew_gather_flat(const SectorDesc& d, const int32_t* __restrict__ tgt,
+                                                  const float* __restrict__ wgt, const float* __restrict__ src,
+                                                  int64_t p) {
+    if (p >= (int64_t)d.H * d.dim_i) return 0.0f;
+    const int r = (int)(p / d.dim_i);
+    const int c = (int)(p - (int64_t)r * d.dim_i);
+    return skew_gather(d, tgt, wgt, src, r, c);
+}
+
+// The last (largest) skewed row whose valid range [r*dim_i+first, r*dim_i+last)
+// covers flat index p, or -1.  Rows can overrun their own width when dim_l >
+// dim_i (non-square grids, transposed sectors: skewEngine.cuh:581 initialises
+// last[] with dim_l); the reference then writes such cells from several rows in
+// row order, so the last covering row's value is the one that stays.
+__device__ __forceinline__ int owner_row(const SectorDesc& d, const int32_t* __restrict__ first,
+                                         const int32_t* __restrict__ last, int64_t p) {
+    int r = (int)(p / d.dim_i);
+    if (r > d.H - 1) r = d.H - 1;
+    for (; r >= 0; r--) {
+        const int64_t base = (int64_t)r * d.dim_i;
+        if (base + d.diml <= p) break;  // no earlier row can reach p either
+        if (p >= base + first[r] && p < base + last[r]) return r;
+    }
+    return -1;
+}
+
+// Grid-stride helpers.
+__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
+
+// Complex double, multiplied the way GCC's std::complex<double> does at -O3
+// without -ffast-math: (ac - bd, ad + bc), and when both parts come out NaN the
+// infinity recovery of ISO C99 Annex G.5.1 (_Cmultd), which libgcc's __muldc3
+// implements.
+struct cd {
+    double re, im;
+};
+
+__device__ __forceinline__ cd cadd(cd a, cd b) { return {__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im)}; }
+__device__ __forceinline__ cd csub(cd a, cd b) { return {__dsub_rn(a.re, b.re), __dsub_rn(a.im, b.im)}; }
+
+static __device__ __noinline__ cd cmul_recover(double a, double b, double c, double d) {
+    const double ac = __dmul_rn(a, c), bd = __dmul_rn(b, d), ad = __dmul_rn(a, d), bc = __dmul_rn(b, c);
+    bool recalc = false;
+    if (isinf(a) || isinf(b)) {
+        a = copysign(isinf(a) ? 1.0 : 0.0, a);
+        b = copysign(isinf(b) ? 1.0 : 0.0, b);
+        if (isnan(c)) c = copysign(0.0, c);
+        if (isnan(d)) d = copysign(0.0, d);
+        recalc = true;
+    }
+    if (isinf(c) || isinf(d)) {
+        c = copysign(isinf(c) ? 1.0 : 0.0, c);
+        d = copysign(isinf(d) ? 1.0 : 0.0, d);
+        if (isnan(a)) a = copysign(0.0, a);
+        if (isnan(b)) b = copysign(0.0, b);
+        recalc = true;
+    }
+    if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
+        if (isnan(a)) a = copysign(0.0, a);
+        if (isnan(b)) b = copysign(0.0, b);
+        if (isnan(c)) c = copysign(0.0, c);
+        if (isnan(d)) d = copysign(0.0, d);
+        recalc = true;
+    }
+    if (recalc) {
+        const double inf = __longlong_as_double(0x7ff0000000000000LL);
+        return {__dmul_rn(inf, __dsub_rn(__dmul_rn(a, c), __dmul_rn(b, d))),
+                __dmul_rn(inf, __dadd_rn(__dmul_rn(a, d), __dmul_rn(b, c)))};
+    }
+    return {__dsub_rn(ac, bd), __dadd_rn(ad, bc)};
+}
+
+__device__ __forceinline__ cd cmul(cd x, cd y) {
+    const double re = __dsub_rn(__dmul_rn(x.re, y.re), __dmul_rn(x.im, y.im));
+    const double im = __dadd_rn(__dmul_rn(x.re, y.im), __dmul_rn(x.im, y.re));
+    if (isnan(re) && isnan(im)) return cmul_recover(x.re, x.im, y.re, y.im);
+    return {re, im};
+}
+
+// 32-bit bit reversal of the low `bits` bits.
+__device__ __forceinline__ unsigned bitrev(unsigned v, unsigned bits) {
+    return bits ? (__brev(v) >> (32 - bits)) : 0u;
+}
+
+}  // namespace ske

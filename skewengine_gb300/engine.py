@@ -1,0 +1,271 @@
+"""Python host interface of the engine, mirroring the reference's skewEngine API.
+
+The reference drives its engine from ``execute()`` (src/main.cu:71-172)::
+
+    skewer->skew(i); skewer->kernel(); skewer->deskew(isMax);   // every sector
+    skewer->reduce(outD, isMax);                                // once
+
+``SkewEngine`` exposes the same per-sector methods (``skew``, ``kernel``,
+``deskew``, ``reduce``) plus ``run``, which executes the whole sector loop on the
+GPU in batched launches.  Arrays may be NumPy arrays (host) or CUDA tensors
+(device, anything exposing ``data_ptr()`` and ``is_cuda``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Params, SectorGeometry, SectorView, check, load
+
+# Operators: the reference KERNELS enum (src/global.h:77).
+KERNEL_SDEM = 0
+KERNEL_IDENTITYDEM = 1
+KERNEL_RADON = 2
+KERNEL_IDENTITYIMG = 3
+KERNEL_CEPSTRUM = 4
+KERNELS = {"sdem": KERNEL_SDEM, "identitydem": KERNEL_IDENTITYDEM, "radon": KERNEL_RADON,
+           "identityimg": KERNEL_IDENTITYIMG, "cepstrum": KERNEL_CEPSTRUM}
+
+ACCUM_REFERENCE = 0
+ACCUM_KAHAN = 1
+_ACCUM = {"reference": ACCUM_REFERENCE, "kahan": ACCUM_KAHAN}
+
+DEFAULT_POVH = float(np.float32(1.5 / 10.0))  # obsheight / step, kernelSDEM.h:159
+
+
+def _kernel_id(k) -> int:
+    return KERNELS[k] if isinstance(k, str) else int(k)
+
+
+def _accum_id(a) -> int:
+    return _ACCUM[a] if isinstance(a, str) else int(a)
+
+
+def _is_device(x) -> bool:
+    return bool(getattr(x, "is_cuda", False))
+
+
+def _ptr(x, shape=None, writable=False):
+    """(pointer, on_device) of a float32 C-contiguous array or CUDA tensor."""
+    if _is_device(x):
+        if str(x.dtype) != "torch.float32" or not x.is_contiguous():
+            raise TypeError("device arrays must be contiguous float32 tensors")
+        if shape is not None and tuple(x.shape) != tuple(shape):
+            raise ValueError(f"expected shape {shape}, got {tuple(x.shape)}")
+        return C.c_void_p(x.data_ptr()), 1
+    if not isinstance(x, np.ndarray) or x.dtype != np.float32 or not x.flags.c_contiguous:
+        raise TypeError("host arrays must be C-contiguous float32 numpy arrays")
+    if writable and not x.flags.writeable:
+        raise ValueError("output array is read-only")
+    if shape is not None and x.shape != tuple(shape):
+        raise ValueError(f"expected shape {shape}, got {x.shape}")
+    return C.c_void_p(x.ctypes.data), 0
+
+
+def params(max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference") -> Params:
+    p = Params()
+    check(load().ske_params_default(C.byref(p)))
+    p.max_sector = max_sector
+    p.povh = povh
+    p.accum = _accum_id(accum)
+    return p
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    check(load().ske_device_count(C.byref(n)))
+    return n.value
+
+
+def geometry(dimx: int, dimy: int, angle: int) -> dict:
+    """Host geometry of one sector: computeParams + skewShape (skewEngine.cuh:504-596)."""
+    lib = load()
+    g = SectorGeometry()
+    check(lib.ske_geometry(dimx, dimy, angle, C.byref(g), None, None, None, None))
+    first = np.zeros(g.skew_height, np.int32)
+    last = np.zeros(g.skew_height, np.int32)
+    target = np.zeros(g.dim_i, np.int32)
+    weight = np.zeros(g.dim_i, np.float32)
+    check(lib.ske_geometry(dimx, dimy, angle, C.byref(g), first.ctypes.data, last.ctypes.data,
+                           target.ctypes.data, weight.ctypes.data))
+    out = {f: getattr(g, f) for f, _ in SectorGeometry._fields_}
+    out.update(first=first, last=last, target=target, weight=weight)
+    return out
+
+
+class SkewEngine:
+    """One engine per grid size, bound to one device and one CUDA stream
+    (``skewEngine<float>`` of skewEngine.cuh:147, one per OpenMP thread)."""
+
+    def __init__(self, dimx: int, dimy: int, device: int = 0, stream: int | None = None):
+        self._lib = load()
+        self.dimx, self.dimy = int(dimx), int(dimy)
+        self.N = self.dimx * self.dimy
+        self.dim_l = max(self.dimx, self.dimy)
+        self.skew_len = 2 * self.N + self.dim_l
+        h = C.c_void_p()
+        check(self._lib.ske_create(C.byref(h), self.dimx, self.dimy, int(device),
+                                   C.c_void_p(stream) if stream else None))
+        self._h = h
+        self._keep = []
+
+    # lifetime -------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            check(self._lib.ske_destroy(self._h))
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        check(self._lib.ske_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    # whole run ------------------------------------------------------------
+    def run(self, kernel, data, out=None, max_sector: int = 180, povh: float = DEFAULT_POVH,
+            accum="reference", angles=None):
+        """Full sector loop (allocate + execute + reduce of the reference)."""
+        shape = (self.dimy, self.dimx)
+        pin, in_dev = _ptr(data, shape)
+        if out is None:
+            if in_dev:
+                import torch
+                out = torch.empty(shape, dtype=torch.float32, device=data.device)
+            else:
+                out = np.empty(shape, np.float32)
+        pout, out_dev = _ptr(out, shape, writable=True)
+        prm = params(max_sector, povh, accum)
+        if angles is None:
+            check(self._lib.ske_run(self._h, _kernel_id(kernel), pin, in_dev, pout, out_dev, C.byref(prm)))
+        else:
+            a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
+            check(self._lib.ske_run_angles(self._h, _kernel_id(kernel), pin, in_dev, pout, out_dev,
+                                           a.ctypes.data, len(a), C.byref(prm)))
+        return out
+
+    def accumulate(self, kernel, data, angles, povh: float = DEFAULT_POVH, accum="reference"):
+        """Run the listed sectors and return (4 x N per-type accumulators, used-type mask)."""
+        pin, in_dev = _ptr(data, (self.dimy, self.dimx))
+        a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
+        acc = np.empty((4, self.N), np.float32)
+        used = C.c_uint32(0)
+        prm = params(180, povh, accum)
+        check(self._lib.ske_accumulate(self._h, _kernel_id(kernel), pin, in_dev, a.ctypes.data if len(a) else None,
+                                       len(a), C.byref(prm), acc.ctypes.data, 0, C.byref(used)))
+        return acc, used.value
+
+    # per-sector API (main.cu:147-164) -------------------------------------
+    def prepare(self, data) -> None:
+        p, dev = _ptr(data, (self.dimy, self.dimx))
+        check(self._lib.ske_prepare(self._h, p, dev))
+
+    def skew(self, angle: int) -> None:
+        check(self._lib.ske_skew(self._h, int(angle)))
+
+    def kernel(self, kernel, povh: float = DEFAULT_POVH) -> None:
+        check(self._lib.ske_kernel(self._h, _kernel_id(kernel), povh))
+
+    def kernel_custom(self, fn, povh: float = DEFAULT_POVH) -> None:
+        """Run ``fn(view: SectorView) -> int`` as the operator of the current sector."""
+        cb = _lib.OPERATOR_FN(lambda user, view: int(fn(view.contents)))
+        self._keep.append(cb)
+        check(self._lib.ske_kernel_custom(self._h, cb, None, povh))
+
+    def deskew(self, is_max: int = 0, accum="reference") -> None:
+        check(self._lib.ske_deskew(self._h, int(is_max), _accum_id(accum)))
+
+    def reduce(self, is_max: int = 0, out=None):
+        shape = (self.dimy, self.dimx)
+        if out is None:
+            out = np.empty(shape, np.float32)
+        p, dev = _ptr(out, shape, writable=True)
+        check(self._lib.ske_reduce(self._h, p, dev, int(is_max)))
+        return out
+
+    def sector(self) -> SectorView:
+        v = SectorView()
+        check(self._lib.ske_sector(self._h, C.byref(v)))
+        return v
+
+    def skewed(self):
+        """(skewed input, skewed output) of the current sector, 2N + dim_l floats each."""
+        si = np.empty(self.skew_len, np.float32)
+        so = np.empty(self.skew_len, np.float32)
+        check(self._lib.ske_copy_skewed(self._h, si.ctypes.data, so.ctypes.data, 0))
+        return si, so
+
+    def sdem_counts(self, angle: int, povh: float = DEFAULT_POVH):
+        """Integer visibility counts cv of every skewed cell of one sector."""
+        out = np.empty(self.skew_len, np.float32)
+        check(self._lib.ske_sdem_counts(self._h, int(angle), povh, out.ctypes.data, 0))
+        return out
+
+    # profiling ------------------------------------------------------------
+    def profile(self, enable: bool = True) -> None:
+        check(self._lib.ske_profile_enable(self._h, int(enable)))
+
+    def profile_get(self, name: str):
+        ms = C.c_double()
+        n = C.c_int64()
+        check(self._lib.ske_profile_get(self._h, name.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        check(self._lib.ske_launch_count(self._h, C.byref(n)))
+        return n.value
+
+
+def execute(kernel, data, max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference",
+            device: int = 0):
+    """One-shot run of the reference's ``execute(skewAlgorithm)`` on a 2-D array."""
+    dimy, dimx = data.shape
+    with SkewEngine(dimx, dimy, device) as eng:
+        return eng.run(kernel, data, max_sector=max_sector, povh=povh, accum=accum)
+
+
+def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference",
+              device: int = 0, outs=None):
+    """Run one operator over many grids of uneven size (``ske_run_batch``)."""
+    grids = list(grids)
+    if not grids:
+        return []
+    dims = [(g.shape[1], g.shape[0]) for g in grids]
+    big = max(dims, key=lambda d: d[0] * d[1])
+    on_dev = _is_device(grids[0])
+    if outs is None:
+        if on_dev:
+            import torch
+            outs = [torch.empty_like(g) for g in grids]
+        else:
+            outs = [np.empty_like(g) for g in grids]
+    ins = (C.c_void_p * len(grids))(*[_ptr(g)[0].value for g in grids])
+    ous = (C.c_void_p * len(grids))(*[_ptr(o, writable=True)[0].value for o in outs])
+    dx = np.array([d[0] for d in dims], np.int32)
+    dy = np.array([d[1] for d in dims], np.int32)
+    prm = params(max_sector, povh, accum)
+    with SkewEngine(big[0], big[1], device) as eng:
+        check(eng._lib.ske_run_batch(eng._h, _kernel_id(kernel), len(grids), dx.ctypes.data, dy.ctypes.data,
+                                     ins, int(on_dev), ous, int(on_dev), C.byref(prm)))
+    return outs
+
+
+def cli_run(argv: list[str]) -> int:
+    """Call the reference-compatible ``run(argc, argv)`` entry point."""
+    args = ["run"] + [str(a) for a in argv]
+    arr = (C.c_char_p * len(args))(*[a.encode() for a in args])
+    return load().run(len(args), arr)

@@ -1,0 +1,81 @@
+"""Sector sharding across ranks (one process per GPU).
+
+The reference spreads sectors over OpenMP threads, one thread per GPU in GPU
+mode (src/main.cu:86-168, src/main.h:102); each thread keeps four per-type
+accumulators and folds them into the shared output inside a critical section
+(``reduce``, skewEngine.cuh:862-914).  Here each rank takes a contiguous block of
+angles, computes its four accumulators on its GPU, and rank 0 gathers them and
+folds them in rank order: the same arithmetic as the reference run with one
+thread per rank and a static schedule.  The only exchange is that one gather of
+4*N floats per rank.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def shard_angles(n_angles: int, world: int, rank: int, costs=None) -> list[int]:
+    """Contiguous block of angles for `rank`.
+
+    With ``costs`` (one per angle) blocks are cut so their summed costs are as
+    even as possible; otherwise blocks have equal length.
+    """
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad world/rank")
+    if costs is None:
+        lo = (n_angles * rank) // world
+        hi = (n_angles * (rank + 1)) // world
+        return list(range(lo, hi))
+    c = np.cumsum(np.asarray(costs, np.float64))
+    total = c[-1] if len(c) else 0.0
+    cuts = [0]
+    for r in range(1, world):
+        cuts.append(int(np.searchsorted(c, total * r / world, side="left")) + 1)
+    cuts.append(n_angles)
+    cuts = np.maximum.accumulate(np.clip(cuts, 0, n_angles))
+    return list(range(int(cuts[rank]), int(cuts[rank + 1])))
+
+
+def _orient_index(dimx: int, dimy: int):
+    """Index of output cell (i, j) inside each orientation's accumulator."""
+    i, j = np.meshgrid(np.arange(dimy), np.arange(dimx), indexing="ij")
+    ci, cj = dimy - 1 - i, dimx - 1 - j
+    return [(i * dimx + j).ravel(), (cj * dimy + ci).ravel(), (j * dimy + ci).ravel(), (i * dimx + cj).ravel()]
+
+
+def fold_accumulators(accs, used_masks, dimx: int, dimy: int, is_max: bool = False) -> np.ndarray:
+    """Fold per-rank accumulators (each 4 x N float32) into the output, rank by
+    rank and type by type, exactly as successive reference ``reduce`` calls
+    (skewEngine.cuh:885-912) on a zeroed output."""
+    idx = _orient_index(dimx, dimy)
+    out = np.zeros(dimx * dimy, np.float32)
+    for acc, used in zip(accs, used_masks):
+        acc = np.asarray(acc, np.float32).reshape(4, dimx * dimy)
+        for t in range(4):
+            if not used & (1 << t):
+                continue
+            v = acc[t][idx[t]]
+            out = np.where(out > v, out, v) if is_max else (out + v).astype(np.float32)
+    return out.reshape(dimy, dimx)
+
+
+def run_sharded(engine, kernel, data, group=None, max_sector: int = 180, povh=None, accum="reference"):
+    """Run one operator with sectors sharded over a torch.distributed group.
+
+    Every rank passes the same input; rank 0 returns the folded result, other
+    ranks return None.
+    """
+    import torch.distributed as dist
+    from .engine import DEFAULT_POVH, KERNEL_CEPSTRUM
+
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    angles = shard_angles(max_sector, world, rank)
+    acc, used = engine.accumulate(kernel, data, angles, povh=DEFAULT_POVH if povh is None else povh, accum=accum)
+    payload = {"acc": np.asarray(acc, np.float32), "used": int(used)}
+    gathered = [None] * world if rank == 0 else None
+    dist.gather_object(payload, gathered, dst=0, group=group)
+    if rank != 0:
+        return None
+    return fold_accumulators([g["acc"] for g in gathered], [g["used"] for g in gathered], engine.dimx,
+                             engine.dimy, is_max=int(kernel) == KERNEL_CEPSTRUM)

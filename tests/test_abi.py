@@ -1,0 +1,126 @@
+"""The C ABI surface, host-only entry points and error behaviour (no GPU needed)."""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN, ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from skewengine_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def declared_functions() -> list[str]:
+    text = open(os.path.join(ROOT, "include", "skewengine.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    # Function declarations: `<type> name(` at line start (typedefs excluded).
+    return re.findall(r"^(?:const\s+char\s*\*|int|void)\s+(\w+)\s*\(", text, flags=re.M)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert "ske_run" in names and "run" in names and len(names) >= 25
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_python_signatures_cover_header(lib):
+    from skewengine_gb300._lib import SIGNATURES
+    bound = {s[0] for s in SIGNATURES}
+    assert set(declared_functions()) <= bound
+
+
+def test_version_and_defaults(lib):
+    from skewengine_gb300 import params
+    assert lib.ske_abi_version() == 1
+    p = params()
+    assert p.max_sector == 180 and p.accum == 0 and p.flags == 0
+    assert np.float32(p.povh) == np.float32(1.5 / 10.0)
+
+
+def _geom_digest(g) -> str:
+    h = hashlib.sha256()
+    ii = np.array([g["sector_type"], g["new_angle"], g["dim_i"], g["dim_o"], g["offset"], g["skew_height"],
+                   g["dim_l"]], np.int32)
+    dd = np.array([g["scale"], g["skewness"]], np.float64)
+    for arr in (ii, dd, g["first"].astype(np.uint16), g["last"].astype(np.uint16), g["target"], g["weight"]):
+        h.update(np.ascontiguousarray(arr).tobytes())
+    return h.hexdigest()
+
+
+def test_geometry_matches_reference_small(golden_geometry):
+    from skewengine_gb300 import geometry
+    shapes = sorted({k.split("__")[0] for k in golden_geometry.files})
+    for shp in shapes:
+        dx, dy = map(int, shp.split("x"))
+        ii, dd = golden_geometry[shp + "__iinfo"], golden_geometry[shp + "__dinfo"]
+        off = {"first": 0, "last": 0, "target": 0, "weight": 0}
+        for a in range(180):
+            g = geometry(dx, dy, a)
+            got = [g["sector_type"], g["new_angle"], g["dim_i"], g["dim_o"], g["offset"], g["skew_height"],
+                   g["dim_l"]]
+            assert got == list(ii[a]), (shp, a)
+            assert g["scale"] == dd[a, 0] and g["skewness"] == dd[a, 1], (shp, a)
+            for name in ("first", "last", "target", "weight"):
+                n = len(g[name])
+                ref = golden_geometry[f"{shp}__{name}"][off[name]:off[name] + n]
+                assert np.array_equal(g[name].astype(ref.dtype), ref), (shp, a, name)
+                off[name] += n
+
+
+def test_geometry_matches_reference_benchmark_grids():
+    """SHA-256 of every angle's tables for the benchmark grid sizes (2000^2 ...)."""
+    from skewengine_gb300 import geometry
+    digests = json.load(open(os.path.join(GOLDEN, "geometry_digest.json")))
+    for shp, want in digests.items():
+        dx, dy = map(int, shp.split("x"))
+        for a in range(180):
+            assert _geom_digest(geometry(dx, dy, a)) == want[a], (shp, a)
+
+
+def test_geometry_rejects_bad_arguments():
+    from skewengine_gb300 import SkeError, geometry
+    for args in ((0, 5, 0), (5, 5, 180), (5, 5, -1), (70000, 5, 0)):
+        with pytest.raises(SkeError) as ei:
+            geometry(*args)
+        assert ei.value.status == 1
+
+
+def test_no_gpu_fails_loudly(lib):
+    """Without a GPU the engine refuses to run; there is no CPU fallback."""
+    from skewengine_gb300 import SkeError, SkewEngine, device_count
+    if device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(SkeError) as ei:
+        SkewEngine(16, 16)
+    assert ei.value.status == 3
+    assert "device" in str(ei.value).lower()
+    n = C.c_int64()
+    assert lib.ske_selftest_division(0, 16, C.byref(n), C.byref(C.c_int64()), C.byref(C.c_uint32())) == 3
+
+
+def test_null_engine_is_rejected(lib):
+    from skewengine_gb300 import params
+    p = params()
+    x = np.zeros(4, np.float32)
+    assert lib.ske_run(None, 0, x.ctypes.data, 0, x.ctypes.data, 0, C.byref(p)) == 1
+    assert b"null" in lib.ske_last_error()
+    assert lib.ske_skew(None, 0) == 1
+    assert lib.ske_destroy(None) == 0
+
+
+def test_cli_usage_errors():
+    from skewengine_gb300 import cli_run
+    assert cli_run([]) == 1
+    assert cli_run(["nosuchkernel", "x", "1", "1", "y"]) == 1
+    assert cli_run(["sdem", "/nonexistent/file.raw", "4", "4", "/tmp/out.raw"]) == 1

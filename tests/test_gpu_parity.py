@@ -1,0 +1,239 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the
+reference's golden outputs and the CPU oracle.
+
+Bar: bit-exact (float32 bit patterns) for total viewshed, identity and Radon in
+reference accumulation order, and for the integer visibility counts; cepstrum is
+compared in its output bins (the GPU log may differ from the host libm's in the
+last place) and must also match bit for bit on the golden cases.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from skewengine_gb300 import synthetic
+from tests.conftest import bits_equal, run_cases
+
+pytestmark = pytest.mark.gpu
+
+POVH = np.float32(0.15)
+
+
+@pytest.fixture(scope="module")
+def ske(gpu_lib):
+    import skewengine_gb300 as ske
+    return ske
+
+
+def _run(ske, op, x, **kw):
+    dy, dx = x.shape
+    with ske.SkewEngine(dx, dy) as eng:
+        out = eng.run(op, np.ascontiguousarray(x, np.float32), povh=POVH, **kw)
+        assert eng.launch_count() > 0
+        return out
+
+
+def test_golden_runs_bit_exact(ske, golden_runs):
+    for key, op, x, want in run_cases(golden_runs):
+        got = _run(ske, op, x)
+        assert bits_equal(got, want), (key, float(np.abs(got - want).max()))
+
+
+def test_golden_sectors_per_sector_api(ske, golden_sectors):
+    """skew / kernel / deskew of single sectors reproduce the reference's
+    intermediate buffers."""
+    from tests.golden.make_golden import OPS
+    cases = {}
+    for k in golden_sectors.files:
+        if k.endswith("__iinfo"):
+            name, kind, shape, seed, a = k[: -len("__iinfo")].split("__")
+            cases.setdefault((name, kind, shape, seed), []).append(int(a[1:]))
+    for (name, kind, shape, seed), angles in sorted(cases.items()):
+        base = "__".join([name, kind, shape, seed])
+        x = golden_sectors[base + "__in"]
+        dy, dx = x.shape
+        with ske.SkewEngine(dx, dy) as eng:
+            for a in sorted(angles):
+                eng.prepare(x)
+                eng.skew(a)
+                eng.kernel(OPS[name], POVH)
+                si, so = eng.skewed()
+                assert bits_equal(si, golden_sectors[f"{base}__a{a}__skew_in"]), (base, a, "skew_in")
+                assert bits_equal(so, golden_sectors[f"{base}__a{a}__skew_out"]), (base, a, "skew_out")
+                eng.deskew(1 if OPS[name] == 4 else 0)
+                acc = eng.reduce(1 if OPS[name] == 4 else 0)
+                assert bits_equal(acc.ravel(), golden_sectors[f"{base}__a{a}__acc"]), (base, a, "acc")
+
+
+@pytest.mark.parametrize("side,side_y,seed", [(96, 96, 1), (128, 80, 2), (80, 128, 3), (200, 200, 4),
+                                              (257, 257, 5)])
+def test_sdem_matches_oracle(ske, oracle, side, side_y, seed):
+    x = synthetic.fractal_dem(side, seed, side_y=side_y)
+    want = oracle.run(0, x, povh=POVH)
+    got = _run(ske, 0, x)
+    assert bits_equal(got, want)
+
+
+def test_sdem_counts_bit_exact(ske, oracle):
+    x = synthetic.fractal_dem(150, 9, side_y=130)
+    with ske.SkewEngine(150, 130) as eng:
+        eng.prepare(x)
+        for a in (0, 1, 30, 44, 45, 46, 60, 89, 90, 91, 120, 134, 135, 150, 179):
+            got = eng.sdem_counts(a, POVH)
+            want = oracle.counts(x, a, povh=POVH)
+            assert bits_equal(got, want), a
+
+
+def test_sector_loop_equals_run(ske):
+    """The per-sector drop-in API driven like main.cu:147-164 equals ske_run."""
+    x = synthetic.fractal_dem(64, 21)
+    with ske.SkewEngine(64, 64) as eng:
+        whole = eng.run(0, x, povh=POVH)
+        eng.prepare(x)
+        for a in range(180):
+            eng.skew(a)
+            eng.kernel(0, POVH)
+            eng.deskew(0)
+        loop = eng.reduce(0)
+    assert bits_equal(whole, loop)
+
+
+@pytest.mark.parametrize("op", [1, 2, 3])
+def test_identity_radon_match_oracle(ske, oracle, op):
+    for side, side_y, seed in ((100, 100, 3), (96, 70, 4)):
+        x = synthetic.ellipse_phantom(side, seed, side_y=side_y) if op == 2 else \
+            synthetic.fractal_dem(side, seed, side_y=side_y)
+        assert bits_equal(_run(ske, op, x), oracle.run(op, x, povh=POVH)), (op, side, side_y)
+
+
+def test_radon_512_matches_oracle(ske, oracle):
+    x = synthetic.ellipse_phantom(512, 7)
+    assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
+
+
+def test_cepstrum_bins_match_oracle(ske, oracle):
+    x, _, _ = synthetic.blurred_texture(72, 11)
+    got = _run(ske, 4, x)
+    want = oracle.run(4, x, povh=POVH)
+    mismatch = np.mean(got != want)
+    assert np.all(got == np.round(got)) and np.all(want == np.round(want))
+    assert mismatch == 0.0, f"bin mismatch rate {mismatch}"
+
+
+def test_subset_of_angles(ske, oracle):
+    x = synthetic.fractal_dem(90, 31)
+    angles = [5, 44, 45, 46, 90, 91, 135, 170]
+    with ske.SkewEngine(90, 90) as eng:
+        got = eng.run(0, x, povh=POVH, angles=angles)
+    assert bits_equal(got, oracle.run_angles(0, x, angles, povh=POVH))
+
+
+def test_kahan_accumulation_close(ske, oracle):
+    x = synthetic.fractal_dem(160, 12)
+    got = _run(ske, 0, x, accum="kahan")
+    want = oracle.run(0, x, povh=POVH).astype(np.float64)
+    rel = np.abs(got - want) / np.maximum(np.abs(want), 1.0)
+    assert rel.max() <= 1e-5
+    assert abs(got.astype(np.float64).sum() - want.sum()) / want.sum() <= 1e-6
+
+
+def test_device_pointers(ske, oracle):
+    torch = pytest.importorskip("torch")
+    x = synthetic.fractal_dem(64, 41)
+    xd = torch.from_numpy(x).cuda()
+    with ske.SkewEngine(64, 64) as eng:
+        out = eng.run(0, xd, povh=POVH)
+    assert out.is_cuda
+    assert bits_equal(out.cpu().numpy(), oracle.run(0, x, povh=POVH))
+
+
+@pytest.mark.parametrize("dims", [(1, 1), (2, 1), (1, 7), (7, 1), (3, 2), (5, 17), (17, 5)])
+def test_tiny_and_degenerate_grids(ske, oracle, dims):
+    dx, dy = dims
+    x = (np.random.default_rng(dx * 31 + dy).random((dy, dx)) * 100).astype(np.float32)
+    for op in (0, 1, 2):
+        assert bits_equal(_run(ske, op, x), oracle.run(op, x, povh=POVH)), (dims, op)
+
+
+def test_special_values_take_exact_path(ske, oracle):
+    """Rows with zeros, huge or non-finite heights use IEEE division and the
+    reference's accumulation order; results still match the oracle."""
+    x = synthetic.fractal_dem(48, 51)
+    x[3, :] = 0.0
+    x[10, 10] = 3e30
+    x[20, 5] = -1e-30
+    x[30, 30] = np.inf
+    x[40, 7] = np.nan
+    got = _run(ske, 0, x)
+    want = oracle.run(0, x, povh=POVH)
+    same = (got.view(np.uint32) == want.view(np.uint32)) | (np.isnan(got) & np.isnan(want))
+    assert same.all()
+
+
+def test_constant_and_zero_dem(ske, oracle):
+    for v in (0.0, 7.5):
+        x = np.full((33, 33), v, np.float32)
+        assert bits_equal(_run(ske, 0, x), oracle.run(0, x, povh=POVH)), v
+
+
+def test_custom_operator_receives_sector(ske):
+    """A custom device operator gets the current sector's geometry and buffers;
+    a failing operator is reported as an error."""
+    seen = {}
+
+    def op(view):
+        seen["h"] = view.geom.skew_height
+        seen["ptrs"] = (view.skew_in, view.skew_out, view.first)
+        return 0
+
+    x = synthetic.fractal_dem(32, 1)
+    with ske.SkewEngine(32, 32) as eng:
+        eng.prepare(x)
+        eng.skew(30)
+        eng.kernel_custom(op)
+        assert seen["h"] == ske.geometry(32, 32, 30)["skew_height"]
+        assert all(seen["ptrs"])
+        with pytest.raises(ske.SkeError):
+            eng.kernel_custom(lambda v: 7)
+
+
+def test_state_errors(ske):
+    with ske.SkewEngine(16, 16) as eng:
+        with pytest.raises(ske.SkeError):
+            eng.skew(3)  # before prepare
+        eng.prepare(np.zeros((16, 16), np.float32))
+        with pytest.raises(ske.SkeError):
+            eng.kernel(0)  # before skew
+        with pytest.raises(ske.SkeError):
+            eng.run(9, np.zeros((16, 16), np.float32))
+
+
+def test_division_exhaustive(gpu_lib):
+    """The sweep's multiply-and-correct division equals IEEE division for every
+    float numerator of the fast-path range and every d in [1, 4095]."""
+    checked, bad, first = C.c_int64(), C.c_int64(), C.c_uint32()
+    assert gpu_lib.ske_selftest_division(0, 4095, C.byref(checked), C.byref(bad), C.byref(first)) == 0
+    assert checked.value > 1.3e13
+    assert bad.value == 0, f"first mismatching numerator bits {first.value:#010x}"
+
+
+def test_accumulate_and_fold(ske, oracle):
+    from skewengine_gb300.parallel import fold_accumulators
+    x = synthetic.fractal_dem(60, 61)
+    with ske.SkewEngine(60, 60) as eng:
+        a0, u0 = eng.accumulate(0, x, list(range(0, 90)), povh=POVH)
+        a1, u1 = eng.accumulate(0, x, list(range(90, 180)), povh=POVH)
+    o0, v0 = oracle.accumulate(0, x, list(range(0, 90)), povh=POVH)
+    assert bits_equal(a0, o0) and u0 == v0
+    got = fold_accumulators([a0, a1], [u0, u1], 60, 60)
+    np.testing.assert_allclose(got, oracle.run(0, x, povh=POVH), rtol=1e-5)
+
+
+def test_run_batch_uneven(ske, oracle):
+    grids = [synthetic.fractal_dem(s, 70 + i, roughness=h) for i, (s, h) in
+             enumerate([(64, 0.6), (80, 0.9), (40, 0.7), (64, 0.8)])]
+    outs = ske.run_batch(0, grids, povh=POVH)
+    for g, o in zip(grids, outs):
+        assert bits_equal(o, oracle.run(0, g, povh=POVH))

@@ -1,0 +1,109 @@
+"""The CPU oracle (oracle/skewport.cpp) against the reference's own outputs.
+
+The golden fixtures were produced by the reference's CPU code compiled from its
+sources (tests/golden/make_golden.py).  Every comparison here is bit for bit.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from tests.conftest import bits_equal, run_cases
+from tests.golden.make_golden import OPS
+
+POVH = np.float32(0.15)
+
+
+def test_golden_runs(oracle, golden_runs):
+    cases = run_cases(golden_runs)
+    assert len(cases) >= 15
+    for key, op, x, want in cases:
+        got = oracle.run(op, x, povh=POVH)
+        assert bits_equal(got, want), key
+
+
+def _sector_cases(golden_sectors):
+    out = []
+    for k in golden_sectors.files:
+        if k.endswith("__iinfo"):
+            base = k[: -len("__iinfo")]
+            name, kind, shape, seed, a = base.split("__")
+            out.append((base, name, "__".join([name, kind, shape, seed]), int(a[1:])))
+    return sorted(out)
+
+
+def test_golden_sectors(oracle, golden_sectors):
+    cases = _sector_cases(golden_sectors)
+    assert len(cases) >= 20
+    for base, name, inkey, angle in cases:
+        x = golden_sectors[inkey + "__in"]
+        si, so, acc = oracle.sector(OPS[name], x, angle, povh=POVH)
+        assert bits_equal(si, golden_sectors[base + "__skew_in"]), base + " skew_in"
+        assert bits_equal(so, golden_sectors[base + "__skew_out"]), base + " skew_out"
+        assert bits_equal(acc.ravel(), golden_sectors[base + "__acc"]), base + " acc"
+
+
+def test_golden_geometry(port, golden_geometry):
+    shapes = sorted({k.split("__")[0] for k in golden_geometry.files})
+    for shp in shapes:
+        dx, dy = map(int, shp.split("x"))
+        ii, dd = golden_geometry[shp + "__iinfo"], golden_geometry[shp + "__dinfo"]
+        offs = {"first": 0, "last": 0, "target": 0, "weight": 0}
+        dl = max(dx, dy)
+        for a in range(180):
+            gi = np.zeros(7, np.int32)
+            gd = np.zeros(2, np.float64)
+            fi = np.zeros(2 * dl + 1, np.uint16)
+            la = np.zeros(2 * dl + 1, np.uint16)
+            ta = np.zeros(dl, np.int32)
+            we = np.zeros(dl, np.float32)
+            assert port.port_geometry(dx, dy, a, gi, gd, fi, la, ta, we) == 0
+            assert np.array_equal(gi, ii[a]), (shp, a)
+            assert np.array_equal(gd.view(np.uint64), dd[a].view(np.uint64)), (shp, a)
+            h, di = int(ii[a, 5]), int(ii[a, 2])
+            for name, arr, n in (("first", fi, h), ("last", la, h), ("target", ta, di), ("weight", we, di)):
+                ref = golden_geometry[f"{shp}__{name}"][offs[name]:offs[name] + n]
+                assert np.array_equal(np.asarray(arr[:n]).view(np.uint8), np.asarray(ref).view(np.uint8)), \
+                    (shp, a, name)
+                offs[name] += n
+
+
+def test_counts_scale_to_output(oracle, golden_sectors):
+    """cv counts times (float)scale^2 reproduce the reference's skewed output."""
+    import math
+    x = golden_sectors["sdem__fractal__32x32__11__in"]
+    for a in (0, 17, 45, 91, 134, 179):
+        cnt = oracle.counts(x, a, povh=POVH)
+        so = golden_sectors[f"sdem__fractal__32x32__11__a{a}__skew_out"]
+        scale = golden_sectors[f"sdem__fractal__32x32__11__a{a}__dinfo"][0]
+        r2 = np.float32(scale * scale)
+        assert np.all(cnt == np.round(cnt)), a
+        assert bits_equal(cnt * r2, so), a
+        assert math.isfinite(float(cnt.sum()))
+
+
+def test_multithread_matches_reference_semantics(oracle, golden_runs):
+    """More threads only change the accumulation order: same values to float
+    rounding (the reference's own multi-thread runs differ the same way)."""
+    x = golden_runs["sdem__fractal__64x64__12__in"]
+    one = oracle.run(0, x, povh=POVH, threads=1)
+    many = oracle.run(0, x, povh=POVH, threads=4)
+    np.testing.assert_allclose(many, one, rtol=1e-5)
+
+
+def test_accumulate_folds_like_reduce(oracle, golden_runs):
+    """Per-type accumulators folded in type order equal the whole run."""
+    x = golden_runs["sdem__fractal__32x32__11__in"]
+    acc, used = oracle.accumulate(0, x, list(range(180)), povh=POVH)
+    assert used == 15
+    from skewengine_gb300.parallel import fold_accumulators
+    out = fold_accumulators([acc], [used], 32, 32, is_max=False)
+    assert bits_equal(out, golden_runs["sdem__fractal__32x32__11__out"])
+
+
+@pytest.mark.parametrize("dims", [(500, 500), (2000, 2000)])
+def test_los_step_counts(port, dims):
+    """Line-of-sight steps of the benchmark grids (the sweep's work units)."""
+    steps = port.port_los_steps(dims[0], dims[1], 180)
+    expect = {500: 1.918e10, 2000: 1.228e12}[dims[0]]
+    assert abs(steps - expect) / expect < 0.01

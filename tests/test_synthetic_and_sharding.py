@@ -1,0 +1,109 @@
+"""Synthetic inputs and the host side of sector sharding (CPU only).
+
+The multi-rank test runs two gloo ranks; each rank's "GPU" is stood in for by
+the CPU oracle through a fake engine, so only the product's sharding, gather and
+fold logic is under test.
+"""
+from __future__ import annotations
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from skewengine_gb300 import parallel, synthetic
+from tests.conftest import bits_equal
+
+
+def test_fractal_dem_deterministic_and_scaled():
+    a = synthetic.fractal_dem(100, 7)
+    b = synthetic.fractal_dem(100, 7)
+    c = synthetic.fractal_dem(100, 8)
+    assert a.dtype == np.float32 and a.shape == (100, 100)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert a.min() == 0.0 and abs(a.max() - 150.0) < 1e-3  # 1500 m / 10 m cells
+    assert synthetic.fractal_dem(48, 3, side_y=20).shape == (20, 48)
+
+
+def test_phantom_and_texture():
+    p = synthetic.ellipse_phantom(64, 1)
+    assert p.shape == (64, 64) and p.dtype == np.float32 and np.abs(p).max() > 0
+    t, length, ang = synthetic.blurred_texture(64, 2)
+    assert t.shape == (64, 64) and 5 <= length <= 40 and 0 <= ang < 180
+    k = synthetic.motion_kernel(10.0, 30.0)
+    assert abs(k.sum() - 1.0) < 1e-12
+
+
+def test_uneven_batch_spec():
+    spec = synthetic.uneven_dem_batch(64, 100)
+    assert len(spec) == 64
+    assert all(256 <= s <= 2000 and 0.6 <= h <= 0.9 for s, h, _ in spec)
+    assert [s for _, _, s in spec] == list(range(100, 164))
+
+
+def test_shard_angles_partition():
+    for world in (1, 2, 3, 4, 7, 8):
+        got = sum((parallel.shard_angles(180, world, r) for r in range(world)), [])
+        assert got == list(range(180))
+    costs = np.linspace(1, 10, 180)
+    blocks = [parallel.shard_angles(180, 4, r, costs) for r in range(4)]
+    assert sum(blocks, []) == list(range(180))
+    sums = [costs[b].sum() for b in blocks]
+    assert max(sums) / min(sums) < 1.2
+
+
+def test_fold_max_mode():
+    acc = np.zeros((4, 6), np.float32)
+    acc[0] = [1, 5, 3, 0, 0, 0]
+    acc[3] = [2, 2, 2, 2, 2, 2]
+    out = parallel.fold_accumulators([acc], [0b1001], 3, 2, is_max=True)
+    assert out.shape == (2, 3) and out.max() == 5
+
+
+class _OracleEngine:
+    """Stands in for SkewEngine on a CPU-only rank: accumulate() via the oracle."""
+
+    def __init__(self, oracle, dimx, dimy):
+        self.oracle, self.dimx, self.dimy = oracle, dimx, dimy
+
+    def accumulate(self, kernel, data, angles, povh, accum="reference"):
+        return self.oracle.accumulate(kernel, data, angles, povh=povh)
+
+
+def _rank_main(rank, world, port_path, x, port_expect, result_path, master_port):
+    import ctypes as C
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(master_port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    lib = C.CDLL(port_path)
+    from tests.conftest import PortOracle
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+    lib.port_accumulate.argtypes = [C.c_int, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, fp, ip]
+    eng = _OracleEngine(PortOracle(lib), x.shape[1], x.shape[0])
+    out = parallel.run_sharded(eng, 0, x, povh=np.float32(0.15))
+    if rank == 0:
+        np.save(result_path, out)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_sharded_run(oracle, port, tmp_path):
+    import torch.multiprocessing as mp
+    x = synthetic.fractal_dem(40, 5)
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        master_port = s.getsockname()[1]
+    port_path = port._name
+    res = str(tmp_path / "out.npy")
+    mp.start_processes(_rank_main, args=(2, port_path, x, None, res, master_port), nprocs=2, join=True,
+                       start_method="spawn")
+    got = np.load(res)
+    # Same arithmetic as two reference threads with a static schedule:
+    a0, u0 = oracle.accumulate(0, x, list(range(0, 90)), povh=np.float32(0.15))
+    a1, u1 = oracle.accumulate(0, x, list(range(90, 180)), povh=np.float32(0.15))
+    want = parallel.fold_accumulators([a0, a1], [u0, u1], 40, 40)
+    assert bits_equal(got, want)
+    single = oracle.run(0, x, povh=np.float32(0.15))
+    np.testing.assert_allclose(got, single, rtol=1e-5)
