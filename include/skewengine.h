@@ -241,6 +241,11 @@ int ske_selftest_division(int device, int dmax, int64_t* checked, int64_t* misma
  * denominator of the total-viewshed sweep.  No reference counterpart. */
 int ske_measure_fp32_peak(int device, double* scalar_ops, double* packed_ops);
 
+/* Binary64 fused multiply-add throughput of `device` in lane operations per
+ * second: the roofline denominator of the Radon transform and cepstrum, which
+ * compute in double precision like the reference.  No reference counterpart. */
+int ske_measure_fp64_peak(int device, double* dfma_ops);
+
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
  * a raw float32 file or a synthetic input and writes the result.  See
  * INTEGRATION.md for the argument list. */

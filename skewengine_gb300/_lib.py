@@ -75,6 +75,7 @@ SIGNATURES = [
     ("ske_selftest_division", C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                         C.POINTER(C.c_uint32)]),
     ("ske_measure_fp32_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("ske_measure_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     ("run", C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
 ]
 
@@ -82,11 +83,12 @@ _lib = None
 
 
 def load(path: str | None = None) -> C.CDLL:
-    """Load libskewengine.so once; raises if it has not been built."""
+    """Load libskewengine.so once (``path``, else $SKE_LIBRARY, else the in-tree
+    build); raises if it has not been built."""
     global _lib
     if _lib is not None:
         return _lib
-    path = path or LIB_PATH
+    path = path or os.environ.get("SKE_LIBRARY") or LIB_PATH
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build it with `python -m skewengine_gb300.build`")
     lib = C.CDLL(path)

@@ -76,6 +76,8 @@ struct ProfEntry {
 
 }  // namespace
 
+int ske::set_last_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 struct ske_engine_s {
     int dimx = 0, dimy = 0, device = 0, num_sms = 0;
     cudaStream_t stream = nullptr;
@@ -809,6 +811,20 @@ int ske_measure_fp32_peak(int device, double* scalar_ops, double* packed_ops) {
     int sms = 0;
     SKE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     SKE_CK(measure_fp32_peak(sms, 5, scalar_ops, packed_ops));
+    return SKE_OK;
+}
+
+int ske_measure_fp64_peak(int device, double* dfma_ops) {
+    if (!dfma_ops) return fail(SKE_ERR_INVALID, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return fail(SKE_ERR_NO_DEVICE, "device %d not available", device);
+    }
+    SKE_CK(cudaSetDevice(device));
+    int sms = 0;
+    SKE_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    SKE_CK(measure_fp64_peak(sms, 3, dfma_ops));
     return SKE_OK;
 }
 

@@ -70,69 +70,98 @@ __global__ void k_identity(DevGeometry g, Batch b, const float* __restrict__ SI,
         out[p] = owner_row(d, first, last, p) >= 0 ? in[p] : 0.0f;
 }
 
-// One thread per accumulator cell of one orientation (blockIdx.y = type).
-__global__ void k_deskew_add(DevGeometry g, TypeLists tl, const float* __restrict__ SO, int64_t stride,
-                             float* __restrict__ acc, float* __restrict__ comp, int dimx, int dimy,
-                             int kahan) {
-    const int t = blockIdx.y;
+// Deskew + accumulate, tiled.  A CTA owns a kDeskewRows x 32 tile of one
+// orientation's accumulator (blockIdx.z = sector type) and keeps it in registers
+// while it walks that type's sectors of the batch in order.  For each sector
+// the skewed rows the tile needs, [i0 + t(j0), i1 + t(j0+31)], are staged in
+// shared memory with coalesced 128-byte row loads; every thread then combines
+// its two cells (rows i+t_j and i+t_j+1 of its column) exactly as the reference
+// does.  Accumulator traffic: one read and one write per batch instead of per
+// sector.
+constexpr int kDeskewRows = 64;
+constexpr int kDeskewBand = kDeskewRows + 34;  // rows + 1 + max column drift over 32 columns (+1)
+enum { kDeskewAdd = 0, kDeskewKahan = 1, kDeskewMax = 2 };
+
+template <int kMode>
+__global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, const float* __restrict__ SO,
+                                                int64_t stride, float* __restrict__ acc, float* __restrict__ comp,
+                                                int dimx, int dimy) {
+    __shared__ float band[kDeskewBand][kTile];
+    constexpr int kPer = kDeskewRows / 8;
+    const int t = blockIdx.z;
     const int cnt = tl.count[t];
     if (cnt == 0) return;
     const int64_t n = (int64_t)dimx * dimy;
     const int dim_i = (t == 1 || t == 2) ? dimy : dimx;
+    const int dim_o = (t == 1 || t == 2) ? dimx : dimy;
+    const int j0 = blockIdx.x * kTile, i0 = blockIdx.y * kDeskewRows;
+    if (j0 >= dim_i || i0 >= dim_o) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int j = j0 + tx;
+    const bool col_ok = j < dim_i;
+    const int jlast = min(j0 + kTile, dim_i) - 1;
+    const int i_end = min(i0 + kDeskewRows, dim_o);
     float* A = acc + t * n;
-    float* C = comp ? comp + t * n : nullptr;
-    for (int64_t idx = gtid(); idx < n; idx += gstride()) {
-        const int i = (int)(idx / dim_i);
-        const int j = (int)(idx - (int64_t)i * dim_i);
-        float s = A[idx];
-        float c = C ? C[idx] : 0.0f;
-        for (int k = 0; k < cnt; k++) {
-            const SectorDesc& d = g.desc[tl.angle[t][k]];
-            const int tj = g.target[d.col_off + j];
-            const float w = g.weight[d.col_off + j];
-            const float* so = SO + tl.slot[t][k] * stride;
-            const float lo = so[(int64_t)(i + tj) * dim_i + j];
-            const float hi = so[(int64_t)(i + tj + 1) * dim_i + j];
-            const float v = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), lo), __fmul_rn(w, hi));
-            if (kahan) {
-                const float y = __fsub_rn(v, c);
-                const float tsum = __fadd_rn(s, y);
-                c = __fsub_rn(__fsub_rn(tsum, s), y);
-                s = tsum;
+    float s[kPer], c[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int i = i0 + ty + 8 * k;
+        s[k] = (col_ok && i < i_end) ? A[(int64_t)i * dim_i + j] : 0.0f;
+        c[k] = (kMode == kDeskewKahan && col_ok && i < i_end) ? comp[t * n + (int64_t)i * dim_i + j] : 0.0f;
+    }
+    for (int q = 0; q < cnt; q++) {
+        const SectorDesc& d = g.desc[tl.angle[t][q]];
+        const int32_t* tg = g.target + d.col_off;
+        const int tmin = tg[j0], tmax = tg[jlast];
+        const int tj = col_ok ? tg[j] : tmin;
+        const float w = col_ok ? g.weight[d.col_off + j] : 0.0f;
+        // Rows r0 .. r0+nrows-1 hold every (i+t_j, i+t_j+1) of the tile.
+        const int r0 = i0 + tmin;
+        const int nrows = (i_end - i0) + 1 + (tmax - tmin);
+        const float* so = SO + tl.slot[t][q] * stride;
+        // Steep sectors of elongated grids (tan > 1) can drift more than the band
+        // holds; those tiles read the skewed cells directly.
+        const bool staged = nrows <= kDeskewBand;
+        if (staged) {
+            __syncthreads();  // previous sector's band fully consumed
+            for (int rr = ty; rr < nrows; rr += 8)
+                band[rr][tx] = (j0 + tx <= jlast) ? so[(int64_t)(r0 + rr) * dim_i + j0 + tx] : 0.0f;
+            __syncthreads();
+        }
+        if (!col_ok) continue;
+        const int off = tj - tmin;
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+            const int ii = ty + 8 * k;
+            if (i0 + ii >= i_end) continue;
+            const float lo = staged ? band[ii + off][tx] : so[(int64_t)(i0 + ii + tj) * dim_i + j];
+            const float hi = staged ? band[ii + off + 1][tx] : so[(int64_t)(i0 + ii + tj + 1) * dim_i + j];
+            if (kMode == kDeskewMax) {
+                const float m = (lo < hi) ? hi : lo;  // std::max(lo, hi)
+                float v = (s[k] < m) ? m : s[k];      // std::max(acc, m)
+                // a + 1000*(int)(v/1000): the low decimal digits carry the angle.
+                const int qq = __float2int_rz(__fdiv_rn(v, 1000.0f));
+                s[k] = __int2float_rn(d.angle + 1000 * qq);
             } else {
-                s = __fadd_rn(s, v);
+                const float v = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), lo), __fmul_rn(w, hi));
+                if (kMode == kDeskewKahan) {
+                    const float y = __fsub_rn(v, c[k]);
+                    const float tsum = __fadd_rn(s[k], y);
+                    c[k] = __fsub_rn(__fsub_rn(tsum, s[k]), y);
+                    s[k] = tsum;
+                } else {
+                    s[k] = __fadd_rn(s[k], v);
+                }
             }
         }
-        A[idx] = s;
-        if (C) C[idx] = c;
     }
-}
-
-__global__ void k_deskew_max(DevGeometry g, TypeLists tl, const float* __restrict__ SO, int64_t stride,
-                             float* __restrict__ acc, int dimx, int dimy) {
-    const int t = blockIdx.y;
-    const int cnt = tl.count[t];
-    if (cnt == 0) return;
-    const int64_t n = (int64_t)dimx * dimy;
-    const int dim_i = (t == 1 || t == 2) ? dimy : dimx;
-    float* A = acc + t * n;
-    for (int64_t idx = gtid(); idx < n; idx += gstride()) {
-        const int i = (int)(idx / dim_i);
-        const int j = (int)(idx - (int64_t)i * dim_i);
-        float s = A[idx];
-        for (int k = 0; k < cnt; k++) {
-            const SectorDesc& d = g.desc[tl.angle[t][k]];
-            const int tj = g.target[d.col_off + j];
-            const float* so = SO + tl.slot[t][k] * stride;
-            const float lo = so[(int64_t)(i + tj) * dim_i + j];
-            const float hi = so[(int64_t)(i + tj + 1) * dim_i + j];
-            const float m = (lo < hi) ? hi : lo;  // std::max(lo, hi)
-            s = (s < m) ? m : s;                  // std::max(s, m)
-            // a + 1000*(int)(s/1000): low decimal digits carry the current angle.
-            const int q = __float2int_rz(__fdiv_rn(s, 1000.0f));
-            s = __int2float_rn(d.angle + 1000 * q);
-        }
-        A[idx] = s;
+    if (!col_ok) return;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int i = i0 + ty + 8 * k;
+        if (i >= i_end) continue;
+        A[(int64_t)i * dim_i + j] = s[k];
+        if (kMode == kDeskewKahan) comp[t * n + (int64_t)i * dim_i + j] = c[k];
     }
 }
 
@@ -190,20 +219,26 @@ cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* S
     return cudaGetLastError();
 }
 
+static dim3 deskew_grid(int dimx, int dimy) {
+    const int dl = dimx > dimy ? dimx : dimy;  // covers both orientations
+    return dim3((dl + kTile - 1) / kTile, (dl + kDeskewRows - 1) / kDeskewRows, 4);
+}
+
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
                               float* acc, float* comp, int dimx, int dimy, int accum_mode, cudaStream_t st) {
-    const int64_t n = (int64_t)dimx * dimy;
-    dim3 grid(blocks_for(n, 256, 8192), 4);
-    k_deskew_add<<<grid, 256, 0, st>>>(g, tl, SO, stride, acc, accum_mode == kAccumKahan ? comp : nullptr,
-                                       dimx, dimy, accum_mode == kAccumKahan);
+    if (accum_mode == kAccumKahan)
+        k_deskew<kDeskewKahan><<<deskew_grid(dimx, dimy), dim3(kTile, 8), 0, st>>>(g, tl, SO, stride, acc, comp,
+                                                                                  dimx, dimy);
+    else
+        k_deskew<kDeskewAdd><<<deskew_grid(dimx, dimy), dim3(kTile, 8), 0, st>>>(g, tl, SO, stride, acc, nullptr,
+                                                                                dimx, dimy);
     return cudaGetLastError();
 }
 
 cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
                               float* acc, int dimx, int dimy, cudaStream_t st) {
-    const int64_t n = (int64_t)dimx * dimy;
-    dim3 grid(blocks_for(n, 256, 8192), 4);
-    k_deskew_max<<<grid, 256, 0, st>>>(g, tl, SO, stride, acc, dimx, dimy);
+    k_deskew<kDeskewMax><<<deskew_grid(dimx, dimy), dim3(kTile, 8), 0, st>>>(g, tl, SO, stride, acc, nullptr, dimx,
+                                                                            dimy);
     return cudaGetLastError();
 }
 

@@ -54,7 +54,49 @@ __global__ void k_fma_packed(float* out, float a, float b, int iters) {
     if (s == 1.2345f) out[0] = s;
 }
 
+__global__ void k_dfma(double* out, double a, double b, int iters) {
+    double acc[kChains];
+#pragma unroll
+    for (int c = 0; c < kChains; c++) acc[c] = a + c + threadIdx.x;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < kChains; c++) acc[c] = __fma_rn(acc[c], a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < kChains; c++) s += acc[c];
+    if (s == 1.2345) out[0] = s;
+}
+
 }  // namespace
+
+// Best of `reps` timed launches of the binary64 probe: DFMA lane ops/s.
+cudaError_t measure_fp64_peak(int num_sms, int reps, double* dfma_ops) {
+    double* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(double));
+    if (e != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int threads = 256, blocks = num_sms * 4, iters = 256;
+    double best = 0;
+    for (int r = 0; r < reps + 1 && e == cudaSuccess; r++) {
+        cudaEventRecord(a);
+        k_dfma<<<blocks, threads>>>(d, 0.999, 0.001, iters);
+        cudaEventRecord(b);
+        e = cudaEventSynchronize(b);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        const double lanes = (double)blocks * threads * iters * kChains;
+        if (r > 0 && ms > 0) best = std::max(best, lanes / (ms * 1e-3));
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(d);
+    *dfma_ops = best;
+    return e;
+}
 
 // Best of `reps` timed launches of each probe; returns lane-op/s (scalar, packed).
 cudaError_t measure_fp32_peak(int num_sms, int reps, double* scalar_ops, double* packed_ops) {

@@ -13,26 +13,37 @@
 //  * The row is staged in shared memory once per item; lanes read it through a
 //    register sliding window refilled by one aligned 16-byte load per 4 steps,
 //    so shared-memory traffic is 1 byte per observer-step.
-//  * The step distance d is warp-uniform, so d, RN(1/d), 2d+1 and d+1 come from a
+//  * The step distance d is warp-uniform, so -d, RN(1/d), 2d+1 and d+1 come from a
 //    constant-memory table.
+//  * Instruction mix: the sweep is bound by issue and by the ALU pipe, so per
+//    step it uses 4 FMA-pipe ops for the slope, 1 compare and 1 max on the ALU
+//    pipe, and the two sums as predicated FMA-pipe adds (no selects).
 //  * Division: the quotient (S[k]-h)/d must be the correctly rounded one,
 //    because visibility compares it strictly against the running maximum.
-//    q0 = RN(a*y), r = fma(-q0, d, a), q = fma(r, y, q0) with y = RN(1/d)
+//    q0 = RN(a*y), r = fma(q0, -d, a), q = fma(r, y, q0) with y = RN(1/d)
 //    (Markstein's correction step, P. Markstein, "Computation of elementary
 //    functions on the IBM RISC System/6000 processor", IBM J. R&D 34(1), 1990).
 //    It is applied only to rows whose values lie in a range where it is exact
-//    for every d <= 4095 (checked exhaustively against IEEE division by the GPU
-//    tests); other rows take the IEEE-division path.
-//  * Accumulation: with v_t the visibility of step t (distance d_t = t+1) and the
-//    last visible run starting at distance rs,
-//        cv = 1 + sum_t v_t (2 d_t + 1) - v_end ((n+1)^2 - rs^2),
-//    which equals the reference's sum of closed runs (each closed run
-//    [o, c) contributes c^2 - o^2 = sum of its ring areas; the +1 and the last
-//    term account for the initial run and the run still open at the row end).
-//    Per step this needs one predicated add and one predicated move.  All terms
-//    are integers below 2^24 for rows up to 4096 cells, so the float result is
-//    exact and equal to the reference's.  Longer rows use the reference-order
-//    path.
+//    for every d <= 4095 (checked exhaustively against IEEE division by
+//    ske_selftest_division); other rows take the IEEE-division path.
+//  * Accumulation: a closed visible run [o, c) contributes c^2 - o^2 to the
+//    reference's cv, which is the sum of the ring areas 2d+1 over its steps
+//    d = o .. c-1.  So each visible step adds 2d+1 to a running sum acc, and
+//    every invisible step (the one that closes a run, or any later one) copies
+//    acc into cl, the sum over closed runs.  The initial run starts at distance
+//    0 (ring 1 not swept), hence cl starts at -1 and cv = 1 + cl; a run still
+//    open at the row end never reaches cl, exactly as the reference does not
+//    count it.  All values are integers below 2^24 for rows up to 4096 cells,
+//    so the float result is exact and equal to the reference's.  Longer rows
+//    use the reference-order path.
+//  * Horizon pruning (exact): after step d the remaining targets k are all
+//    invisible when fl((Smax - h)/(d+1)) <= horizon, Smax an upper bound of the
+//    remaining heights (monotonicity of rounding: every remaining slope is at
+//    most that quotient).  An observer that passes this test is finished: every
+//    later step would be invisible, so cv = 1 + sum (its last run closes at the
+//    next step).  Smax comes from per-8-cell block maxima of the row (suffix
+//    maxima forward, prefix maxima backward); the test runs every kCheck steps
+//    and a warp stops when all its observers are finished.
 #include <algorithm>
 #include <vector>
 
@@ -42,18 +53,21 @@ namespace ske {
 
 namespace {
 
-constexpr int kChunk = 128;       // observers per work item (4 per lane)
-constexpr int kWarps = 8;         // warps per CTA
-constexpr int kPadFront = 136;    // zero cells before the row (backward window overrun)
-constexpr int kPadBack = 144;     // zero cells after the row (forward window overrun)
-constexpr int kFastMaxRow = 4096; // exact float accumulation bound (see header)
+constexpr int kChunk = 128;        // observers per work item (4 per lane)
+constexpr int kWarps = 8;          // warps per CTA
+constexpr int kPadFront = 136;     // zero cells before the row (backward window overrun)
+constexpr int kPadBack = 144;      // zero cells after the row (forward window overrun)
+constexpr int kFastMaxRow = 4096;  // exact float accumulation bound (see header)
+constexpr int kBlk = 8;            // cells per block of the pruning maxima
+constexpr int kCheck = 16;         // steps between pruning tests (multiple of 4)
 
-// {d, RN(1/d), 2d+1, d+1} for d = 0..4095 (entry 0 unused).
+// {-d, RN(1/d), 2d+1, d+1} for d = 0..4095 (entry 0 unused).
 __constant__ float4 c_step[kFastMaxRow];
 
-__host__ __device__ inline int row_capacity(int max_row) {
-    return kPadFront + ((max_row + 3) & ~3) + kPadBack;
-}
+__host__ __device__ inline int row_pad(int max_row) { return kPadFront + ((max_row + 3) & ~3) + kPadBack; }
+__host__ __device__ inline int blocks_pad(int max_row) { return ((max_row + kBlk - 1) / kBlk + 3) & ~3; }
+// Shared floats per warp: the padded row plus suffix and prefix block maxima.
+__host__ __device__ inline int warp_floats(int max_row) { return row_pad(max_row) + 2 * blocks_pad(max_row); }
 
 // Values for which the Markstein quotient is exact: zero, or finite with
 // magnitude in [2^-80, 2^90].  If S[k] and h both qualify, a = S[k]-h is zero or
@@ -63,9 +77,9 @@ __device__ __forceinline__ bool div_safe(float v) {
     return v == 0.0f || (m >= 8.271806125530277e-25f && m <= 1.2379400392853803e27f);
 }
 
-__device__ __forceinline__ float div_fast(float a, float d, float y) {
+__device__ __forceinline__ float div_fast(float a, float negd, float y) {
     const float q0 = __fmul_rn(a, y);
-    const float r = __fmaf_rn(-q0, d, a);
+    const float r = __fmaf_rn(q0, negd, a);
     return __fmaf_rn(r, y, q0);
 }
 
@@ -81,114 +95,113 @@ __device__ __forceinline__ Item decode(uint64_t it) {
     return r;
 }
 
-// Forward scan of observers x0..x0+3 over A[0..L) (A 16-byte aligned, x0 % 4 == 0),
-// fast path.  Returns the four partial cv values.
-__device__ __forceinline__ void scan_fwd_fast(const float* __restrict__ A, int x0, int L, float povh,
-                                              float cv[4]) {
-    int n[4];
-    float h[4], mx[4], acc[4], rs[4];
-    bool vis[4];
+// State of the 4 observers of a lane in one scan direction.  acc is the ring
+// sum of all visible steps; cl is acc at the last invisible step, i.e. the ring
+// sum of the closed runs (-1 before any: the initial run starts at distance 0).
+struct Scan4 {
+    float h[4], mx[4], acc[4], cl[4];
+    int n[4];        // steps of each observer (-1: observer outside the row)
+    bool done[4];    // finished by pruning
+};
+
+// One line-of-sight step of one observer: the correctly rounded slope (FMA
+// pipe), the horizon test and update, and the two sums as predicated adds so
+// they also issue to the FMA pipe (selects would go to the ALU pipe, the
+// sweep's bottleneck).
+__device__ __forceinline__ void los_step(float& mx, float& acc, float& cl, float s, float h, float negd, float y,
+                                         float ring) {
+    const float q = div_fast(__fsub_rn(s, h), negd, y);
+    asm("{\n\t.reg .pred p;\n\t"
+        "setp.gt.f32 p, %3, %2;\n\t"
+        "@p add.rn.f32 %0, %0, %4;\n\t"
+        "@!p add.rn.f32 %1, %0, 0f00000000;\n\t}"
+        : "+f"(acc), "+f"(cl)
+        : "f"(mx), "f"(q), "f"(ring));
+    mx = fmaxf(mx, q);  // rows on this path are finite: max == "q > mx ? q : mx"
+}
+
+// One block of 4 steps d = d0 .. d0+3.  The window holds the 8 row values the
+// block needs: forward w = A[x0+d0 .. x0+d0+7], step e of observer q reads
+// w[e+q]; backward w = A[x0-d0-4 .. x0-d0+3], step e reads w[q-e+4].
+template <bool kFwd, bool kTail>
+__device__ __forceinline__ void block4(Scan4& s, const float w[8], int d0) {
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        n[q] = L - 1 - (x0 + q);
-        h[q] = __fadd_rn(A[x0 + q], povh);
-        mx[q] = -2000.0f;
-        acc[q] = 0.0f;
-        rs[q] = 0.0f;
-        vis[q] = true;
-    }
-    const int dmax = __reduce_max_sync(0xffffffffu, max(n[0], 0));
-    const float4* A4 = reinterpret_cast<const float4*>(A) + (x0 >> 2);
-    float4 cur = A4[0];
-    for (int m = 0; 4 * m <= dmax; m++) {
-        const float4 nxt = A4[m + 1];
-        const float w[8] = {cur.x, cur.y, cur.z, cur.w, nxt.x, nxt.y, nxt.z, nxt.w};
+    for (int e = 0; e < 4; e++) {
+        const int d = d0 + e;
+        if (d == 0) continue;  // only in the first block
+        const float4 st = c_step[d];
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int d = 4 * m + e;
-            if (d == 0 || d > dmax) continue;
-            const float4 st = c_step[d];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (d <= n[q]) {
-                    const float sl = div_fast(__fsub_rn(w[e + q], h[q]), st.x, st.y);
-                    const bool above = sl > mx[q];
-                    if (above) {
-                        mx[q] = sl;
-                        acc[q] = __fadd_rn(acc[q], st.z);
-                    } else {
-                        rs[q] = st.w;
-                    }
-                    vis[q] = above;
-                }
-            }
+        for (int q = 0; q < 4; q++) {
+            if (kTail && d > s.n[q]) continue;
+            los_step(s.mx[q], s.acc[q], s.cl[q], kFwd ? w[e + q] : w[q - e + 4], s.h[q], st.x, st.y, st.z);
         }
-        cur = nxt;
-    }
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        if (n[q] < 0) {
-            cv[q] = 0.0f;
-            continue;
-        }
-        const float e = (float)(n[q] + 1);
-        const float tail = vis[q] ? __fsub_rn(__fmul_rn(e, e), __fmul_rn(rs[q], rs[q])) : 0.0f;
-        cv[q] = __fsub_rn(__fadd_rn(1.0f, acc[q]), tail);
     }
 }
 
-// Backward scan of observers x0..x0+3 (targets k = x - d), fast path.
-__device__ __forceinline__ void scan_bwd_fast(const float* __restrict__ A, int x0, int L, float povh,
-                                              float cv[4]) {
-    int n[4];
-    float h[4], mx[4], acc[4], rs[4];
-    bool vis[4];
+// Pruning test after step dc for the 4 observers: smax is an upper bound of
+// every remaining target height of all four.
+__device__ __forceinline__ void prune4(Scan4& s, float smax, int dc) {
+    const float4 st = c_step[dc + 1];
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        n[q] = (x0 + q < L) ? x0 + q : -1;
-        h[q] = __fadd_rn(A[x0 + q], povh);
-        mx[q] = -2000.0f;
-        acc[q] = 0.0f;
-        rs[q] = 0.0f;
-        vis[q] = true;
+        const float a = __fsub_rn(smax, s.h[q]);
+        const float b = div_fast(a, st.x, st.y);
+        s.done[q] = s.done[q] || (dc < s.n[q] && a >= 0.0f && b <= s.mx[q]);
     }
-    const int dmax = __reduce_max_sync(0xffffffffu, max(max(n[3], n[2]), max(n[1], max(n[0], 0))));
+}
+
+// Scan of the lane's observers x0..x0+3 in one direction (fast path).
+// A: the row (16-byte aligned, zero padded), bmax: suffix (forward) or prefix
+// (backward) maxima of kBlk-cell blocks.
+template <bool kFwd>
+__device__ __forceinline__ void scan_fast(const float* __restrict__ A, const float* __restrict__ bmax, int x0, int L,
+                                          float povh, float cv[4]) {
+    Scan4 s;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int x = x0 + q;
+        s.n[q] = x < L ? (kFwd ? L - 1 - x : x) : -1;
+        s.h[q] = __fadd_rn(A[x], povh);
+        s.mx[q] = -2000.0f;
+        s.acc[q] = 0.0f;
+        s.cl[q] = -1.0f;
+        s.done[q] = false;
+    }
+    // Steps every observer of the warp takes (no bounds test) and the most any takes.
+    const int lane_min = kFwd ? s.n[3] : s.n[0];
+    const int lane_max = max(max(s.n[0], s.n[1]), max(max(s.n[2], s.n[3]), 0));
+    const int dmain = __reduce_min_sync(0xffffffffu, lane_min < 0 ? 0 : lane_min);
+    const int dall = __reduce_max_sync(0xffffffffu, lane_max);
     const float4* A4 = reinterpret_cast<const float4*>(A) + (x0 >> 2);
     float4 cur = A4[0];
-    for (int m = 0; 4 * m <= dmax; m++) {
-        const float4 prv = A4[-m - 1];
-        const float w[8] = {prv.x, prv.y, prv.z, prv.w, cur.x, cur.y, cur.z, cur.w};
+    for (int m = 0; 4 * m <= dall; m++) {
+        const float4 nx = kFwd ? A4[m + 1] : A4[-m - 1];
+        const float4 lo = kFwd ? cur : nx, hi = kFwd ? nx : cur;
+        const float w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+        if (4 * m + 3 <= dmain) block4<kFwd, false>(s, w, 4 * m);
+        else block4<kFwd, true>(s, w, 4 * m);
+        cur = nx;
+        const int dc = 4 * m + 3;
+        if ((dc + 1) % kCheck == 0 && dc < dall) {
+            // Remaining targets: forward x+dc+1 .., backward .. x-dc-1 (all four
+            // observers' targets lie on the same side of the bound's block).
+            // Backward: the lane's largest in-row observer bounds its targets.
+            const int k = kFwd ? x0 + dc + 1 : min(x0 + 3, L - 1) - dc - 1;
+            if (kFwd ? k < L : k >= 0) prune4(s, bmax[k / kBlk], dc);
+            bool fin = true;
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int d = 4 * m + e;
-            if (d == 0 || d > dmax) continue;
-            const float4 st = c_step[d];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if (d <= n[q]) {
-                    const float sl = div_fast(__fsub_rn(w[q - e + 4], h[q]), st.x, st.y);
-                    const bool above = sl > mx[q];
-                    if (above) {
-                        mx[q] = sl;
-                        acc[q] = __fadd_rn(acc[q], st.z);
-                    } else {
-                        rs[q] = st.w;
-                    }
-                    vis[q] = above;
-                }
-            }
+            for (int q = 0; q < 4; q++) fin = fin && (s.done[q] || dc >= s.n[q]);
+            if (__all_sync(0xffffffffu, fin)) break;
         }
-        cur = prv;
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        if (n[q] < 0) {
+        if (s.n[q] < 0) {
             cv[q] = 0.0f;
             continue;
         }
-        const float e = (float)(n[q] + 1);
-        const float tail = vis[q] ? __fsub_rn(__fmul_rn(e, e), __fmul_rn(rs[q], rs[q])) : 0.0f;
-        cv[q] = __fsub_rn(__fadd_rn(1.0f, acc[q]), tail);
+        // A pruned observer's open run closes at its next step: every run counts.
+        cv[q] = __fadd_rn(1.0f, s.done[q] ? s.acc[q] : s.cl[q]);
     }
 }
 
@@ -216,12 +229,51 @@ __device__ float scan_reference(const float* __restrict__ A, int x, int L, float
     return cv;
 }
 
+// Block maxima for pruning: suf[b] = max A[kBlk*b ..] (to the row end),
+// pre[b] = max A[.. kBlk*b + kBlk-1] (from the row start).  Rows on the fast
+// path are finite.
+__device__ void block_maxima(const float* __restrict__ A, int L, float* suf, float* pre, int lane) {
+    const float ninf = __int_as_float(0xff800000);
+    const int nb = (L + kBlk - 1) / kBlk;
+    const int per = (nb + 31) / 32;
+    const int b0 = lane * per, b1 = min(b0 + per, nb);
+    float run = ninf;
+    for (int b = b0; b < b1; b++) {  // block maxima, then lane-local prefix
+        float m = ninf;
+        for (int c = b * kBlk; c < min(b * kBlk + kBlk, L); c++) m = fmaxf(m, A[c]);
+        suf[b] = m;
+        run = fmaxf(run, m);
+        pre[b] = run;
+    }
+    // Inclusive prefix / suffix max of the lane totals (Hillis-Steele), then
+    // shift by one lane for the exclusive values.
+    float inc_p = run, inc_s = run;
+    for (int off = 1; off < 32; off <<= 1) {
+        const float up = __shfl_up_sync(0xffffffffu, inc_p, off);
+        const float dn = __shfl_down_sync(0xffffffffu, inc_s, off);
+        if (lane >= off) inc_p = fmaxf(inc_p, up);
+        if (lane + off < 32) inc_s = fmaxf(inc_s, dn);
+    }
+    float before = __shfl_up_sync(0xffffffffu, inc_p, 1);
+    float after = __shfl_down_sync(0xffffffffu, inc_s, 1);
+    if (lane == 0) before = ninf;
+    if (lane == 31) after = ninf;
+    float r = after;
+    for (int b = b1 - 1; b >= b0; b--) {
+        r = fmaxf(r, suf[b]);
+        suf[b] = r;
+    }
+    for (int b = b0; b < b1; b++) pre[b] = fmaxf(pre[b], before);
+}
+
 __global__ void __launch_bounds__(kWarps * 32) k_sdem(SdemLaunch a) {
     extern __shared__ float4 smem4[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int cap = row_capacity(a.max_row);
-    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * cap;
+    const int wf = warp_floats(a.max_row);
+    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * wf;
     float* A = buf + kPadFront;
+    float* suf = buf + row_pad(a.max_row);
+    float* pre = suf + blocks_pad(a.max_row);
     for (;;) {
         unsigned idx = 0;
         if (lane == 0) idx = atomicAdd(a.counter, 1u);
@@ -250,13 +302,17 @@ __global__ void __launch_bounds__(kWarps * 32) k_sdem(SdemLaunch a) {
         for (int x = L + lane; x < tail_end; x += 32) A[x] = 0.0f;
         const bool fast = __all_sync(0xffffffffu, ok) && L <= kFastMaxRow && div_safe(a.povh);
         __syncwarp();
+        if (fast) {
+            block_maxima(A, L, suf, pre, lane);
+            __syncwarp();
+        }
 
         const int x0 = it.chunk * kChunk + 4 * lane;
         float cv[4];
         if (fast) {
             float cb[4];
-            scan_fwd_fast(A, x0, L, a.povh, cv);
-            scan_bwd_fast(A, x0, L, a.povh, cb);
+            scan_fast<true>(A, suf, x0, L, a.povh, cv);
+            scan_fast<false>(A, pre, x0, L, a.povh, cb);
 #pragma unroll
             for (int q = 0; q < 4; q++) cv[q] = __fadd_rn(cv[q], cb[q]);
         } else {
@@ -291,7 +347,7 @@ __global__ void k_div_check(int dmax, unsigned long long* checked, unsigned long
         for (int d = 1; d <= dmax; d++) {
             const float4 st = c_step[d];
             const float q = div_fast(a, st.x, st.y);
-            const float ref = __fdiv_rn(a, st.x);
+            const float ref = __fdiv_rn(a, -st.x);
             if (__float_as_uint(q) != __float_as_uint(ref) && !(q == 0.0f && ref == 0.0f)) {
                 n_bad++;
                 atomicCAS(first_bad, 0xffffffffu, (unsigned)u);
@@ -332,13 +388,21 @@ cudaError_t sdem_division_selftest(int dmax, int num_sms, unsigned long long* h_
 
 int sdem_chunk() { return kChunk; }
 
-cudaError_t sdem_init_tables() {
-    std::vector<float4> tab(kFastMaxRow);
-    for (int d = 0; d < kFastMaxRow; d++) {
-        const float df = (float)d;
-        tab[d] = make_float4(df, d ? 1.0f / df : 0.0f, 2.0f * df + 1.0f, df + 1.0f);
+namespace {
+struct StepTable {
+    float4 v[kFastMaxRow];
+    StepTable() {
+        for (int d = 0; d < kFastMaxRow; d++) {
+            const float df = (float)d;
+            v[d] = make_float4(-df, d ? 1.0f / df : 0.0f, 2.0f * df + 1.0f, df + 1.0f);
+        }
     }
-    return cudaMemcpyToSymbol(c_step, tab.data(), sizeof(float4) * kFastMaxRow);
+};
+}  // namespace
+
+cudaError_t sdem_init_tables() {
+    static const StepTable tab;  // built once, thread-safe, no heap
+    return cudaMemcpyToSymbol(c_step, tab.v, sizeof(tab.v));
 }
 
 void sdem_items(const Geometry& geo, const Batch& b, std::vector<uint64_t>& items, int* max_row) {
@@ -379,7 +443,7 @@ void sdem_items(const Geometry& geo, const Batch& b, std::vector<uint64_t>& item
 
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (a.n_items == 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * (size_t)row_capacity(a.max_row) * kWarps;
+    const size_t smem = sizeof(float) * (size_t)warp_floats(a.max_row) * kWarps;
     cudaError_t e = cudaFuncSetAttribute(k_sdem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -396,3 +460,4 @@ cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
 }
 
 }  // namespace ske
+

@@ -83,10 +83,14 @@ cudaError_t launch_cepstrum(const DevGeometry& g, const Batch& b, const float* S
 // Constant tables used by the SDEM sweep, uploaded once per device.
 cudaError_t sdem_init_tables();
 
+// Record `msg` as the calling thread's last error (ske_last_error) and return code.
+int set_last_error(int code, const char* msg);
+
 // Exhaustive comparison of the sweep's division with IEEE division over every
 // float numerator in the sweep's fast-path range and every d in [1, dmax]
 // (synchronous, on the current device).
 cudaError_t measure_fp32_peak(int num_sms, int reps, double* scalar_ops, double* packed_ops);
+cudaError_t measure_fp64_peak(int num_sms, int reps, double* dfma_ops);
 
 cudaError_t sdem_division_selftest(int dmax, int num_sms, unsigned long long* checked,
                                    unsigned long long* bad, unsigned* first_bad);
