@@ -214,6 +214,34 @@ int ske_copy_skewed(ske_engine e, float* skew_in, float* skew_out, int on_device
  * scale factor; other cells 0.  counts: 2*dimx*dimy + dim_l floats. */
 int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_device);
 
+/* Total-viewshed sweep of ONE skewed sector that allocates nothing.  No
+ * counterpart in the reference.
+ *
+ * For callers that cannot call cudaMalloc -- code that runs under a fixed GPU
+ * memory budget, inside another framework's allocator, or on a path where
+ * allocation is forbidden -- this runs the engine's sweep over a skewed sector
+ * the caller already holds in device memory: `skew_in` (row stride dim_i;
+ * every row segment r*dim_i + [first[r], last[r]) must lie inside it),
+ * `first`/`last` (skew_height int32 entries, device), and writes cv*scale2 to
+ * every valid cell of `skew_out` (other cells are left as they are: zero the
+ * buffer first, as resetSkew does, skewEngine.cuh:542-570).  Results equal the
+ * built-in SDEM operator's on the same sector bit for bit.
+ *
+ * Its scratch (sector descriptor, work-queue head, status word, work items) is
+ * a file-scope device array of about 8 MiB that every GPU loading this library
+ * holds until the process exits; limits: dim_l <= 4096, skew_height <= 131072,
+ * at most 2^20 work items of 128 observers.  Larger sectors are rejected with
+ * SKE_ERR_INVALID and a message.  No cudaMalloc, cudaFree or allocating library
+ * routine is called.  The first call on a device takes the array's device
+ * address and uploads the sweep's constant table; make that first call before
+ * any stream capture.  Every call shares the array and keeps the last call's
+ * contents (the queue head and status are cleared on each call); calls that
+ * overlap on the GPU race, calls from several host threads are serialised.
+ * Synchronous with respect to `stream` (a cudaStream_t, NULL = default). */
+int ske_sdem_sector_noalloc(int device, const float* skew_in, float* skew_out, int dim_i,
+                            int skew_height, int dim_l, const int32_t* first, const int32_t* last,
+                            float scale2, float povh, void* stream);
+
 /* Profiling ----------------------------------------------------------------*/
 
 /* Enable (1) / disable (0) CUDA-event timing of every kernel launch. */

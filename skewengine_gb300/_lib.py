@@ -69,6 +69,8 @@ SIGNATURES = [
     ("ske_sector", C.c_int, [C.c_void_p, C.POINTER(SectorView)]),
     ("ske_copy_skewed", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
     ("ske_sdem_counts", C.c_int, [C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_int]),
+    ("ske_sdem_sector_noalloc", C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p,
+                                          C.c_void_p, C.c_float, C.c_float, C.c_void_p]),
     ("ske_profile_enable", C.c_int, [C.c_void_p, C.c_int]),
     ("ske_profile_get", C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]),
     ("ske_launch_count", C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
