@@ -117,6 +117,11 @@ struct ske_engine_s {
     std::vector<Pending> pending;
     std::vector<cudaEvent_t> event_pool;
     int64_t launches = 0;
+    // Batches of uneven grids: one cached child engine per other grid size.
+    // A child borrows the parent's skew-buffer slots and Radon scratch (the
+    // parent's stride holds the child's skewed grids) and owns the rest.
+    ske_engine parent = nullptr;
+    std::map<std::pair<int, int>, ske_engine> children;
 };
 
 namespace {
@@ -224,6 +229,14 @@ int check_status(ske_engine e) {
 
 // Make room for `want` sector slots of skewed buffers (and Radon scratch).
 int ensure_slots(ske_engine e, int want) {
+    if (e->parent) {  // borrowed from the parent, which may grow them
+        SKE_TRY(ensure_slots(e->parent, want));
+        e->d_SI = e->parent->d_SI;
+        e->d_SO = e->parent->d_SO;
+        e->d_P = e->parent->d_P;
+        e->slots = e->parent->slots;
+        return SKE_OK;
+    }
     if (want <= e->slots) return SKE_OK;
     SKE_CK(cudaStreamSynchronize(e->stream));
     cudaFree(e->d_SI);
@@ -467,7 +480,16 @@ int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32
     return SKE_OK;
 }
 
+namespace {
+int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream, ske_engine parent);
+}
+
 int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) {
+    return create_engine(out, dimx, dimy, device, stream, nullptr);
+}
+
+namespace {
+int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream, ske_engine parent) {
     if (!out) return fail(SKE_ERR_INVALID, "null engine pointer");
     *out = nullptr;
     if (dimx < 1 || dimy < 1 || dimx > 65535 || dimy > 65535)
@@ -499,6 +521,11 @@ int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) {
     build_geometry(dimx, dimy, e->geo);
     while (e->max_H2 < e->geo.max_H) e->max_H2 <<= 1;
     e->pstride = e->max_H2;
+    if (parent && parent->stride >= e->len && parent->pstride >= e->max_H2) {
+        e->parent = parent;  // skewed grids fit the parent's slots: borrow them
+        e->stride = parent->stride;
+        e->pstride = parent->pstride;
+    }
     // Geometry tables.
     SKE_TRY(dev_alloc(&e->d_desc, e->geo.desc.size()));
     SKE_TRY(dev_alloc(&e->d_target, e->geo.target.size()));
@@ -539,11 +566,15 @@ int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) {
     *out = e.release();
     return SKE_OK;
 }
+}  // namespace
 
 int ske_destroy(ske_engine e) {
     if (!e) return SKE_OK;
+    for (auto& kv : e->children) ske_destroy(kv.second);
+    e->children.clear();
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->parent) e->d_SI = e->d_SO = nullptr, e->d_P = nullptr;  // borrowed
     for (auto& kv : e->item_plans) cudaFree(kv.second.d_items);
     for (auto& p : e->pending) {
         cudaEventDestroy(p.a);
@@ -604,29 +635,25 @@ int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, cons
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (count < 0 || (count > 0 && (!dimx || !dimy || !inputs || !outputs)))
         return fail(SKE_ERR_INVALID, "bad batch arguments");
-    std::map<std::pair<int, int>, ske_engine> engines;
+    // One child engine per other grid size, created on first use and kept with
+    // the parent (geometry, work lists and buffers are reused by later batches).
     int rc = SKE_OK;
     for (int i = 0; i < count && rc == SKE_OK; i++) {
-        ske_engine sub = nullptr;
-        if (dimx[i] == e->dimx && dimy[i] == e->dimy) {
-            sub = e;
-        } else {
-            auto key = std::make_pair((int)dimx[i], (int)dimy[i]);
-            auto it = engines.find(key);
-            if (it == engines.end()) {
-                rc = ske_create(&sub, dimx[i], dimy[i], e->device, (void*)e->stream);
+        ske_engine sub = e;
+        if (dimx[i] != e->dimx || dimy[i] != e->dimy) {
+            const auto key = std::make_pair((int)dimx[i], (int)dimy[i]);
+            auto it = e->children.find(key);
+            if (it == e->children.end()) {
+                rc = create_engine(&sub, dimx[i], dimy[i], e->device, (void*)e->stream, e);
                 if (rc != SKE_OK) break;
-                engines[key] = sub;
+                e->children[key] = sub;
             } else {
                 sub = it->second;
             }
         }
+        const int64_t before = sub->launches;
         rc = ske_run(sub, kernel, inputs[i], inputs_on_device, outputs[i], outputs_on_device, p);
-        if (sub != e) e->launches += 0;
-    }
-    for (auto& kv : engines) {
-        e->launches += kv.second->launches;
-        ske_destroy(kv.second);
+        if (sub != e) e->launches += sub->launches - before;
     }
     return rc;
 }

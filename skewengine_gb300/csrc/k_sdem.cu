@@ -13,11 +13,10 @@
 //  * The row is staged in shared memory once per item; lanes read it through a
 //    register sliding window refilled by one aligned 16-byte load per 4 steps,
 //    so shared-memory traffic is 1 byte per observer-step.
-//  * The step distance d is warp-uniform, so -d, RN(1/d), 2d+1 and d+1 come from a
-//    constant-memory table.
-//  * Instruction mix: the sweep is bound by issue and by the ALU pipe, so per
-//    step it uses 4 FMA-pipe ops for the slope, 1 compare and 1 max on the ALU
-//    pipe, and the two sums as predicated FMA-pipe adds (no selects).
+//  * The step distance d is warp-uniform, so -d, RN(1/d) and 2d+1 come from a
+//    constant-memory table.  The slopes of two observers at a time use packed
+//    f32x2 instructions (the sweep is issue-bound: packing halves the slope's
+//    issue slots; measured 15% faster than scalar).
 //  * Division: the quotient (S[k]-h)/d must be the correctly rounded one,
 //    because visibility compares it strictly against the running maximum.
 //    q0 = RN(a*y), r = fma(q0, -d, a), q = fma(r, y, q0) with y = RN(1/d)
@@ -59,7 +58,7 @@ constexpr int kPadFront = 136;     // zero cells before the row (backward window
 constexpr int kPadBack = 144;      // zero cells after the row (forward window overrun)
 constexpr int kFastMaxRow = 4096;  // exact float accumulation bound (see header)
 constexpr int kBlk = 8;            // cells per block of the pruning maxima
-constexpr int kCheck = 16;         // steps between pruning tests (multiple of 4)
+constexpr int kCheck = 32;         // steps between pruning tests (multiple of 4)
 
 // {-d, RN(1/d), 2d+1, d+1} for d = 0..4095 (entry 0 unused).
 __constant__ float4 c_step[kFastMaxRow];
@@ -83,6 +82,36 @@ __device__ __forceinline__ float div_fast(float a, float negd, float y) {
     return __fmaf_rn(r, y, q0);
 }
 
+// Packed pairs of floats for the f32x2 instructions: two independent IEEE
+// operations, round to nearest, no flush to zero.
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& a, float& b) { asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v)); }
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+// Both halves of a/d correctly rounded (div_fast on each half).
+__device__ __forceinline__ f2 div2(f2 a, f2 negd, f2 y) {
+    const f2 q0 = mul2(a, y);
+    return fma2(fma2(q0, negd, a), y, q0);
+}
+
 struct Item {
     int slot, row, chunk;
 };
@@ -104,25 +133,11 @@ struct Scan4 {
     bool done[4];    // finished by pruning
 };
 
-// One line-of-sight step of one observer: the correctly rounded slope (FMA
-// pipe), the horizon test and update, and the two sums as predicated adds so
-// they also issue to the FMA pipe (selects would go to the ALU pipe, the
-// sweep's bottleneck).
-__device__ __forceinline__ void los_step(float& mx, float& acc, float& cl, float s, float h, float negd, float y,
-                                         float ring) {
-    const float q = div_fast(__fsub_rn(s, h), negd, y);
-    asm("{\n\t.reg .pred p;\n\t"
-        "setp.gt.f32 p, %3, %2;\n\t"
-        "@p add.rn.f32 %0, %0, %4;\n\t"
-        "@!p add.rn.f32 %1, %0, 0f00000000;\n\t}"
-        : "+f"(acc), "+f"(cl)
-        : "f"(mx), "f"(q), "f"(ring));
-    mx = fmaxf(mx, q);  // rows on this path are finite: max == "q > mx ? q : mx"
-}
-
 // One block of 4 steps d = d0 .. d0+3.  The window holds the 8 row values the
 // block needs: forward w = A[x0+d0 .. x0+d0+7], step e of observer q reads
-// w[e+q]; backward w = A[x0-d0-4 .. x0-d0+3], step e reads w[q-e+4].
+// w[e+q]; backward w = A[x0-d0-4 .. x0-d0+3], step e reads w[q-e+4].  Slopes of
+// observer pairs (0,1) and (2,3) use packed f32x2 operations; the horizon test,
+// the horizon update and the two sums are per observer.
 template <bool kFwd, bool kTail>
 __device__ __forceinline__ void block4(Scan4& s, const float w[8], int d0) {
 #pragma unroll
@@ -130,10 +145,20 @@ __device__ __forceinline__ void block4(Scan4& s, const float w[8], int d0) {
         const int d = d0 + e;
         if (d == 0) continue;  // only in the first block
         const float4 st = c_step[d];
+        const f2 nd2 = pk(st.x, st.x), y2 = pk(st.y, st.y);
+        const float ring = st.z;
+        float qv[4];
+#define SKE_W(q) (kFwd ? w[e + (q)] : w[(q)-e + 4])
+        upk(div2(sub2(pk(SKE_W(0), SKE_W(1)), pk(s.h[0], s.h[1])), nd2, y2), qv[0], qv[1]);
+        upk(div2(sub2(pk(SKE_W(2), SKE_W(3)), pk(s.h[2], s.h[3])), nd2, y2), qv[2], qv[3]);
+#undef SKE_W
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             if (kTail && d > s.n[q]) continue;
-            los_step(s.mx[q], s.acc[q], s.cl[q], kFwd ? w[e + q] : w[q - e + 4], s.h[q], st.x, st.y, st.z);
+            const bool above = qv[q] > s.mx[q];
+            s.mx[q] = above ? qv[q] : s.mx[q];
+            s.cl[q] = above ? s.cl[q] : s.acc[q];
+            s.acc[q] = above ? __fadd_rn(s.acc[q], ring) : s.acc[q];
         }
     }
 }
