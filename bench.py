@@ -47,6 +47,10 @@ SIDE = 2000
 ANGLES = 180
 DIR_SECTORS = 2 * ANGLES  # each skewed row is scanned both ways (kernelSDEM.h:189-217)
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (read + write) of one sweep launch per skewed cell, from an ncu
+# capture of the 512x512 sweep (350.1 MB over 68.0 M skewed cells); the sweep's
+# traffic grows with the skewed cells it reads and writes.
+SWEEP_DRAM_BYTES_PER_SKEWED_CELL = 5.148
 
 
 def _env_int(name, default):
@@ -159,6 +163,12 @@ class ClockSampler:
         reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+def skewed_cells(dimx: int, dimy: int, angles) -> int:
+    """Cells of the skewed grids of the given angles (skew height x row length)."""
+    import skewengine_gb300 as ske
+    return sum(int(g["skew_height"]) * int(g["dim_i"]) for g in (ske.geometry(dimx, dimy, a) for a in angles))
 
 
 def los_steps(dimx: int, dimy: int, angles) -> float:
@@ -278,6 +288,56 @@ def secondary_workload(args):
     return 0
 
 
+def batch_workload(args):
+    """Total viewshed of 64 seeded fractal DEMs with uneven sides (256-2000,
+    roughness 0.6-0.9) through ske_run_batch, 180 angles each; Kahan
+    accumulation.  Reports Mpoint*sectors/s over the whole batch."""
+    import torch
+    import skewengine_gb300 as ske
+    from skewengine_gb300 import build, synthetic
+    build.build()
+    spec = synthetic.uneven_dem_batch(64, 3000)
+    grids = [torch.from_numpy(synthetic.fractal_dem(s, seed, roughness=h)).cuda() for s, h, seed in spec]
+    outs = [torch.empty_like(g) for g in grids]
+    cells = sum(g.numel() for g in grids)
+    big = max(grids, key=lambda g: g.numel())
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    eng = ske.SkewEngine(big.shape[1], big.shape[0], stream=stream.cuda_stream)
+    dx = np.array([g.shape[1] for g in grids], np.int32)
+    dy = np.array([g.shape[0] for g in grids], np.int32)
+    ins = (C.c_void_p * len(grids))(*[g.data_ptr() for g in grids])
+    ous = (C.c_void_p * len(grids))(*[o.data_ptr() for o in outs])
+    prm = ske.params(180, ske.DEFAULT_POVH, "kahan")
+    lib = ske.engine.load()
+
+    def step():
+        ske.engine.check(lib.ske_run_batch(eng._h, ske.KERNEL_SDEM, len(grids), dx.ctypes.data, dy.ctypes.data,
+                                           ins, 1, ous, 1, C.byref(prm)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = eng.launch_count()
+    t0.record(stream)
+    for _ in range(args.steps):
+        step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    line = {"metric": "Batched viewshed Mpoint·sectors/s (64 uneven DEMs 256-2000², 360 sect)",
+            "value": cells * DIR_SECTORS / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (64 seeded diamond-square DEMs)",
+            "config": {"workload": "64 DEMs, sides uniform 256-2000, roughness 0.6-0.9, Kahan accumulation",
+                       "cells": cells, "sides": [int(s) for s, _, _ in spec]},
+            "gpu_launches": int((eng.launch_count() - launches0) / args.steps)}
+    print(json.dumps(line), flush=True)
+    eng.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -287,13 +347,15 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--side", type=int, default=SIDE,
                     help="DEM side (the metric is quoted at 2000; smaller sides are for profiling)")
-    ap.add_argument("--workload", choices=["sdem", "radon", "cepstrum"], default="sdem",
-                    help="sdem = the headline metric; radon / cepstrum = secondary measurements")
+    ap.add_argument("--workload", choices=["sdem", "radon", "cepstrum", "sdem_batch"], default="sdem",
+                    help="sdem = the headline metric; the others are secondary measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "sdem_batch":
+        return batch_workload(args)
     if args.workload != "sdem":
         return secondary_workload(args)
 
@@ -422,7 +484,11 @@ def main():
                 "ms_per_step": e2e_ms},
         "roofline": {"bound": "fp32", "kernel": "sdem_sweep", "achieved": achieved / 1e12,
                      "peak": peak / 1e12, "unit": "Tops/s (FP32 lane ops)", "frac": achieved / peak,
-                     "traffic": None, "work_per_launch": ops_per_launch,
+                     "traffic": SWEEP_DRAM_BYTES_PER_SKEWED_CELL * skewed_cells(side, side, range(ANGLES))
+                                / launches_per_step,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the 512x512 sweep "
+                                       "launch, scaled by skewed cells",
+                     "work_per_launch": ops_per_launch,
                      "work": "3 FP32 lane ops (sub, div, max) per line-of-sight step; "
                              f"{steps_total:.4g} steps per DEM",
                      "launch_ms": sweep_per_launch_ms, "launches": int(sweep_n),

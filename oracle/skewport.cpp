@@ -291,6 +291,42 @@ struct Worker {
     std::vector<float> acc[4];
 };
 
+// ---- binary64 restatement (error reference for Radon and cepstrum) ----------
+
+void op_radon_f64(const Sector& s, const double* S, double* O) {
+    const int H = s.H;
+    const int H2 = (int)pow(2, ceil(log2(H)));
+    std::vector<cplx> p(H2, cplx(0, 0));
+    for (int i = 0; i < H; i++)
+        for (int j = s.first[i]; j < s.last[i]; j++) p[i] = cplx(p[i].real() + S[(size_t)s.dim_i * i + j], 0);
+    fft_dif(p.data(), (unsigned)H2, false);
+    for (int i = 0; i < H2; i++) p[i] = i > H / 2 ? cplx(0) : ((double)i / H) * p[i];
+    ifft(p.data(), (unsigned)H2);
+    for (int i = 0; i < H; i++)
+        for (int j = s.first[i]; j < s.last[i]; j++) O[(size_t)s.dim_i * i + j] += p[i].real();
+}
+
+void op_cepstrum_f64(const Sector& s, const double* S, double* O) {
+    cplx w1[kWin], w2[kWin / 2];
+    double samples[kWin / 4];
+    for (int row = 0; row < s.H; row++) {
+        const int lo = s.first[row], hi = s.last[row];
+        const double* v = S + (size_t)s.dim_i * row;
+        for (int j = lo; j < hi; j++) {
+            for (int m = 0; m < kWin; m++) {
+                const int idx = j - kWin / 2 + m;
+                w1[m] = (idx < lo || idx >= hi) ? cplx(0, 0) : cplx(v[idx], 0);
+            }
+            fft_dif(w1, kWin, true);
+            for (int k = 0; k < kWin / 2; k++)
+                w2[k] = cplx(log(pow(w1[k].real(), 2) + pow(w1[k].imag(), 2)), 0);
+            fft_dif(w2, kWin / 2, true);
+            for (int k = 0; k < kWin / 4; k++) samples[k] = -std::min(0.0, w2[k].real());
+            O[(size_t)s.dim_i * row + j] = blur_peak(samples, kWin / 4) * 10000;
+        }
+    }
+}
+
 void run_sector(int op, int dimx, int dimy, const std::vector<float> src[4], int angle, float povh,
                 Worker& w) {
     Sector s;
@@ -418,6 +454,60 @@ int port_accumulate(int op, const float* input, int dimx, int dimy, const int* a
         }
     }
     *used_mask = mask;
+    return 0;
+}
+
+int port_run_f64(int op, const float* input, double* output, int dimx, int dimy, int nsect, float povh) {
+    (void)povh;
+    if (dimx <= 0 || dimy <= 0 || nsect <= 0 || nsect > 180) return 1;
+    if (op != PORT_RADON && op != PORT_CEPSTRUM && op != PORT_IDENTITYDEM && op != PORT_IDENTITYIMG) return 1;
+    std::vector<float> srcf[4];
+    orientations(input, dimx, dimy, srcf);
+    const size_t n = (size_t)dimx * dimy;
+    const bool max_mode = op == PORT_CEPSTRUM;
+    std::vector<double> S(2 * n + std::max(dimx, dimy)), O(S.size());
+    std::vector<double> acc[4];
+    for (int a = 0; a < nsect; a++) {
+        Sector s;
+        make_sector(dimx, dimy, a, s);
+        std::fill(S.begin(), S.end(), 0.0);
+        std::fill(O.begin(), O.end(), 0.0);
+        const float* src = srcf[s.type].data();
+        for (int i = 0; i < s.dim_o; i++)  // skew with the exact drift fraction
+            for (int j = 0; j < s.dim_i; j++) {
+                const double w = s.skewness * j - s.target[j];
+                const double v = src[(size_t)s.dim_i * i + j];
+                S[(size_t)(i + s.target[j]) * s.dim_i + j] += (1.0 - w) * v;
+                S[(size_t)(i + s.target[j] + 1) * s.dim_i + j] += w * v;
+            }
+        if (op == PORT_RADON) op_radon_f64(s, S.data(), O.data());
+        else if (op == PORT_CEPSTRUM) op_cepstrum_f64(s, S.data(), O.data());
+        else
+            for (int r = 0; r < s.H; r++)
+                for (int j = s.first[r]; j < s.last[r]; j++) O[(size_t)s.dim_i * r + j] = S[(size_t)s.dim_i * r + j];
+        if (acc[s.type].empty()) acc[s.type].assign(n, 0.0);
+        for (int i = 0; i < s.dim_o; i++)
+            for (int j = 0; j < s.dim_i; j++) {
+                const double w = s.skewness * j - s.target[j];
+                const double lo = O[(size_t)(i + s.target[j]) * s.dim_i + j];
+                const double hi = O[(size_t)(i + s.target[j] + 1) * s.dim_i + j];
+                double& cell = acc[s.type][(size_t)i * s.dim_i + j];
+                if (max_mode) cell = s.a + 1000.0 * std::floor(std::max(cell, std::max(lo, hi)) / 1000.0);
+                else cell += (1.0 - w) * lo + w * hi;
+            }
+    }
+    for (int i = 0; i < dimy; i++)
+        for (int j = 0; j < dimx; j++) {
+            const int ci = dimy - 1 - i, cj = dimx - 1 - j;
+            const size_t idx[4] = {(size_t)i * dimx + j, (size_t)cj * dimy + ci, (size_t)j * dimy + ci,
+                                   (size_t)i * dimx + cj};
+            double o = 0.0;
+            for (int t = 0; t < 4; t++) {
+                if (acc[t].empty()) continue;
+                o = max_mode ? std::max(o, acc[t][idx[t]]) : o + acc[t][idx[t]];
+            }
+            output[(size_t)i * dimx + j] = o;
+        }
     return 0;
 }
 

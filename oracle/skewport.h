@@ -53,6 +53,12 @@ int port_sdem_counts(const float* input, int dimx, int dimy, int angle, float po
 int port_accumulate(int op, const float* input, int dimx, int dimy, const int* angles, int nangles,
                     float povh, float* acc, int* used_mask);
 
+// The same sector loop carried out entirely in binary64 (skew weights, skewed
+// grids, operator, deskew and fold), for the Radon transform and the cepstrum:
+// the FP64 reference against which the float pipeline's error is stated.
+// output: dimx*dimy doubles.
+int port_run_f64(int op, const float* input, double* output, int dimx, int dimy, int nsect, float povh);
+
 // Sum over sectors 0..nsect-1 and rows of L*(L-1), L = last-first: the number of
 // line-of-sight steps kernelSDEM performs (both directions).
 double port_los_steps(int dimx, int dimy, int nsect);

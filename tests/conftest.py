@@ -45,6 +45,7 @@ def port():
     lib.port_los_steps.argtypes = [C.c_int, C.c_int, C.c_int]
     lib.port_los_steps.restype = C.c_double
     lib.port_accumulate.argtypes = [C.c_int, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, fp, ip]
+    lib.port_run_f64.argtypes = [C.c_int, fp, dp, C.c_int, C.c_int, C.c_int, C.c_float]
     return lib
 
 
@@ -56,6 +57,13 @@ class PortOracle:
         dy, dx = x.shape
         out = np.zeros_like(x)
         assert self.lib.port_run(op, np.ascontiguousarray(x, np.float32), out, dx, dy, nsect, povh, threads) == 0
+        return out
+
+    def run_f64(self, op, x, nsect=180, povh=0.15):
+        """The same run carried out in binary64 throughout (error reference)."""
+        dy, dx = x.shape
+        out = np.zeros(x.shape, np.float64)
+        assert self.lib.port_run_f64(op, np.ascontiguousarray(x, np.float32), out, dx, dy, nsect, povh) == 0
         return out
 
     def run_angles(self, op, x, angles, povh=0.15, threads=1):
