@@ -99,6 +99,8 @@ struct ske_engine_s {
     int64_t tw_off_host[32] = {0};
     unsigned* d_counter = nullptr;
     int* d_status = nullptr;
+    int4* d_lists = nullptr;  // survivor lists of the viewshed sweep
+    size_t list_bytes = 0;
     float* h_pin = nullptr;
     std::map<std::vector<int>, ItemPlan> item_plans;
     // per-sector API state
@@ -118,8 +120,8 @@ struct ske_engine_s {
     std::vector<cudaEvent_t> event_pool;
     int64_t launches = 0;
     // Batches of uneven grids: one cached child engine per other grid size.
-    // A child borrows the parent's skew-buffer slots and Radon scratch (the
-    // parent's stride holds the child's skewed grids) and owns the rest.
+    // A child borrows the parent's skew-buffer slots, Radon scratch and sweep
+    // lists (the parent's stride holds the child's skewed grids) and owns the rest.
     ske_engine parent = nullptr;
     std::map<std::pair<int, int>, ske_engine> children;
 };
@@ -252,6 +254,24 @@ int ensure_slots(ske_engine e, int want) {
     return SKE_OK;
 }
 
+// Make room for `bytes` of survivor-list scratch for the viewshed sweep.
+int ensure_lists(ske_engine e, size_t bytes) {
+    if (e->parent) {
+        SKE_TRY(ensure_lists(e->parent, bytes));
+        e->d_lists = e->parent->d_lists;
+        e->list_bytes = e->parent->list_bytes;
+        return SKE_OK;
+    }
+    if (bytes <= e->list_bytes) return SKE_OK;
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    cudaFree(e->d_lists);
+    e->d_lists = nullptr;
+    e->list_bytes = 0;
+    SKE_TRY(dev_alloc(&e->d_lists, (bytes + sizeof(int4) - 1) / sizeof(int4)));
+    e->list_bytes = bytes;
+    return SKE_OK;
+}
+
 // Sectors per launch: as many as fit in a quarter of free memory (at most 180).
 int batch_capacity(ske_engine e, int nangles) {
     size_t free_b = 0, total_b = 0;
@@ -291,6 +311,7 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             ItemPlan* plan = nullptr;
             SKE_TRY(get_items(e, b, &plan));
             SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
+            SKE_TRY(ensure_lists(e, sdem_list_bytes(std::max(plan->max_row, 1), e->num_sms)));
             SdemLaunch a;
             a.g = e->dg;
             a.b = b;
@@ -304,6 +325,8 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             a.max_row = std::max(plan->max_row, 1);
             a.counts_only = counts_only;
             a.status = e->d_status;
+            a.lists = e->d_lists;
+            a.list_bytes = e->list_bytes;
             LaunchScope ls(e, "sdem_sweep", plan->n_items > 0 ? 1 : 0);
             return ls.done(launch_sdem(a, e->num_sms, e->stream));
         }
@@ -574,7 +597,7 @@ int ske_destroy(ske_engine e) {
     e->children.clear();
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
-    if (e->parent) e->d_SI = e->d_SO = nullptr, e->d_P = nullptr;  // borrowed
+    if (e->parent) e->d_SI = e->d_SO = nullptr, e->d_P = nullptr, e->d_lists = nullptr;  // borrowed
     for (auto& kv : e->item_plans) cudaFree(kv.second.d_items);
     for (auto& p : e->pending) {
         cudaEventDestroy(p.a);
@@ -582,7 +605,8 @@ int ske_destroy(ske_engine e) {
     }
     for (cudaEvent_t ev : e->event_pool) cudaEventDestroy(ev);
     void* bufs[] = {e->d_desc, e->d_target, e->d_first, e->d_last, e->d_weight, e->d_in, e->d_orient, e->d_acc,
-                    e->d_comp, e->d_out, e->d_SI, e->d_SO, e->d_P, e->d_tw, e->d_tw_off, e->d_counter, e->d_status};
+                    e->d_comp, e->d_out, e->d_SI, e->d_SO, e->d_P, e->d_tw, e->d_tw_off, e->d_counter, e->d_status,
+                    e->d_lists};
     for (void* b : bufs) cudaFree(b);
     if (e->h_pin) cudaFreeHost(e->h_pin);
     if (e->own_stream) cudaStreamDestroy(e->stream);

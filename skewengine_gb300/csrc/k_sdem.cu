@@ -6,7 +6,30 @@
 // beats the horizon, and every visible run that closes before the row end adds
 // d_close^2 - d_open^2 to cv.  The output is cv * (float)scale^2.
 //
-// GB300 mapping
+// Two sweeps share the arithmetic below.
+//
+// Compacting sweep (k_sdem, the engine's)
+//  * Persistent kernel; a warp takes one skewed row (sector slot, row) from a
+//    global queue ordered longest row first and scans it forward, then backward.
+//  * Work proceeds in levels of kLevel steps.  Level 0 takes every observer of
+//    the row; after each level an exact horizon test (below) retires the
+//    observers that can see nothing further, and the survivors are appended to a
+//    per-warp list in global scratch.  The next level processes only that list,
+//    in batches of 64 observers (2 per lane).  An observer's work therefore ends
+//    within kLevel steps of the test that retires it, instead of with the
+//    slowest of a fixed group: on 2000x2000 fractal terrain this runs about 29%
+//    of the line-of-sight steps (counting empty slots), against 68% for the
+//    chunked sweep.  64-step levels measured faster than 32 or 128 (fewer list
+//    passes against more steps past an observer's end).
+//  * All observers of a batch are at the same step distance d, so -d, RN(1/d)
+//    and 2d+1 still come from the constant table; each lane reads its two
+//    observers' targets with one shared-memory load per step each, and computes
+//    both slopes with packed f32x2 instructions.
+//  * The forward result of an observer goes to the output cell; the backward
+//    pass adds its own and applies the scale (both are integers below 2^24, so
+//    the sum is exact in either order).
+//
+// Chunked sweep (k_sdem_chunked, the allocation-free entry point's)
 //  * Persistent kernel; a warp takes one work item = (sector slot, skewed row,
 //    chunk of 128 consecutive observers) from a global queue ordered longest row
 //    first.  Every lane owns 4 consecutive observers.
@@ -15,8 +38,9 @@
 //    so shared-memory traffic is 1 byte per observer-step.
 //  * The step distance d is warp-uniform, so -d, RN(1/d) and 2d+1 come from a
 //    constant-memory table.  The slopes of two observers at a time use packed
-//    f32x2 instructions (the sweep is issue-bound: packing halves the slope's
-//    issue slots; measured 15% faster than scalar).
+//    f32x2 instructions.
+//
+// Common to both
 //  * Division: the quotient (S[k]-h)/d must be the correctly rounded one,
 //    because visibility compares it strictly against the running maximum.
 //    q0 = RN(a*y), r = fma(q0, -d, a), q = fma(r, y, q0) with y = RN(1/d)
@@ -35,14 +59,17 @@
 //    count it.  All values are integers below 2^24 for rows up to 4096 cells,
 //    so the float result is exact and equal to the reference's.  Longer rows
 //    use the reference-order path.
-//  * Horizon pruning (exact): after step d the remaining targets k are all
-//    invisible when fl((Smax - h)/(d+1)) <= horizon, Smax an upper bound of the
-//    remaining heights (monotonicity of rounding: every remaining slope is at
-//    most that quotient).  An observer that passes this test is finished: every
-//    later step would be invisible, so cv = 1 + sum (its last run closes at the
-//    next step).  Smax comes from per-8-cell block maxima of the row (suffix
-//    maxima forward, prefix maxima backward); the test runs every kCheck steps
-//    and a warp stops when all its observers are finished.
+//  * Horizon pruning (exact): after step d the remaining targets (distances
+//    d+1 .. n) are all invisible when the bound b = fl(a/(d+1)) for a >= 0, or
+//    b = fl(a/n) for a < 0, is at most the horizon, with a = fl(Smax - h) and
+//    Smax an upper bound of the remaining heights.  Rounding is monotonic, so
+//    every remaining slope fl(fl(S[k]-h)/d') is at most fl(a/d'), and a/d' is
+//    largest at d' = d+1 when a >= 0 and at d' = n when a < 0.  An observer that
+//    passes is finished: every later step would be invisible, so cv = 1 + sum
+//    (its last run closes at the next step).  Smax comes from per-8-cell block
+//    maxima of the row (suffix maxima forward, prefix maxima backward).  The
+//    chunked sweep tests every kCheck steps with the a >= 0 bound and stops a
+//    warp when all its observers are finished.
 #include <algorithm>
 #include <vector>
 
@@ -291,7 +318,7 @@ __device__ void block_maxima(const float* __restrict__ A, int L, float* suf, flo
     for (int b = b0; b < b1; b++) pre[b] = fmaxf(pre[b], before);
 }
 
-__global__ void __launch_bounds__(kWarps * 32) k_sdem(SdemLaunch a) {
+__global__ void __launch_bounds__(kWarps * 32) k_sdem_chunked(SdemLaunch a) {
     extern __shared__ float4 smem4[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wf = warp_floats(a.max_row);
@@ -352,6 +379,261 @@ __global__ void __launch_bounds__(kWarps * 32) k_sdem(SdemLaunch a) {
             const int64_t p = rowbase + x;
             if (owner_row(d, first, last, p) != it.row) continue;
             out[p] = a.counts_only ? cv[q] : __fmul_rn(cv[q], d.r2);
+        }
+        __syncwarp();
+    }
+}
+
+// ---- compacting sweep --------------------------------------------------------
+
+constexpr int kLevel = 64;  // line-of-sight steps per level
+constexpr int kUnroll = 8;  // steps per unrolled block of a level
+constexpr int kSlots = 2;   // observers per lane in a batch (one packed pair)
+static_assert(kLevel % kUnroll == 0, "a level is whole blocks");
+constexpr int kBatch = 32 * kSlots;
+constexpr int kLWarps = 4;  // warps per CTA
+constexpr int kLPad = 64;   // zero cells on both sides of the row (>= kLevel - 1)
+// Longest row on the fast path: every step distance a level touches (at most
+// the last survivor's n + kLevel) stays inside the constant table.
+constexpr int kLFastMaxRow = kFastMaxRow - kLevel;
+static_assert(kSlots == 2, "level_steps packs exactly one pair per lane");
+
+// {-n, RN(1/n)} for n = 0..4095, for lane-divergent lookups (the a < 0 bound).
+__device__ float2 g_recip[kFastMaxRow];
+
+__host__ __device__ inline int lrow_pad(int max_row) { return kLPad + ((max_row + 3) & ~3) + kLPad; }
+// Shared floats per warp: the padded row plus suffix and prefix block maxima.
+__host__ __device__ inline int lwarp_floats(int max_row) { return lrow_pad(max_row) + 2 * blocks_pad(max_row); }
+
+// One lane's observers of a batch, in one scan direction.
+struct Slots {
+    int x[kSlots];  // position in the row
+    int n[kSlots];  // steps in this direction
+    bool valid[kSlots];  // false: empty slot (its steps run, its state is dropped)
+    float h[kSlots], mx[kSlots], acc[kSlots], cl[kSlots];
+    float prev[kSlots];  // backward pass: the forward result held in the output cell
+};
+
+__device__ __forceinline__ void visit(Slots& s, int q, float sl, float ring) {
+    const bool above = sl > s.mx[q];
+    s.mx[q] = above ? sl : s.mx[q];
+    s.cl[q] = above ? s.cl[q] : s.acc[q];
+    s.acc[q] = above ? __fadd_rn(s.acc[q], ring) : s.acc[q];
+}
+
+// Steps d0 .. d0+kLevel-1 of the lane's two observers.  kTail: some observer of
+// the warp ends inside the level; its later steps are skipped.  Reads run at
+// most kLevel-1 cells past an observer's last target, into the row's zero
+// padding.  The level runs as a loop over blocks of kUnroll steps: fully
+// unrolled levels overflow the instruction cache (four copies: two directions,
+// with and without the tail test).
+template <bool kFwd, bool kTail>
+__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0) {
+    const float* p0 = A + (kFwd ? s.x[0] + d0 : s.x[0] - d0);
+    const float* p1 = A + (kFwd ? s.x[1] + d0 : s.x[1] - d0);
+    const f2 hh = pk(s.h[0], s.h[1]);
+#pragma unroll 1
+    for (int k0 = 0; k0 < kLevel; k0 += kUnroll) {
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const int d = d0 + k0 + k;
+            const float4 st = c_step[d];
+            const float z0 = kFwd ? p0[k] : p0[-k];
+            const float z1 = kFwd ? p1[k] : p1[-k];
+            float q0, q1;
+            upk(div2(sub2(pk(z0, z1), hh), pk(st.x, st.x), pk(st.y, st.y)), q0, q1);
+            if (!kTail || d <= s.n[0]) visit(s, 0, q0, st.z);
+            if (!kTail || d <= s.n[1]) visit(s, 1, q1, st.z);
+        }
+        p0 += kFwd ? kUnroll : -kUnroll;
+        p1 += kFwd ? kUnroll : -kUnroll;
+    }
+}
+
+// Where a row's results go.
+struct RowOut {
+    float* out;           // the sector's output grid
+    int64_t rowbase;      // flat index of the row's first valid cell
+    int first;            // its column
+    int row;
+    const SectorDesc* sd;
+    const int32_t* rfirst;
+    const int32_t* rlast;
+    int counts_only;
+};
+
+// Cells that lie in the row's own span of the flat grid (column < dim_i) are
+// always the row's; cells past it may belong to a later row (owner_row).
+__device__ __forceinline__ bool owns(const RowOut& o, int x) {
+    return o.first + x < o.sd->dim_i || owner_row(*o.sd, o.rfirst, o.rlast, o.rowbase + x) == o.row;
+}
+
+// All levels of one scan direction of the row.  Level 0 takes every observer
+// 0..L-1; each later level takes the previous level's survivors from a list.
+template <bool kFwd>
+__device__ void sweep_dir(const float* __restrict__ A, const float* __restrict__ bmax, int L, float povh,
+                          int4* __restrict__ list0, int4* __restrict__ list1, const RowOut& o, int lane) {
+    const unsigned below = (1u << lane) - 1u;
+    const int4* in = nullptr;
+    int4* outl = list0;
+    int count = L;
+    for (int d0 = 1; count > 0; d0 += kLevel) {
+        const int dc = d0 + kLevel - 1;  // last step of the level
+        int produced = 0;
+        // List entries of the next batch are loaded one batch ahead.
+        int4 nxt[kSlots];
+#pragma unroll
+        for (int q = 0; q < kSlots; q++) {
+            const int idx = lane + 32 * q;
+            nxt[q] = (in && idx < count) ? in[idx] : make_int4(0, 0, 0, 0);
+        }
+        for (int base = 0; base < count; base += kBatch) {
+            int4 cur[kSlots];
+#pragma unroll
+            for (int q = 0; q < kSlots; q++) {
+                cur[q] = nxt[q];
+                const int idx = base + kBatch + lane + 32 * q;
+                nxt[q] = (in && idx < count) ? in[idx] : make_int4(0, 0, 0, 0);
+            }
+            Slots s;
+            bool tail = false;
+#pragma unroll
+            for (int q = 0; q < kSlots; q++) {
+                const int idx = base + lane + 32 * q;
+                if (idx < count) {
+                    if (in) {
+                        const int4 e = cur[q];
+                        s.x[q] = e.x;
+                        s.mx[q] = __int_as_float(e.y);
+                        s.acc[q] = __int_as_float(e.z);
+                        s.cl[q] = __int_as_float(e.w);
+                    } else {
+                        s.x[q] = idx;
+                        s.mx[q] = -2000.0f;
+                        s.acc[q] = 0.0f;
+                        s.cl[q] = -1.0f;
+                    }
+                    s.n[q] = kFwd ? L - 1 - s.x[q] : s.x[q];
+                    s.valid[q] = true;
+                    s.h[q] = __fadd_rn(A[s.x[q]], povh);
+                    s.prev[q] = kFwd ? 0.0f : o.out[o.rowbase + s.x[q]];
+                } else {
+                    // Empty: its reads stay in A[-(kLevel-1) .. kLevel-1]; it needs
+                    // no tail test.
+                    s.x[q] = kFwd ? -d0 : d0;
+                    s.n[q] = dc;
+                    s.valid[q] = false;
+                    s.h[q] = s.mx[q] = s.acc[q] = s.cl[q] = s.prev[q] = 0.0f;
+                }
+                tail = tail || s.n[q] < dc;
+            }
+            if (__any_sync(0xffffffffu, tail)) level_steps<kFwd, true>(s, A, d0);
+            else level_steps<kFwd, false>(s, A, d0);
+
+            // Retire finished observers, keep the others for the next level.
+#pragma unroll
+            for (int q = 0; q < kSlots; q++) {
+                bool keep = false;
+                if (s.valid[q]) {
+                    bool done = false;
+                    if (s.n[q] > dc) {
+                        const int k = kFwd ? s.x[q] + dc + 1 : s.x[q] - dc - 1;
+                        const float a = __fsub_rn(bmax[k / kBlk], s.h[q]);
+                        float negd, y;
+                        if (a >= 0.0f) {
+                            const float4 st = c_step[dc + 1];
+                            negd = st.x;
+                            y = st.y;
+                        } else {
+                            const float2 t = g_recip[s.n[q]];
+                            negd = t.x;
+                            y = t.y;
+                        }
+                        done = div_fast(a, negd, y) <= s.mx[q];
+                        keep = !done;
+                    }
+                    if (!keep && owns(o, s.x[q])) {
+                        const float cv = __fadd_rn(1.0f, done ? s.acc[q] : s.cl[q]);
+                        float* cell = o.out + o.rowbase + s.x[q];
+                        if (kFwd) {
+                            *cell = cv;
+                        } else {
+                            const float t = __fadd_rn(s.prev[q], cv);
+                            *cell = o.counts_only ? t : __fmul_rn(t, o.sd->r2);
+                        }
+                    }
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep)
+                    outl[produced + __popc(m & below)] = make_int4(
+                        s.x[q], __float_as_int(s.mx[q]), __float_as_int(s.acc[q]), __float_as_int(s.cl[q]));
+                produced += __popc(m);
+            }
+        }
+        __syncwarp();  // this level's list and results are visible to every lane
+        in = outl;
+        outl = outl == list0 ? list1 : list0;
+        count = produced;
+    }
+}
+
+__global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
+    extern __shared__ float4 smem4[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * lwarp_floats(a.max_row);
+    float* A = buf + kLPad;
+    float* suf = buf + lrow_pad(a.max_row);
+    float* pre = suf + blocks_pad(a.max_row);
+    const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    int4* list0 = a.lists + gwarp * 2 * (int64_t)a.max_row;
+    int4* list1 = list0 + a.max_row;
+    for (;;) {
+        unsigned idx = 0;
+        if (lane == 0) idx = atomicAdd(a.counter, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if ((int64_t)idx >= a.n_items) break;
+        const Item it = decode(a.items[idx]);
+        const SectorDesc& d = a.g.desc[a.b.angle[it.slot]];
+        const int32_t* first = a.g.first + d.row_off;
+        const int32_t* last = a.g.last + d.row_off;
+        const int f = first[it.row];
+        const int L = last[it.row] - f;
+        if (L > a.max_row || L <= 0) {
+            if (lane == 0) atomicExch(a.status, 1);
+            continue;
+        }
+        RowOut o;
+        o.out = a.SO + it.slot * a.stride;
+        o.rowbase = (int64_t)it.row * d.dim_i + f;
+        o.first = f;
+        o.row = it.row;
+        o.sd = &d;
+        o.rfirst = first;
+        o.rlast = last;
+        o.counts_only = a.counts_only;
+        const float* src = a.SI + it.slot * a.stride + o.rowbase;
+        bool ok = true;
+        for (int x = lane; x < L; x += 32) {
+            const float v = src[x];
+            A[x] = v;
+            ok = ok && div_safe(v) && div_safe(__fadd_rn(v, a.povh));
+        }
+        for (int x = lane; x < kLPad; x += 32) buf[x] = 0.0f;
+        const int tail_end = ((L + 3) & ~3) + kLPad;
+        for (int x = L + lane; x < tail_end; x += 32) A[x] = 0.0f;
+        const bool fast = __all_sync(0xffffffffu, ok) && L <= kLFastMaxRow && div_safe(a.povh);
+        __syncwarp();
+        if (fast) {
+            block_maxima(A, L, suf, pre, lane);
+            __syncwarp();
+            sweep_dir<true>(A, suf, L, a.povh, list0, list1, o, lane);
+            sweep_dir<false>(A, pre, L, a.povh, list0, list1, o, lane);
+        } else {
+            for (int x = lane; x < L; x += 32) {
+                if (!owns(o, x)) continue;
+                const float cv = scan_reference(A, x, L, a.povh);
+                o.out[o.rowbase + x] = a.counts_only ? cv : __fmul_rn(cv, d.r2);
+            }
         }
         __syncwarp();
     }
@@ -427,52 +709,83 @@ struct StepTable {
 
 cudaError_t sdem_init_tables() {
     static const StepTable tab;  // built once, thread-safe, no heap
-    return cudaMemcpyToSymbol(c_step, tab.v, sizeof(tab.v));
+    static float2 recip[kFastMaxRow];
+    for (int n = 0; n < kFastMaxRow; n++) recip[n] = make_float2(tab.v[n].x, tab.v[n].y);
+    cudaError_t e = cudaMemcpyToSymbol(c_step, tab.v, sizeof(tab.v));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_recip, recip, sizeof(recip));
+    return e;
 }
 
 void sdem_items(const Geometry& geo, const Batch& b, std::vector<uint64_t>& items, int* max_row) {
-    // Counting sort of rows by valid length, longest first: every chunk of a row
-    // costs about L + 126 warp steps, so long rows go first.
+    // Counting sort of rows by valid length, longest first: a row's work grows
+    // about as L^2, so long rows go first.
     int lmax = 0;
     for (int s = 0; s < b.count; s++) {
         const SectorDesc& d = geo.desc[b.angle[s]];
         for (int r = 0; r < d.H; r++) lmax = std::max(lmax, geo.last[d.row_off + r] - geo.first[d.row_off + r]);
     }
-    std::vector<int64_t> bucket(lmax + 2, 0);
+    std::vector<int64_t> start(lmax + 2, 0);
     for (int s = 0; s < b.count; s++) {
         const SectorDesc& d = geo.desc[b.angle[s]];
         for (int r = 0; r < d.H; r++) {
             const int L = geo.last[d.row_off + r] - geo.first[d.row_off + r];
-            if (L > 0) bucket[L] += (L + kChunk - 1) / kChunk;
+            if (L > 0) start[L]++;
         }
     }
-    std::vector<int64_t> start(lmax + 2, 0);
     int64_t total = 0;
     for (int L = lmax; L >= 1; L--) {
+        const int64_t cnt = start[L];
         start[L] = total;
-        total += bucket[L];
+        total += cnt;
     }
     items.assign(total, 0);
     for (int s = 0; s < b.count; s++) {
         const SectorDesc& d = geo.desc[b.angle[s]];
         for (int r = 0; r < d.H; r++) {
             const int L = geo.last[d.row_off + r] - geo.first[d.row_off + r];
-            if (L <= 0) continue;
-            const int nc = (L + kChunk - 1) / kChunk;
-            for (int c = 0; c < nc; c++)
-                items[start[L]++] = ((uint64_t)s << 48) | ((uint64_t)(uint32_t)r << 16) | (uint64_t)c;
+            if (L > 0) items[start[L]++] = ((uint64_t)s << 48) | ((uint64_t)(uint32_t)r << 16);
         }
     }
     *max_row = lmax;
 }
 
+size_t sdem_list_bytes(int max_row, int num_sms) {
+    // Two lists of max_row entries per warp, for as many warps as an SM holds.
+    int dev = 0, threads = 2048;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    return (size_t)num_sms * (size_t)(threads / 32) * 2 * (size_t)std::max(max_row, 1) * sizeof(int4);
+}
+
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (a.n_items == 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * (size_t)warp_floats(a.max_row) * kWarps;
+    const size_t smem = sizeof(float) * (size_t)lwarp_floats(a.max_row) * kLWarps;
     cudaError_t e = cudaFuncSetAttribute(k_sdem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdem, kWarps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdem, kLWarps * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int64_t blocks = (int64_t)per_sm * num_sms;
+    const int64_t need = (a.n_items + kLWarps - 1) / kLWarps;
+    if (blocks > need) blocks = need;
+    // Every warp owns two lists of max_row entries in the scratch.
+    const size_t list_per_block = (size_t)kLWarps * 2 * (size_t)a.max_row * sizeof(int4);
+    const int64_t fit = a.lists ? (int64_t)(a.list_bytes / list_per_block) : 0;
+    if (fit < 1) return cudaErrorInvalidValue;
+    if (blocks > fit) blocks = fit;
+    e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_sdem<<<(int)blocks, kLWarps * 32, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sdem_chunked(const SdemLaunch& a, int num_sms, cudaStream_t st) {
+    if (a.n_items == 0) return cudaSuccess;
+    const size_t smem = sizeof(float) * (size_t)warp_floats(a.max_row) * kWarps;
+    cudaError_t e = cudaFuncSetAttribute(k_sdem_chunked, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdem_chunked, kWarps * 32, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     int64_t blocks = (int64_t)per_sm * num_sms;
@@ -480,7 +793,7 @@ cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (blocks > need) blocks = need;
     e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_sdem<<<(int)blocks, kWarps * 32, smem, st>>>(a);
+    k_sdem_chunked<<<(int)blocks, kWarps * 32, smem, st>>>(a);
     return cudaGetLastError();
 }
 

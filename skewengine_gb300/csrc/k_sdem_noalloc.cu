@@ -157,12 +157,14 @@ extern "C" int ske_sdem_sector_noalloc(int device, const float* skew_in, float* 
     a.stride = 0;
     a.items = d_items;
     a.n_items = total;
-    a.counter = d_counter;  // cleared by launch_sdem
+    a.counter = d_counter;  // cleared by launch_sdem_chunked
     a.povh = povh;
     a.max_row = std::max(lmax, 1);
     a.counts_only = 0;
     a.status = d_status;
-    e = launch_sdem(a, sms, st);
+    a.lists = nullptr;
+    a.list_bytes = 0;
+    e = launch_sdem_chunked(a, sms, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&h_status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e);

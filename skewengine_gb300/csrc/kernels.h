@@ -62,11 +62,19 @@ struct SdemLaunch {
     int max_row;        // longest valid row length of the batch
     int counts_only;    // 1: write integer cv instead of cv*r2
     int* status;        // device error word (0 = ok)
+    int4* lists;        // survivor-list scratch (compacting sweep only)
+    size_t list_bytes;  // its size; at least sdem_list_bytes(max_row, num_sms)
 };
+// Compacting sweep (the engine's): items are (slot, row), one per valid row.
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st);
-// Work items of a batch, longest first: (slot, row, chunk of 128 observers).
+// Bytes of survivor-list scratch launch_sdem needs for rows up to max_row cells.
+size_t sdem_list_bytes(int max_row, int num_sms);
+// Work items of a batch for launch_sdem, longest row first: (slot, row).
 void sdem_items(const struct Geometry& geo, const Batch& b, std::vector<uint64_t>& items,
                 int* max_row);
+// Chunked sweep (the allocation-free entry point's): items are (slot, row,
+// chunk of sdem_chunk() observers); needs no scratch beyond the item list.
+cudaError_t launch_sdem_chunked(const SdemLaunch& a, int num_sms, cudaStream_t st);
 int sdem_chunk();
 
 // Radon / filtered back-projection (k_radon.cu).  P: per-slot complex scratch
