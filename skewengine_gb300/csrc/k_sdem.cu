@@ -401,9 +401,39 @@ static_assert(kSlots == 2, "level_steps packs exactly one pair per lane");
 // {-n, RN(1/n)} for n = 0..4095, for lane-divergent lookups (the a < 0 bound).
 __device__ float2 g_recip[kFastMaxRow];
 
+// Retirement bound terms: kT blocks of kB1 cells, then kT blocks of kB2 cells,
+// then the suffix (prefix) maximum of everything beyond.
+constexpr int kB1 = 16, kB1Log = 4;
+constexpr int kB2 = 128, kB2Log = 7;
+constexpr int kT = 4;
+constexpr int kMPad = 8;  // -inf entries on both sides of the kB1 and kB2 maxima
+// 1 - 2^-20: the factor that keeps fl(fl(mx * kShrink) * ds) below mx * ds.
+constexpr float kShrink = 0.99999904632568359375f;
+
 __host__ __device__ inline int lrow_pad(int max_row) { return kLPad + ((max_row + 3) & ~3) + kLPad; }
-// Shared floats per warp: the padded row plus suffix and prefix block maxima.
-__host__ __device__ inline int lwarp_floats(int max_row) { return lrow_pad(max_row) + 2 * blocks_pad(max_row); }
+__host__ __device__ inline int nblk(int max_row, int size) { return (max_row + size - 1) / size; }
+
+// Per-warp shared memory of the compacting sweep, in floats from the warp's base:
+// the padded row; suffix maxima of kBlk-cell blocks (one -inf entry after);
+// prefix maxima (one -inf entry before); kB1-cell and kB2-cell block maxima
+// (kMPad -inf entries on both sides).
+struct LLayout {
+    int suf, pre, b16, b128, total;
+    __host__ __device__ explicit LLayout(int max_row) {
+        const int n8 = nblk(max_row, kBlk), n16 = nblk(max_row, kB1), n128 = nblk(max_row, kB2);
+        suf = lrow_pad(max_row);
+        pre = suf + n8 + 2;
+        b16 = pre + n8 + kMPad;
+        b128 = b16 + n16 + 2 * kMPad;
+        total = b128 + n128 + kMPad;
+    }
+};
+
+// The block maxima of the row being swept.
+struct RowMax {
+    const float *suf, *pre, *b16, *b128;
+    int n8;
+};
 
 // One lane's observers of a batch, in one scan direction.
 struct Slots {
@@ -468,10 +498,87 @@ __device__ __forceinline__ bool owns(const RowOut& o, int x) {
     return o.first + x < o.sd->dim_i || owner_row(*o.sd, o.rfirst, o.rlast, o.rowbase + x) == o.row;
 }
 
+// kB1- and kB2-cell block maxima of the row, the -inf padding of every maxima
+// array, after block_maxima has filled suf and pre.
+__device__ void coarse_maxima(const float* __restrict__ A, int L, float* suf, float* pre, float* b16, float* b128,
+                              int lane) {
+    const float ninf = __int_as_float(0xff800000);
+    const int n8 = nblk(L, kBlk), n16 = nblk(L, kB1), n128 = nblk(L, kB2);
+    for (int b = lane; b < n16; b += 32) {
+        float m = ninf;
+        for (int c = b * kB1; c < min(b * kB1 + kB1, L); c++) m = fmaxf(m, A[c]);
+        b16[b] = m;
+    }
+    if (lane < kMPad) {
+        b16[-1 - lane] = ninf;
+        b16[n16 + lane] = ninf;
+        b128[-1 - lane] = ninf;
+        b128[n128 + lane] = ninf;
+    }
+    if (lane == 0) {
+        suf[n8] = ninf;
+        pre[-1] = ninf;
+    }
+    __syncwarp();
+    constexpr int kPer = kB2 / kB1;
+    for (int b = lane; b < n128; b += 32) {
+        float m = ninf;
+        for (int c = b * kPer; c < min(b * kPer + kPer, n16); c++) m = fmaxf(m, b16[c]);
+        b128[b] = m;
+    }
+}
+
+// Retirement test after step dc: true when no target beyond distance dc can be
+// visible from observer x (n steps in this direction, height h, horizon mx).
+//  * mx < 0: every remaining slope is at most fl(a/n), a = fl(Smax - h) < 0
+//    (Smax the suffix or prefix maximum), as in the header.
+//  * mx >= 0: a block of remaining targets with maximum M and nearest
+//    remaining distance ds holds no visible target when
+//    M - h <= fl(fl(mx * kShrink) * ds): that product is below mx * ds, so
+//    every target u = fl(z - h) <= M - h at distance d' >= ds has
+//    u / d' <= mx (u >= 0) or u / d' < 0 <= mx (u < 0), and fl(u / d') <= mx.
+//    The blocks: kT of kB1 cells from the one holding the nearest target, kT
+//    of kB2 cells from the next uncovered cell, and the suffix (prefix) maximum
+//    beyond.  Blocks past the row end read -inf.
+template <bool kFwd>
+__device__ __forceinline__ bool retire(const RowMax& rm, int x, int n, int dc, float h, float mx) {
+    const int k = kFwd ? x + dc + 1 : x - dc - 1;  // nearest remaining target
+    if (mx < 0.0f) {
+        const float a = __fsub_rn(kFwd ? rm.suf[k >> 3] : rm.pre[k >> 3], h);
+        if (!(a < 0.0f)) return false;
+        const float2 t = g_recip[n];
+        return div_fast(a, t.x, t.y) <= mx;
+    }
+    const float mxc = __fmul_rn(mx, kShrink);
+    int b = k >> kB1Log;
+    bool ok = __fsub_rn(rm.b16[b], h) <= __fmul_rn(mxc, __int2float_rn(dc + 1));
+    float ds = __int2float_rn(kFwd ? (b + 1) * kB1 - x : x - (b * kB1 - 1));
+#pragma unroll
+    for (int j = 1; j < kT; j++) {
+        b += kFwd ? 1 : -1;
+        ok &= __fsub_rn(rm.b16[b], h) <= __fmul_rn(mxc, ds);
+        ds = __fadd_rn(ds, (float)kB1);
+    }
+    int c = kFwd ? (b + 1) * kB1 : b * kB1 - 1;  // first uncovered cell
+    int b2 = c >> kB2Log;                          // arithmetic shift: floor
+    ok &= __fsub_rn(rm.b128[b2], h) <= __fmul_rn(mxc, __int2float_rn(kFwd ? c - x : x - c));
+    ds = __int2float_rn(kFwd ? (b2 + 1) * kB2 - x : x - (b2 * kB2 - 1));
+#pragma unroll
+    for (int j = 1; j < kT; j++) {
+        b2 += kFwd ? 1 : -1;
+        ok &= __fsub_rn(rm.b128[b2], h) <= __fmul_rn(mxc, ds);
+        ds = __fadd_rn(ds, (float)kB2);
+    }
+    c = kFwd ? (b2 + 1) * kB2 : b2 * kB2 - 1;
+    const int i8 = kFwd ? min(c >> 3, rm.n8) : max(c >> 3, -1);
+    ok &= __fsub_rn(kFwd ? rm.suf[i8] : rm.pre[i8], h) <= __fmul_rn(mxc, ds);
+    return ok;
+}
+
 // All levels of one scan direction of the row.  Level 0 takes every observer
 // 0..L-1; each later level takes the previous level's survivors from a list.
 template <bool kFwd>
-__device__ void sweep_dir(const float* __restrict__ A, const float* __restrict__ bmax, int L, float povh,
+__device__ void sweep_dir(const float* __restrict__ A, const RowMax& rm, int L, float povh,
                           int4* __restrict__ list0, int4* __restrict__ list1, const RowOut& o, int lane) {
     const unsigned below = (1u << lane) - 1u;
     const int4* in = nullptr;
@@ -537,19 +644,7 @@ __device__ void sweep_dir(const float* __restrict__ A, const float* __restrict__
                 if (s.valid[q]) {
                     bool done = false;
                     if (s.n[q] > dc) {
-                        const int k = kFwd ? s.x[q] + dc + 1 : s.x[q] - dc - 1;
-                        const float a = __fsub_rn(bmax[k / kBlk], s.h[q]);
-                        float negd, y;
-                        if (a >= 0.0f) {
-                            const float4 st = c_step[dc + 1];
-                            negd = st.x;
-                            y = st.y;
-                        } else {
-                            const float2 t = g_recip[s.n[q]];
-                            negd = t.x;
-                            y = t.y;
-                        }
-                        done = div_fast(a, negd, y) <= s.mx[q];
+                        done = retire<kFwd>(rm, s.x[q], s.n[q], dc, s.h[q], s.mx[q]);
                         keep = !done;
                     }
                     if (!keep && owns(o, s.x[q])) {
@@ -580,10 +675,13 @@ __device__ void sweep_dir(const float* __restrict__ A, const float* __restrict__
 __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
     extern __shared__ float4 smem4[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * lwarp_floats(a.max_row);
+    const LLayout lay(a.max_row);
+    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * lay.total;
     float* A = buf + kLPad;
-    float* suf = buf + lrow_pad(a.max_row);
-    float* pre = suf + blocks_pad(a.max_row);
+    float* suf = buf + lay.suf;
+    float* pre = buf + lay.pre;
+    float* b16 = buf + lay.b16;
+    float* b128 = buf + lay.b128;
     const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
     int4* list0 = a.lists + gwarp * 2 * (int64_t)a.max_row;
     int4* list1 = list0 + a.max_row;
@@ -626,8 +724,11 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
         if (fast) {
             block_maxima(A, L, suf, pre, lane);
             __syncwarp();
-            sweep_dir<true>(A, suf, L, a.povh, list0, list1, o, lane);
-            sweep_dir<false>(A, pre, L, a.povh, list0, list1, o, lane);
+            coarse_maxima(A, L, suf, pre, b16, b128, lane);
+            __syncwarp();
+            const RowMax rm{suf, pre, b16, b128, nblk(L, kBlk)};
+            sweep_dir<true>(A, rm, L, a.povh, list0, list1, o, lane);
+            sweep_dir<false>(A, rm, L, a.povh, list0, list1, o, lane);
         } else {
             for (int x = lane; x < L; x += 32) {
                 if (!owns(o, x)) continue;
@@ -758,7 +859,7 @@ size_t sdem_list_bytes(int max_row, int num_sms) {
 
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (a.n_items == 0) return cudaSuccess;
-    const size_t smem = sizeof(float) * (size_t)lwarp_floats(a.max_row) * kLWarps;
+    const size_t smem = sizeof(float) * (size_t)LLayout(a.max_row).total * kLWarps;
     cudaError_t e = cudaFuncSetAttribute(k_sdem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
