@@ -392,7 +392,7 @@ constexpr int kSlots = 2;   // observers per lane in a batch (one packed pair)
 static_assert(kLevel % kUnroll == 0, "a level is whole blocks");
 constexpr int kBatch = 32 * kSlots;
 constexpr int kLWarps = 4;  // warps per CTA
-constexpr int kLPad = 64;   // zero cells on both sides of the row (>= kLevel - 1)
+constexpr int kLPad = 64;   // NaN cells on both sides of the row (>= kLevel - 1)
 // Longest row on the fast path: every step distance a level touches (at most
 // the last survivor's n + kLevel) stays inside the constant table.
 constexpr int kLFastMaxRow = kFastMaxRow - kLevel;
@@ -444,20 +444,22 @@ struct Slots {
     float prev[kSlots];  // backward pass: the forward result held in the output cell
 };
 
+// Visibility update.  The comparison is unordered (true for a NaN slope): a
+// step past the observer's last target reads the row's NaN padding, counts as
+// visible and so leaves cl, the only value a finished observer keeps, as it
+// was.  For finite slopes it is the reference's sl > mx.
 __device__ __forceinline__ void visit(Slots& s, int q, float sl, float ring) {
-    const bool above = sl > s.mx[q];
+    const bool above = !(sl <= s.mx[q]);
     s.mx[q] = above ? sl : s.mx[q];
     s.cl[q] = above ? s.cl[q] : s.acc[q];
     s.acc[q] = above ? __fadd_rn(s.acc[q], ring) : s.acc[q];
 }
 
-// Steps d0 .. d0+kLevel-1 of the lane's two observers.  kTail: some observer of
-// the warp ends inside the level; its later steps are skipped.  Reads run at
-// most kLevel-1 cells past an observer's last target, into the row's zero
-// padding.  The level runs as a loop over blocks of kUnroll steps: fully
-// unrolled levels overflow the instruction cache (four copies: two directions,
-// with and without the tail test).
-template <bool kFwd, bool kTail>
+// Steps d0 .. d0+kLevel-1 of the lane's two observers.  An observer that ends
+// inside the level reads at most kLevel-1 cells of the row's NaN padding (see
+// visit).  The level runs as a loop over blocks of kUnroll steps: fully
+// unrolled levels overflow the instruction cache.
+template <bool kFwd>
 __device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0) {
     const float* p0 = A + (kFwd ? s.x[0] + d0 : s.x[0] - d0);
     const float* p1 = A + (kFwd ? s.x[1] + d0 : s.x[1] - d0);
@@ -472,8 +474,8 @@ __device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ 
             const float z1 = kFwd ? p1[k] : p1[-k];
             float q0, q1;
             upk(div2(sub2(pk(z0, z1), hh), pk(st.x, st.x), pk(st.y, st.y)), q0, q1);
-            if (!kTail || d <= s.n[0]) visit(s, 0, q0, st.z);
-            if (!kTail || d <= s.n[1]) visit(s, 1, q1, st.z);
+            visit(s, 0, q0, st.z);
+            visit(s, 1, q1, st.z);
         }
         p0 += kFwd ? kUnroll : -kUnroll;
         p1 += kFwd ? kUnroll : -kUnroll;
@@ -603,7 +605,6 @@ __device__ void sweep_dir(const float* __restrict__ A, const RowMax& rm, int L, 
                 nxt[q] = (in && idx < count) ? in[idx] : make_int4(0, 0, 0, 0);
             }
             Slots s;
-            bool tail = false;
 #pragma unroll
             for (int q = 0; q < kSlots; q++) {
                 const int idx = base + lane + 32 * q;
@@ -625,17 +626,14 @@ __device__ void sweep_dir(const float* __restrict__ A, const RowMax& rm, int L, 
                     s.h[q] = __fadd_rn(A[s.x[q]], povh);
                     s.prev[q] = kFwd ? 0.0f : o.out[o.rowbase + s.x[q]];
                 } else {
-                    // Empty: its reads stay in A[-(kLevel-1) .. kLevel-1]; it needs
-                    // no tail test.
+                    // Empty: its reads stay in A[-(kLevel-1) .. kLevel-1].
                     s.x[q] = kFwd ? -d0 : d0;
                     s.n[q] = dc;
                     s.valid[q] = false;
                     s.h[q] = s.mx[q] = s.acc[q] = s.cl[q] = s.prev[q] = 0.0f;
                 }
-                tail = tail || s.n[q] < dc;
             }
-            if (__any_sync(0xffffffffu, tail)) level_steps<kFwd, true>(s, A, d0);
-            else level_steps<kFwd, false>(s, A, d0);
+            level_steps<kFwd>(s, A, d0);
 
             // Retire finished observers, keep the others for the next level.
 #pragma unroll
@@ -716,9 +714,10 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
             A[x] = v;
             ok = ok && div_safe(v) && div_safe(__fadd_rn(v, a.povh));
         }
-        for (int x = lane; x < kLPad; x += 32) buf[x] = 0.0f;
+        const float pad = __int_as_float(0x7fc00000);  // NaN (see visit)
+        for (int x = lane; x < kLPad; x += 32) buf[x] = pad;
         const int tail_end = ((L + 3) & ~3) + kLPad;
-        for (int x = L + lane; x < tail_end; x += 32) A[x] = 0.0f;
+        for (int x = L + lane; x < tail_end; x += 32) A[x] = pad;
         const bool fast = __all_sync(0xffffffffu, ok) && L <= kLFastMaxRow && div_safe(a.povh);
         __syncwarp();
         if (fast) {
