@@ -49,6 +49,11 @@ extern "C" {
 #define SKE_KERNEL_RADON 2       /* Radon + filtered back-projection, kernelRADN.h:213*/
 #define SKE_KERNEL_IDENTITYIMG 3 /* identity, kernelUNIT.h:16                         */
 #define SKE_KERNEL_CEPSTRUM 4    /* cepstrum blur estimation, kernelBLUR.h:267        */
+/* The reference's Radon operator with its LRT switch set (kernelRADN.h:212-220):
+   the local Radon transform pointRadon (kernelRADN.h:114-182) of every skewed
+   cell, added back like the global transform.  The reference has no operator id
+   for it; 5 follows its enum. */
+#define SKE_KERNEL_LOCAL_RADON 5
 
 /* Cross-sector accumulation of the additive operators. */
 #define SKE_ACCUM_REFERENCE 0 /* float adds in sector order, bit-identical to the

@@ -169,4 +169,12 @@ int skref_sector(int alg, const float* input, int dx, int dy, int angle, float p
     return 0;
 }
 
+// The reference's Radon operator switch (kernelRADN.h:212, `bool LRT`): false =
+// global Radon / filtered back-projection (the reference default), true = the
+// local Radon transform pointRadon (kernelRADN.h:114-182) per skewed cell.
+int skref_set_local_radon(int on) {
+    LRT = on != 0;
+    return 0;
+}
+
 }  // extern "C"

@@ -233,6 +233,51 @@ void op_cepstrum(const Sector& s, const float* S, float* O) {
 }
 
 // identity (kernelUNIT.h:16-23).
+// pointRadon (kernelRADN.h:114-182), the local Radon transform of one skewed
+// cell (i, j), called for every valid cell when LRT is set (kernelRADN.h:215-220):
+// 64 rows k = i-32 .. i+31, each summed in binary64 over the 65 columns
+// j-32 .. j+32 that lie in the row's valid range (rows outside the grid give 0),
+// weighted by exp(-(k-i)^2 / (2 sigma^2)), sigma = (64/5)/scale; a normalised
+// FFT; the real parts tapered by sin(k/(25.6-1) * pi/2) for k <= 25.6 and zeroed
+// above; a second normalised FFT; and getParameter (kernelRADN.h:89-102): from
+// index 5 the first |v_i|^2 > |v_{i-1}|^2 gives |v_{i-1}|^2, none gives 0.
+const int kLrWin = 64;  // winSize (kernelRADN.h:19)
+float local_radon_cell(const Sector& s, const float* S, int i, int j) {
+    const int w2 = kLrWin / 2;
+    const double dws = kLrWin;
+    double sigma = kLrWin / 5.0;
+    sigma = sigma / s.scale;
+    cplx in1[kLrWin];
+    for (int k = i - w2; k < i + w2; k++) {
+        double accum = 0;
+        if (k >= 0 && k < s.H) {
+            const int fi = s.first[k], la = s.last[k];
+            for (int l = j - w2; l <= j + w2; l++)
+                accum += (l < fi || l >= la) ? 0 : S[(size_t)k * s.dim_i + l];
+        }
+        const int kk = k - (i - w2);
+        const double gauss = exp(-(kk - w2) * (kk - w2) / (2 * sigma * sigma));
+        in1[kk] = {accum * gauss, 0};
+    }
+    fft_dif(in1, kLrWin, true);
+    const double cutoff = 0.4;
+    cplx in2[kLrWin];
+    for (int k = 0; k < kLrWin; k++)
+        in2[k] = k > cutoff * dws ? 0 : sin((k / (cutoff * dws - 1)) * M_PI_2) * in1[k].real();
+    fft_dif(in2, kLrWin, true);
+    double v = 0;
+    int m;
+    for (m = 5; m < w2; m++)
+        if (std::norm(in2[m]) > std::norm(in2[m - 1])) break;
+    if (m < w2) v = std::norm(in2[m - 1]);
+    return (float)v;
+}
+
+void op_local_radon(const Sector& s, const float* S, float* O) {
+    for (int i = 0; i < s.H; i++)
+        for (int j = s.first[i]; j < s.last[i]; j++) O[(size_t)s.dim_i * i + j] = local_radon_cell(s, S, i, j);
+}
+
 void op_identity(const Sector& s, const float* S, float* O) {
     for (int row = 0; row < s.H; row++)
         for (int j = s.first[row]; j < s.last[row]; j++)
@@ -244,6 +289,7 @@ void run_operator(int op, const Sector& s, const float* S, float* O, float povh)
         case PORT_SDEM: op_sdem(s, S, O, povh, false); break;
         case PORT_RADON: op_radon(s, S, O); break;
         case PORT_CEPSTRUM: op_cepstrum(s, S, O); break;
+        case PORT_LOCAL_RADON: op_local_radon(s, S, O); break;
         default: op_identity(s, S, O); break;
     }
 }

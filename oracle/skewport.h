@@ -14,8 +14,11 @@
 extern "C" {
 #endif
 
-// Operator ids follow the reference KERNELS enum (src/global.h:77).
-enum { PORT_SDEM = 0, PORT_IDENTITYDEM = 1, PORT_RADON = 2, PORT_IDENTITYIMG = 3, PORT_CEPSTRUM = 4 };
+// Operator ids follow the reference KERNELS enum (src/global.h:77); 5 is the
+// reference's Radon operator with LRT set (kernelRADN.h:212-220), the local Radon
+// transform.
+enum { PORT_SDEM = 0, PORT_IDENTITYDEM = 1, PORT_RADON = 2, PORT_IDENTITYIMG = 3, PORT_CEPSTRUM = 4,
+       PORT_LOCAL_RADON = 5 };
 
 // Per-sector geometry, restating skewEngine::computeParams (skewEngine.cuh:504-539)
 // and skewEngine::skewShape (skewEngine.cuh:573-596).

@@ -2,15 +2,16 @@
 
 For every angle the engine skews a 2-D grid so lines at that angle become memory
 rows, runs a per-row operator (total viewshed, Radon / filtered back-projection,
-cepstrum blur estimation, identity), deskews the result and accumulates it.  The
+local Radon transform, cepstrum blur estimation, identity), deskews the result and accumulates it.  The
 compute runs as hand-written sm_103a CUDA kernels behind the C ABI in
 ``include/skewengine.h``; this package is its Python host interface.
 """
 from .engine import (ACCUM_KAHAN, ACCUM_REFERENCE, DEFAULT_POVH, KERNEL_CEPSTRUM, KERNEL_IDENTITYDEM,
-                     KERNEL_IDENTITYIMG, KERNEL_RADON, KERNEL_SDEM, KERNELS, SkewEngine, cli_run, device_count,
-                     execute, geometry, params, run_batch)
+                     KERNEL_IDENTITYIMG, KERNEL_LOCAL_RADON, KERNEL_RADON, KERNEL_SDEM, KERNELS, SkewEngine,
+                     cli_run, device_count, execute, geometry, params, run_batch)
 from ._lib import SkeError
 
 __all__ = ["SkewEngine", "SkeError", "execute", "run_batch", "geometry", "params", "device_count", "cli_run",
            "KERNEL_SDEM", "KERNEL_IDENTITYDEM", "KERNEL_RADON", "KERNEL_IDENTITYIMG", "KERNEL_CEPSTRUM",
+           "KERNEL_LOCAL_RADON",
            "KERNELS", "ACCUM_REFERENCE", "ACCUM_KAHAN", "DEFAULT_POVH"]

@@ -3,8 +3,8 @@
 //
 //   run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]
 //
-//   kernel     sdem | identitydem | radon | identityimg | cepstrum, or 0..4
-//              (KERNELS enum, src/global.h:77)
+//   kernel     sdem | identitydem | radon | identityimg | cepstrum | localradon,
+//              or 0..5 (KERNELS enum, src/global.h:77; 5 = radon with LRT set)
 //   input      raw little-endian float32 grid (dimy rows of dimx), or an ESRI
 //              .bil int16 grid whose values are divided by 10 as readBilData does
 //              (src/kernelSDEM.h:43-50); dimx/dimy 0 take NCOLS/NROWS from the
@@ -28,12 +28,12 @@
 namespace {
 
 int parse_kernel(const char* s) {
-    static const char* names[] = {"sdem", "identitydem", "radon", "identityimg", "cepstrum"};
-    for (int i = 0; i < 5; i++)
+    static const char* names[] = {"sdem", "identitydem", "radon", "identityimg", "cepstrum", "localradon"};
+    for (int i = 0; i < 6; i++)
         if (!strcmp(s, names[i])) return i;
     char* end = nullptr;
     long v = strtol(s, &end, 10);
-    if (end && *end == 0 && v >= 0 && v <= 4) return (int)v;
+    if (end && *end == 0 && v >= SKE_KERNEL_SDEM && v <= SKE_KERNEL_LOCAL_RADON) return (int)v;
     return -1;
 }
 

@@ -53,7 +53,7 @@ int ensure_device_tables(int device) {
     return SKE_OK;
 }
 
-bool valid_kernel(int k) { return k >= SKE_KERNEL_SDEM && k <= SKE_KERNEL_CEPSTRUM; }
+bool valid_kernel(int k) { return k >= SKE_KERNEL_SDEM && k <= SKE_KERNEL_LOCAL_RADON; }
 
 template <typename T>
 int dev_alloc(T** p, size_t count) {
@@ -97,6 +97,7 @@ struct ske_engine_s {
     double* d_tw = nullptr;
     int64_t* d_tw_off = nullptr;
     int64_t tw_off_host[32] = {0};
+    int64_t lr_gauss_off = 0, lr_taper_off = 0;  // local Radon tables inside d_tw
     unsigned* d_counter = nullptr;
     int* d_status = nullptr;
     int4* d_lists = nullptr;  // survivor lists of the viewshed sweep
@@ -335,6 +336,13 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             return ls.done(launch_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_P, e->pstride, e->d_tw,
                                         e->d_tw_off, e->max_H2, e->stream));
         }
+        case SKE_KERNEL_LOCAL_RADON: {
+            SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
+            LaunchScope ls(e, "local_radon", 1);
+            return ls.done(launch_local_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->geo.max_H,
+                                              std::max(e->dimx, e->dimy), e->d_tw + e->lr_gauss_off,
+                                              e->d_tw + e->lr_taper_off, e->d_tw + e->tw_off_host[6], e->stream));
+        }
         case SKE_KERNEL_CEPSTRUM: {
             LaunchScope ls(e, "cepstrum", 1);
             return ls.done(launch_cepstrum(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_tw + e->tw_off_host[6],
@@ -569,6 +577,13 @@ int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream,
         fft_twiddles(1u << k, tw);
         all.insert(all.end(), tw.begin(), tw.end());
     }
+    // Local Radon weights (180 x 64) and taper.
+    std::vector<double> gauss, taper;
+    local_radon_tables(e->geo, gauss, taper);
+    e->lr_gauss_off = (int64_t)all.size();
+    all.insert(all.end(), gauss.begin(), gauss.end());
+    e->lr_taper_off = (int64_t)all.size();
+    all.insert(all.end(), taper.begin(), taper.end());
     all.push_back(0.0);
     SKE_TRY(dev_alloc(&e->d_tw, all.size()));
     SKE_TRY(dev_alloc(&e->d_tw_off, 32));

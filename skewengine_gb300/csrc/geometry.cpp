@@ -108,4 +108,18 @@ void fft_twiddles(unsigned n, std::vector<double>& re_im) {
     }
 }
 
+void local_radon_tables(const Geometry& g, std::vector<double>& gauss, std::vector<double>& taper) {
+    const int w2 = kLocalRadonWindow / 2;
+    gauss.assign((size_t)kLocalRadonWindow * g.desc.size(), 0.0);
+    for (size_t a = 0; a < g.desc.size(); a++) {
+        double sigma = kLocalRadonWindow / 5.0;  // kernelRADN.h:123-126
+        sigma = sigma / g.desc[a].scale;
+        for (int kk = 0; kk < kLocalRadonWindow; kk++)  // kernelRADN.h:138
+            gauss[a * kLocalRadonWindow + kk] = exp(-(kk - w2) * (kk - w2) / (2 * sigma * sigma));
+    }
+    const double dws = kLocalRadonWindow, cutoff = 0.4;  // kernelRADN.h:157-161
+    taper.assign(kLocalRadonKeep, 0.0);
+    for (int k = 0; k < kLocalRadonKeep; k++) taper[k] = sin((k / (cutoff * dws - 1)) * M_PI_2);
+}
+
 }  // namespace ske

@@ -21,32 +21,6 @@ namespace {
 constexpr int kWin = kBlurWindow;  // 64
 constexpr int kWarpsPerBlock = 8;
 
-// DIF FFT of x[0..n) (n <= 64) by one warp, in place, then bit reversal.
-__device__ __forceinline__ void warp_fft(cd* x, int n, const double* __restrict__ tw, int lane) {
-    for (int h = n >> 1; h >= 1; h >>= 1) {
-        const double* t = tw + 2 * (n - 2 * h);
-        for (int k = lane; k < (n >> 1); k += 32) {
-            const int l = k & (h - 1);
-            const int a = (k / h) * 2 * h + l;
-            const int bb = a + h;
-            const cd xa = x[a], xb = x[bb];
-            x[a] = cadd(xa, xb);
-            x[bb] = cmul(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
-        }
-        __syncwarp();
-    }
-    const unsigned bits = 31 - __clz(n);
-    for (int i = lane; i < n; i += 32) {
-        const int j = (int)bitrev((unsigned)i, bits);
-        if (j > i) {
-            const cd tmp = x[i];
-            x[i] = x[j];
-            x[j] = tmp;
-        }
-    }
-    __syncwarp();
-}
-
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_cepstrum(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO, int64_t stride,
                int64_t len, const double* __restrict__ tw64, const double* __restrict__ tw32) {

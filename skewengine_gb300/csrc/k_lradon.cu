@@ -1,0 +1,143 @@
+// Local Radon transform (pointRadon, src/kernelRADN.h:114-182), the reference's
+// Radon operator with its LRT switch set (kernelRADN.h:212-220).
+//
+// For every valid skewed cell (i, j) of a sector:
+//   W(k, j) = sum over l = j-32 .. j+32 of S[k, l]   (binary64, in increasing l;
+//             columns outside row k's valid range and rows outside the grid add 0)
+//   x[m]    = W(i-32+m, j) * gauss[m],  m < 64,  gauss from the sector's scale
+//   X       = FFT(x) / 8;  Y[k] = taper[k] * Re X[k] for k <= 25, else 0
+//   Z       = FFT(Y) / 8;  out = getParameter(Z): from m = 5 the first
+//             |Z_m|^2 > |Z_{m-1}|^2 gives |Z_{m-1}|^2 (none: 0), stored as float.
+//
+// GB300 mapping
+//  * W(k, j) is shared by the 64 cells (k-32 .. k+31, j): a CTA takes a tile of
+//    kTI x kTJ cells, stages the skewed rows it needs (kTI+63 rows, kTJ+64
+//    columns, zeros outside the valid ranges) in shared memory and forms every
+//    W of the tile once, each as the reference's sequential binary64 sum, so
+//    the result is the reference's to the bit.
+//  * One warp per cell then gathers its column of 64 W values, applies the
+//    weights and runs both 64-point FFTs with one butterfly per lane per stage
+//    (warp_fft: the reference's DIF order and twiddle sequence, binary64,
+//    no fused operations).  The 1/sqrt(64) scaling is the reference's complex
+//    multiplication by (0.125, 0).
+//  * The Gaussian weights and the taper use host libm (local_radon_tables), as
+//    the reference computes them on the host.
+//  * Output cells past a row's span of the flat grid belong to the last row
+//    covering them (owner_row), as in the reference's row-order writes.
+#include "kernels.h"
+
+namespace ske {
+
+namespace {
+
+constexpr int kW = kLocalRadonWindow;  // 64
+constexpr int kHalf = kW / 2;          // 32
+constexpr int kTI = 32;                // cell rows per tile
+constexpr int kTJ = 32;                // cell columns per tile
+constexpr int kRows = kTI + kW - 1;    // W rows a tile needs
+constexpr int kCols = kTJ + kW;        // staged columns: kTJ windows of 65
+constexpr int kWarps = 8;
+
+struct Smem {
+    float s[kRows][kCols];
+    double w[kRows][kTJ];
+    cd x[kWarps][kW];
+    double gauss[kW];
+    double taper[kLocalRadonKeep];
+    double tw[2 * (kW - 1)];
+};
+
+__global__ void __launch_bounds__(kWarps * 32)
+    k_lradon(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO, int64_t stride,
+             int tiles_j, const double* __restrict__ gauss_all, const double* __restrict__ taper,
+             const double* __restrict__ tw64) {
+    extern __shared__ double smem_d[];
+    Smem& sm = *reinterpret_cast<Smem*>(smem_d);
+    const int slot = blockIdx.y;
+    const SectorDesc& d = g.desc[b.angle[slot]];
+    const int i0 = (blockIdx.x / tiles_j) * kTI, j0 = (blockIdx.x % tiles_j) * kTJ;
+    if (i0 >= d.H) return;
+    const int32_t* first = g.first + d.row_off;
+    const int32_t* last = g.last + d.row_off;
+    // Skip tiles without a valid cell.
+    int any = 0;
+    for (int r = threadIdx.x; r < kTI; r += blockDim.x) {
+        const int i = i0 + r;
+        if (i < d.H && first[i] < j0 + kTJ && last[i] > j0 && first[i] < last[i]) any = 1;
+    }
+    if (!__syncthreads_or(any)) return;
+
+    const float* in = SI + slot * stride;
+    for (int t = threadIdx.x; t < kRows * kCols; t += blockDim.x) {
+        const int r = t / kCols, c = t % kCols;
+        const int k = i0 - kHalf + r, l = j0 - kHalf + c;
+        float v = 0.0f;
+        if (k >= 0 && k < d.H && l >= first[k] && l < last[k]) v = in[(int64_t)k * d.dim_i + l];
+        sm.s[r][c] = v;
+    }
+    for (int t = threadIdx.x; t < kW; t += blockDim.x) sm.gauss[t] = gauss_all[(int64_t)b.angle[slot] * kW + t];
+    for (int t = threadIdx.x; t < kLocalRadonKeep; t += blockDim.x) sm.taper[t] = taper[t];
+    for (int t = threadIdx.x; t < 2 * (kW - 1); t += blockDim.x) sm.tw[t] = tw64[t];
+    __syncthreads();
+    for (int t = threadIdx.x; t < kRows * kTJ; t += blockDim.x) {
+        const int r = t / kTJ, c = t % kTJ;
+        double acc = 0.0;
+        for (int m = 0; m <= kW; m++) acc = __dadd_rn(acc, (double)sm.s[r][c + m]);
+        sm.w[r][c] = acc;
+    }
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    cd* x = sm.x[warp];
+    const cd scale{0.125, 0.0};  // 1/sqrt(64) (helper.h:102-104)
+    float* out = SO + slot * stride;
+    for (int cell = warp; cell < kTI * kTJ; cell += kWarps) {
+        const int ci = cell / kTJ, cj = cell % kTJ;
+        const int i = i0 + ci, j = j0 + cj;
+        if (i >= d.H || j < first[i] || j >= last[i]) continue;  // warp-uniform
+        const int64_t p = (int64_t)i * d.dim_i + j;
+        if (j >= d.dim_i && owner_row(d, first, last, p) != i) continue;
+        for (int m = lane; m < kW; m += 32) x[m] = cd{__dmul_rn(sm.w[ci + m][cj], sm.gauss[m]), 0.0};
+        __syncwarp();
+        warp_fft(x, kW, sm.tw, lane);
+        for (int m = lane; m < kW; m += 32) {
+            const double re = cmul(x[m], scale).re;
+            x[m] = cd{m < kLocalRadonKeep ? __dmul_rn(sm.taper[m], re) : 0.0, 0.0};
+        }
+        __syncwarp();
+        warp_fft(x, kW, sm.tw, lane);
+        for (int m = lane; m < kW; m += 32) x[m] = cmul(x[m], scale);
+        __syncwarp();
+        if (lane == 0) {
+            double prev = __dadd_rn(__dmul_rn(x[4].re, x[4].re), __dmul_rn(x[4].im, x[4].im));
+            double v = 0.0;
+            for (int m = 5; m < kHalf; m++) {
+                const double nm = __dadd_rn(__dmul_rn(x[m].re, x[m].re), __dmul_rn(x[m].im, x[m].im));
+                if (nm > prev) {
+                    v = prev;
+                    break;
+                }
+                prev = nm;
+            }
+            out[p] = __double2float_rn(v);
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_local_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
+                               int max_H, int max_cols, const double* gauss, const double* taper, const double* tw64,
+                               cudaStream_t st) {
+    if (b.count == 0) return cudaSuccess;
+    const int tiles_i = (max_H + kTI - 1) / kTI, tiles_j = (max_cols + kTJ - 1) / kTJ;
+    const size_t smem = sizeof(Smem);
+    cudaError_t e = cudaFuncSetAttribute(k_lradon, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    k_lradon<<<dim3((unsigned)(tiles_i * tiles_j), b.count), kWarps * 32, smem, st>>>(g, b, SI, SO, stride, tiles_j,
+                                                                                      gauss, taper, tw64);
+    return cudaGetLastError();
+}
+
+}  // namespace ske

@@ -83,6 +83,12 @@ cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, 
                          int64_t stride, int64_t len, double* P, int64_t pstride, const double* twiddles,
                          const int64_t* tw_off, int max_H2, cudaStream_t st);
 
+// Local Radon transform (k_lradon.cu): tiles of every sector up to max_H rows
+// and max_cols columns; gauss: 180 x 64 weights, taper: the kept bins' factors.
+cudaError_t launch_local_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
+                               int max_H, int max_cols, const double* gauss, const double* taper, const double* tw64,
+                               cudaStream_t st);
+
 // Cepstrum blur estimation (k_cepstrum.cu).
 cudaError_t launch_cepstrum(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
                             int64_t stride, int64_t len, const double* tw64, const double* tw32,

@@ -134,4 +134,34 @@ __device__ __forceinline__ unsigned bitrev(unsigned v, unsigned bits) {
     return bits ? (__brev(v) >> (32 - bits)) : 0u;
 }
 
+// helper::fft (helper.h:59-106) of x[0..n) (n <= 64, a power of two) by one
+// warp, in place: radix-2 decimation in frequency, one butterfly per lane per
+// stage, with the reference's twiddle sequence tw (fft_twiddles: for the stage
+// of half-span h, entries 2*(n - 2h) .. give T^l as (re, im)), then the bit
+// reversal.  No scaling.
+__device__ __forceinline__ void warp_fft(cd* x, int n, const double* __restrict__ tw, int lane) {
+    for (int h = n >> 1; h >= 1; h >>= 1) {
+        const double* t = tw + 2 * (n - 2 * h);
+        for (int k = lane; k < (n >> 1); k += 32) {
+            const int l = k & (h - 1);
+            const int a = (k / h) * 2 * h + l;
+            const int bb = a + h;
+            const cd xa = x[a], xb = x[bb];
+            x[a] = cadd(xa, xb);
+            x[bb] = cmul(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+        }
+        __syncwarp();
+    }
+    const unsigned bits = 31 - __clz(n);
+    for (int i = lane; i < n; i += 32) {
+        const int j = (int)bitrev((unsigned)i, bits);
+        if (j > i) {
+            const cd tmp = x[i];
+            x[i] = x[j];
+            x[j] = tmp;
+        }
+    }
+    __syncwarp();
+}
+
 }  // namespace ske

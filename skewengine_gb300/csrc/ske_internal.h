@@ -57,6 +57,14 @@ void build_geometry(int dimx, int dimy, Geometry& g);
 // advances it.  n-1 entries in total (none for n == 1).
 void fft_twiddles(unsigned n, std::vector<double>& re_im);
 
+// Constants of the local Radon transform (pointRadon, kernelRADN.h:114-182),
+// computed on the host with the reference's expressions: gauss[64*a + m] =
+// exp(-(m-32)^2 / (2 sigma^2)), sigma = (64/5)/scale of angle a, for a < 180;
+// taper[k] = sin(k/(25.6-1) * pi/2) for k <= 25 (the bins the filter keeps).
+constexpr int kLocalRadonWindow = 64;  // winSize (kernelRADN.h:19)
+constexpr int kLocalRadonKeep = 26;    // bins k <= 0.4 * 64
+void local_radon_tables(const Geometry& g, std::vector<double>& gauss, std::vector<double>& taper);
+
 // Size of the skewed buffers of a grid: 2*N + dim_l floats
 // (skewEngine.cuh:425-426, the CPU path's buffer size).
 inline int64_t skew_buffer_len(int dimx, int dimy) {

@@ -25,8 +25,11 @@ KERNEL_IDENTITYDEM = 1
 KERNEL_RADON = 2
 KERNEL_IDENTITYIMG = 3
 KERNEL_CEPSTRUM = 4
+# The reference's Radon operator with LRT set (kernelRADN.h:212-220): the local
+# Radon transform of every skewed cell (no id in the reference's enum).
+KERNEL_LOCAL_RADON = 5
 KERNELS = {"sdem": KERNEL_SDEM, "identitydem": KERNEL_IDENTITYDEM, "radon": KERNEL_RADON,
-           "identityimg": KERNEL_IDENTITYIMG, "cepstrum": KERNEL_CEPSTRUM}
+           "identityimg": KERNEL_IDENTITYIMG, "cepstrum": KERNEL_CEPSTRUM, "localradon": KERNEL_LOCAL_RADON}
 
 ACCUM_REFERENCE = 0
 ACCUM_KAHAN = 1

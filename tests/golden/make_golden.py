@@ -33,7 +33,10 @@ sys.path.insert(0, ROOT)
 
 from skewengine_gb300 import synthetic  # noqa: E402
 
-OPS = {"sdem": 0, "identitydem": 1, "radon": 2, "identityimg": 3, "cepstrum": 4}
+OPS = {"sdem": 0, "identitydem": 1, "radon": 2, "identityimg": 3, "cepstrum": 4, "localradon": 5}
+# The reference has no operator id for the local Radon transform: it is its Radon
+# operator (2) with the LRT switch set (kernelRADN.h:212-220).
+LOCAL_RADON = 5
 POVH = float(synthetic.POVH)
 
 
@@ -47,7 +50,14 @@ def load_ref(ref_root: str):
     lib.skref_run.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int]
     lib.skref_sector.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_int, C.c_float, ip, dp, fp, fp,
                                  up, up, ip, fp, fp]
+    lib.skref_set_local_radon.argtypes = [C.c_int]
     return lib
+
+
+def ref_op(lib, op: int) -> int:
+    """Reference operator id for `op`, setting the LRT switch for the local Radon."""
+    lib.skref_set_local_radon(1 if op == LOCAL_RADON else 0)
+    return 2 if op == LOCAL_RADON else op
 
 
 def input_for(kind: str, dx: int, dy: int, seed: int) -> np.ndarray:
@@ -74,6 +84,8 @@ RUN_CASES = [
     ("radon", "uniform", 2, 2, 44),
     ("cepstrum", "texture", 32, 32, 51), ("cepstrum", "texture", 40, 24, 52),
     ("cepstrum", "texture", 24, 40, 53),
+    ("localradon", "phantom", 32, 32, 61), ("localradon", "phantom", 40, 24, 62),
+    ("localradon", "texture", 24, 36, 63),
 ]
 
 SECTOR_CASES = [
@@ -81,6 +93,7 @@ SECTOR_CASES = [
     ("identitydem", "uniform", 48, 32, 22, [0, 20, 33, 34, 60, 90, 100, 146, 147, 170]),
     ("radon", "phantom", 64, 64, 41, [0, 30, 45, 90, 135]),
     ("cepstrum", "texture", 32, 32, 51, [0, 45, 100]),
+    ("localradon", "phantom", 32, 32, 61, [0, 45, 100, 160]),
 ]
 
 GEOMETRY_SMALL = [(32, 32), (48, 32), (32, 48), (7, 5), (1, 1), (3, 2)]
@@ -99,8 +112,8 @@ def sector_dump(lib, op: int, x: np.ndarray, angle: int):
     ta = np.zeros(dl, np.int32)
     we = np.zeros(dl, np.float32)
     acc = np.zeros(n, np.float32)
-    assert lib.skref_sector(op, np.ascontiguousarray(x), dx, dy, angle, POVH, ii, dd, si, so, fi, la, ta,
-                            we, acc) == 0
+    assert lib.skref_sector(ref_op(lib, op), np.ascontiguousarray(x), dx, dy, angle, POVH, ii, dd, si, so, fi,
+                            la, ta, we, acc) == 0
     h = int(ii[5])
     return ii, dd, si, so, fi[:h].copy(), la[:h].copy(), ta, we, acc
 
@@ -128,7 +141,7 @@ def main() -> None:
     for name, kind, dx, dy, seed in RUN_CASES:
         x = input_for(kind, dx, dy, seed)
         y = np.zeros_like(x)
-        assert lib.skref_run(OPS[name], x, y, dx, dy, 180, POVH, 1) == 0
+        assert lib.skref_run(ref_op(lib, OPS[name]), x, y, dx, dy, 180, POVH, 1) == 0
         key = f"{name}__{kind}__{dx}x{dy}__{seed}"
         runs[key + "__in"] = x
         runs[key + "__out"] = y

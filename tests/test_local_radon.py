@@ -1,0 +1,49 @@
+"""Local Radon transform (the reference's Radon operator with LRT set,
+kernelRADN.h:114-182 and :212-220): the sm_103a operator against the oracle,
+bit for bit.  The oracle itself is pinned to the reference by the golden cases
+``localradon__*`` (tests/test_oracle_golden.py)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from skewengine_gb300 import synthetic
+from tests.conftest import bits_equal
+
+POVH = np.float32(0.15)
+# The oracle runs on one thread: with several, sectors are folded per thread
+# (the reference's own behaviour), which changes the order of the float adds.
+
+
+def test_oracle_local_radon_zero_input(oracle):
+    """A zero grid transforms to zero everywhere (every window sum is +0)."""
+    x = np.zeros((20, 24), np.float32)
+    assert not np.any(oracle.run(5, x, povh=POVH))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,dx,dy,seed", [("phantom", 64, 48, 1), ("dem", 56, 56, 2), ("texture", 40, 70, 3),
+                                            ("phantom", 1, 1, 4), ("phantom", 3, 2, 5), ("dem", 60, 5, 6)])
+def test_local_radon_matches_oracle(gpu_lib, oracle, kind, dx, dy, seed):
+    import skewengine_gb300 as ske
+    if kind == "phantom":
+        x = synthetic.ellipse_phantom(dx, seed, side_y=dy)
+    elif kind == "dem":
+        x = synthetic.fractal_dem(dx, seed, side_y=dy)
+    else:
+        x = synthetic.blurred_texture(max(dx, dy), seed)[0][:dy, :dx]
+    x = np.ascontiguousarray(x, np.float32)
+    with ske.SkewEngine(dx, dy) as eng:
+        got = eng.run(ske.KERNEL_LOCAL_RADON, x, povh=POVH)
+    want = oracle.run(5, x, povh=POVH)
+    assert bits_equal(got, want), (kind, dx, dy, float(np.abs(got - want).max()))
+
+
+@pytest.mark.gpu
+def test_local_radon_angle_subset_and_name(gpu_lib, oracle):
+    import skewengine_gb300 as ske
+    x = synthetic.ellipse_phantom(64, 9)
+    angles = [0, 13, 44, 45, 46, 90, 91, 135, 179]
+    with ske.SkewEngine(64, 64) as eng:
+        got = eng.run("localradon", x, povh=POVH, angles=angles)
+    assert bits_equal(got, oracle.run_angles(5, x, angles, povh=POVH))
