@@ -55,7 +55,13 @@ __global__ void k_skew(DevGeometry g, Batch b, const float* __restrict__ orient,
     const int32_t* tgt = g.target + d.col_off;
     const float* wgt = g.weight + d.col_off;
     float* out = SI + slot * stride;
-    for (int64_t p = gtid(); p < len; p += gstride()) out[p] = skew_gather_flat(d, tgt, wgt, src, p);
+    // Row by row (no flat-index division), then zeros past H*dim_i.
+    for (int r = blockIdx.x; r < d.H; r += gridDim.x)
+        for (int c = threadIdx.x; c < d.dim_i; c += blockDim.x)
+            out[(int64_t)r * d.dim_i + c] = skew_gather(d, tgt, wgt, src, r, c);
+    const int64_t z0 = (int64_t)d.H * d.dim_i;
+    for (int64_t p = z0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < len; p += (int64_t)gridDim.x * blockDim.x)
+        out[p] = 0.0f;
 }
 
 __global__ void k_identity(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO,
@@ -207,7 +213,7 @@ cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, c
 
 cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells, float* SI,
                         int64_t stride, int64_t len, cudaStream_t st) {
-    dim3 grid(blocks_for(len, 256, 4096), b.count);
+    dim3 grid(1024, b.count);
     k_skew<<<grid, 256, 0, st>>>(g, b, orient, n_cells, SI, stride, len);
     return cudaGetLastError();
 }
