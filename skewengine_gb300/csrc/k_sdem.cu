@@ -10,24 +10,26 @@
 //
 // Compacting sweep (k_sdem, the engine's)
 //  * Persistent kernel; a warp takes one skewed row (sector slot, row) from a
-//    global queue ordered longest row first and scans it forward, then backward.
+//    global queue ordered longest row first and scans it in both directions.
 //  * Work proceeds in levels of kLevel steps.  Level 0 takes every observer of
 //    the row; after each level an exact horizon test (below) retires the
 //    observers that can see nothing further, and the survivors are appended to a
-//    per-warp list in global scratch.  The next level processes only that list,
-//    in batches of 64 observers (2 per lane).  An observer's work therefore ends
-//    within kLevel steps of the test that retires it, instead of with the
-//    slowest of a fixed group: on 2000x2000 fractal terrain this runs about 29%
-//    of the line-of-sight steps (counting empty slots), against 68% for the
-//    chunked sweep.  64-step levels measured faster than 32 or 128 (fewer list
-//    passes against more steps past an observer's end).
+//    per-warp list (one per direction) in global scratch.  The next level
+//    processes only those lists, in batches of 64 observers (2 per lane): full
+//    batches of one direction, then the two lists' remainders paired (a forward
+//    observer in slot 0, a backward one in slot 1).  An observer's work
+//    therefore ends within kLevel steps of the test that retires it, instead of
+//    with the slowest of a fixed group: on 2000x2000 fractal terrain this runs
+//    about 22% of the line-of-sight steps (counting empty slots), against 68%
+//    for the chunked sweep.  64-step levels measured faster than 32 or 128
+//    (fewer list passes against more steps past an observer's end).
 //  * All observers of a batch are at the same step distance d, so -d, RN(1/d)
 //    and 2d+1 still come from the constant table; each lane reads its two
 //    observers' targets with one shared-memory load per step each, and computes
 //    both slopes with packed f32x2 instructions.
-//  * The forward result of an observer goes to the output cell; the backward
-//    pass adds its own and applies the scale (both are integers below 2^24, so
-//    the sum is exact in either order).
+//  * Each direction's count of an observer goes to a per-warp scratch array;
+//    after the last level the two are added (forward + backward, integers below
+//    2^24) and scaled into the output cell.
 //
 // Chunked sweep (k_sdem_chunked, the allocation-free entry point's)
 //  * Persistent kernel; a warp takes one work item = (sector slot, skewed row,
@@ -390,8 +392,10 @@ constexpr int kLevel = 64;  // line-of-sight steps per level
 constexpr int kUnroll = 8;  // steps per unrolled block of a level
 constexpr int kSlots = 2;   // observers per lane in a batch (one packed pair)
 static_assert(kLevel % kUnroll == 0, "a level is whole blocks");
-constexpr int kBatch = 32 * kSlots;
 constexpr int kLWarps = 4;  // warps per CTA
+// Per-warp scratch, in units of max_row int4 entries: four survivor lists and
+// the two directions' counts (2*max_row floats, within one more unit).
+constexpr int kListsPerWarp = 5;
 constexpr int kLPad = 64;   // NaN cells on both sides of the row (>= kLevel - 1)
 // Longest row on the fast path: every step distance a level touches (at most
 // the last survivor's n + kLevel) stays inside the constant table.
@@ -435,13 +439,13 @@ struct RowMax {
     int n8;
 };
 
-// One lane's observers of a batch, in one scan direction.
+// One lane's two observers of a batch.  Slot q scans forward when the batch's
+// template flag for it is set, backward otherwise.
 struct Slots {
     int x[kSlots];  // position in the row
-    int n[kSlots];  // steps in this direction
+    int n[kSlots];  // steps in the slot's direction
     bool valid[kSlots];  // false: empty slot (its steps run, its state is dropped)
     float h[kSlots], mx[kSlots], acc[kSlots], cl[kSlots];
-    float prev[kSlots];  // backward pass: the forward result held in the output cell
 };
 
 // Visibility update.  The comparison is unordered (true for a NaN slope): a
@@ -455,14 +459,14 @@ __device__ __forceinline__ void visit(Slots& s, int q, float sl, float ring) {
     s.acc[q] = above ? __fadd_rn(s.acc[q], ring) : s.acc[q];
 }
 
-// Steps d0 .. d0+kLevel-1 of the lane's two observers.  An observer that ends
-// inside the level reads at most kLevel-1 cells of the row's NaN padding (see
-// visit).  The level runs as a loop over blocks of kUnroll steps: fully
-// unrolled levels overflow the instruction cache.
-template <bool kFwd>
+// Steps d0 .. d0+kLevel-1 of the lane's two observers (directions kF0, kF1).
+// An observer that ends inside the level reads at most kLevel-1 cells of the
+// row's NaN padding (see visit).  The level runs as a loop over blocks of
+// kUnroll steps: fully unrolled levels overflow the instruction cache.
+template <bool kF0, bool kF1>
 __device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0) {
-    const float* p0 = A + (kFwd ? s.x[0] + d0 : s.x[0] - d0);
-    const float* p1 = A + (kFwd ? s.x[1] + d0 : s.x[1] - d0);
+    const float* p0 = A + (kF0 ? s.x[0] + d0 : s.x[0] - d0);
+    const float* p1 = A + (kF1 ? s.x[1] + d0 : s.x[1] - d0);
     const f2 hh = pk(s.h[0], s.h[1]);
 #pragma unroll 1
     for (int k0 = 0; k0 < kLevel; k0 += kUnroll) {
@@ -470,15 +474,15 @@ __device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ 
         for (int k = 0; k < kUnroll; k++) {
             const int d = d0 + k0 + k;
             const float4 st = c_step[d];
-            const float z0 = kFwd ? p0[k] : p0[-k];
-            const float z1 = kFwd ? p1[k] : p1[-k];
+            const float z0 = kF0 ? p0[k] : p0[-k];
+            const float z1 = kF1 ? p1[k] : p1[-k];
             float q0, q1;
             upk(div2(sub2(pk(z0, z1), hh), pk(st.x, st.x), pk(st.y, st.y)), q0, q1);
             visit(s, 0, q0, st.z);
             visit(s, 1, q1, st.z);
         }
-        p0 += kFwd ? kUnroll : -kUnroll;
-        p1 += kFwd ? kUnroll : -kUnroll;
+        p0 += kF0 ? kUnroll : -kUnroll;
+        p1 += kF1 ? kUnroll : -kUnroll;
     }
 }
 
@@ -577,96 +581,114 @@ __device__ __forceinline__ bool retire(const RowMax& rm, int x, int n, int dc, f
     return ok;
 }
 
-// All levels of one scan direction of the row.  Level 0 takes every observer
-// 0..L-1; each later level takes the previous level's survivors from a list.
-template <bool kFwd>
-__device__ void sweep_dir(const float* __restrict__ A, const RowMax& rm, int L, float povh,
-                          int4* __restrict__ list0, int4* __restrict__ list1, const RowOut& o, int lane) {
-    const unsigned below = (1u << lane) - 1u;
-    const int4* in = nullptr;
-    int4* outl = list0;
-    int count = L;
-    for (int d0 = 1; count > 0; d0 += kLevel) {
-        const int dc = d0 + kLevel - 1;  // last step of the level
-        int produced = 0;
-        // List entries of the next batch are loaded one batch ahead.
-        int4 nxt[kSlots];
-#pragma unroll
-        for (int q = 0; q < kSlots; q++) {
-            const int idx = lane + 32 * q;
-            nxt[q] = (in && idx < count) ? in[idx] : make_int4(0, 0, 0, 0);
-        }
-        for (int base = 0; base < count; base += kBatch) {
-            int4 cur[kSlots];
-#pragma unroll
-            for (int q = 0; q < kSlots; q++) {
-                cur[q] = nxt[q];
-                const int idx = base + kBatch + lane + 32 * q;
-                nxt[q] = (in && idx < count) ? in[idx] : make_int4(0, 0, 0, 0);
-            }
-            Slots s;
-#pragma unroll
-            for (int q = 0; q < kSlots; q++) {
-                const int idx = base + lane + 32 * q;
-                if (idx < count) {
-                    if (in) {
-                        const int4 e = cur[q];
-                        s.x[q] = e.x;
-                        s.mx[q] = __int_as_float(e.y);
-                        s.acc[q] = __int_as_float(e.z);
-                        s.cl[q] = __int_as_float(e.w);
-                    } else {
-                        s.x[q] = idx;
-                        s.mx[q] = -2000.0f;
-                        s.acc[q] = 0.0f;
-                        s.cl[q] = -1.0f;
-                    }
-                    s.n[q] = kFwd ? L - 1 - s.x[q] : s.x[q];
-                    s.valid[q] = true;
-                    s.h[q] = __fadd_rn(A[s.x[q]], povh);
-                    s.prev[q] = kFwd ? 0.0f : o.out[o.rowbase + s.x[q]];
-                } else {
-                    // Empty: its reads stay in A[-(kLevel-1) .. kLevel-1].
-                    s.x[q] = kFwd ? -d0 : d0;
-                    s.n[q] = dc;
-                    s.valid[q] = false;
-                    s.h[q] = s.mx[q] = s.acc[q] = s.cl[q] = s.prev[q] = 0.0f;
-                }
-            }
-            level_steps<kFwd>(s, A, d0);
+// The survivor lists and results of one row's sweep (per-warp global scratch).
+struct RowLists {
+    const int4* in[2];  // this level's survivors, forward / backward (null: level 0)
+    int4* out[2];       // the next level's, forward / backward
+    int n[2];           // entries of in[]
+    int used[2];        // entries of in[] taken by this level's batches so far
+    int made[2];        // entries appended to out[]
+    float* cv[2];       // finished observers' counts by position, forward / backward
+};
 
-            // Retire finished observers, keep the others for the next level.
+// One batch of a level: slot q takes entry used[dir] + lane + 32*qi of its
+// direction's list, where qi counts the batch's earlier slots of that direction.
+template <bool kF0, bool kF1>
+__device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const RowMax& rm, int L, float povh,
+                                            RowLists& rl, int d0, int lane) {
+    constexpr bool kDir[kSlots] = {kF0, kF1};
+    const unsigned below = (1u << lane) - 1u;
+    const int dc = d0 + kLevel - 1;  // last step of the level
+    Slots s;
 #pragma unroll
-            for (int q = 0; q < kSlots; q++) {
-                bool keep = false;
-                if (s.valid[q]) {
-                    bool done = false;
-                    if (s.n[q] > dc) {
-                        done = retire<kFwd>(rm, s.x[q], s.n[q], dc, s.h[q], s.mx[q]);
-                        keep = !done;
-                    }
-                    if (!keep && owns(o, s.x[q])) {
-                        const float cv = __fadd_rn(1.0f, done ? s.acc[q] : s.cl[q]);
-                        float* cell = o.out + o.rowbase + s.x[q];
-                        if (kFwd) {
-                            *cell = cv;
-                        } else {
-                            const float t = __fadd_rn(s.prev[q], cv);
-                            *cell = o.counts_only ? t : __fmul_rn(t, o.sd->r2);
-                        }
-                    }
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, keep);
-                if (keep)
-                    outl[produced + __popc(m & below)] = make_int4(
-                        s.x[q], __float_as_int(s.mx[q]), __float_as_int(s.acc[q]), __float_as_int(s.cl[q]));
-                produced += __popc(m);
+    for (int q = 0; q < kSlots; q++) {
+        const int dir = kDir[q] ? 0 : 1;
+        const int idx = rl.used[dir] + lane + (q == 1 && kF0 == kF1 ? 32 : 0);
+        if (idx < rl.n[dir]) {
+            if (rl.in[dir]) {
+                const int4 e = rl.in[dir][idx];
+                s.x[q] = e.x;
+                s.mx[q] = __int_as_float(e.y);
+                s.acc[q] = __int_as_float(e.z);
+                s.cl[q] = __int_as_float(e.w);
+            } else {
+                s.x[q] = idx;
+                s.mx[q] = -2000.0f;
+                s.acc[q] = 0.0f;
+                s.cl[q] = -1.0f;
             }
+            s.n[q] = kDir[q] ? L - 1 - s.x[q] : s.x[q];
+            s.valid[q] = true;
+            s.h[q] = __fadd_rn(A[s.x[q]], povh);
+        } else {
+            // Empty: its reads stay in A[-(kLevel-1) .. kLevel-1].
+            s.x[q] = kDir[q] ? -d0 : d0;
+            s.n[q] = dc;
+            s.valid[q] = false;
+            s.h[q] = s.mx[q] = s.acc[q] = s.cl[q] = 0.0f;
         }
-        __syncwarp();  // this level's list and results are visible to every lane
-        in = outl;
-        outl = outl == list0 ? list1 : list0;
-        count = produced;
+    }
+    if (kF0 == kF1) rl.used[kF0 ? 0 : 1] += 64;
+    else rl.used[0] += 32, rl.used[1] += 32;
+    level_steps<kF0, kF1>(s, A, d0);
+
+    // Retire finished observers, keep the others for the next level.
+#pragma unroll
+    for (int q = 0; q < kSlots; q++) {
+        const int dir = kDir[q] ? 0 : 1;
+        bool keep = false;
+        if (s.valid[q]) {
+            bool done = false;
+            if (s.n[q] > dc) {
+                done = kDir[q] ? retire<true>(rm, s.x[q], s.n[q], dc, s.h[q], s.mx[q])
+                               : retire<false>(rm, s.x[q], s.n[q], dc, s.h[q], s.mx[q]);
+                keep = !done;
+            }
+            if (!keep) rl.cv[dir][s.x[q]] = __fadd_rn(1.0f, done ? s.acc[q] : s.cl[q]);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep)
+            rl.out[dir][rl.made[dir] + __popc(m & below)] =
+                make_int4(s.x[q], __float_as_int(s.mx[q]), __float_as_int(s.acc[q]), __float_as_int(s.cl[q]));
+        rl.made[dir] += __popc(m);
+    }
+}
+
+// Both scan directions of the row, level by level.  Level 0 takes every
+// observer 0..L-1 in each direction; each later level takes the previous
+// level's survivors.  A level runs full batches of one direction while a list
+// has 64 entries left, then pairs what remains of the two (a forward observer
+// in slot 0, a backward one in slot 1), so short lists share batches.
+// lists: four lists of L_max entries (forward in/out, backward in/out);
+// cvf, cvb: the two directions' counts, added and scaled at the end.
+__device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, float povh, int4* lists,
+                          int max_row, float* cvf, float* cvb, const RowOut& o, int lane) {
+    RowLists rl;
+    rl.in[0] = rl.in[1] = nullptr;
+    rl.out[0] = lists;
+    rl.out[1] = lists + 2 * (int64_t)max_row;
+    rl.n[0] = rl.n[1] = L;
+    rl.cv[0] = cvf;
+    rl.cv[1] = cvb;
+    for (int d0 = 1; rl.n[0] > 0 || rl.n[1] > 0; d0 += kLevel) {
+        rl.used[0] = rl.used[1] = 0;
+        rl.made[0] = rl.made[1] = 0;
+        while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true>(A, rm, L, povh, rl, d0, lane);
+        while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false>(A, rm, L, povh, rl, d0, lane);
+        while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1]) sweep_batch<true, false>(A, rm, L, povh, rl, d0, lane);
+        __syncwarp();  // this level's lists and counts are visible to every lane
+#pragma unroll
+        for (int dir = 0; dir < 2; dir++) {
+            int4* base = lists + 2 * (int64_t)max_row * dir;
+            rl.in[dir] = rl.out[dir];
+            rl.out[dir] = rl.out[dir] == base ? base + max_row : base;
+            rl.n[dir] = rl.made[dir];
+        }
+    }
+    for (int x = lane; x < L; x += 32) {
+        if (!owns(o, x)) continue;
+        const float t = __fadd_rn(cvf[x], cvb[x]);  // forward count, then backward
+        o.out[o.rowbase + x] = o.counts_only ? t : __fmul_rn(t, o.sd->r2);
     }
 }
 
@@ -681,8 +703,9 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
     float* b16 = buf + lay.b16;
     float* b128 = buf + lay.b128;
     const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
-    int4* list0 = a.lists + gwarp * 2 * (int64_t)a.max_row;
-    int4* list1 = list0 + a.max_row;
+    int4* lists = a.lists + gwarp * kListsPerWarp * (int64_t)a.max_row;
+    float* cvf = reinterpret_cast<float*>(lists + 4 * (int64_t)a.max_row);
+    float* cvb = cvf + a.max_row;
     for (;;) {
         unsigned idx = 0;
         if (lane == 0) idx = atomicAdd(a.counter, 1u);
@@ -726,8 +749,7 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
             coarse_maxima(A, L, suf, pre, b16, b128, lane);
             __syncwarp();
             const RowMax rm{suf, pre, b16, b128, nblk(L, kBlk)};
-            sweep_dir<true>(A, rm, L, a.povh, list0, list1, o, lane);
-            sweep_dir<false>(A, rm, L, a.povh, list0, list1, o, lane);
+            sweep_row(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane);
         } else {
             for (int x = lane; x < L; x += 32) {
                 if (!owns(o, x)) continue;
@@ -850,10 +872,10 @@ void sdem_items(const Geometry& geo, const Batch& b, std::vector<uint64_t>& item
 }
 
 size_t sdem_list_bytes(int max_row, int num_sms) {
-    // Two lists of max_row entries per warp, for as many warps as an SM holds.
+    // kListsPerWarp units of max_row entries per warp, for as many warps as an SM holds.
     int dev = 0, threads = 2048;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&threads, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
-    return (size_t)num_sms * (size_t)(threads / 32) * 2 * (size_t)std::max(max_row, 1) * sizeof(int4);
+    return (size_t)num_sms * (size_t)(threads / 32) * kListsPerWarp * (size_t)std::max(max_row, 1) * sizeof(int4);
 }
 
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
@@ -868,8 +890,8 @@ cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     int64_t blocks = (int64_t)per_sm * num_sms;
     const int64_t need = (a.n_items + kLWarps - 1) / kLWarps;
     if (blocks > need) blocks = need;
-    // Every warp owns two lists of max_row entries in the scratch.
-    const size_t list_per_block = (size_t)kLWarps * 2 * (size_t)a.max_row * sizeof(int4);
+    // Every warp owns kListsPerWarp units of max_row entries in the scratch.
+    const size_t list_per_block = (size_t)kLWarps * kListsPerWarp * (size_t)a.max_row * sizeof(int4);
     const int64_t fit = a.lists ? (int64_t)(a.list_bytes / list_per_block) : 0;
     if (fit < 1) return cudaErrorInvalidValue;
     if (blocks > fit) blocks = fit;
