@@ -157,6 +157,19 @@ def test_tiny_and_degenerate_grids(ske, oracle, dims):
         assert bits_equal(_run(ske, op, x), oracle.run(op, x, povh=POVH)), (dims, op)
 
 
+@pytest.mark.parametrize("dx", [4032, 4040])
+def test_long_rows_at_fast_path_limit(ske, oracle, dx):
+    """Rows of 4032 cells are the longest the sweep's fast path takes; 4040-cell
+    rows take the reference-order path.  Both match the oracle bit for bit.
+    (Angle 0 only: the transposed sectors of so flat a grid have rows that
+    overrun the 3-cell width up to dim_l, about 6.6e10 steps for the oracle.)"""
+    x = synthetic.fractal_dem(dx, 21, side_y=3)
+    angles = [0]
+    with ske.SkewEngine(dx, 3) as eng:
+        got = eng.run(0, np.ascontiguousarray(x), povh=POVH, angles=angles)
+    assert bits_equal(got, oracle.run_angles(0, x, angles, povh=POVH)), dx
+
+
 def test_special_values_take_exact_path(ske, oracle):
     """Rows with zeros, huge or non-finite heights use IEEE division and the
     reference's accumulation order; results still match the oracle."""
