@@ -10,8 +10,9 @@
 // One warp per cell: the window lives in shared memory as complex doubles and
 // each lane performs one butterfly per stage of the reference radix-2
 // decimation-in-frequency FFT (helper.h:59-106) with the reference's twiddle
-// sequence, in binary64 without fused operations.  The logarithm is CUDA's
-// double-precision log().
+// sequence, in binary64 without fused operations; cells whose FFT input is
+// finite use warp_fft_real (same values up to the sign of zeros, which the
+// outputs cannot see).  The logarithm is CUDA's double-precision log().
 #include "kernels.h"
 
 namespace ske {
@@ -49,12 +50,17 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         const int64_t base = (int64_t)r * d.dim_i;
         const int j = (int)(p - base);
         const int f = first[r], l = last[r];
+        bool fin = true;
         for (int m = lane; m < kWin; m += 32) {
             const int idx = j - kWin / 2 + m;
             x[m] = (idx < f || idx >= l) ? cd{0.0, 0.0} : cd{(double)in[base + idx], 0.0};
+            fin = fin && isfinite(x[m].re);
         }
         __syncwarp();
-        warp_fft(x, kWin, twa, lane);
+        // Finite real input: the reduced-work FFT gives the same values up to the
+        // sign of zeros, which neither |X|^2 nor -min(0, c) can see.
+        if (__all_sync(0xffffffffu, fin)) warp_fft_real(x, kWin, twa, lane);
+        else warp_fft(x, kWin, twa, lane);
         // |X_k|^2 of the 1/sqrt(64)-scaled spectrum, k < 32, then its log.
         {
             const cd v = x[lane];
@@ -64,7 +70,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
             x[lane] = {log(ps), 0.0};
         }
         __syncwarp();
-        warp_fft(x, kWin / 2, twb, lane);
+        // A zero power gives log = -inf: such cells keep the exact FFT.
+        if (__all_sync(0xffffffffu, isfinite(x[lane].re))) warp_fft_real(x, kWin / 2, twb, lane);
+        else warp_fft(x, kWin / 2, twb, lane);
         if (lane == 0) {
             double s[kWin / 4];
 #pragma unroll

@@ -20,6 +20,10 @@
 //    (warp_fft: the reference's DIF order and twiddle sequence, binary64,
 //    no fused operations).  The 1/sqrt(64) scaling is the reference's complex
 //    multiplication by (0.125, 0).
+//  * Tiles whose staged values are all finite use warp_fft_real (real-input
+//    first stage, multiplication-free last stage) and real scalings: the same
+//    values up to the sign of zeros, so the squared magnitudes, and the output,
+//    are bit-identical; other tiles keep every operation of the reference.
 //  * The Gaussian weights and the taper use host libm (local_radon_tables), as
 //    the reference computes them on the host.
 //  * Output cells past a row's span of the flat grid belong to the last row
@@ -68,13 +72,18 @@ __global__ void __launch_bounds__(kWarps * 32)
     if (!__syncthreads_or(any)) return;
 
     const float* in = SI + slot * stride;
+    int bad = 0;
     for (int t = threadIdx.x; t < kRows * kCols; t += blockDim.x) {
         const int r = t / kCols, c = t % kCols;
         const int k = i0 - kHalf + r, l = j0 - kHalf + c;
         float v = 0.0f;
         if (k >= 0 && k < d.H && l >= first[k] && l < last[k]) v = in[(int64_t)k * d.dim_i + l];
         sm.s[r][c] = v;
+        bad |= !isfinite(v);
     }
+    // Finite tiles take the reduced-work FFT (warp_fft_real); any non-finite
+    // input keeps every operation of the reference.
+    const bool finite = !__syncthreads_or(bad);
     for (int t = threadIdx.x; t < kW; t += blockDim.x) sm.gauss[t] = gauss_all[(int64_t)b.angle[slot] * kW + t];
     for (int t = threadIdx.x; t < kLocalRadonKeep; t += blockDim.x) sm.taper[t] = taper[t];
     for (int t = threadIdx.x; t < 2 * (kW - 1); t += blockDim.x) sm.tw[t] = tw64[t];
@@ -99,14 +108,18 @@ __global__ void __launch_bounds__(kWarps * 32)
         if (j >= d.dim_i && owner_row(d, first, last, p) != i) continue;
         for (int m = lane; m < kW; m += 32) x[m] = cd{__dmul_rn(sm.w[ci + m][cj], sm.gauss[m]), 0.0};
         __syncwarp();
-        warp_fft(x, kW, sm.tw, lane);
+        if (finite) warp_fft_real(x, kW, sm.tw, lane);
+        else warp_fft(x, kW, sm.tw, lane);
         for (int m = lane; m < kW; m += 32) {
-            const double re = cmul(x[m], scale).re;
+            // Finite: x * (0.125, 0) is (re/8, im/8) up to the sign of zeros.
+            const double re = finite ? __dmul_rn(x[m].re, 0.125) : cmul(x[m], scale).re;
             x[m] = cd{m < kLocalRadonKeep ? __dmul_rn(sm.taper[m], re) : 0.0, 0.0};
         }
         __syncwarp();
-        warp_fft(x, kW, sm.tw, lane);
-        for (int m = lane; m < kW; m += 32) x[m] = cmul(x[m], scale);
+        if (finite) warp_fft_real(x, kW, sm.tw, lane);
+        else warp_fft(x, kW, sm.tw, lane);
+        for (int m = lane; m < kW; m += 32)
+            x[m] = finite ? cd{__dmul_rn(x[m].re, 0.125), __dmul_rn(x[m].im, 0.125)} : cmul(x[m], scale);
         __syncwarp();
         if (lane == 0) {
             double prev = __dadd_rn(__dmul_rn(x[4].re, x[4].re), __dmul_rn(x[4].im, x[4].im));
