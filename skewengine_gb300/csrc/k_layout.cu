@@ -129,9 +129,18 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
         // holds; those tiles read the skewed cells directly.
         const bool staged = nrows <= kDeskewBand;
         if (staged) {
+            // All of this thread's band loads are issued before any store.
+            constexpr int kLoads = (kDeskewBand + 7) / 8;
+            float v[kLoads];
+#pragma unroll
+            for (int u = 0; u < kLoads; u++) {
+                const int rr = ty + 8 * u;
+                v[u] = (rr < nrows && j0 + tx <= jlast) ? so[(int64_t)(r0 + rr) * dim_i + j0 + tx] : 0.0f;
+            }
             __syncthreads();  // previous sector's band fully consumed
-            for (int rr = ty; rr < nrows; rr += 8)
-                band[rr][tx] = (j0 + tx <= jlast) ? so[(int64_t)(r0 + rr) * dim_i + j0 + tx] : 0.0f;
+#pragma unroll
+            for (int u = 0; u < kLoads; u++)
+                if (ty + 8 * u < nrows) band[ty + 8 * u][tx] = v[u];
             __syncthreads();
         }
         if (!col_ok) continue;

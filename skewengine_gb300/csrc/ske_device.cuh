@@ -164,13 +164,21 @@ __device__ __forceinline__ void warp_fft(cd* x, int n, const double* __restrict_
     __syncwarp();
 }
 
+// The product of cmul without its infinity recovery, for operands known to be
+// finite with finite products.
+__device__ __forceinline__ cd cmul_finite(cd x, cd y) {
+    return {__dsub_rn(__dmul_rn(x.re, y.re), __dmul_rn(x.im, y.im)),
+            __dadd_rn(__dmul_rn(x.re, y.im), __dmul_rn(x.im, y.re))};
+}
+
 // warp_fft for finite input whose imaginary parts are all zero (n = 64 or 32),
 // with the same values as warp_fft up to the sign of zero results:
 //  * first stage: the operands are real, so (a - b) * T is (d*T.re, d*T.im)
 //    (the reference's extra terms are products with an exact zero);
-//  * last stage: its only twiddle is exactly (1, 0), so x[b] = a - b.
-// Finite float-derived values stay far from overflow, so no NaN arises and the
-// reference's infinity recovery never applies.  Callers use it only when every
+//  * last stage: its only twiddle is exactly (1, 0), so x[b] = a - b;
+//  * other stages: cmul_finite.  Finite float-derived values stay far from
+//    overflow, so no NaN arises and the reference's infinity recovery never
+//    applies.  Callers use it only when every
 // input is finite; results that feed squared magnitudes or comparisons of
 // magnitudes are then bit-identical to warp_fft's.
 __device__ __forceinline__ void warp_fft_real(cd* x, int n, const double* __restrict__ tw, int lane) {
@@ -193,7 +201,7 @@ __device__ __forceinline__ void warp_fft_real(cd* x, int n, const double* __rest
             const int bb = a + h;
             const cd xa = x[a], xb = x[bb];
             x[a] = cadd(xa, xb);
-            x[bb] = cmul(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+            x[bb] = cmul_finite(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
         }
         __syncwarp();
     }
