@@ -47,17 +47,6 @@ __device__ __forceinline__ float skew_gather(const SectorDesc& d, const int32_t*
     return acc;
 }
 
-// Skewed input at flat index p of the (2N + dim_l)-float skewed buffer: cells
-// past H*dim_i are zero.
-__device__ __forceinline__ float skew_gather_flat(const SectorDesc& d, const int32_t* __restrict__ tgt,
-                                                  const float* __restrict__ wgt, const float* __restrict__ src,
-                                                  int64_t p) {
-    if (p >= (int64_t)d.H * d.dim_i) return 0.0f;
-    const int r = (int)(p / d.dim_i);
-    const int c = (int)(p - (int64_t)r * d.dim_i);
-    return skew_gather(d, tgt, wgt, src, r, c);
-}
-
 // The last (largest) skewed row whose valid range [r*dim_i+first, r*dim_i+last)
 // covers flat index p, or -1.  Rows can overrun their own width when dim_l >
 // dim_i (non-square grids, transposed sectors: skewEngine.cuh:581 initialises
