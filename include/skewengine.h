@@ -224,8 +224,9 @@ int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_d
  *
  * For callers that cannot call cudaMalloc -- code that runs under a fixed GPU
  * memory budget, inside another framework's allocator, or on a path where
- * allocation is forbidden -- this runs the engine's sweep over a skewed sector
- * the caller already holds in device memory: `skew_in` (row stride dim_i;
+ * allocation is forbidden -- this runs the viewshed sweep (its chunked form,
+ * whose only scratch is its work list) over a skewed sector the caller already
+ * holds in device memory: `skew_in` (row stride dim_i;
  * every row segment r*dim_i + [first[r], last[r]) must lie inside it),
  * `first`/`last` (skew_height int32 entries, device), and writes cv*scale2 to
  * every valid cell of `skew_out` (other cells are left as they are: zero the

@@ -4,9 +4,11 @@
 // Some callers cannot call cudaMalloc: code that must not grow GPU memory while
 // it runs (a service with a fixed memory budget, another framework's
 // allocator-owned context, or a driver layer that forbids allocation on its
-// call path).  For them this entry point runs the engine's sweep kernel over a
-// skewed sector the caller already holds in device memory, with every piece of
-// the sweep's scratch in static storage: the sector descriptor, the work-queue
+// call path).  For them this entry point runs the chunked viewshed sweep (the
+// one whose only scratch is its work list; the engine's compacting sweep needs
+// survivor lists that grow with the grid) over a skewed sector the caller
+// already holds in device memory, with every piece of the sweep's scratch in
+// static storage: the sector descriptor, the work-queue
 // head, the status word and the sorted work-item list in one file-scope device
 // array, the row limits and the item list being built in file-scope host
 // arrays.  No cudaMalloc, cudaFree or other allocating routine is called.
@@ -89,8 +91,8 @@ extern "C" int ske_sdem_sector_noalloc(int device, const float* skew_in, float* 
     const int rc = setup(device);
     if (rc != SKE_OK) return rc;
 
-    // Row limits to the host, then work items (row, chunk of 128 observers)
-    // sorted longest row first, as the engine builds them.
+    // Row limits to the host, then the chunked sweep's work items (row, chunk
+    // of 128 observers) sorted longest row first.
     e = cudaMemcpyAsync(h_first, first, sizeof(int32_t) * skew_height, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_last, last, sizeof(int32_t) * skew_height, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
