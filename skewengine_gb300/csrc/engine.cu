@@ -104,6 +104,9 @@ struct ske_engine_s {
     size_t list_bytes = 0;
     float* h_pin = nullptr;
     std::map<std::vector<int>, ItemPlan> item_plans;
+    // Per angle: every skewed row's valid range lies within dim_i (no row
+    // overruns into the next, so each skewed cell belongs to one row at most).
+    std::vector<char> rows_in_width;
     // per-sector API state
     bool prepared = false;
     int cur_angle = -1;
@@ -306,7 +309,8 @@ int get_items(ske_engine e, const Batch& b, ItemPlan** out) {
     return SKE_OK;
 }
 
-int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int counts_only) {
+// rows_only (Radon): filter the row sums but skip the back-projection into SO.
+int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int counts_only, bool rows_only = false) {
     switch (kernel) {
         case SKE_KERNEL_SDEM: {
             ItemPlan* plan = nullptr;
@@ -332,9 +336,9 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             return ls.done(launch_sdem(a, e->num_sms, e->stream));
         }
         case SKE_KERNEL_RADON: {
-            LaunchScope ls(e, "radon", 3);
+            LaunchScope ls(e, "radon", rows_only ? 2 : 3);
             return ls.done(launch_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_P, e->pstride, e->d_tw,
-                                        e->d_tw_off, e->max_H2, e->stream));
+                                        e->d_tw_off, e->max_H2, e->stream, !rows_only));
         }
         case SKE_KERNEL_LOCAL_RADON: {
             SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
@@ -360,7 +364,9 @@ int run_skew(ske_engine e, const Batch& b) {
     return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, e->stream));
 }
 
-int run_deskew(ske_engine e, const Batch& b, int is_max, int accum) {
+// rows_from_p: the batch is Radon sectors whose back-projection was skipped;
+// the deskew reads their filtered row values from the Radon scratch.
+int run_deskew(ske_engine e, const Batch& b, int is_max, int accum, bool rows_from_p = false) {
     TypeLists tl;
     memset(&tl, 0, sizeof(tl));
     for (int s = 0; s < b.count; s++) {
@@ -373,7 +379,8 @@ int run_deskew(ske_engine e, const Batch& b, int is_max, int accum) {
     LaunchScope ls(e, "deskew", 1);
     if (is_max) return ls.done(launch_deskew_max(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->dimx, e->dimy, e->stream));
     return ls.done(launch_deskew_add(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->d_comp, e->dimx, e->dimy, accum,
-                                     e->stream));
+                                     e->stream, rows_from_p ? reinterpret_cast<const cd*>(e->d_P) : nullptr,
+                                     e->pstride));
 }
 
 int run_prepare(ske_engine e, const float* input, int on_device) {
@@ -436,8 +443,12 @@ int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on
         b.count = std::min(cap, nangles - s0);
         for (int s = 0; s < b.count; s++) b.angle[s] = angles[s0 + s];
         SKE_TRY(run_skew(e, b));
-        SKE_TRY(run_operator(e, kernel, b, prm->povh, 0));
-        SKE_TRY(run_deskew(e, b, is_max, prm->accum));
+        // Radon sectors whose rows stay within their width are deskewed from
+        // their filtered row values; the back-projection into SO is skipped.
+        bool rows_only = kernel == SKE_KERNEL_RADON;
+        for (int s = 0; s < b.count && rows_only; s++) rows_only = e->rows_in_width[b.angle[s]] != 0;
+        SKE_TRY(run_operator(e, kernel, b, prm->povh, 0, rows_only));
+        SKE_TRY(run_deskew(e, b, is_max, prm->accum, rows_only));
     }
     e->accum_mode = prm->accum;
     return SKE_OK;
@@ -550,6 +561,12 @@ int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream,
     e->len = skew_buffer_len(dimx, dimy);
     e->stride = (e->len + 63) & ~(int64_t)63;
     build_geometry(dimx, dimy, e->geo);
+    e->rows_in_width.assign(e->geo.desc.size(), 1);
+    for (size_t a = 0; a < e->geo.desc.size(); a++) {
+        const SectorDesc& d = e->geo.desc[a];
+        for (int r = 0; r < d.H; r++)
+            if (e->geo.last[d.row_off + r] > d.dim_i) e->rows_in_width[a] = 0;
+    }
     while (e->max_H2 < e->geo.max_H) e->max_H2 <<= 1;
     e->pstride = e->max_H2;
     if (parent && parent->stride >= e->len && parent->pstride >= e->max_H2) {

@@ -88,11 +88,28 @@ constexpr int kDeskewRows = 64;
 constexpr int kDeskewBand = kDeskewRows + 34;  // rows + 1 + max column drift over 32 columns (+1)
 enum { kDeskewAdd = 0, kDeskewKahan = 1, kDeskewMax = 2 };
 
-template <int kMode>
+// Skewed output cell (r, c), c < dim_i, of a Radon sector read from its
+// filtered row values q instead of SO: the back-projection writes
+// 0.0f + q[r] (in binary64, then rounded) on every valid cell of row r
+// (kernelRADN.h:251-257), and zero elsewhere.  Only for sectors whose rows stay
+// within dim_i, where no two rows share a cell.
+__device__ __forceinline__ float row_cell(const SectorDesc& d, const int32_t* __restrict__ first,
+                                          const int32_t* __restrict__ last, const cd* __restrict__ q, int r, int c) {
+    return (r < d.H && c >= first[r] && c < last[r]) ? __double2float_rn(__dadd_rn(0.0, q[r].re)) : 0.0f;
+}
+
+// kRows: the batch's skewed outputs are Radon sectors given as per-row values
+// (Q: pstride complex doubles per slot, real part) rather than SO.
+template <int kMode, bool kRows = false>
 __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, const float* __restrict__ SO,
                                                 int64_t stride, float* __restrict__ acc, float* __restrict__ comp,
-                                                int dimx, int dimy) {
-    __shared__ float band[kDeskewBand][kTile];
+                                                int dimx, int dimy, const cd* __restrict__ Q = nullptr,
+                                                int64_t pstride = 0) {
+    __shared__ float band[kRows ? 1 : kDeskewBand][kTile];
+    // kRows: the band's rows as (value, valid range); a cell is its row's value
+    // inside the range and zero outside.
+    __shared__ float rq[kRows ? kDeskewBand : 1];
+    __shared__ int rf[kRows ? kDeskewBand : 1], rl[kRows ? kDeskewBand : 1];
     constexpr int kPer = kDeskewRows / 8;
     const int t = blockIdx.z;
     const int cnt = tl.count[t];
@@ -125,10 +142,24 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
         const int r0 = i0 + tmin;
         const int nrows = (i_end - i0) + 1 + (tmax - tmin);
         const float* so = SO + tl.slot[t][q] * stride;
+        const cd* qv = kRows ? Q + tl.slot[t][q] * pstride : nullptr;
+        const int32_t* rfirst = g.first + d.row_off;
+        const int32_t* rlast = g.last + d.row_off;
         // Steep sectors of elongated grids (tan > 1) can drift more than the band
         // holds; those tiles read the skewed cells directly.
         const bool staged = nrows <= kDeskewBand;
-        if (staged) {
+        if (staged && kRows) {
+            __syncthreads();  // previous sector's rows fully consumed
+            const int tid = ty * kTile + tx;
+            if (tid < nrows) {
+                const int r = r0 + tid;
+                const bool in = r < d.H;
+                rq[tid] = in ? __double2float_rn(__dadd_rn(0.0, qv[r].re)) : 0.0f;
+                rf[tid] = in ? rfirst[r] : 0;
+                rl[tid] = in ? rlast[r] : 0;
+            }
+            __syncthreads();
+        } else if (staged) {
             // All of this thread's band loads are issued before any store.
             constexpr int kLoads = (kDeskewBand + 7) / 8;
             float v[kLoads];
@@ -149,8 +180,18 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
         for (int k = 0; k < kPer; k++) {
             const int ii = ty + 8 * k;
             if (i0 + ii >= i_end) continue;
-            const float lo = staged ? band[ii + off][tx] : so[(int64_t)(i0 + ii + tj) * dim_i + j];
-            const float hi = staged ? band[ii + off + 1][tx] : so[(int64_t)(i0 + ii + tj + 1) * dim_i + j];
+            float lo, hi;
+            if (kRows && staged) {
+                const int k = ii + off;
+                lo = (j >= rf[k] && j < rl[k]) ? rq[k] : 0.0f;
+                hi = (j >= rf[k + 1] && j < rl[k + 1]) ? rq[k + 1] : 0.0f;
+            } else if (kRows) {
+                lo = row_cell(d, rfirst, rlast, qv, i0 + ii + tj, j);
+                hi = row_cell(d, rfirst, rlast, qv, i0 + ii + tj + 1, j);
+            } else {
+                lo = staged ? band[ii + off][tx] : so[(int64_t)(i0 + ii + tj) * dim_i + j];
+                hi = staged ? band[ii + off + 1][tx] : so[(int64_t)(i0 + ii + tj + 1) * dim_i + j];
+            }
             if (kMode == kDeskewMax) {
                 const float m = (lo < hi) ? hi : lo;  // std::max(lo, hi)
                 float v = (s[k] < m) ? m : s[k];      // std::max(acc, m)
@@ -240,13 +281,20 @@ static dim3 deskew_grid(int dimx, int dimy) {
 }
 
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
-                              float* acc, float* comp, int dimx, int dimy, int accum_mode, cudaStream_t st) {
-    if (accum_mode == kAccumKahan)
-        k_deskew<kDeskewKahan><<<deskew_grid(dimx, dimy), dim3(kTile, 8), 0, st>>>(g, tl, SO, stride, acc, comp,
-                                                                                  dimx, dimy);
-    else
-        k_deskew<kDeskewAdd><<<deskew_grid(dimx, dimy), dim3(kTile, 8), 0, st>>>(g, tl, SO, stride, acc, nullptr,
-                                                                                dimx, dimy);
+                              float* acc, float* comp, int dimx, int dimy, int accum_mode, cudaStream_t st,
+                              const cd* Q, int64_t pstride) {
+    const dim3 grid = deskew_grid(dimx, dimy), block(kTile, 8);
+    if (Q) {
+        if (accum_mode == kAccumKahan)
+            k_deskew<kDeskewKahan, true><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, comp, dimx, dimy, Q, pstride);
+        else
+            k_deskew<kDeskewAdd, true><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, nullptr, dimx, dimy, Q,
+                                                              pstride);
+    } else if (accum_mode == kAccumKahan) {
+        k_deskew<kDeskewKahan><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, comp, dimx, dimy);
+    } else {
+        k_deskew<kDeskewAdd><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, nullptr, dimx, dimy);
+    }
     return cudaGetLastError();
 }
 

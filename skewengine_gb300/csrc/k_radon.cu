@@ -120,7 +120,7 @@ __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict
 
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
                          int64_t len, double* P, int64_t pstride, const double* twiddles, const int64_t* tw_off,
-                         int max_H2, cudaStream_t st) {
+                         int max_H2, cudaStream_t st, bool backproject) {
     cd* Pc = reinterpret_cast<cd*>(P);
     dim3 g1((max_H2 + 255) / 256, b.count);
     k_radon_sums<<<g1, 256, 0, st>>>(g, b, SI, stride, Pc, pstride);
@@ -128,7 +128,7 @@ cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, 
     if (e != cudaSuccess) return e;
     k_radon_transform<<<b.count, 1024, 0, st>>>(g, b, Pc, pstride, twiddles, tw_off);
     e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess || !backproject) return e;
     int64_t blocks = (len + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     k_radon_backproject<<<dim3((unsigned)blocks, b.count), 256, 0, st>>>(g, b, Pc, pstride, SO, stride, len);

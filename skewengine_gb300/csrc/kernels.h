@@ -35,9 +35,12 @@ cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* S
 
 // Deskew + accumulate (skewEngine.cuh:772-792) of every slot of the batch into
 // the per-type accumulators acc[t*N ...] (and comp[] in Kahan mode).
+// With Q set, the slots are Radon sectors whose rows stay within dim_i, read
+// from their filtered row values (Q: pstride complex doubles per slot) instead
+// of SO: what the back-projection would write, without writing it.
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO,
                               int64_t stride, float* acc, float* comp, int dimx, int dimy,
-                              int accum_mode, cudaStream_t st);
+                              int accum_mode, cudaStream_t st, const cd* Q = nullptr, int64_t pstride = 0);
 // Max mode with angle encoding (skewEngine.cuh:774-785).
 cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const float* SO,
                               int64_t stride, float* acc, int dimx, int dimy, cudaStream_t st);
@@ -79,9 +82,10 @@ int sdem_chunk();
 
 // Radon / filtered back-projection (k_radon.cu).  P: per-slot complex scratch
 // of pstride complex doubles; re: per-slot max_H doubles.
+// backproject = false leaves SO untouched (the deskew reads P instead).
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
                          int64_t stride, int64_t len, double* P, int64_t pstride, const double* twiddles,
-                         const int64_t* tw_off, int max_H2, cudaStream_t st);
+                         const int64_t* tw_off, int max_H2, cudaStream_t st, bool backproject = true);
 
 // Local Radon transform (k_lradon.cu): tiles of every sector up to max_H rows
 // and max_cols columns; gauss: 180 x 64 weights, taper: the kept bins' factors.
