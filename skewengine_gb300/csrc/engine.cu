@@ -309,7 +309,9 @@ int get_items(ske_engine e, const Batch& b, ItemPlan** out) {
     return SKE_OK;
 }
 
-// rows_only (Radon): filter the row sums but skip the back-projection into SO.
+// rows_only (Radon, sectors whose rows stay within dim_i): the row sums gather
+// the skewed cells from the oriented input (no skew needed) and the
+// back-projection into SO is skipped.
 int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int counts_only, bool rows_only = false) {
     switch (kernel) {
         case SKE_KERNEL_SDEM: {
@@ -338,7 +340,8 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
         case SKE_KERNEL_RADON: {
             LaunchScope ls(e, "radon", rows_only ? 2 : 3);
             return ls.done(launch_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_P, e->pstride, e->d_tw,
-                                        e->d_tw_off, e->max_H2, e->stream, !rows_only));
+                                        e->d_tw_off, e->max_H2, e->stream, !rows_only,
+                                        rows_only ? e->d_orient : nullptr, e->N));
         }
         case SKE_KERNEL_LOCAL_RADON: {
             SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
@@ -442,11 +445,12 @@ int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on
         Batch b;
         b.count = std::min(cap, nangles - s0);
         for (int s = 0; s < b.count; s++) b.angle[s] = angles[s0 + s];
-        SKE_TRY(run_skew(e, b));
-        // Radon sectors whose rows stay within their width are deskewed from
-        // their filtered row values; the back-projection into SO is skipped.
+        // Radon sectors whose rows stay within their width: the row sums gather
+        // the skewed cells themselves and the deskew reads the filtered row
+        // values, so neither the skew nor the back-projection runs.
         bool rows_only = kernel == SKE_KERNEL_RADON;
         for (int s = 0; s < b.count && rows_only; s++) rows_only = e->rows_in_width[b.angle[s]] != 0;
+        if (!rows_only) SKE_TRY(run_skew(e, b));
         SKE_TRY(run_operator(e, kernel, b, prm->povh, 0, rows_only));
         SKE_TRY(run_deskew(e, b, is_max, prm->accum, rows_only));
     }

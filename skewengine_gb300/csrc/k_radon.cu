@@ -8,8 +8,13 @@
 // (helper.h:59-106) with its exact twiddle sequence, computed in binary64 with
 // no fused operations, so the result is bit-identical to the reference.
 //
-// Three launches per batch: row sums (one thread per row, sequential double
-// adds), transform (one CTA per sector), back-projection (one thread per cell).
+// Three launches per batch: row sums (one warp per row), transform (one CTA per
+// sector), back-projection (one thread per cell).  For sectors whose rows stay
+// within their width the engine skips the back-projection (its deskew reads the
+// filtered row values) and the skew (the row sums gather the skewed cells from
+// the oriented input themselves).
+#include <climits>
+
 #include "kernels.h"
 
 namespace ske {
@@ -22,21 +27,100 @@ __device__ __forceinline__ int pow2_at_least(int h) {
     return p;
 }
 
-__global__ void k_radon_sums(DevGeometry g, Batch b, const float* __restrict__ SI, int64_t stride,
-                             cd* __restrict__ P, int64_t pstride) {
+// Row sums p[r] = the reference's left-to-right binary64 sum of row r's valid
+// cells (kernelRADN.h:223-229); p[r] = 0 for H <= r < H2.  One warp per row.
+// Every float is m * 2^e with an integer m of at most 24 bits; in units of the
+// row's smallest 2^e the values are integers, and when the sum of their
+// magnitudes stays below 2^53 every partial sum of the reference is exactly
+// representable, i.e. its result is the exact sum, which does not depend on the
+// order of additions.  The warp then forms that sum with coalesced loads and
+// 64-bit integer partial sums (exponent spread <= 28, rows <= 2048 cells: no
+// overflow) and returns sum * 2^emin.  Rows with a non-finite value or failing
+// these conditions are added in binary64, left to right, by one lane.
+//
+// kGather: the cells are formed from the oriented input as the skew forms them
+// (skew_gather), instead of read from the skewed grid; only for sectors whose
+// rows stay within dim_i, where cell (r, j) is the skew's value at r*dim_i + j.
+constexpr int kSumWarps = 8;
+constexpr int kMaxSpread = 28;
+constexpr int kMaxExactRow = 2048;
+
+template <bool kGather>
+__global__ void __launch_bounds__(kSumWarps * 32)
+    k_radon_sums(DevGeometry g, Batch b, const float* __restrict__ SI, int64_t stride, const float* __restrict__ orient,
+                 int64_t n_cells, cd* __restrict__ P, int64_t pstride) {
+    const int lane = threadIdx.x & 31;
     const int slot = blockIdx.y;
     const SectorDesc d = g.desc[b.angle[slot]];
     const int H2 = pow2_at_least(d.H);
     const float* in = SI + slot * stride;
+    const float* src = orient + (int64_t)d.type * n_cells;
+    const int32_t* tgt = g.target + d.col_off;
+    const float* wgt = g.weight + d.col_off;
     cd* p = P + slot * pstride;
-    for (int64_t r = gtid(); r < H2; r += gstride()) {
-        double s = 0.0;
-        if (r < d.H) {
-            const int f = g.first[d.row_off + r], l = g.last[d.row_off + r];
-            const float* row = in + r * d.dim_i;
-            for (int j = f; j < l; j++) s = __dadd_rn(s, (double)row[j]);
+    const int nwarps = gridDim.x * kSumWarps;
+    for (int r = blockIdx.x * kSumWarps + (threadIdx.x >> 5); r < H2; r += nwarps) {
+        if (r >= d.H) {
+            if (lane == 0) p[r] = {0.0, 0.0};
+            continue;
         }
-        p[r] = {s, 0.0};
+        const int f = g.first[d.row_off + r], l = g.last[d.row_off + r];
+        const float* row = in + (int64_t)r * d.dim_i;
+        auto cell = [&](int j) { return kGather ? skew_gather(d, tgt, wgt, src, r, j) : row[j]; };
+        // Per lane: integer sum in units of 2^emin (rescaled when emin drops).
+        unsigned long long sum = 0, mag = 0;
+        int emin = INT_MAX, emax = INT_MIN;
+        bool bad = false;
+        for (int j = f + lane; j < l; j += 32) {
+            const unsigned u = __float_as_uint(cell(j));
+            const int ef = (int)((u >> 23) & 0xffu);
+            const unsigned m = ef ? ((u & 0x7fffffu) | 0x800000u) : (u & 0x7fffffu);
+            bad |= ef == 0xff;
+            if (m == 0 || bad) continue;
+            const int e = ef ? ef - 150 : -149;
+            if (e < emin) {
+                if (emin != INT_MAX) {
+                    if (emin - e > kMaxSpread) {
+                        bad = true;
+                        continue;
+                    }
+                    sum <<= emin - e;
+                    mag <<= emin - e;
+                }
+                emin = e;
+            }
+            emax = max(emax, e);
+            if (emax - emin > kMaxSpread) {
+                bad = true;
+                continue;
+            }
+            const unsigned long long v = (unsigned long long)m << (e - emin);
+            sum += (u >> 31) ? 0ull - v : v;
+            mag += v;
+        }
+        int gmin = emin, gmax = emax;
+        for (int o = 16; o > 0; o >>= 1) {
+            gmin = min(gmin, __shfl_xor_sync(0xffffffffu, gmin, o));
+            gmax = max(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+        }
+        bad = __any_sync(0xffffffffu, bad) || l - f > kMaxExactRow || (gmin != INT_MAX && gmax - gmin > kMaxSpread);
+        double s = 0.0;
+        if (!bad && gmin != INT_MAX) {
+            // Lane sums in units of 2^gmin: |values| < 2^52, at most 64 per lane.
+            if (emin != INT_MAX) {
+                sum <<= emin - gmin;
+                mag <<= emin - gmin;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                mag += __shfl_xor_sync(0xffffffffu, mag, o);
+            }
+            if (mag < (1ull << 53)) s = ldexp((double)(long long)sum, gmin);  // |sum| < 2^53: exact
+            else bad = true;
+        }
+        if (bad && lane == 0)
+            for (int j = f; j < l; j++) s = __dadd_rn(s, (double)cell(j));
+        if (lane == 0) p[r] = {s, 0.0};
     }
 }
 
@@ -120,10 +204,14 @@ __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict
 
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
                          int64_t len, double* P, int64_t pstride, const double* twiddles, const int64_t* tw_off,
-                         int max_H2, cudaStream_t st, bool backproject) {
+                         int max_H2, cudaStream_t st, bool backproject, const float* orient, int64_t n_cells) {
+    if (orient && backproject) return cudaErrorInvalidValue;  // the gathered cells are not kept for SO
     cd* Pc = reinterpret_cast<cd*>(P);
-    dim3 g1((max_H2 + 255) / 256, b.count);
-    k_radon_sums<<<g1, 256, 0, st>>>(g, b, SI, stride, Pc, pstride);
+    dim3 g1((max_H2 + kSumWarps - 1) / kSumWarps, b.count);
+    if (orient)
+        k_radon_sums<true><<<g1, kSumWarps * 32, 0, st>>>(g, b, SI, stride, orient, n_cells, Pc, pstride);
+    else
+        k_radon_sums<false><<<g1, kSumWarps * 32, 0, st>>>(g, b, SI, stride, orient, n_cells, Pc, pstride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     k_radon_transform<<<b.count, 1024, 0, st>>>(g, b, Pc, pstride, twiddles, tw_off);

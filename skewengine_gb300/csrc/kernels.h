@@ -82,10 +82,14 @@ int sdem_chunk();
 
 // Radon / filtered back-projection (k_radon.cu).  P: per-slot complex scratch
 // of pstride complex doubles; re: per-slot max_H doubles.
-// backproject = false leaves SO untouched (the deskew reads P instead).
+// backproject = false leaves SO untouched (the deskew reads P instead).  With
+// orient set (only with backproject = false, for sectors whose rows stay within
+// dim_i) the row sums gather the skewed cells from the oriented input (n_cells
+// per orientation) and SI is not read: the batch needs no skew launch.
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
                          int64_t stride, int64_t len, double* P, int64_t pstride, const double* twiddles,
-                         const int64_t* tw_off, int max_H2, cudaStream_t st, bool backproject = true);
+                         const int64_t* tw_off, int max_H2, cudaStream_t st, bool backproject = true,
+                         const float* orient = nullptr, int64_t n_cells = 0);
 
 // Local Radon transform (k_lradon.cu): tiles of every sector up to max_H rows
 // and max_cols columns; gauss: 180 x 64 weights, taper: the kept bins' factors.
