@@ -106,10 +106,12 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
                                                 int dimx, int dimy, const cd* __restrict__ Q = nullptr,
                                                 int64_t pstride = 0) {
     __shared__ float band[kRows ? 1 : kDeskewBand][kTile];
-    // kRows: the band's rows as (value, valid range); a cell is its row's value
-    // inside the range and zero outside.
-    __shared__ float rq[kRows ? kDeskewBand : 1];
-    __shared__ int rf[kRows ? kDeskewBand : 1], rl[kRows ? kDeskewBand : 1];
+    // kRows: the band's rows as (value, mask of the tile's columns inside the
+    // row's valid range); a cell is its row's value inside the range, else zero.
+    __shared__ float2 rqm[kRows ? kDeskewBand : 1];
+    // Thread (tx, ty) owns rows ty*kPer .. ty*kPer+kPer-1 of the tile in column
+    // j0+tx: consecutive rows share a skewed cell (row k's upper cell is row
+    // k+1's lower one), so kPer+1 cells per sector serve its kPer rows.
     constexpr int kPer = kDeskewRows / 8;
     const int t = blockIdx.z;
     const int cnt = tl.count[t];
@@ -125,10 +127,12 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
     const int jlast = min(j0 + kTile, dim_i) - 1;
     const int i_end = min(i0 + kDeskewRows, dim_o);
     float* A = acc + t * n;
+    const int ib = ty * kPer;
+    const int nv = min(kPer, i_end - i0 - ib);  // this thread's rows inside the grid
     float s[kPer], c[kPer];
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
-        const int i = i0 + ty + 8 * k;
+        const int i = i0 + ib + k;
         s[k] = (col_ok && i < i_end) ? A[(int64_t)i * dim_i + j] : 0.0f;
         c[k] = (kMode == kDeskewKahan && col_ok && i < i_end) ? comp[t * n + (int64_t)i * dim_i + j] : 0.0f;
     }
@@ -153,10 +157,14 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
             const int tid = ty * kTile + tx;
             if (tid < nrows) {
                 const int r = r0 + tid;
-                const bool in = r < d.H;
-                rq[tid] = in ? __double2float_rn(__dadd_rn(0.0, qv[r].re)) : 0.0f;
-                rf[tid] = in ? rfirst[r] : 0;
-                rl[tid] = in ? rlast[r] : 0;
+                float v = 0.0f;
+                unsigned m = 0;
+                if (r < d.H) {
+                    v = __double2float_rn(__dadd_rn(0.0, qv[r].re));
+                    const int lo_c = max(rfirst[r] - j0, 0), hi_c = min(rlast[r] - j0, kTile);
+                    if (hi_c > lo_c) m = (hi_c >= 32 ? 0xffffffffu : (1u << hi_c) - 1u) & ~((1u << lo_c) - 1u);
+                }
+                rqm[tid] = make_float2(v, __uint_as_float(m));
             }
             __syncthreads();
         } else if (staged) {
@@ -174,24 +182,29 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
                 if (ty + 8 * u < nrows) band[ty + 8 * u][tx] = v[u];
             __syncthreads();
         }
-        if (!col_ok) continue;
+        if (!col_ok || nv <= 0) continue;
         const int off = tj - tmin;
+        // Cells of skewed rows i0+ib+tj .. i0+ib+tj+nv (band rows ib+off ..).
+        float cell[kPer + 1];
+#pragma unroll
+        for (int kk = 0; kk <= kPer; kk++) {
+            cell[kk] = 0.0f;
+            if (kk > nv) continue;
+            const int br = ib + kk + off;
+            const int r = i0 + ib + kk + tj;
+            if (kRows && staged) {
+                const float2 e = rqm[br];
+                cell[kk] = ((__float_as_uint(e.y) >> tx) & 1u) ? e.x : 0.0f;
+            } else if (kRows) {
+                cell[kk] = row_cell(d, rfirst, rlast, qv, r, j);
+            } else {
+                cell[kk] = staged ? band[br][tx] : so[(int64_t)r * dim_i + j];
+            }
+        }
 #pragma unroll
         for (int k = 0; k < kPer; k++) {
-            const int ii = ty + 8 * k;
-            if (i0 + ii >= i_end) continue;
-            float lo, hi;
-            if (kRows && staged) {
-                const int k = ii + off;
-                lo = (j >= rf[k] && j < rl[k]) ? rq[k] : 0.0f;
-                hi = (j >= rf[k + 1] && j < rl[k + 1]) ? rq[k + 1] : 0.0f;
-            } else if (kRows) {
-                lo = row_cell(d, rfirst, rlast, qv, i0 + ii + tj, j);
-                hi = row_cell(d, rfirst, rlast, qv, i0 + ii + tj + 1, j);
-            } else {
-                lo = staged ? band[ii + off][tx] : so[(int64_t)(i0 + ii + tj) * dim_i + j];
-                hi = staged ? band[ii + off + 1][tx] : so[(int64_t)(i0 + ii + tj + 1) * dim_i + j];
-            }
+            if (k >= nv) continue;
+            const float lo = cell[k], hi = cell[k + 1];
             if (kMode == kDeskewMax) {
                 const float m = (lo < hi) ? hi : lo;  // std::max(lo, hi)
                 float v = (s[k] < m) ? m : s[k];      // std::max(acc, m)
@@ -214,7 +227,7 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
     if (!col_ok) return;
 #pragma unroll
     for (int k = 0; k < kPer; k++) {
-        const int i = i0 + ty + 8 * k;
+        const int i = i0 + ib + k;
         if (i >= i_end) continue;
         A[(int64_t)i * dim_i + j] = s[k];
         if (kMode == kDeskewKahan) comp[t * n + (int64_t)i * dim_i + j] = c[k];

@@ -125,16 +125,32 @@ __global__ void __launch_bounds__(kSumWarps * 32)
 }
 
 // In-place reference DIF FFT of x[0..n) by one CTA, then bit reversal.
+// kFinite (every input finite): butterflies with the twiddle (1, 0) skip the
+// multiplication, the others use cmul_finite, and with kRealIn (all imaginary
+// parts zero) the first stage multiplies the real difference only.  The values
+// are the reference's up to the sign of zero results (finite float-derived
+// sums cannot overflow, so no infinity or NaN arises).
+template <bool kFinite, bool kRealIn>
 __device__ void cta_fft(cd* x, int n, const double* __restrict__ tw) {
     for (int h = n >> 1; h >= 1; h >>= 1) {
         const double* t = tw + 2 * (size_t)(n - 2 * h);
+        const bool real_stage = kRealIn && h == (n >> 1);
         for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) {
             const int l = k & (h - 1);
-            const int a = (k / h) * 2 * h + l;
+            const int a = ((k - l) << 1) + l;
             const int bb = a + h;
             const cd xa = x[a], xb = x[bb];
-            x[a] = cadd(xa, xb);
-            x[bb] = cmul(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+            if (!kFinite) {
+                x[a] = cadd(xa, xb);
+                x[bb] = cmul(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+            } else if (real_stage) {
+                const double dr = __dsub_rn(xa.re, xb.re);
+                x[a] = cd{__dadd_rn(xa.re, xb.re), 0.0};
+                x[bb] = cd{__dmul_rn(dr, t[2 * l]), __dmul_rn(dr, t[2 * l + 1])};
+            } else {
+                x[a] = cadd(xa, xb);
+                x[bb] = l == 0 ? csub(xa, xb) : cmul_finite(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+            }
         }
         __syncthreads();
     }
@@ -150,17 +166,9 @@ __device__ void cta_fft(cd* x, int n, const double* __restrict__ tw) {
     __syncthreads();
 }
 
-__global__ void k_radon_transform(DevGeometry g, Batch b, cd* __restrict__ P, int64_t pstride,
-                                  const double* __restrict__ twiddles, const int64_t* __restrict__ tw_off) {
-    const int slot = blockIdx.x;
-    const SectorDesc d = g.desc[b.angle[slot]];
-    const int H = d.H;
-    const int H2 = pow2_at_least(H);
-    cd* x = P + slot * pstride;
-    const double* tw = twiddles + tw_off[31 - __clz(H2)];
-    cta_fft(x, H2, tw);
-    // Ramp filter: i > H/2 -> 0, else (i/H) * P_i (real scalar times complex),
-    // then the conjugation that starts the inverse transform (helper.h:110).
+// Ramp filter: i > H/2 -> 0, else (i/H) * P_i (real scalar times complex),
+// then the conjugation that starts the inverse transform (helper.h:110).
+__device__ void ramp_filter(cd* x, int H, int H2) {
     for (int i = threadIdx.x; i < H2; i += blockDim.x) {
         cd v = x[i];
         if (i > H / 2) {
@@ -172,9 +180,44 @@ __global__ void k_radon_transform(DevGeometry g, Batch b, cd* __restrict__ P, in
         x[i] = {v.re, -v.im};
     }
     __syncthreads();
-    cta_fft(x, H2, tw);
+}
+
+// One CTA per sector.  Sectors with H2 <= kSmemH2 transform a copy of their
+// row sums in shared memory (smem > 0), larger ones work in place in P.  The
+// final division by H2 (kernelRADN.h:255) is a multiplication by the exact
+// power of two 1/H2: the same correctly rounded quotient.
+constexpr int kTransformThreads = 256;
+constexpr int kSmemH2 = 8192;
+
+__global__ void __launch_bounds__(kTransformThreads)
+    k_radon_transform(DevGeometry g, Batch b, cd* __restrict__ P, int64_t pstride,
+                      const double* __restrict__ twiddles, const int64_t* __restrict__ tw_off, int smem) {
+    extern __shared__ cd xs[];
+    const int slot = blockIdx.x;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const int H = d.H;
+    const int H2 = pow2_at_least(H);
+    cd* p = P + slot * pstride;
+    cd* x = smem ? xs : p;
+    const double* tw = twiddles + tw_off[31 - __clz(H2)];
+    int bad = 0;
+    for (int i = threadIdx.x; i < H2; i += blockDim.x) {
+        const cd v = p[i];
+        if (smem) x[i] = v;
+        bad |= !isfinite(v.re);
+    }
+    if (!__syncthreads_or(bad)) {
+        cta_fft<true, true>(x, H2, tw);
+        ramp_filter(x, H, H2);
+        cta_fft<true, false>(x, H2, tw);
+    } else {
+        cta_fft<false, false>(x, H2, tw);
+        ramp_filter(x, H, H2);
+        cta_fft<false, false>(x, H2, tw);
+    }
     // conj, then divide by H2: only the real part is used (kernelRADN.h:255).
-    for (int i = threadIdx.x; i < H; i += blockDim.x) x[i].re = __ddiv_rn(x[i].re, (double)H2);
+    const double inv = 1.0 / (double)H2;
+    for (int i = threadIdx.x; i < H; i += blockDim.x) p[i].re = __dmul_rn(x[i].re, inv);
 }
 
 __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict__ P, int64_t pstride,
@@ -214,7 +257,12 @@ cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, 
         k_radon_sums<false><<<g1, kSumWarps * 32, 0, st>>>(g, b, SI, stride, orient, n_cells, Pc, pstride);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_radon_transform<<<b.count, 1024, 0, st>>>(g, b, Pc, pstride, twiddles, tw_off);
+    const int smem = max_H2 <= kSmemH2 ? max_H2 * (int)sizeof(cd) : 0;
+    if (smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(k_radon_transform, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_radon_transform<<<b.count, kTransformThreads, smem, st>>>(g, b, Pc, pstride, twiddles, tw_off, smem);
     e = cudaGetLastError();
     if (e != cudaSuccess || !backproject) return e;
     int64_t blocks = (len + 255) / 256;
