@@ -123,6 +123,33 @@ def test_radon_rows_within_width_non_square(ske, oracle):
     assert np.abs(kahan - want).max() <= 1e-5 * np.abs(want).max()
 
 
+@pytest.mark.parametrize("case", ["wide", "nonfinite"])
+def test_radon_special_values_bit_exact(ske, oracle, case):
+    """Rows outside the exact integer row sums' conditions (exponent spread
+    above 28 binades, magnitude sums at or above 2^53 units, subnormals,
+    cancellation to zero) take the sequential binary64 sum; non-finite row sums
+    take the transform's exact complex products.  Results equal the oracle's
+    (NaNs compared as NaNs)."""
+    x = synthetic.ellipse_phantom(64, 21).astype(np.float32)
+    if case == "wide":
+        x[5, :] = 1e30
+        x[5, 1::2] = -1e30
+        x[7, 3] = 1e-30
+        x[9, :] = 1e-40
+        x[12, :20] = 3.0e7
+        x[12, 20:24] = 1e-3
+        x[15, :] = np.where(np.arange(64) % 2, 1.5, -1.5)
+        x[20:40, 50] = 6e-39
+    else:
+        x[11, 11] = np.inf
+        x[30, 2] = np.nan
+        x[40, 40] = -np.inf
+    got = _run(ske, 2, x)
+    want = oracle.run(2, x, povh=POVH)
+    same = (got.view(np.uint32) == want.view(np.uint32)) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), (case, int((~same).sum()))
+
+
 def test_radon_512_matches_oracle(ske, oracle):
     x = synthetic.ellipse_phantom(512, 7)
     assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
