@@ -45,6 +45,46 @@ constexpr int kSumWarps = 8;
 constexpr int kMaxSpread = 28;
 constexpr int kMaxExactRow = 2048;
 
+// x << n for 0 <= n; n >= 64 gives 0 (PTX clamps the shift amount).
+__device__ __forceinline__ unsigned long long shl64(unsigned long long x, int n) {
+    unsigned long long y;
+    asm("shl.b64 %0, %1, %2;" : "=l"(y) : "l"(x), "r"(n));
+    return y;
+}
+
+// Per-lane part of an exact row sum.  A float with biased exponent field e8
+// and significand m (hidden bit included) is m * 2^(max(e8, 1) - 150).  The
+// lane keeps the sums of its positive and of its negative values as integers
+// in units of 2^(emin - 150), emin its smallest exponent of a nonzero value so
+// far (they are shifted left when emin drops); emax is its largest exponent
+// field (255 for an infinity or NaN).  Values far apart in exponent may wrap
+// the integers: the spread test at the end rejects those rows.
+struct ExactPart {
+    unsigned long long pos = 0, neg = 0;
+    int emin = INT_MAX, emax = 0;
+    __device__ __forceinline__ void add(float v) {
+        const unsigned u = __float_as_uint(v);
+        const int e8 = (int)((u >> 23) & 0xffu);
+        const unsigned m = (u & 0x7fffffu) | (e8 ? 0x800000u : 0u);
+        const int ee = m ? max(e8, 1) : INT_MAX;  // zeros leave emin alone
+        if (ee < emin) {
+            const int sh = emin == INT_MAX ? 0 : emin - ee;
+            pos = shl64(pos, sh);
+            neg = shl64(neg, sh);
+            emin = ee;
+        }
+        emax = max(emax, e8);
+        const unsigned long long x = shl64(m, ee - emin);  // m = 0: shift clamps, x = 0
+        const unsigned long long xn = (u >> 31) ? x : 0ull;
+        neg += xn;
+        pos += x - xn;
+    }
+    // Not an exact candidate: a non-finite value or a spread above kMaxSpread.
+    __device__ __forceinline__ bool bad() const {
+        return emax == 0xff || (emin != INT_MAX && emax - emin > kMaxSpread);
+    }
+};
+
 template <bool kGather>
 __global__ void __launch_bounds__(kSumWarps * 32)
     k_radon_sums(DevGeometry g, Batch b, const float* __restrict__ SI, int64_t stride, const float* __restrict__ orient,
@@ -67,56 +107,33 @@ __global__ void __launch_bounds__(kSumWarps * 32)
         const int f = g.first[d.row_off + r], l = g.last[d.row_off + r];
         const float* row = in + (int64_t)r * d.dim_i;
         auto cell = [&](int j) { return kGather ? skew_gather(d, tgt, wgt, src, r, j) : row[j]; };
-        // Per lane: integer sum in units of 2^emin (rescaled when emin drops).
-        unsigned long long sum = 0, mag = 0;
-        int emin = INT_MAX, emax = INT_MIN;
-        bool bad = false;
-        for (int j = f + lane; j < l; j += 32) {
-            const unsigned u = __float_as_uint(cell(j));
-            const int ef = (int)((u >> 23) & 0xffu);
-            const unsigned m = ef ? ((u & 0x7fffffu) | 0x800000u) : (u & 0x7fffffu);
-            bad |= ef == 0xff;
-            if (m == 0 || bad) continue;
-            const int e = ef ? ef - 150 : -149;
-            if (e < emin) {
-                if (emin != INT_MAX) {
-                    if (emin - e > kMaxSpread) {
-                        bad = true;
-                        continue;
-                    }
-                    sum <<= emin - e;
-                    mag <<= emin - e;
-                }
-                emin = e;
-            }
-            emax = max(emax, e);
-            if (emax - emin > kMaxSpread) {
-                bad = true;
-                continue;
-            }
-            const unsigned long long v = (unsigned long long)m << (e - emin);
-            sum += (u >> 31) ? 0ull - v : v;
-            mag += v;
-        }
-        int gmin = emin, gmax = emax;
+        ExactPart a;
+#pragma unroll 2
+        for (int j = f + lane; j < l; j += 32) a.add(cell(j));
+        const bool lane_bad = a.bad();
+        int gmin = a.emin, gmax = a.emax;
         for (int o = 16; o > 0; o >>= 1) {
             gmin = min(gmin, __shfl_xor_sync(0xffffffffu, gmin, o));
             gmax = max(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
         }
-        bad = __any_sync(0xffffffffu, bad) || l - f > kMaxExactRow || (gmin != INT_MAX && gmax - gmin > kMaxSpread);
+        bool bad = __any_sync(0xffffffffu, lane_bad) || l - f > kMaxExactRow ||
+                   (gmin != INT_MAX && gmax - gmin > kMaxSpread);  // gmax: largest field, >= any nonzero's
+
         double s = 0.0;
         if (!bad && gmin != INT_MAX) {
-            // Lane sums in units of 2^gmin: |values| < 2^52, at most 64 per lane.
-            if (emin != INT_MAX) {
-                sum <<= emin - gmin;
-                mag <<= emin - gmin;
-            }
+            // Units of 2^(gmin - 150): every value < 2^52, at most 2048 of them.
+            const int sh = a.emin == INT_MAX ? 0 : a.emin - gmin;
+            unsigned long long pos = shl64(a.pos, sh), neg = shl64(a.neg, sh);
             for (int o = 16; o > 0; o >>= 1) {
-                sum += __shfl_xor_sync(0xffffffffu, sum, o);
-                mag += __shfl_xor_sync(0xffffffffu, mag, o);
+                pos += __shfl_xor_sync(0xffffffffu, pos, o);
+                neg += __shfl_xor_sync(0xffffffffu, neg, o);
             }
-            if (mag < (1ull << 53)) s = ldexp((double)(long long)sum, gmin);  // |sum| < 2^53: exact
-            else bad = true;
+            if (pos + neg < (1ull << 53)) {  // every partial sum exact: the exact sum
+                const double scale = __longlong_as_double((long long)(gmin - 150 + 1023) << 52);
+                s = __dmul_rn(__ll2double_rn((long long)(pos - neg)), scale);
+            } else {
+                bad = true;
+            }
         }
         if (bad && lane == 0)
             for (int j = f; j < l; j++) s = __dadd_rn(s, (double)cell(j));

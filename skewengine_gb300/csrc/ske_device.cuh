@@ -38,12 +38,15 @@ __device__ __forceinline__ float skew_gather(const SectorDesc& d, const int32_t*
                                              int r, int c) {
     const int t = tgt[c];
     const float w = wgt[c];
-    float acc = 0.0f;
     const int i0 = r - t - 1;
-    if (i0 >= 0 && i0 < d.dim_o) acc = __fadd_rn(acc, __fmul_rn(w, src[(int64_t)i0 * d.dim_i + c]));
-    const int i1 = r - t;
-    if (i1 >= 0 && i1 < d.dim_o)
-        acc = __fadd_rn(acc, __fmul_rn(__fsub_rn(1.0f, w), src[(int64_t)i1 * d.dim_i + c]));
+    // Branch-free: both loads predicated, the additions selected.
+    const bool v0 = (unsigned)i0 < (unsigned)d.dim_o, v1 = (unsigned)(i0 + 1) < (unsigned)d.dim_o;
+    const float* p0 = src + ((int64_t)i0 * d.dim_i + c);
+    const float a = v0 ? p0[0] : 0.0f;
+    const float b = v1 ? p0[d.dim_i] : 0.0f;
+    float acc = 0.0f;
+    acc = v0 ? __fadd_rn(acc, __fmul_rn(w, a)) : acc;
+    acc = v1 ? __fadd_rn(acc, __fmul_rn(__fsub_rn(1.0f, w), b)) : acc;
     return acc;
 }
 
