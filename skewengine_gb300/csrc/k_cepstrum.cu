@@ -22,7 +22,7 @@ namespace {
 constexpr int kWin = kBlurWindow;  // 64
 constexpr int kWarpsPerBlock = 8;
 
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
     k_cepstrum(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO, int64_t stride,
                int64_t len, const double* __restrict__ tw64, const double* __restrict__ tw32) {
     __shared__ cd xs[kWarpsPerBlock][kWin];
@@ -73,25 +73,27 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
         // A zero power gives log = -inf: such cells keep the exact FFT.
         if (__all_sync(0xffffffffu, isfinite(x[lane].re))) warp_fft_real(x, kWin / 2, twb, lane);
         else warp_fft(x, kWin / 2, twb, lane);
-        if (lane == 0) {
-            double s[kWin / 4];
-#pragma unroll
-            for (int k = 0; k < kWin / 4; k++) {
-                const double c = __dmul_rn(x[k].re, norm32);
-                s[k] = -((c < 0.0) ? c : 0.0);  // -std::min(0.0, c)
+        // s_k = -min(0, c_k) for k < 16 (lane k), then getBlurParameter2: from
+        // index 5 skip the non-ascending head; the result is the sample before
+        // the first ascent or any larger sample after the ascending one.  The
+        // samples are -0 or positive (never +0 or NaN), so the reference's
+        // sequential `s > best` scan and a max reduction give the same value.
+        const int k = lane & (kWin / 4 - 1);
+        const double c = __dmul_rn(x[k].re, norm32);
+        const double sk = -((c < 0.0) ? c : 0.0);  // -std::min(0.0, c)
+        const double prev = __shfl_up_sync(0xffffffffu, sk, 1);
+        const unsigned asc = __ballot_sync(0xffffffffu, lane >= 5 && lane < kWin / 4 && sk > prev);
+        double best = 0.0;
+        if (asc) {
+            const int i = __ffs(asc) - 1;  // first ascent
+            double m = (lane == i - 1 || (lane > i && lane < kWin / 4)) ? sk : -0.0;
+            for (int o = 16; o > 0; o >>= 1) {
+                const double t = __shfl_xor_sync(0xffffffffu, m, o);
+                m = t > m ? t : m;
             }
-            // getBlurParameter2: skip the non-ascending head from index 5, then the
-            // largest sample after the first ascent (that sample itself skipped).
-            int i = 5;
-            while (i < kWin / 4 && !(s[i] > s[i - 1])) i++;
-            double best = 0.0;
-            if (i < kWin / 4) {
-                best = s[i - 1];
-                for (int k = i + 1; k < kWin / 4; k++)
-                    if (s[k] > best) best = s[k];
-            }
-            out[p] = __double2float_rn(__dmul_rn(best, 10000.0));
+            best = m;
         }
+        if (lane == 0) out[p] = __double2float_rn(__dmul_rn(best, 10000.0));
         __syncwarp();
     }
 }
