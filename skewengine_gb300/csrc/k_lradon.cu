@@ -121,19 +121,15 @@ __global__ void __launch_bounds__(kWarps * 32)
         for (int m = lane; m < kW; m += 32)
             x[m] = finite ? cd{__dmul_rn(x[m].re, 0.125), __dmul_rn(x[m].im, 0.125)} : cmul(x[m], scale);
         __syncwarp();
-        if (lane == 0) {
-            double prev = __dadd_rn(__dmul_rn(x[4].re, x[4].re), __dmul_rn(x[4].im, x[4].im));
-            double v = 0.0;
-            for (int m = 5; m < kHalf; m++) {
-                const double nm = __dadd_rn(__dmul_rn(x[m].re, x[m].re), __dmul_rn(x[m].im, x[m].im));
-                if (nm > prev) {
-                    v = prev;
-                    break;
-                }
-                prev = nm;
-            }
-            out[p] = __double2float_rn(v);
-        }
+        // getParameter: from m = 5 the first |Z_m|^2 > |Z_{m-1}|^2 gives
+        // |Z_{m-1}|^2 (none: 0).  Lane m forms |Z_m|^2 (the reference's
+        // products and sum); a ballot finds the first ascent.
+        const double nm = __dadd_rn(__dmul_rn(x[lane].re, x[lane].re), __dmul_rn(x[lane].im, x[lane].im));
+        const double prev = __shfl_up_sync(0xffffffffu, nm, 1);
+        const unsigned asc = __ballot_sync(0xffffffffu, lane >= 5 && lane < kHalf && nm > prev);
+        const int ia = asc ? __ffs(asc) - 1 : 1;
+        const double v = __shfl_sync(0xffffffffu, nm, ia - 1);
+        if (lane == 0) out[p] = __double2float_rn(asc ? v : 0.0);
         __syncwarp();
     }
 }
