@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
         __syncwarp();
         // Finite real input: the reduced-work FFT gives the same values up to the
         // sign of zeros, which neither |X|^2 nor -min(0, c) can see.
-        if (__all_sync(0xffffffffu, fin)) warp_fft_real(x, kWin, twa, lane);
+        if (__all_sync(0xffffffffu, fin)) warp_fft_real<kKeepLow>(x, kWin, twa, lane);  // X_k, k < 32
         else warp_fft(x, kWin, twa, lane);
         // |X_k|^2 of the 1/sqrt(64)-scaled spectrum, k < 32, then its log.
         {
@@ -71,7 +71,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 6)
         }
         __syncwarp();
         // A zero power gives log = -inf: such cells keep the exact FFT.
-        if (__all_sync(0xffffffffu, isfinite(x[lane].re))) warp_fft_real(x, kWin / 2, twb, lane);
+        if (__all_sync(0xffffffffu, isfinite(x[lane].re)))
+            warp_fft_real<kKeepLowRe>(x, kWin / 2, twb, lane);  // Re c_k, k < 16
         else warp_fft(x, kWin / 2, twb, lane);
         // s_k = -min(0, c_k) for k < 16 (lane k), then getBlurParameter2: from
         // index 5 skip the non-ascending head; the result is the sample before

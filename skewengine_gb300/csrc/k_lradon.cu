@@ -108,18 +108,23 @@ __global__ void __launch_bounds__(kWarps * 32)
         if (j >= d.dim_i && owner_row(d, first, last, p) != i) continue;
         for (int m = lane; m < kW; m += 32) x[m] = cd{__dmul_rn(sm.w[ci + m][cj], sm.gauss[m]), 0.0};
         __syncwarp();
-        if (finite) warp_fft_real(x, kW, sm.tw, lane);
+        // Only Re X_k for k < 26 is read: the pruned FFT forms Re X_k, k < 32.
+        if (finite) warp_fft_real<kKeepLowRe>(x, kW, sm.tw, lane);
         else warp_fft(x, kW, sm.tw, lane);
         for (int m = lane; m < kW; m += 32) {
-            // Finite: x * (0.125, 0) is (re/8, im/8) up to the sign of zeros.
-            const double re = finite ? __dmul_rn(x[m].re, 0.125) : cmul(x[m], scale).re;
-            x[m] = cd{m < kLocalRadonKeep ? __dmul_rn(sm.taper[m], re) : 0.0, 0.0};
+            double y = 0.0;
+            if (m < kLocalRadonKeep) {
+                // Finite: x * (0.125, 0) is (re/8, im/8) up to the sign of zeros.
+                const double re = finite ? __dmul_rn(x[m].re, 0.125) : cmul(x[m], scale).re;
+                y = __dmul_rn(sm.taper[m], re);
+            }
+            x[m] = cd{y, 0.0};
         }
         __syncwarp();
-        if (finite) warp_fft_real(x, kW, sm.tw, lane);
+        // Y is zero from bin 26 on; only Z_m for m < 32 is read.
+        if (finite) warp_fft_real<kKeepLow, true>(x, kW, sm.tw, lane);
         else warp_fft(x, kW, sm.tw, lane);
-        for (int m = lane; m < kW; m += 32)
-            x[m] = finite ? cd{__dmul_rn(x[m].re, 0.125), __dmul_rn(x[m].im, 0.125)} : cmul(x[m], scale);
+        x[lane] = finite ? cd{__dmul_rn(x[lane].re, 0.125), __dmul_rn(x[lane].im, 0.125)} : cmul(x[lane], scale);
         __syncwarp();
         // getParameter: from m = 5 the first |Z_m|^2 > |Z_{m-1}|^2 gives
         // |Z_{m-1}|^2 (none: 0).  Lane m forms |Z_m|^2 (the reference's

@@ -163,6 +163,11 @@ __device__ __forceinline__ cd cmul_finite(cd x, cd y) {
             __dadd_rn(__dmul_rn(x.re, y.im), __dmul_rn(x.im, y.re))};
 }
 
+// Outputs a warp_fft_real caller reads: all of them, X_k for k < n/2, or only
+// Re X_k for k < n/2.  The pruned variants leave out work whose results are
+// never read; the values they do produce are the same.
+enum FftKeep { kKeepAll = 0, kKeepLow = 1, kKeepLowRe = 2 };
+
 // warp_fft for finite input whose imaginary parts are all zero (n = 64 or 32),
 // with the same values as warp_fft up to the sign of zero results:
 //  * first stage: the operands are real, so (a - b) * T is (d*T.re, d*T.im)
@@ -173,15 +178,27 @@ __device__ __forceinline__ cd cmul_finite(cd x, cd y) {
 //    applies.  Callers use it only when every
 // input is finite; results that feed squared magnitudes or comparisons of
 // magnitudes are then bit-identical to warp_fft's.
+// kKeep: the last stage's butterfly (2k, 2k+1) produces X_r and X_{r+n/2}
+// (r = bitrev(2k)), so kKeepLow forms only the sums; kKeepLowRe also forms
+// only the real parts in the last two stages.  With kZeroHigh the upper half
+// of the input is known to be zero: the first stage's sums are the lower
+// half itself (up to zero signs).
+template <int kKeep = kKeepAll, bool kZeroHigh = false>
 __device__ __forceinline__ void warp_fft_real(cd* x, int n, const double* __restrict__ tw, int lane) {
     {  // first stage, h = n/2: butterfly k pairs k and k + n/2 with twiddle T^k
         const int h = n >> 1;
         const double* t = tw;  // stage of half-span n/2 starts at entry 0
         for (int k = lane; k < h; k += 32) {
-            const double xa = x[k].re, xb = x[k + h].re;
-            const double d = __dsub_rn(xa, xb);
-            x[k] = cd{__dadd_rn(xa, xb), 0.0};
-            x[k + h] = cd{__dmul_rn(d, t[2 * k]), __dmul_rn(d, t[2 * k + 1])};
+            const double xa = x[k].re;
+            if (kZeroHigh) {
+                x[k] = cd{xa, 0.0};
+                x[k + h] = cd{__dmul_rn(xa, t[2 * k]), __dmul_rn(xa, t[2 * k + 1])};
+            } else {
+                const double xb = x[k + h].re;
+                const double d = __dsub_rn(xa, xb);
+                x[k] = cd{__dadd_rn(xa, xb), 0.0};
+                x[k + h] = cd{__dmul_rn(d, t[2 * k]), __dmul_rn(d, t[2 * k + 1])};
+            }
         }
         __syncwarp();
     }
@@ -192,15 +209,26 @@ __device__ __forceinline__ void warp_fft_real(cd* x, int n, const double* __rest
             const int a = (k / h) * 2 * h + l;
             const int bb = a + h;
             const cd xa = x[a], xb = x[bb];
-            x[a] = cadd(xa, xb);
-            x[bb] = cmul_finite(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+            if (kKeep == kKeepLowRe && h == 2) {
+                // Only the real parts feed the last stage's real sums.
+                const cd dd = csub(xa, xb);
+                x[a].re = __dadd_rn(xa.re, xb.re);
+                x[bb].re = __dsub_rn(__dmul_rn(dd.re, t[2 * l]), __dmul_rn(dd.im, t[2 * l + 1]));
+            } else {
+                x[a] = cadd(xa, xb);
+                x[bb] = cmul_finite(csub(xa, xb), cd{t[2 * l], t[2 * l + 1]});
+            }
         }
         __syncwarp();
     }
     for (int k = lane; k < (n >> 1); k += 32) {  // last stage, h = 1, twiddle (1, 0)
         const cd xa = x[2 * k], xb = x[2 * k + 1];
-        x[2 * k] = cadd(xa, xb);
-        x[2 * k + 1] = csub(xa, xb);
+        if (kKeep == kKeepLowRe) {
+            x[2 * k].re = __dadd_rn(xa.re, xb.re);
+        } else {
+            x[2 * k] = cadd(xa, xb);
+            if (kKeep == kKeepAll) x[2 * k + 1] = csub(xa, xb);
+        }
     }
     __syncwarp();
     const unsigned bits = 31 - __clz(n);
