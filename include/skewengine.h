@@ -280,6 +280,39 @@ int ske_measure_fp32_peak(int device, double* scalar_ops, double* packed_ops);
  * compute in double precision like the reference.  No reference counterpart. */
 int ske_measure_fp64_peak(int device, double* dfma_ops);
 
+/* ---- Image input/output (host only; no GPU) ------------------------------
+ * The reference's image operators read their input with helper::read_png
+ * (src/helper.h:167-184: decode to 8-bit RGBA, then R + G + B per pixel) and
+ * write results as PNG images coloured by showResults / showResultsRADN /
+ * showResultsCEPS (src/main.h:124-141, src/kernelRADN.h:384-400,
+ * src/kernelBLUR.h:396-410) with HSVtoRGB (src/color.cpp:80-115).
+ * Every function returns SKE_OK or SKE_ERR_INVALID (unreadable or malformed
+ * file, buffer too small, bad argument). */
+
+/* Width and height of a PNG file. */
+int ske_png_size(const char* path, int* width, int* height);
+/* Decode a PNG (any colour type, bit depth, interlacing) to 8-bit RGBA, as the
+ * reference's PNG library does; capacity in bytes (>= 4 * width * height). */
+int ske_png_read_rgba(const char* path, uint8_t* rgba, size_t capacity);
+/* The reference's image input: one float per pixel, R + G + B of the decoded
+ * RGBA (replaces read_png + configureRADN/configureCEPS, src/kernelRADN.h:77-87);
+ * capacity in floats (>= width * height). */
+int ske_png_read_image(const char* path, float* image, size_t capacity);
+/* Write 8-bit grey (channels 1) or RGB (channels 3) pixels as a PNG file
+ * (replaces lodepng::encode(..., LCT_GREY / LCT_RGB) in the result writers). */
+int ske_png_write(const char* path, const uint8_t* pixels, int width, int height, int channels);
+/* HSVtoRGB (src/color.cpp:80-115) with the reference's float arithmetic. */
+void ske_hsv_to_rgb(float h, float s, float v, uint8_t* rgb);
+/* The reference's colouring of an operator's output grid into 3 * dimx * dimy
+ * RGB bytes: Radon (and local Radon) grey with the automatic scale
+ * 255 / (max - min) shifted by min, image identity grey / 540, cepstrum and DEM
+ * identity as HSV (hue = output mod 360).  SKE_KERNEL_SDEM has no colouring in
+ * the reference (it writes raw floats) and returns SKE_ERR_INVALID. */
+int ske_render(int kernel, const float* output, int dimx, int dimy, uint8_t* rgb);
+/* The grey image the result writers store beside it: (R + G + B) / 3 of the
+ * input image given as ske_png_read_image returns it. */
+int ske_render_input(const float* image, int count, uint8_t* grey);
+
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
  * a raw float32 file or a synthetic input and writes the result.  See
  * INTEGRATION.md for the argument list. */

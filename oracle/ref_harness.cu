@@ -177,4 +177,67 @@ int skref_set_local_radon(int on) {
     return 0;
 }
 
+// Result rendering and PNG coding as the reference does them: HSVtoRGB from
+// src/color.cpp:80-115, helper::getMinMax (src/helper.h:190-201) and the
+// reference's vendored lodepng (src/third-party/Lodepng.cpp), which its
+// read_png (src/helper.h:167-184) and result writers (kernelRADN.h:384-400,
+// kernelBLUR.h:396-410) call.  Used only to generate golden fixtures.
+int skref_hsv_to_rgb(float h, float s, float v, unsigned char* rgb) {
+    const rgbColor c = HSVtoRGB({h, s, v});
+    rgb[0] = c.R;
+    rgb[1] = c.G;
+    rgb[2] = c.B;
+    return 0;
+}
+
+int skref_min_max(float* data, int n, float* mn, float* mx) {
+    dimx = n;
+    dimy = 1;
+    const pair_t p = helper::getMinMax(data);
+    *mn = p.min;
+    *mx = p.max;
+    return 0;
+}
+
+// Encode 8-bit RGBA pixels as a PNG of the given colour type and bit depth
+// (lodepng's own conversion), optionally Adam7-interlaced.
+int skref_png_encode(const char* path, const unsigned char* rgba, unsigned w, unsigned h, int colortype,
+                     int bitdepth, int interlace) {
+    lodepng::State st;
+    st.info_raw.colortype = LCT_RGBA;
+    st.info_raw.bitdepth = 8;
+    st.info_png.color.colortype = (LodePNGColorType)colortype;
+    st.info_png.color.bitdepth = (unsigned)bitdepth;
+    st.info_png.interlace_method = (unsigned)interlace;
+    st.encoder.auto_convert = LAC_NO;
+    std::vector<unsigned char> img(rgba, rgba + (size_t)w * h * 4), png;
+    const unsigned err = lodepng::encode(png, img, w, h, st);
+    if (err) return (int)err;
+    return (int)lodepng_save_file(png.data(), png.size(), path);
+}
+
+// Encode with lodepng's automatic choice of the smallest lossless colour type
+// (palette, grey, low bit depths), optionally interlaced.
+int skref_png_encode_auto(const char* path, const unsigned char* rgba, unsigned w, unsigned h, int interlace) {
+    lodepng::State st;
+    st.info_raw.colortype = LCT_RGBA;
+    st.info_raw.bitdepth = 8;
+    st.info_png.interlace_method = (unsigned)interlace;
+    st.encoder.auto_convert = LAC_AUTO;
+    std::vector<unsigned char> img(rgba, rgba + (size_t)w * h * 4), png;
+    const unsigned err = lodepng::encode(png, img, w, h, st);
+    if (err) return (int)err;
+    return (int)lodepng_save_file(png.data(), png.size(), path);
+}
+
+// Decode to 8-bit RGBA as read_png does (lodepng::decode's default).
+int skref_png_decode(const char* path, unsigned char* rgba, size_t cap, unsigned* w, unsigned* h) {
+    std::vector<unsigned char> img;
+    const unsigned err = lodepng::decode(img, *w, *h, path);
+    if (err) return (int)err;
+    if (img.size() > cap) return -1;
+    memcpy(rgba, img.data(), img.size());
+    return 0;
+}
+
 }  // extern "C"

@@ -78,6 +78,13 @@ SIGNATURES = [
                                         C.POINTER(C.c_uint32)]),
     ("ske_measure_fp32_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("ske_measure_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    ("ske_png_size", C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("ske_png_read_rgba", C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t]),
+    ("ske_png_read_image", C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t]),
+    ("ske_png_write", C.c_int, [C.c_char_p, C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    ("ske_hsv_to_rgb", None, [C.c_float, C.c_float, C.c_float, C.c_void_p]),
+    ("ske_render", C.c_int, [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    ("ske_render_input", C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     ("run", C.c_int, [C.c_int, C.POINTER(C.c_char_p)]),
 ]
 

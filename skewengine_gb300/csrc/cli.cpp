@@ -10,8 +10,14 @@
 //              (src/kernelSDEM.h:43-50); dimx/dimy 0 take NCOLS/NROWS from the
 //              .hdr beside it, else a square grid from the file size
 //              (check_dem, src/kernelSDEM.h:98-142)
+//              A .png input is an image read as the reference's image operators
+//              read theirs (helper::read_png, src/helper.h:167-184: R + G + B per
+//              pixel); dimx/dimy 0 take its size.
 //   output     raw float32 grid (the .flt dump of showResultsSDEM,
-//              src/kernelSDEM.h:433-439)
+//              src/kernelSDEM.h:433-439), or, for a name ending in .png, the
+//              reference's coloured result image (showResults, src/main.h:124-141)
+//              and, for an image input, its grey copy as <stem>_input.png (the
+//              reference's salida2.png and salida1.png)
 //   max_sector angles 0..max_sector-1 (default 180), povh observer height in cell
 //              units (default 0.15), accum 0 reference order / 1 Kahan.
 //
@@ -69,6 +75,22 @@ long file_size(const char* path) {
 }
 
 int load_input(const std::string& path, int* dimx, int* dimy, std::vector<float>& out) {
+    if (ends_with(path, ".png")) {
+        int w = 0, h = 0;
+        int rc = ske_png_size(path.c_str(), &w, &h);
+        if (rc != SKE_OK) {
+            fprintf(stderr, "run: cannot read image %s\n", path.c_str());
+            return rc;
+        }
+        if ((*dimx > 0 && *dimx != w) || (*dimy > 0 && *dimy != h)) {
+            fprintf(stderr, "run: %s is %dx%d, not %dx%d\n", path.c_str(), w, h, *dimx, *dimy);
+            return SKE_ERR_INVALID;
+        }
+        *dimx = w;
+        *dimy = h;
+        out.resize((size_t)w * h);
+        return ske_png_read_image(path.c_str(), out.data(), out.size());
+    }
     const bool bil = ends_with(path, ".bil");
     const long bytes = file_size(path.c_str());
     if (bytes < 0) {
@@ -136,9 +158,23 @@ extern "C" int run(int argc, char** argv) {
     if (rc != SKE_OK) fprintf(stderr, "run: %s\n", ske_last_error());
     ske_destroy(e);
     if (rc != SKE_OK) return rc;
-    FILE* f = fopen(argv[5], "wb");
+    const std::string dst = argv[5];
+    if (ends_with(dst, ".png")) {
+        std::vector<uint8_t> rgb(out.size() * 3);
+        rc = ske_render(kernel, out.data(), dimx, dimy, rgb.data());
+        if (rc == SKE_OK) rc = ske_png_write(dst.c_str(), rgb.data(), dimx, dimy, 3);
+        if (rc == SKE_OK && ends_with(argv[2], ".png")) {
+            std::vector<uint8_t> grey(in.size());
+            rc = ske_render_input(in.data(), (int)in.size(), grey.data());
+            if (rc == SKE_OK)
+                rc = ske_png_write((dst.substr(0, dst.size() - 4) + "_input.png").c_str(), grey.data(), dimx, dimy, 1);
+        }
+        if (rc != SKE_OK) fprintf(stderr, "run: cannot render or write %s\n", dst.c_str());
+        return rc;
+    }
+    FILE* f = fopen(dst.c_str(), "wb");
     if (!f) {
-        fprintf(stderr, "run: cannot write %s\n", argv[5]);
+        fprintf(stderr, "run: cannot write %s\n", dst.c_str());
         return SKE_ERR_INVALID;
     }
     fwrite(out.data(), sizeof(float), out.size(), f);

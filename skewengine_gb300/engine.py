@@ -267,6 +267,53 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
     return outs
 
 
+def png_size(path: str) -> tuple[int, int]:
+    """(width, height) of a PNG file."""
+    w, h = C.c_int(), C.c_int()
+    check(load().ske_png_size(str(path).encode(), C.byref(w), C.byref(h)))
+    return w.value, h.value
+
+
+def read_png_rgba(path: str) -> np.ndarray:
+    """The PNG decoded to 8-bit RGBA (height x width x 4)."""
+    w, h = png_size(path)
+    out = np.zeros((h, w, 4), np.uint8)
+    check(load().ske_png_read_rgba(str(path).encode(), out.ctypes.data, out.nbytes))
+    return out
+
+
+def read_image(path: str) -> np.ndarray:
+    """The reference's image input (helper::read_png, src/helper.h:167-184): a
+    float32 grid of R + G + B per pixel."""
+    w, h = png_size(path)
+    out = np.zeros((h, w), np.float32)
+    check(load().ske_png_read_image(str(path).encode(), out.ctypes.data, out.size))
+    return out
+
+
+def write_png(path: str, pixels: np.ndarray) -> None:
+    """Write uint8 grey (h x w) or RGB (h x w x 3) pixels as a PNG file."""
+    px = np.ascontiguousarray(pixels, np.uint8)
+    ch = 1 if px.ndim == 2 else px.shape[2]
+    check(load().ske_png_write(str(path).encode(), px.ctypes.data, px.shape[1], px.shape[0], ch))
+
+
+def render(kernel, output: np.ndarray) -> np.ndarray:
+    """The reference's colouring of an operator's output (h x w x 3 uint8)."""
+    out = np.ascontiguousarray(output, np.float32)
+    rgb = np.zeros(out.shape + (3,), np.uint8)
+    check(load().ske_render(_kernel_id(kernel), out.ctypes.data, out.shape[1], out.shape[0], rgb.ctypes.data))
+    return rgb
+
+
+def render_input(image: np.ndarray) -> np.ndarray:
+    """The grey input image the reference writes beside a result: (R + G + B) / 3."""
+    img = np.ascontiguousarray(image, np.float32)
+    grey = np.zeros(img.shape, np.uint8)
+    check(load().ske_render_input(img.ctypes.data, img.size, grey.ctypes.data))
+    return grey
+
+
 def cli_run(argv: list[str]) -> int:
     """Call the reference-compatible ``run(argc, argv)`` entry point."""
     args = ["run"] + [str(a) for a in argv]

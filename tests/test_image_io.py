@@ -1,0 +1,135 @@
+"""Image input/output (host only): PNG decoding against the reference's PNG
+library, PNG writing, HSVtoRGB and the result colourings against the
+reference's own code (fixtures from tests/golden/make_image_golden.py)."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+from tests.conftest import GOLDEN
+
+
+@pytest.fixture(scope="module")
+def ske():
+    from skewengine_gb300 import build
+    build.build()
+    import skewengine_gb300 as m
+    return m
+
+
+@pytest.fixture(scope="module")
+def images():
+    return np.load(os.path.join(GOLDEN, "images.npz"))
+
+
+def test_hsv_to_rgb_matches_reference(ske, images):
+    import ctypes as C
+    lib = ske.engine.load()
+    rgb = (C.c_ubyte * 3)()
+    got = np.zeros_like(images["hsv_out"])
+    for i, (h, s, v) in enumerate(images["hsv_in"]):
+        lib.ske_hsv_to_rgb(C.c_float(h), C.c_float(s), C.c_float(v), rgb)
+        got[i] = list(rgb)
+    assert np.array_equal(got, images["hsv_out"])
+
+
+def test_png_decode_matches_reference_library(ske, images, tmp_path):
+    meta = images["png_meta"]
+    kinds = set()
+    for k, (ct, bd, il, w, h) in enumerate(meta):
+        path = tmp_path / f"{k}.png"
+        path.write_bytes(images[f"png_{k}"].tobytes())
+        assert ske.png_size(path) == (w, h)
+        assert np.array_equal(ske.read_png_rgba(path), images[f"rgba_{k}"]), (ct, bd, il, w, h)
+        kinds.add((int(ct), int(bd), int(il)))
+    # every colour type / depth the library writes, plain and interlaced
+    assert {(6, 8, 1), (6, 16, 0), (2, 16, 1), (4, 16, 0), (0, 1, 1), (0, 2, 0), (0, 4, 1), (0, 16, 1)} <= kinds
+
+
+def test_read_image_is_rgb_sum(ske, images, tmp_path):
+    k = 3
+    path = tmp_path / "img.png"
+    path.write_bytes(images[f"png_{k}"].tobytes())
+    rgba = images[f"rgba_{k}"].astype(np.int32)
+    assert np.array_equal(ske.read_image(path), (rgba[..., 0] + rgba[..., 1] + rgba[..., 2]).astype(np.float32))
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (5, 9), (300, 257)])
+def test_png_write_round_trip(ske, tmp_path, shape):
+    rng = np.random.default_rng(shape[0] * 7 + shape[1])
+    grey = rng.integers(0, 256, shape, dtype=np.uint8)
+    rgb = rng.integers(0, 256, shape + (3,), dtype=np.uint8)
+    ske.write_png(tmp_path / "g.png", grey)
+    ske.write_png(tmp_path / "c.png", rgb)
+    g = ske.read_png_rgba(tmp_path / "g.png")
+    c = ske.read_png_rgba(tmp_path / "c.png")
+    assert np.array_equal(g[..., 0], grey) and np.array_equal(g[..., 2], grey) and (g[..., 3] == 255).all()
+    assert np.array_equal(c[..., :3], rgb) and (c[..., 3] == 255).all()
+
+
+def test_png_rejects_damaged_files(ske, images, tmp_path):
+    from skewengine_gb300 import SkeError
+    good = images["png_5"].tobytes()
+    bad_crc = bytearray(good)
+    bad_crc[20] ^= 1  # inside IHDR: its CRC no longer matches
+    cases = {"sig": b"\x00" + good[1:], "crc": bytes(bad_crc), "cut": good[: len(good) // 2], "empty": b""}
+    for name, data in cases.items():
+        p = tmp_path / f"{name}.png"
+        p.write_bytes(data)
+        with pytest.raises(SkeError):
+            ske.read_png_rgba(p)
+    with pytest.raises(SkeError):
+        ske.read_png_rgba(tmp_path / "missing.png")
+
+
+def test_min_max_of_renderer_matches_reference(ske, images):
+    """The Radon colouring's scale comes from getMinMax; an all-negative grid
+    reports FLT_MIN as its maximum in the reference."""
+    for g, n, (lo, hi) in zip(images["minmax_in"], images["minmax_len"], images["minmax_out"]):
+        x = g[:n].reshape(1, n)
+        with np.errstate(divide="ignore", invalid="ignore"):  # all-zero grid: 0 * inf, byte 0 as on x86-64
+            esc = np.float32(255) / (np.float32(hi) - np.float32(lo))
+            want = ((x - np.float32(lo)).astype(np.int32).astype(np.float32) * esc).astype(np.int32).astype(np.uint8)
+        got = ske.render(2, x)
+        assert np.array_equal(got[..., 0], want) and np.array_equal(got[..., 1], want)
+
+
+def test_render_colourings(ske, images):
+    rng = np.random.default_rng(5)
+    out = rng.uniform(0, 2e6, (9, 11)).astype(np.float32)
+    # image identity: (int)out * (1/540), truncated to a byte
+    ident = ske.render(3, out)
+    want = (out.astype(np.int32).astype(np.float32) * np.float32(1.0 / 540)).astype(np.int32).astype(np.uint8)
+    assert np.array_equal(ident[..., 0], want)
+    # cepstrum: HSV with hue = int(out) mod 360, value min(100, out / 540000)
+    import ctypes as C
+    lib = ske.engine.load()
+    ceps = ske.render(4, out)
+    rgb = (C.c_ubyte * 3)()
+    for (i, j), v in np.ndenumerate(out):
+        val = np.float32(v) / np.float32(540000.0)
+        lib.ske_hsv_to_rgb(C.c_float(float(int(v) % 360)), C.c_float(100.0), C.c_float(min(float(val), 100.0)), rgb)
+        assert list(ceps[i, j]) == list(rgb)
+    from skewengine_gb300 import SkeError
+    with pytest.raises(SkeError):
+        ske.render(0, out)  # the reference writes no image of a viewshed
+    grey = ske.render_input(np.array([[0, 3, 765, 382]], np.float32))
+    assert list(grey[0]) == [0, 1, 255, 127]
+
+
+@pytest.mark.gpu
+def test_cli_png_in_png_out(ske, tmp_path):
+    """run(argc, argv) with an image input and an image output: the engine runs on
+    the R + G + B grid, the result is written coloured, the input in grey."""
+    from skewengine_gb300 import synthetic
+    x = synthetic.ellipse_phantom(64, 3)
+    px = np.clip((x - x.min()) / (x.max() - x.min()) * 255, 0, 255).astype(np.uint8)
+    ske.write_png(tmp_path / "in.png", np.stack([px, px, px], axis=2))
+    img = ske.read_image(tmp_path / "in.png")
+    assert ske.cli_run(["radon", str(tmp_path / "in.png"), 0, 0, str(tmp_path / "out.png")]) == 0
+    with ske.SkewEngine(64, 64) as eng:
+        want = eng.run(2, img)
+    assert np.array_equal(ske.read_png_rgba(tmp_path / "out.png")[..., :3], ske.render(2, want))
+    assert np.array_equal(ske.read_png_rgba(tmp_path / "out_input.png")[..., 0], ske.render_input(img))
