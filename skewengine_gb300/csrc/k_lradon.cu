@@ -28,6 +28,8 @@
 //    the reference computes them on the host.
 //  * Output cells past a row's span of the flat grid belong to the last row
 //    covering them (owner_row), as in the reference's row-order writes.
+#include <climits>
+
 #include "kernels.h"
 
 namespace ske {
@@ -45,7 +47,7 @@ constexpr int kWarps = 8;
 struct Smem {
     float s[kRows][kCols];
     double w[kRows][kTJ];
-    cd x[kWarps][kW];
+    cd x[kWarps][kW];  // per-warp FFT buffer; before the cell loop, a row's prefix sums
     double gauss[kW];
     double taper[kLocalRadonKeep];
     double tw[2 * (kW - 1)];
@@ -88,15 +90,72 @@ __global__ void __launch_bounds__(kWarps * 32)
     for (int t = threadIdx.x; t < kLocalRadonKeep; t += blockDim.x) sm.taper[t] = taper[t];
     for (int t = threadIdx.x; t < 2 * (kW - 1); t += blockDim.x) sm.tw[t] = tw64[t];
     __syncthreads();
-    for (int t = threadIdx.x; t < kRows * kTJ; t += blockDim.x) {
-        const int r = t / kTJ, c = t % kTJ;
-        double acc = 0.0;
-        for (int m = 0; m <= kW; m++) acc = __dadd_rn(acc, (double)sm.s[r][c + m]);
-        sm.w[r][c] = acc;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Window sums, one warp per staged row.  Every float is an integer multiple
+    // of 2^(e - 150); when the row's exponents span at most 28 binades and the
+    // sum of its magnitudes in units of its smallest 2^e stays below 2^53, every
+    // partial sum of the reference's sequential binary64 loop is exact, so each
+    // window sum is the exact sum: a difference of two 64-bit integer prefix
+    // sums.  Other rows (or a non-finite value) keep the sequential adds.
+    static_assert(kCols == 3 * 32, "three staged cells per lane");
+    static_assert(sizeof(cd) * kW >= sizeof(long long) * (kCols + 1), "prefix sums fit the FFT buffer");
+    for (int r = warp; r < kRows; r += kWarps) {
+        const float* row = sm.s[r];
+        unsigned u[3], m[3];
+        int ee[3], emin = INT_MAX, emax = 0;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            u[k] = __float_as_uint(row[3 * lane + k]);
+            const int e8 = (int)((u[k] >> 23) & 0xffu);
+            m[k] = (u[k] & 0x7fffffu) | (e8 ? 0x800000u : 0u);
+            ee[k] = m[k] ? max(e8, 1) : INT_MAX;
+            emin = min(emin, ee[k]);
+            emax = max(emax, e8);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            emin = min(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+            emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        }
+        bool exact = emax != 0xff && (emin == INT_MAX || emax - emin <= 28);
+        if (exact && emin != INT_MAX) {
+            long long v[3];
+            unsigned long long mag = 0;
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                const long long x = m[k] ? (long long)m[k] << (ee[k] - emin) : 0;  // < 2^52
+                v[k] = (u[k] >> 31) ? -x : x;
+                mag += (unsigned long long)x;
+            }
+            long long incl = v[0] + v[1] + v[2];
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            for (int o = 16; o > 0; o >>= 1) mag += __shfl_xor_sync(0xffffffffu, mag, o);
+            exact = mag < (1ull << 53);
+            if (exact) {
+                long long* pre = reinterpret_cast<long long*>(sm.x[warp]);  // idle until the cell loop
+                const long long excl = incl - (v[0] + v[1] + v[2]);
+                pre[3 * lane] = excl;
+                pre[3 * lane + 1] = excl + v[0];
+                pre[3 * lane + 2] = excl + v[0] + v[1];
+                if (lane == 31) pre[kCols] = incl;
+                __syncwarp();
+                const double scale = __longlong_as_double((long long)(emin - 150 + 1023) << 52);
+                sm.w[r][lane] = __dmul_rn(__ll2double_rn(pre[lane + kW + 1] - pre[lane]), scale);
+                __syncwarp();
+            }
+        } else if (exact) {
+            sm.w[r][lane] = 0.0;  // all cells zero
+        }
+        if (!exact) {
+            double acc = 0.0;
+            for (int k = 0; k <= kW; k++) acc = __dadd_rn(acc, (double)row[lane + k]);
+            sm.w[r][lane] = acc;
+        }
     }
     __syncthreads();
 
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     cd* x = sm.x[warp];
     const cd scale{0.125, 0.0};  // 1/sqrt(64) (helper.h:102-104)
     float* out = SO + slot * stride;

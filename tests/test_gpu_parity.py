@@ -150,6 +150,19 @@ def test_radon_special_values_bit_exact(ske, oracle, case):
     assert same.all(), (case, int((~same).sum()))
 
 
+def test_radon_long_rows_and_large_transforms(ske, oracle):
+    """Rows over 2048 cells take the sequential binary64 row sum; sectors with
+    H2 > 8192 transform in global memory instead of shared memory."""
+    x = synthetic.ellipse_phantom(2100, 17, side_y=24)
+    assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
+    x = synthetic.ellipse_phantom(8300, 18, side_y=4)
+    angles = [0, 30, 88, 89, 90, 91, 135]
+    assert max(ske.geometry(8300, 4, a)["skew_height"] for a in angles) > 8192
+    with ske.SkewEngine(8300, 4) as eng:
+        got = eng.run(2, np.ascontiguousarray(x), povh=POVH, angles=angles)
+    assert bits_equal(got, oracle.run_angles(2, x, angles, povh=POVH))
+
+
 def test_radon_512_matches_oracle(ske, oracle):
     x = synthetic.ellipse_phantom(512, 7)
     assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
