@@ -171,6 +171,30 @@ int ske_accumulate(ske_engine e, int kernel, const float* input, int input_on_de
                    const int32_t* angles, int nangles, const ske_params* p, float* acc,
                    int acc_on_device, uint32_t* used_mask);
 
+/* Test hook (no reference counterpart): the device or pinned-host allocation
+ * `after` allocations from now fails as if out of memory (0 = the next one);
+ * negative turns injection off.  Calls that hit it return SKE_ERR_CUDA with
+ * nothing leaked; used to test failure handling without faulting a GPU. */
+int ske_inject_alloc_failure(int64_t after);
+
+/* Checkpoint / resume at sector granularity.  Like ske_accumulate, but the
+ * per-type accumulators start from the state in acc (4*N floats), comp (4*N
+ * Kahan compensations; Kahan mode only, else may be null) and *used_mask
+ * instead of from zero, and return the state after the listed sectors in the
+ * same buffers (host or device, state_on_device).  Accumulating angles [0,k)
+ * and then [k,180) this way leaves the same bits as one pass over [0,180):
+ * the additions continue in the same order.  The reference has no such call;
+ * its sector loop (main.cu:147-164) keeps this state in the engine. */
+int ske_accumulate_resume(ske_engine e, int kernel, const float* input, int input_on_device,
+                          const int32_t* angles, int nangles, const ske_params* p, float* acc,
+                          float* comp, int state_on_device, uint32_t* used_mask);
+
+/* Fold a saved accumulator state into the output grid exactly as ske_run's
+ * final reduce does (skewEngine.cuh:862-914): max for the cepstrum, sums
+ * otherwise (compensated in Kahan mode). */
+int ske_fold(ske_engine e, int kernel, const float* acc, const float* comp, int state_on_device,
+             uint32_t used_mask, int accum, float* output, int output_on_device);
+
 /* Batched total viewshed (SDEM) over `count` square or rectangular DEMs of
  * uneven sizes: inputs[i]/outputs[i] are dimx[i] x dimy[i] host or device
  * arrays.  All DEMs and all their sectors are scheduled together.  Engines are

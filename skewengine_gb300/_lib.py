@@ -78,6 +78,12 @@ SIGNATURES = [
                                         C.POINTER(C.c_uint32)]),
     ("ske_measure_fp32_peak", C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("ske_measure_fp64_peak", C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+    ("ske_inject_alloc_failure", C.c_int, [C.c_int64]),
+    ("ske_accumulate_resume", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                        C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_int,
+                                        C.POINTER(C.c_uint32)]),
+    ("ske_fold", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_uint32, C.c_int, C.c_void_p,
+                           C.c_int]),
     ("ske_png_size", C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("ske_png_read_rgba", C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t]),
     ("ske_png_read_image", C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t]),

@@ -1,6 +1,7 @@
 // C ABI of the skew engine (include/skewengine.h): engine object, device
 // buffers, the batched sector loop and the per-sector drop-in API.
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -55,11 +56,30 @@ int ensure_device_tables(int device) {
 
 bool valid_kernel(int k) { return k >= SKE_KERNEL_SDEM && k <= SKE_KERNEL_LOCAL_RADON; }
 
+// Allocation fault injection for tests (ske_inject_alloc_failure): the
+// allocation this many allocations from now fails; negative = off.
+std::atomic<int64_t> g_alloc_fail_in{-1};
+
+bool injected_alloc_failure() {
+    int64_t n = g_alloc_fail_in.load();
+    while (n >= 0 && !g_alloc_fail_in.compare_exchange_weak(n, n - 1)) {
+    }
+    return n == 0;
+}
+
 template <typename T>
 int dev_alloc(T** p, size_t count) {
     *p = nullptr;
     if (count == 0) return SKE_OK;
+    if (injected_alloc_failure()) return fail(SKE_ERR_CUDA, "injected device allocation failure");
     SKE_CK(cudaMalloc((void**)p, sizeof(T) * count));
+    return SKE_OK;
+}
+
+int pinned_alloc(float** p, size_t count) {
+    *p = nullptr;
+    if (injected_alloc_failure()) return fail(SKE_ERR_CUDA, "injected pinned allocation failure");
+    SKE_CK(cudaHostAlloc((void**)p, sizeof(float) * count, cudaHostAllocPortable));
     return SKE_OK;
 }
 
@@ -425,9 +445,36 @@ int validate_params(const ske_params* p, ske_params* out) {
     return SKE_OK;
 }
 
-// Prepare + every listed sector (skew, operator, deskew) into the accumulators.
+// Accumulator state a run starts from instead of zero (checkpoint/resume).
+struct StartState {
+    const float* acc;   // 4 x N per-type accumulators
+    const float* comp;  // 4 x N Kahan compensations (Kahan mode only)
+    uint32_t used;      // types that already received a sector
+    int on_device;
+};
+
+int load_state(ske_engine e, const StartState& st, int accum) {
+    for (int t = 0; t < 4; t++) {
+        const int64_t off = (int64_t)t * e->N;
+        if (st.on_device) {
+            SKE_CK(cudaMemcpyAsync(e->d_acc + off, st.acc + off, sizeof(float) * e->N, cudaMemcpyDeviceToDevice,
+                                   e->stream));
+            if (accum == SKE_ACCUM_KAHAN)
+                SKE_CK(cudaMemcpyAsync(e->d_comp + off, st.comp + off, sizeof(float) * e->N,
+                                       cudaMemcpyDeviceToDevice, e->stream));
+        } else {
+            SKE_TRY(upload(e, e->d_acc + off, st.acc + off, e->N));
+            if (accum == SKE_ACCUM_KAHAN) SKE_TRY(upload(e, e->d_comp + off, st.comp + off, e->N));
+        }
+    }
+    e->used = st.used & 0xfu;
+    return SKE_OK;
+}
+
+// Prepare + every listed sector (skew, operator, deskew) into the accumulators,
+// which start from zero or, with `start`, from a saved state.
 int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on_device, const int32_t* angles,
-                      int nangles, const ske_params* p, ske_params* prm) {
+                      int nangles, const ske_params* p, ske_params* prm, const StartState* start = nullptr) {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
     if (!input) return fail(SKE_ERR_INVALID, "null input");
@@ -438,6 +485,12 @@ int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on
     SKE_TRY(set_device(e));
     const int is_max = kernel == SKE_KERNEL_CEPSTRUM;
     SKE_TRY(run_prepare(e, input, input_on_device));
+    if (start) {
+        if (!start->acc || (prm->accum == SKE_ACCUM_KAHAN && !start->comp))
+            return fail(SKE_ERR_INVALID, "null accumulator state");
+        SKE_TRY(load_state(e, *start, prm->accum));
+    }
+    e->accum_mode = prm->accum;
     if (nangles == 0) return SKE_OK;
     const int cap = batch_capacity(e, nangles);
     SKE_TRY(ensure_slots(e, cap));
@@ -528,6 +581,7 @@ int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32
 
 namespace {
 int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream, ske_engine parent);
+int init_engine(ske_engine e, int dimx, int dimy, int device, void* stream, ske_engine parent);
 }
 
 int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) {
@@ -548,7 +602,17 @@ int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream,
                     err != cudaSuccess ? cudaGetErrorString(err) : "0 devices");
     }
     if (device < 0 || device >= ndev) return fail(SKE_ERR_INVALID, "device %d outside [0,%d)", device, ndev);
-    std::unique_ptr<ske_engine_s> e(new ske_engine_s());
+    ske_engine e = new ske_engine_s();
+    const int rc = init_engine(e, dimx, dimy, device, stream, parent);
+    if (rc != SKE_OK) {
+        ske_destroy(e);  // frees whatever was allocated before the failure
+        return rc;
+    }
+    *out = e;
+    return SKE_OK;
+}
+
+int init_engine(ske_engine e, int dimx, int dimy, int device, void* stream, ske_engine parent) {
     e->dimx = dimx;
     e->dimy = dimy;
     e->device = device;
@@ -619,11 +683,8 @@ int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream,
     SKE_TRY(dev_alloc(&e->d_counter, 1));
     SKE_TRY(dev_alloc(&e->d_status, 1));
     SKE_CK(cudaMemset(e->d_status, 0, sizeof(int)));
-    SKE_CK(cudaHostAlloc((void**)&e->h_pin, sizeof(float) * (size_t)std::max<int64_t>(e->N, e->len),
-                         cudaHostAllocPortable));
-    SKE_TRY(ensure_slots(e.get(), 1));
-    *out = e.release();
-    return SKE_OK;
+    SKE_TRY(pinned_alloc(&e->h_pin, (size_t)std::max<int64_t>(e->N, e->len)));
+    return ensure_slots(e, 1);
 }
 }  // namespace
 
@@ -647,6 +708,11 @@ int ske_destroy(ske_engine e) {
     if (e->h_pin) cudaFreeHost(e->h_pin);
     if (e->own_stream) cudaStreamDestroy(e->stream);
     delete e;
+    return SKE_OK;
+}
+
+int ske_inject_alloc_failure(int64_t after) {
+    g_alloc_fail_in.store(after < 0 ? -1 : after);
     return SKE_OK;
 }
 
@@ -687,6 +753,46 @@ int ske_accumulate(ske_engine e, int kernel, const float* input, int input_on_de
     *used_mask = e->used;
     e->prepared = false;
     return check_status(e);
+}
+
+int ske_accumulate_resume(ske_engine e, int kernel, const float* input, int input_on_device, const int32_t* angles,
+                          int nangles, const ske_params* p, float* acc, float* comp, int state_on_device,
+                          uint32_t* used_mask) {
+    if (!acc || !used_mask) return fail(SKE_ERR_INVALID, "null accumulator state");
+    const StartState st{acc, comp, *used_mask, state_on_device};
+    ske_params prm;
+    SKE_TRY(accumulate_angles(e, kernel, input, input_on_device, angles, nangles, p, &prm, &st));
+    for (int t = 0; t < 4; t++) {
+        const int64_t off = (int64_t)t * e->N;
+        if (state_on_device) {
+            SKE_CK(cudaMemcpyAsync(acc + off, e->d_acc + off, sizeof(float) * e->N, cudaMemcpyDeviceToDevice,
+                                   e->stream));
+            if (prm.accum == SKE_ACCUM_KAHAN)
+                SKE_CK(cudaMemcpyAsync(comp + off, e->d_comp + off, sizeof(float) * e->N, cudaMemcpyDeviceToDevice,
+                                       e->stream));
+        } else {
+            SKE_TRY(download(e, acc + off, e->d_acc + off, e->N));
+            if (prm.accum == SKE_ACCUM_KAHAN) SKE_TRY(download(e, comp + off, e->d_comp + off, e->N));
+        }
+    }
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    *used_mask = e->used;
+    e->prepared = false;
+    return check_status(e);
+}
+
+int ske_fold(ske_engine e, int kernel, const float* acc, const float* comp, int state_on_device, uint32_t used_mask,
+             int accum, float* output, int output_on_device) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
+    if (accum != SKE_ACCUM_REFERENCE && accum != SKE_ACCUM_KAHAN)
+        return fail(SKE_ERR_INVALID, "unknown accumulation mode %d", accum);
+    if (!acc || !output || (accum == SKE_ACCUM_KAHAN && !comp)) return fail(SKE_ERR_INVALID, "null argument");
+    SKE_TRY(set_device(e));
+    SKE_TRY(load_state(e, StartState{acc, comp, used_mask, state_on_device}, accum));
+    SKE_TRY(run_reduce(e, output, output_on_device, kernel == SKE_KERNEL_CEPSTRUM, accum));
+    SKE_CK(cudaStreamSynchronize(e->stream));
+    return SKE_OK;
 }
 
 int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,

@@ -171,6 +171,68 @@ class SkewEngine:
                                        len(a), C.byref(prm), acc.ctypes.data, 0, C.byref(used)))
         return acc, used.value
 
+    # checkpoint / resume --------------------------------------------------
+    def accumulate_resume(self, kernel, data, angles, state=None, povh: float = DEFAULT_POVH, accum="reference"):
+        """Continue an accumulation over the listed sectors from ``state`` (a dict
+        with ``acc``, ``comp`` (4 x N float32) and ``used``; None = zero) and
+        return the new state."""
+        pin, in_dev = _ptr(data, (self.dimy, self.dimx))
+        a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
+        if state is None:
+            state = {"acc": np.zeros((4, self.N), np.float32), "comp": np.zeros((4, self.N), np.float32), "used": 0}
+        acc = np.array(state["acc"], np.float32, copy=True).reshape(4, self.N)
+        comp = np.array(state["comp"], np.float32, copy=True).reshape(4, self.N)
+        used = C.c_uint32(int(state["used"]))
+        prm = params(180, povh, accum)
+        check(self._lib.ske_accumulate_resume(self._h, _kernel_id(kernel), pin, in_dev,
+                                              a.ctypes.data if len(a) else None, len(a), C.byref(prm),
+                                              acc.ctypes.data, comp.ctypes.data, 0, C.byref(used)))
+        return {"acc": acc, "comp": comp, "used": used.value}
+
+    def fold(self, kernel, state, accum="reference", out=None):
+        """The output grid of a saved accumulator state (the final reduce)."""
+        shape = (self.dimy, self.dimx)
+        if out is None:
+            out = np.empty(shape, np.float32)
+        p, dev = _ptr(out, shape, writable=True)
+        acc = np.ascontiguousarray(state["acc"], np.float32)
+        comp = np.ascontiguousarray(state["comp"], np.float32)
+        check(self._lib.ske_fold(self._h, _kernel_id(kernel), acc.ctypes.data, comp.ctypes.data, 0,
+                                 int(state["used"]), _accum_id(accum), p, dev))
+        return out
+
+    def run_checkpointed(self, kernel, data, path, chunk: int = 30, max_sector: int = 180,
+                         povh: float = DEFAULT_POVH, accum="reference", stop_after=None):
+        """Whole run in chunks of ``chunk`` sectors, saving the accumulator state
+        and the next sector index to ``path`` (.npz) after each chunk and resuming
+        from it when it exists.  ``stop_after`` (chunks) ends the call early, as an
+        interrupted job would; the result equals ``run`` bit for bit."""
+        import os
+        start, state = 0, None
+        if os.path.exists(path):
+            z = np.load(path)
+            if (int(z["kernel"]), int(z["max_sector"]), str(z["accum"]), int(z["dimx"]), int(z["dimy"])) != \
+                    (_kernel_id(kernel), max_sector, str(accum), self.dimx, self.dimy):
+                raise ValueError(f"checkpoint {path} belongs to another run")
+            start = int(z["next_sector"])
+            state = {"acc": z["acc"], "comp": z["comp"], "used": int(z["used"])}
+        done = 0
+        while start < max_sector:
+            if stop_after is not None and done >= stop_after:
+                return None
+            angles = list(range(start, min(start + chunk, max_sector)))
+            state = self.accumulate_resume(kernel, data, angles, state, povh=povh, accum=accum)
+            start = angles[-1] + 1
+            tmp = str(path) + ".tmp.npz"
+            np.savez(tmp, acc=state["acc"], comp=state["comp"], used=state["used"], next_sector=start,
+                     kernel=_kernel_id(kernel), max_sector=max_sector, accum=str(accum), dimx=self.dimx,
+                     dimy=self.dimy)
+            os.replace(tmp, path)
+            done += 1
+        if state is None:
+            state = self.accumulate_resume(kernel, data, [], None, povh=povh, accum=accum)
+        return self.fold(kernel, state, accum=accum)
+
     # per-sector API (main.cu:147-164) -------------------------------------
     def prepare(self, data) -> None:
         p, dev = _ptr(data, (self.dimy, self.dimx))

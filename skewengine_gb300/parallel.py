@@ -79,3 +79,52 @@ def run_sharded(engine, kernel, data, group=None, max_sector: int = 180, povh=No
         return None
     return fold_accumulators([g["acc"] for g in gathered], [g["used"] for g in gathered], engine.dimx,
                              engine.dimy, is_max=int(kernel) == KERNEL_CEPSTRUM)
+
+
+def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, max_sector: int = 180, povh=None,
+                          accum="reference", timeout: float = 60.0, poll: float = 0.01):
+    """Sector sharding with failure detection and recovery on the host.
+
+    Each rank accumulates its block of angles and posts the result under
+    ``acc/<rank>`` of a shared key-value store (a ``torch.distributed.Store``:
+    TCPStore, FileStore ...), or its error message under ``err/<rank>`` when its
+    work raises.  Rank 0 waits for every rank: one that reports an error or posts
+    nothing within ``timeout`` seconds (it died, hung or never started) is taken
+    over, and rank 0 accumulates that block itself.  No collective runs on the
+    data path, so a lost rank cannot block the others; the fold is in block
+    order, so the result has the same bits as a run without failures.
+
+    Returns (output, recovered ranks) on rank 0 and (None, []) elsewhere.
+    """
+    import pickle
+    import time
+    from .engine import DEFAULT_POVH, KERNEL_CEPSTRUM
+
+    pv = DEFAULT_POVH if povh is None else povh
+    blocks = [shard_angles(max_sector, world, r) for r in range(world)]
+    if rank != 0:
+        try:
+            acc, used = engine.accumulate(kernel, data, blocks[rank], povh=pv, accum=accum)
+            store.set(f"acc/{rank}", pickle.dumps({"acc": np.asarray(acc, np.float32), "used": int(used)}))
+        except Exception as exc:  # report, then let the caller see the failure too
+            store.set(f"err/{rank}", repr(exc).encode())
+            raise
+        return None, []
+    results = {0: engine.accumulate(kernel, data, blocks[0], povh=pv, accum=accum)}
+    recovered = []
+    deadline = time.monotonic() + timeout
+    for r in range(1, world):
+        got = None
+        while got is None:
+            if store.check([f"acc/{r}"]):
+                got = pickle.loads(store.get(f"acc/{r}"))
+                results[r] = (got["acc"], got["used"])
+            elif store.check([f"err/{r}"]) or time.monotonic() > deadline:
+                results[r] = engine.accumulate(kernel, data, blocks[r], povh=pv, accum=accum)
+                recovered.append(r)
+                break
+            else:
+                time.sleep(poll)
+    out = fold_accumulators([results[r][0] for r in range(world)], [results[r][1] for r in range(world)],
+                            engine.dimx, engine.dimy, is_max=int(kernel) == KERNEL_CEPSTRUM)
+    return out, recovered

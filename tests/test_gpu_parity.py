@@ -163,6 +163,69 @@ def test_radon_long_rows_and_large_transforms(ske, oracle):
     assert bits_equal(got, oracle.run_angles(2, x, angles, povh=POVH))
 
 
+@pytest.mark.parametrize("op,accum", [(0, "reference"), (0, "kahan"), (2, "reference"), (4, "reference")])
+def test_checkpoint_resume_bit_exact(ske, op, accum, tmp_path):
+    """A run interrupted after two chunks of 40 sectors and resumed from its
+    checkpoint file gives the bits of an uninterrupted run."""
+    if op == 4:
+        x = synthetic.blurred_texture(40, 3)[0]
+    elif op == 2:
+        x = synthetic.ellipse_phantom(40, 3)
+    else:
+        x = synthetic.fractal_dem(40, 9)
+    x = np.ascontiguousarray(x, np.float32)
+    path = str(tmp_path / "run.npz")
+    with ske.SkewEngine(40, 40) as eng:
+        full = eng.run(op, x, povh=POVH, accum=accum)
+        assert eng.run_checkpointed(op, x, path, chunk=40, povh=POVH, accum=accum, stop_after=2) is None
+        got = eng.run_checkpointed(op, x, path, chunk=40, povh=POVH, accum=accum)
+        assert bits_equal(got, full)
+        other = 1 if op != 1 else 0
+        with pytest.raises(ValueError):
+            eng.run_checkpointed(other, x, path, chunk=40, povh=POVH, accum=accum)
+
+
+def test_allocation_failures_are_clean(ske, oracle):
+    """Every device or pinned allocation of engine creation and of a run is made
+    to fail in turn (host-side injection): each call returns an error, the
+    engine can be destroyed, no device memory is left behind, and once the
+    failure point lies past the last allocation the run is bit-exact."""
+    import torch
+    from skewengine_gb300 import SkeError
+    lib = ske.engine.load()
+    x = synthetic.fractal_dem(300, 4)
+    want = oracle.run(0, x, povh=POVH)
+    with ske.SkewEngine(300, 300) as eng:  # device tables and context set up once
+        eng.run(0, x, povh=POVH)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    failures = 0
+    try:
+        for k in range(200):
+            lib.ske_inject_alloc_failure(k)
+            eng = None
+            try:
+                eng = ske.SkewEngine(300, 300)
+                got = eng.run(0, x, povh=POVH)
+            except SkeError as exc:
+                assert "injected" in str(exc)
+                failures += 1
+                continue
+            finally:
+                lib.ske_inject_alloc_failure(-1)
+                if eng is not None:
+                    eng.close()
+            assert bits_equal(got, want)
+            break
+        else:
+            raise AssertionError("the run never got past the injected failures")
+    finally:
+        lib.ske_inject_alloc_failure(-1)
+    assert failures >= 10, failures
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] >= free0 - (4 << 20), "device memory leaked"
+
+
 def test_radon_512_matches_oracle(ske, oracle):
     x = synthetic.ellipse_phantom(512, 7)
     assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))

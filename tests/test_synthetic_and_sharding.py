@@ -107,3 +107,59 @@ def test_two_rank_sharded_run(oracle, port, tmp_path):
     assert bits_equal(got, want)
     single = oracle.run(0, x, povh=np.float32(0.15))
     np.testing.assert_allclose(got, single, rtol=1e-5)
+
+
+class _FailingEngine(_OracleEngine):
+    def accumulate(self, *a, **k):
+        raise RuntimeError("injected failure of this rank's sectors")
+
+
+def _resilient_main(rank, world, port_path, x, result_path, store_port, mode):
+    import ctypes as C
+    import json
+    from datetime import timedelta
+    import torch.distributed as dist
+    if mode == "fail" and rank == 2:
+        return  # dies before contributing anything
+    store = dist.TCPStore("127.0.0.1", store_port, world, rank == 0, timedelta(seconds=60), wait_for_workers=False)
+    lib = C.CDLL(port_path)
+    from tests.conftest import PortOracle
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+    lib.port_accumulate.argtypes = [C.c_int, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, fp, ip]
+    cls = _FailingEngine if (mode == "fail" and rank == 1) else _OracleEngine
+    eng = cls(PortOracle(lib), x.shape[1], x.shape[0])
+    try:
+        out, recovered = parallel.run_sharded_resilient(eng, 0, x, store, rank, world, povh=np.float32(0.15),
+                                                        timeout=5.0)
+    except RuntimeError:
+        assert mode == "fail" and rank == 1
+        return
+    if rank == 0:
+        np.save(result_path, out)
+        with open(result_path + ".json", "w") as f:
+            json.dump(recovered, f)
+
+
+@pytest.mark.parametrize("mode", ["ok", "fail"])
+def test_resilient_sharding_recovers_failed_ranks(oracle, port, tmp_path, mode):
+    """Three CPU ranks; with mode "fail" rank 1 raises inside its work and rank 2
+    exits before contributing.  Rank 0 detects both on the host (an error key,
+    a deadline) and runs their sectors itself; the output has the same bits as
+    the run without failures."""
+    import json
+    import torch.multiprocessing as mp
+    x = synthetic.fractal_dem(36, 8)
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        store_port = s.getsockname()[1]
+    res = str(tmp_path / "out.npy")
+    mp.start_processes(_resilient_main, args=(3, port._name, x, res, store_port, mode), nprocs=3, join=True,
+                       start_method="spawn")
+    got = np.load(res)
+    blocks = [parallel.shard_angles(180, 3, r) for r in range(3)]
+    parts = [oracle.accumulate(0, x, b, povh=np.float32(0.15)) for b in blocks]
+    want = parallel.fold_accumulators([p[0] for p in parts], [p[1] for p in parts], 36, 36)
+    assert bits_equal(got, want)
+    with open(res + ".json") as f:
+        assert json.load(f) == ([1, 2] if mode == "fail" else [])
