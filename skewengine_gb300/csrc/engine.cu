@@ -332,12 +332,16 @@ int get_items(ske_engine e, const Batch& b, ItemPlan** out) {
 // rows_only (Radon, sectors whose rows stay within dim_i): the row sums gather
 // the skewed cells from the oriented input (no skew needed) and the
 // back-projection into SO is skipped.
-int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int counts_only, bool rows_only = false) {
+// so_masked (batched total viewshed, every sector's rows within dim_i): SO is
+// not zeroed first; the sweep writes every valid cell and the deskew reads the
+// others as zero.
+int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int counts_only, bool rows_only = false,
+                 bool so_masked = false) {
     switch (kernel) {
         case SKE_KERNEL_SDEM: {
             ItemPlan* plan = nullptr;
             SKE_TRY(get_items(e, b, &plan));
-            SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
+            if (!so_masked) SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
             SKE_TRY(ensure_lists(e, sdem_list_bytes(std::max(plan->max_row, 1), e->num_sms)));
             SdemLaunch a;
             a.g = e->dg;
@@ -382,14 +386,16 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
     }
 }
 
-int run_skew(ske_engine e, const Batch& b) {
+// zero_tail false (batched runs): sectors whose rows stay within dim_i leave
+// the slot past H*dim_i unwritten, since no operator of the batch reads it.
+int run_skew(ske_engine e, const Batch& b, bool zero_tail = true) {
     LaunchScope ls(e, "skew", 1);
-    return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, e->stream));
+    return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, e->stream, zero_tail));
 }
 
 // rows_from_p: the batch is Radon sectors whose back-projection was skipped;
 // the deskew reads their filtered row values from the Radon scratch.
-int run_deskew(ske_engine e, const Batch& b, int is_max, int accum, bool rows_from_p = false) {
+int run_deskew(ske_engine e, const Batch& b, int is_max, int accum, bool rows_from_p = false, bool so_masked = false) {
     TypeLists tl;
     memset(&tl, 0, sizeof(tl));
     for (int s = 0; s < b.count; s++) {
@@ -403,7 +409,7 @@ int run_deskew(ske_engine e, const Batch& b, int is_max, int accum, bool rows_fr
     if (is_max) return ls.done(launch_deskew_max(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->dimx, e->dimy, e->stream));
     return ls.done(launch_deskew_add(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->d_comp, e->dimx, e->dimy, accum,
                                      e->stream, rows_from_p ? reinterpret_cast<const cd*>(e->d_P) : nullptr,
-                                     e->pstride));
+                                     e->pstride, so_masked));
 }
 
 int run_prepare(ske_engine e, const float* input, int on_device) {
@@ -501,11 +507,13 @@ int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on
         // Radon sectors whose rows stay within their width: the row sums gather
         // the skewed cells themselves and the deskew reads the filtered row
         // values, so neither the skew nor the back-projection runs.
-        bool rows_only = kernel == SKE_KERNEL_RADON;
-        for (int s = 0; s < b.count && rows_only; s++) rows_only = e->rows_in_width[b.angle[s]] != 0;
-        if (!rows_only) SKE_TRY(run_skew(e, b));
-        SKE_TRY(run_operator(e, kernel, b, prm->povh, 0, rows_only));
-        SKE_TRY(run_deskew(e, b, is_max, prm->accum, rows_only));
+        bool in_width = true;
+        for (int s = 0; s < b.count; s++) in_width = in_width && e->rows_in_width[b.angle[s]] != 0;
+        const bool rows_only = kernel == SKE_KERNEL_RADON && in_width;
+        const bool so_masked = kernel == SKE_KERNEL_SDEM && in_width;
+        if (!rows_only) SKE_TRY(run_skew(e, b, false));
+        SKE_TRY(run_operator(e, kernel, b, prm->povh, 0, rows_only, so_masked));
+        SKE_TRY(run_deskew(e, b, is_max, prm->accum, rows_only, so_masked));
     }
     e->accum_mode = prm->accum;
     return SKE_OK;
@@ -631,9 +639,10 @@ int init_engine(ske_engine e, int dimx, int dimy, int device, void* stream, ske_
     build_geometry(dimx, dimy, e->geo);
     e->rows_in_width.assign(e->geo.desc.size(), 1);
     for (size_t a = 0; a < e->geo.desc.size(); a++) {
-        const SectorDesc& d = e->geo.desc[a];
+        SectorDesc& d = e->geo.desc[a];
         for (int r = 0; r < d.H; r++)
             if (e->geo.last[d.row_off + r] > d.dim_i) e->rows_in_width[a] = 0;
+        d.in_width = e->rows_in_width[a];
     }
     while (e->max_H2 < e->geo.max_H) e->max_H2 <<= 1;
     e->pstride = e->max_H2;

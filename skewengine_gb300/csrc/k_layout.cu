@@ -48,7 +48,7 @@ __global__ void k_prepare(const float* __restrict__ in, float* __restrict__ orie
 }
 
 __global__ void k_skew(DevGeometry g, Batch b, const float* __restrict__ orient, int64_t n_cells,
-                       float* __restrict__ SI, int64_t stride, int64_t len) {
+                       float* __restrict__ SI, int64_t stride, int64_t len, bool zero_tail) {
     const int slot = blockIdx.y;
     const SectorDesc d = g.desc[b.angle[slot]];
     const float* src = orient + (int64_t)d.type * n_cells;
@@ -59,6 +59,7 @@ __global__ void k_skew(DevGeometry g, Batch b, const float* __restrict__ orient,
     for (int r = blockIdx.x; r < d.H; r += gridDim.x)
         for (int c = threadIdx.x; c < d.dim_i; c += blockDim.x)
             out[(int64_t)r * d.dim_i + c] = skew_gather(d, tgt, wgt, src, r, c);
+    if (!zero_tail && d.in_width) return;  // nothing reads past H*dim_i
     const int64_t z0 = (int64_t)d.H * d.dim_i;
     for (int64_t p = z0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < len; p += (int64_t)gridDim.x * blockDim.x)
         out[p] = 0.0f;
@@ -100,12 +101,16 @@ __device__ __forceinline__ float row_cell(const SectorDesc& d, const int32_t* __
 
 // kRows: the batch's skewed outputs are Radon sectors given as per-row values
 // (Q: pstride complex doubles per slot, real part) rather than SO.
-template <int kMode, bool kRows = false>
+// kMasked: SO is defined only on its sectors' valid cells (rows within dim_i,
+// not zeroed first): a staged row carries the mask of the tile's columns in
+// its valid range and other cells read as zero.
+template <int kMode, bool kRows = false, bool kMasked = false>
 __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, const float* __restrict__ SO,
                                                 int64_t stride, float* __restrict__ acc, float* __restrict__ comp,
                                                 int dimx, int dimy, const cd* __restrict__ Q = nullptr,
                                                 int64_t pstride = 0) {
     __shared__ float band[kRows ? 1 : kDeskewBand][kTile];
+    __shared__ unsigned bmask[kMasked ? kDeskewBand : 1];
     // kRows: the band's rows as (value, mask of the tile's columns inside the
     // row's valid range); a cell is its row's value inside the range, else zero.
     __shared__ float2 rqm[kRows ? kDeskewBand : 1];
@@ -176,10 +181,20 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
                 const int rr = ty + 8 * u;
                 v[u] = (rr < nrows && j0 + tx <= jlast) ? so[(int64_t)(r0 + rr) * dim_i + j0 + tx] : 0.0f;
             }
+            unsigned m = 0;
+            const int tid = ty * kTile + tx;
+            if (kMasked && tid < nrows) {
+                const int r = r0 + tid;
+                if (r < d.H) {
+                    const int lo_c = max(rfirst[r] - j0, 0), hi_c = min(rlast[r] - j0, kTile);
+                    if (hi_c > lo_c) m = (hi_c >= 32 ? 0xffffffffu : (1u << hi_c) - 1u) & ~((1u << lo_c) - 1u);
+                }
+            }
             __syncthreads();  // previous sector's band fully consumed
 #pragma unroll
             for (int u = 0; u < kLoads; u++)
                 if (ty + 8 * u < nrows) band[ty + 8 * u][tx] = v[u];
+            if (kMasked && tid < nrows) bmask[tid] = m;
             __syncthreads();
         }
         if (!col_ok || nv <= 0) continue;
@@ -197,6 +212,10 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
                 cell[kk] = ((__float_as_uint(e.y) >> tx) & 1u) ? e.x : 0.0f;
             } else if (kRows) {
                 cell[kk] = row_cell(d, rfirst, rlast, qv, r, j);
+            } else if (kMasked) {
+                const bool ok = staged ? ((bmask[br] >> tx) & 1u) != 0
+                                       : (r < d.H && j >= rfirst[r] && j < rlast[r]);
+                cell[kk] = ok ? (staged ? band[br][tx] : so[(int64_t)r * dim_i + j]) : 0.0f;
             } else {
                 cell[kk] = staged ? band[br][tx] : so[(int64_t)r * dim_i + j];
             }
@@ -275,9 +294,9 @@ cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, c
 }
 
 cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells, float* SI,
-                        int64_t stride, int64_t len, cudaStream_t st) {
+                        int64_t stride, int64_t len, cudaStream_t st, bool zero_tail) {
     dim3 grid(1024, b.count);
-    k_skew<<<grid, 256, 0, st>>>(g, b, orient, n_cells, SI, stride, len);
+    k_skew<<<grid, 256, 0, st>>>(g, b, orient, n_cells, SI, stride, len, zero_tail);
     return cudaGetLastError();
 }
 
@@ -295,8 +314,15 @@ static dim3 deskew_grid(int dimx, int dimy) {
 
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
                               float* acc, float* comp, int dimx, int dimy, int accum_mode, cudaStream_t st,
-                              const cd* Q, int64_t pstride) {
+                              const cd* Q, int64_t pstride, bool masked) {
     const dim3 grid = deskew_grid(dimx, dimy), block(kTile, 8);
+    if (masked && !Q) {
+        if (accum_mode == kAccumKahan)
+            k_deskew<kDeskewKahan, false, true><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, comp, dimx, dimy);
+        else
+            k_deskew<kDeskewAdd, false, true><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, nullptr, dimx, dimy);
+        return cudaGetLastError();
+    }
     if (Q) {
         if (accum_mode == kAccumKahan)
             k_deskew<kDeskewKahan, true><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, comp, dimx, dimy, Q, pstride);

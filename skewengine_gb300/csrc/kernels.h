@@ -26,8 +26,10 @@ cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, c
 
 // Skewed input of every sector of the batch into slot s of SI (stride floats per
 // slot, `len` = 2N + dim_l cells each, zero past H*dim_i).
+// zero_tail false: sectors whose rows stay within dim_i leave the cells past
+// H*dim_i as they were.
 cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells,
-                        float* SI, int64_t stride, int64_t len, cudaStream_t st);
+                        float* SI, int64_t stride, int64_t len, cudaStream_t st, bool zero_tail = true);
 
 // Identity operator (kernelUNIT.h:16-23): SO = SI on covered cells, 0 elsewhere.
 cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
@@ -38,9 +40,12 @@ cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* S
 // With Q set, the slots are Radon sectors whose rows stay within dim_i, read
 // from their filtered row values (Q: pstride complex doubles per slot) instead
 // of SO: what the back-projection would write, without writing it.
+// masked: SO holds defined values only on its sectors' valid cells (rows within
+// dim_i, SO not zeroed first); every other cell is read as zero.
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO,
                               int64_t stride, float* acc, float* comp, int dimx, int dimy,
-                              int accum_mode, cudaStream_t st, const cd* Q = nullptr, int64_t pstride = 0);
+                              int accum_mode, cudaStream_t st, const cd* Q = nullptr, int64_t pstride = 0,
+                              bool masked = false);
 // Max mode with angle encoding (skewEngine.cuh:774-785).
 cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const float* SO,
                               int64_t stride, float* acc, int dimx, int dimy, cudaStream_t st);

@@ -26,7 +26,7 @@ struct SectorDesc {
     int32_t H;          // skewHeight
     int32_t diml;       // max(dimx, dimy)
     float r2;           // (float)(scale*scale), kernelSDEM.h:171
-    int32_t pad0;
+    int32_t in_width;   // 1: every row's last <= dim_i (no row reaches into the next row's span)
     double scale;       // 1/cos(newAngle)
     double skewness;    // tan(newAngle)
     int64_t col_off;    // first entry of this sector in target/weight tables
