@@ -105,7 +105,7 @@ __device__ __forceinline__ float row_cell(const SectorDesc& d, const int32_t* __
 // not zeroed first): a staged row carries the mask of the tile's columns in
 // its valid range and other cells read as zero.
 template <int kMode, bool kRows = false, bool kMasked = false>
-__global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, const float* __restrict__ SO,
+__global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4) k_deskew(DevGeometry g, TypeLists tl, const float* __restrict__ SO,
                                                 int64_t stride, float* __restrict__ acc, float* __restrict__ comp,
                                                 int dimx, int dimy, const cd* __restrict__ Q = nullptr,
                                                 int64_t pstride = 0) {
@@ -157,6 +157,7 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
         // Steep sectors of elongated grids (tan > 1) can drift more than the band
         // holds; those tiles read the skewed cells directly.
         const bool staged = nrows <= kDeskewBand;
+        bool full = false;  // kMasked: every staged cell of the tile is valid
         if (staged && kRows) {
             __syncthreads();  // previous sector's rows fully consumed
             const int tid = ty * kTile + tx;
@@ -194,8 +195,13 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
 #pragma unroll
             for (int u = 0; u < kLoads; u++)
                 if (ty + 8 * u < nrows) band[ty + 8 * u][tx] = v[u];
-            if (kMasked && tid < nrows) bmask[tid] = m;
-            __syncthreads();
+            if (kMasked) {
+                if (tid < nrows) bmask[tid] = m;
+                // Tiles whose staged rows cover all 32 columns need no mask.
+                full = __syncthreads_and(tid >= nrows || m == 0xffffffffu);
+            } else {
+                __syncthreads();
+            }
         }
         if (!col_ok || nv <= 0) continue;
         const int off = tj - tmin;
@@ -212,7 +218,7 @@ __global__ void __launch_bounds__(256) k_deskew(DevGeometry g, TypeLists tl, con
                 cell[kk] = ((__float_as_uint(e.y) >> tx) & 1u) ? e.x : 0.0f;
             } else if (kRows) {
                 cell[kk] = row_cell(d, rfirst, rlast, qv, r, j);
-            } else if (kMasked) {
+            } else if (kMasked && !full) {
                 const bool ok = staged ? ((bmask[br] >> tx) & 1u) != 0
                                        : (r < d.H && j >= rfirst[r] && j < rlast[r]);
                 cell[kk] = ok ? (staged ? band[br][tx] : so[(int64_t)r * dim_i + j]) : 0.0f;
