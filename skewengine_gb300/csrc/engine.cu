@@ -390,7 +390,8 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
 // the slot past H*dim_i unwritten, since no operator of the batch reads it.
 int run_skew(ske_engine e, const Batch& b, bool zero_tail = true) {
     LaunchScope ls(e, "skew", 1);
-    return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, e->stream, zero_tail));
+    return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, std::max(e->dimx, e->dimy),
+                               e->geo.max_H, e->stream, zero_tail));
 }
 
 // rows_from_p: the batch is Radon sectors whose back-projection was skipped;

@@ -47,22 +47,51 @@ __global__ void k_prepare(const float* __restrict__ in, float* __restrict__ orie
     }
 }
 
-__global__ void k_skew(DevGeometry g, Batch b, const float* __restrict__ orient, int64_t n_cells,
-                       float* __restrict__ SI, int64_t stride, int64_t len, bool zero_tail) {
-    const int slot = blockIdx.y;
+// Skewed input of every sector: thread = one column c of kSkewRows consecutive
+// rows.  Cell (r, c) = 0 + w_c*x[r-t_c-1][c] + (1-w_c)*x[r-t_c][c] (skew_gather):
+// the column's target and weight stay in registers, and the second source value
+// of row r is the first of row r+1, so each cell loads one new value.  Then the
+// slot's cells past H*dim_i are zeroed (all blocks share that work), unless the
+// caller skips it for sectors whose rows stay within dim_i.
+constexpr int kSkewRows = 32;
+constexpr int kSkewCols = 256;
+
+__global__ void __launch_bounds__(kSkewCols) k_skew(DevGeometry g, Batch b, const float* __restrict__ orient,
+                                                    int64_t n_cells, float* __restrict__ SI, int64_t stride,
+                                                    int64_t len, bool zero_tail) {
+    const int slot = blockIdx.z;
     const SectorDesc d = g.desc[b.angle[slot]];
-    const float* src = orient + (int64_t)d.type * n_cells;
-    const int32_t* tgt = g.target + d.col_off;
-    const float* wgt = g.weight + d.col_off;
     float* out = SI + slot * stride;
-    // Row by row (no flat-index division), then zeros past H*dim_i.
-    for (int r = blockIdx.x; r < d.H; r += gridDim.x)
-        for (int c = threadIdx.x; c < d.dim_i; c += blockDim.x)
-            out[(int64_t)r * d.dim_i + c] = skew_gather(d, tgt, wgt, src, r, c);
+    const int c = blockIdx.x * kSkewCols + threadIdx.x;
+    const int r0 = blockIdx.y * kSkewRows;
+    if (r0 < d.H && c < d.dim_i) {
+        const float* src = orient + (int64_t)d.type * n_cells;
+        const int t = g.target[d.col_off + c];
+        const float w = g.weight[d.col_off + c], w1 = __fsub_rn(1.0f, w);
+        int i0 = r0 - t - 1;  // source row of the w term
+        const float* p = src + ((int64_t)i0 * d.dim_i + c);
+        float* o = out + ((int64_t)r0 * d.dim_i + c);
+        float a = (unsigned)i0 < (unsigned)d.dim_o ? p[0] : 0.0f;
+        const int r1 = min(r0 + kSkewRows, d.H);
+        for (int r = r0; r < r1; r++) {
+            const bool v0 = (unsigned)i0 < (unsigned)d.dim_o, v1 = (unsigned)(i0 + 1) < (unsigned)d.dim_o;
+            const float bv = v1 ? p[d.dim_i] : 0.0f;
+            float acc = 0.0f;
+            acc = v0 ? __fadd_rn(acc, __fmul_rn(w, a)) : acc;
+            acc = v1 ? __fadd_rn(acc, __fmul_rn(w1, bv)) : acc;
+            *o = acc;
+            a = bv;
+            i0++;
+            p += d.dim_i;
+            o += d.dim_i;
+        }
+    }
     if (!zero_tail && d.in_width) return;  // nothing reads past H*dim_i
     const int64_t z0 = (int64_t)d.H * d.dim_i;
-    for (int64_t p = z0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < len; p += (int64_t)gridDim.x * blockDim.x)
-        out[p] = 0.0f;
+    const int64_t nthreads = (int64_t)gridDim.x * gridDim.y * kSkewCols;
+    for (int64_t q = z0 + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * kSkewCols + threadIdx.x; q < len;
+         q += nthreads)
+        out[q] = 0.0f;
 }
 
 __global__ void k_identity(DevGeometry g, Batch b, const float* __restrict__ SI, float* __restrict__ SO,
@@ -300,9 +329,9 @@ cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, c
 }
 
 cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells, float* SI,
-                        int64_t stride, int64_t len, cudaStream_t st, bool zero_tail) {
-    dim3 grid(1024, b.count);
-    k_skew<<<grid, 256, 0, st>>>(g, b, orient, n_cells, SI, stride, len, zero_tail);
+                        int64_t stride, int64_t len, int max_cols, int max_rows, cudaStream_t st, bool zero_tail) {
+    dim3 grid((max_cols + kSkewCols - 1) / kSkewCols, (max_rows + kSkewRows - 1) / kSkewRows, b.count);
+    k_skew<<<grid, kSkewCols, 0, st>>>(g, b, orient, n_cells, SI, stride, len, zero_tail);
     return cudaGetLastError();
 }
 

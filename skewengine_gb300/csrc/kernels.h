@@ -28,8 +28,10 @@ cudaError_t launch_prepare(const float* in, float* orient, int dimx, int dimy, c
 // slot, `len` = 2N + dim_l cells each, zero past H*dim_i).
 // zero_tail false: sectors whose rows stay within dim_i leave the cells past
 // H*dim_i as they were.
+// max_cols / max_rows: the largest dim_i / H of any sector (the grid's extent).
 cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells,
-                        float* SI, int64_t stride, int64_t len, cudaStream_t st, bool zero_tail = true);
+                        float* SI, int64_t stride, int64_t len, int max_cols, int max_rows, cudaStream_t st,
+                        bool zero_tail = true);
 
 // Identity operator (kernelUNIT.h:16-23): SO = SI on covered cells, 0 elsewhere.
 cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
