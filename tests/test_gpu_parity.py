@@ -67,6 +67,23 @@ def test_golden_sectors_per_sector_api(ske, golden_sectors):
                 assert bits_equal(acc.ravel(), golden_sectors[f"{base}__a{a}__acc"]), (base, a, "acc")
 
 
+def test_per_sector_after_batched_run(ske, oracle):
+    """Batched runs leave the skew buffers' unused cells unwritten; the per-sector
+    API on the same engine afterwards still sees the reference's buffers (zeros
+    past the sector's rows, a cleared output)."""
+    x = synthetic.fractal_dem(64, 13)
+    with ske.SkewEngine(64, 64) as eng:
+        full = eng.run(0, x, povh=POVH)
+        assert bits_equal(full, oracle.run(0, x, povh=POVH))
+        for a in (0, 20, 45, 90, 133):
+            eng.prepare(x)
+            eng.skew(a)
+            eng.kernel(0, POVH)
+            si, so = eng.skewed()
+            want_si, want_so, _ = oracle.sector(0, x, a, povh=POVH)
+            assert bits_equal(si, want_si) and bits_equal(so, want_so), a
+
+
 @pytest.mark.parametrize("side,side_y,seed", [(96, 96, 1), (128, 80, 2), (80, 128, 3), (200, 200, 4),
                                               (257, 257, 5)])
 def test_sdem_matches_oracle(ske, oracle, side, side_y, seed):
