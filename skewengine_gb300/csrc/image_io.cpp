@@ -34,20 +34,21 @@
 namespace {
 
 // ---------------------------------------------------------------- checksums
-uint32_t crc_table[256];
-bool crc_ready = false;
-
-uint32_t crc32_update(uint32_t crc, const uint8_t* p, size_t n) {
-    if (!crc_ready) {
+struct CrcTable {
+    uint32_t v[256];
+    CrcTable() {
         for (uint32_t i = 0; i < 256; i++) {
             uint32_t c = i;
             for (int k = 0; k < 8; k++) c = (c & 1u) ? 0xedb88320u ^ (c >> 1) : c >> 1;
-            crc_table[i] = c;
+            v[i] = c;
         }
-        crc_ready = true;
     }
+};
+
+uint32_t crc32_update(uint32_t crc, const uint8_t* p, size_t n) {
+    static const CrcTable table;  // initialised once, thread-safe
     crc ^= 0xffffffffu;
-    for (size_t i = 0; i < n; i++) crc = crc_table[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
+    for (size_t i = 0; i < n; i++) crc = table.v[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
     return crc ^ 0xffffffffu;
 }
 
