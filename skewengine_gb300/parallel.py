@@ -96,7 +96,6 @@ def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, ma
 
     Returns (output, recovered ranks) on rank 0 and (None, []) elsewhere.
     """
-    import pickle
     import time
     from .engine import DEFAULT_POVH, KERNEL_CEPSTRUM
 
@@ -105,7 +104,10 @@ def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, ma
     if rank != 0:
         try:
             acc, used = engine.accumulate(kernel, data, blocks[rank], povh=pv, accum=accum)
-            store.set(f"acc/{rank}", pickle.dumps({"acc": np.asarray(acc, np.float32), "used": int(used)}))
+            # Raw float32 bytes and the type mask (no pickle: nothing on rank 0
+            # executes what a store holds).  The accumulator key is set last.
+            store.set(f"used/{rank}", str(int(used)))
+            store.set(f"acc/{rank}", np.ascontiguousarray(acc, np.float32).tobytes())
         except Exception as exc:  # report, then let the caller see the failure too
             store.set(f"err/{rank}", repr(exc).encode())
             raise
@@ -117,8 +119,10 @@ def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, ma
         got = None
         while got is None:
             if store.check([f"acc/{r}"]):
-                got = pickle.loads(store.get(f"acc/{r}"))
-                results[r] = (got["acc"], got["used"])
+                got = np.frombuffer(store.get(f"acc/{r}"), np.float32)
+                if got.size != 4 * engine.dimx * engine.dimy:
+                    raise ValueError(f"rank {r} posted {got.size} accumulator values")
+                results[r] = (got.reshape(4, -1), int(store.get(f"used/{r}")))
             elif store.check([f"err/{r}"]) or time.monotonic() > deadline:
                 results[r] = engine.accumulate(kernel, data, blocks[r], povh=pv, accum=accum)
                 recovered.append(r)
