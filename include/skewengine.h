@@ -337,6 +337,21 @@ int ske_render(int kernel, const float* output, int dimx, int dimy, uint8_t* rgb
  * input image given as ske_png_read_image returns it. */
 int ske_render_input(const float* image, int count, uint8_t* grey);
 
+/* ---- Learned total-viewshed surrogate (no reference counterpart) ----------
+ * The convolutions of a U-Net that approximates the engine's total-viewshed
+ * output on DEM tiles.  3x3, stride 1, zero padding 1, NHWC bfloat16 tensors
+ * on the device, ordered on `stream`: y = relu?(conv(x, w) + bias).
+ * w: cout x kpad bfloat16, kpad = 9*cin rounded up to a multiple of 32, entry
+ * [co][(ky*3 + kx)*cin + ci], zero past 9*cin; bias: cout floats or null.
+ * cin a multiple of 8, cout even. */
+int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
+                     int cin, int cout, int relu, void* stream);
+/* Weight gradient of ske_conv3x3_bf16, added into dw (cout x kpad float32):
+ * dw[co][k] += sum over pixels of dy[pixel][co] * (im2col x)[pixel][k].
+ * cout a multiple of 8. */
+int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
+                           int cout, void* stream);
+
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
  * a raw float32 file or a synthetic input and writes the result.  See
  * INTEGRATION.md for the argument list. */

@@ -1,0 +1,297 @@
+"""Learned total-viewshed surrogate.
+
+A 4-level U-Net (32 base channels, 3x3 convolutions, bfloat16 weights and
+activations, float32 accumulation) maps a 256 x 256 DEM tile to the log of the
+visible area of each cell that the engine computes for that tile (kernelSDEM,
+180 angles = 360 directional sectors).  The reference has no such model: it is
+trained on the engine's own outputs, and at inference the engine itself checks
+a sample of tiles and recomputes every tile whose error exceeds the bound.
+
+The convolutions are the engine's hand-written implicit-GEMM kernels
+(``ske_conv3x3_bf16`` forward and data gradient, ``ske_conv3x3_wgrad_bf16``
+weight gradient, tensor-core mma.sync with bfloat16 operands); pooling,
+upsampling, concatenation, the 1x1 output layer, the loss and the optimiser are
+PyTorch operations around them.
+
+Tensors are NHWC.  Input channels: 0 = the tile's heights minus their mean,
+divided by the tile's height range (or 1 for a flat tile), 1 = log(1 + range)
+(the relief amplitude, which visibility depends on), 2-7 = 0 (the kernels need
+a multiple of 8 channels).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+
+import numpy as np
+
+from . import synthetic
+from ._lib import check, load
+
+TILE = 256
+IN_CH = 8
+BASE = 32
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "surrogate_unet32.npz")
+
+
+def kpad(cin: int) -> int:
+    """Padded reduction length of a 3x3 convolution with cin input channels."""
+    return (9 * cin + 31) // 32 * 32
+
+
+def _stream(t):
+    import torch
+    return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
+
+
+def conv3x3(x, w, bias=None, relu: bool = False):
+    """y = relu?(conv3x3(x, w) + bias); x (N, H, W, Cin) bf16, w (Cout, kpad(Cin)) bf16."""
+    import torch
+    n, h, wd, cin = x.shape
+    cout = w.shape[0]
+    assert x.is_contiguous() and w.is_contiguous() and x.dtype == torch.bfloat16 and w.dtype == torch.bfloat16
+    assert w.shape[1] == kpad(cin)
+    y = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x.device)
+    check(load().ske_conv3x3_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
+                                  C.c_void_p(bias.data_ptr()) if bias is not None else None,
+                                  C.c_void_p(y.data_ptr()), n, h, wd, cin, cout, int(relu), _stream(x)))
+    return y
+
+
+def conv3x3_wgrad(x, dy, cout: int):
+    """dW (Cout, kpad(Cin)) float32 of conv3x3 for input x and output gradient dy."""
+    import torch
+    n, h, wd, cin = x.shape
+    dw = torch.zeros((cout, kpad(cin)), dtype=torch.float32, device=x.device)
+    check(load().ske_conv3x3_wgrad_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(dy.data_ptr()),
+                                        C.c_void_p(dw.data_ptr()), n, h, wd, cin, cout, _stream(x)))
+    return dw
+
+
+def flip_transpose(w, cin: int, cout: int):
+    """Weights of the data gradient: W'[ci][(ky*3+kx)*cout + co] = W[co][((2-ky)*3 + 2-kx)*cin + ci]."""
+    import torch
+    w9 = w[:, : 9 * cin].reshape(cout, 9, cin).flip(1).permute(2, 1, 0).reshape(cin, 9 * cout)
+    out = torch.zeros((cin, kpad(cout)), dtype=w.dtype, device=w.device)
+    out[:, : 9 * cout] = w9
+    return out
+
+
+def _conv_fn():
+    import torch
+
+    class Conv3x3(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, x, w32, b, relu):
+            w = w32.to(torch.bfloat16)
+            y = conv3x3(x, w, b, relu)
+            ctx.save_for_backward(x, w, y)
+            ctx.relu = relu
+            return y
+
+        @staticmethod
+        def backward(ctx, dy):
+            x, w, y = ctx.saved_tensors
+            if ctx.relu:
+                dy = dy * (y > 0)
+            dy = dy.to(torch.bfloat16).contiguous()
+            cin, cout = x.shape[3], w.shape[0]
+            dx = conv3x3(dy, flip_transpose(w, cin, cout)) if ctx.needs_input_grad[0] else None
+            dw = conv3x3_wgrad(x, dy, cout)
+            db = dy.float().sum((0, 1, 2))
+            return dx, dw, db, None
+
+    return Conv3x3
+
+
+_CONV = None
+
+
+def conv_op(x, w32, b, relu=True):
+    global _CONV
+    if _CONV is None:
+        _CONV = _conv_fn()
+    return _CONV.apply(x, w32, b, relu)
+
+
+# Channel plan: (name, cin, cout).
+LAYERS = [("e1a", IN_CH, BASE), ("e1b", BASE, BASE),
+          ("e2a", BASE, 2 * BASE), ("e2b", 2 * BASE, 2 * BASE),
+          ("e3a", 2 * BASE, 4 * BASE), ("e3b", 4 * BASE, 4 * BASE),
+          ("b4a", 4 * BASE, 8 * BASE), ("b4b", 8 * BASE, 8 * BASE),
+          ("d3a", 12 * BASE, 4 * BASE), ("d3b", 4 * BASE, 4 * BASE),
+          ("d2a", 6 * BASE, 2 * BASE), ("d2b", 2 * BASE, 2 * BASE),
+          ("d1a", 3 * BASE, BASE), ("d1b", BASE, BASE)]
+
+
+def conv_flops_per_tile(size: int = TILE) -> float:
+    """2 * 9 * Cin * Cout * H * W summed over the network's 3x3 convolutions."""
+    res = {"e1": size, "e2": size // 2, "e3": size // 4, "b4": size // 8, "d3": size // 4, "d2": size // 2,
+           "d1": size}
+    return float(sum(2 * 9 * cin * cout * res[name[:2]] ** 2 for name, cin, cout in LAYERS))
+
+
+def make_net(seed: int = 0, device="cuda"):
+    import torch
+
+    class UNet(torch.nn.Module):
+        def __init__(self):
+            super().__init__()
+            g = torch.Generator().manual_seed(seed)
+            self.w = torch.nn.ParameterDict()
+            self.b = torch.nn.ParameterDict()
+            for name, cin, cout in LAYERS:
+                w = torch.zeros(cout, kpad(cin))
+                w[:, : 9 * cin] = torch.randn(cout, 9 * cin, generator=g) * math.sqrt(2.0 / (9 * cin))
+                self.w[name] = torch.nn.Parameter(w)
+                self.b[name] = torch.nn.Parameter(torch.zeros(cout))
+            self.head_w = torch.nn.Parameter(torch.randn(BASE, 1, generator=g) * math.sqrt(1.0 / BASE))
+            self.head_b = torch.nn.Parameter(torch.full((1,), 8.0))
+
+        def c(self, x, name):
+            return conv_op(x, self.w[name], self.b[name], True)
+
+        @staticmethod
+        def pool(x):
+            import torch.nn.functional as F
+            return F.max_pool2d(x.permute(0, 3, 1, 2), 2).permute(0, 2, 3, 1).contiguous()
+
+        @staticmethod
+        def up(x):
+            import torch.nn.functional as F
+            return F.interpolate(x.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
+
+        def forward(self, x):
+            e1 = self.c(self.c(x, "e1a"), "e1b")
+            e2 = self.c(self.c(self.pool(e1), "e2a"), "e2b")
+            e3 = self.c(self.c(self.pool(e2), "e3a"), "e3b")
+            b4 = self.c(self.c(self.pool(e3), "b4a"), "b4b")
+            d3 = self.c(self.c(torch.cat([self.up(b4), e3], 3).contiguous(), "d3a"), "d3b")
+            d2 = self.c(self.c(torch.cat([self.up(d3), e2], 3).contiguous(), "d2a"), "d2b")
+            d1 = self.c(self.c(torch.cat([self.up(d2), e1], 3).contiguous(), "d1a"), "d1b")
+            return (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log area
+
+    import torch  # noqa: F811  (used inside forward)
+    return UNet().to(device)
+
+
+def encode_tiles(tiles: np.ndarray):
+    """(N, 256, 256) float32 heights -> (N, 256, 256, 8) bfloat16 network input (CUDA)."""
+    import torch
+    t = torch.as_tensor(np.ascontiguousarray(tiles, np.float32), device="cuda")
+    mean = t.mean((1, 2), keepdim=True)
+    rng = (t.amax((1, 2), keepdim=True) - t.amin((1, 2), keepdim=True))
+    x = torch.zeros(t.shape + (IN_CH,), dtype=torch.float32, device="cuda")
+    x[..., 0] = (t - mean) / torch.where(rng > 0, rng, torch.ones_like(rng))
+    x[..., 1] = torch.log1p(rng).expand_as(t)
+    return x.to(torch.bfloat16).contiguous()
+
+
+def label_tiles(tiles: np.ndarray, engine=None):
+    """The engine's total visible area of every cell of each tile (180 angles), as log(1 + area)."""
+    import torch
+    from .engine import SkewEngine
+    eng = engine or SkewEngine(tiles.shape[2], tiles.shape[1])
+    out = torch.empty(tiles.shape, dtype=torch.float32, device="cuda")
+    for i in range(len(tiles)):
+        x = torch.as_tensor(np.ascontiguousarray(tiles[i], np.float32), device="cuda")
+        eng.run(0, x, out[i])
+    torch.cuda.synchronize()
+    if engine is None:
+        eng.close()
+    return torch.log1p(out)
+
+
+def make_tiles(count: int, seed: int) -> np.ndarray:
+    """Seeded fractal DEM tiles (roughness 0.6-0.9, 0-1500 m relief, 10 m cells)."""
+    rng = np.random.default_rng(seed)
+    return np.stack([synthetic.fractal_dem(TILE, int(rng.integers(1 << 30)), roughness=float(rng.uniform(0.6, 0.9)))
+                     for _ in range(count)])
+
+
+def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 0, log=None):
+    """Adam on the mean squared error of log area; returns the per-step losses."""
+    import torch
+    opt = torch.optim.Adam(net.parameters(), lr=lr)
+    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, max(steps, 1))
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    losses = []
+    for step in range(steps):
+        idx = torch.randint(0, x.shape[0], (batch,), generator=g).to(x.device)
+        pred = net(x[idx])
+        loss = torch.mean((pred - y[idx]) ** 2)
+        opt.zero_grad(set_to_none=True)
+        loss.backward()
+        opt.step()
+        sched.step()
+        losses.append(float(loss.detach()))
+        if log and (step % 200 == 0 or step == steps - 1):
+            log(f"step {step} loss {losses[-1]:.4f}")
+    return losses
+
+
+def save(net, path: str = WEIGHTS) -> None:
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    arrs = {k: v.detach().float().cpu().numpy() for k, v in net.state_dict().items()}
+    np.savez_compressed(path, **arrs)
+
+
+def load_net(path: str = WEIGHTS, device="cuda"):
+    import torch
+    net = make_net(device=device)
+    z = np.load(path)
+    net.load_state_dict({k: torch.as_tensor(z[k]) for k in z.files})
+    return net
+
+
+def tile_area_error(pred_log, true_log):
+    """Per tile: |sum(pred area) - sum(true area)| / sum(true area)."""
+    import torch
+    pa = torch.expm1(pred_log.float()).clamp_min(0).sum((1, 2))
+    ta = torch.expm1(true_log.float()).sum((1, 2))
+    return ((pa - ta).abs() / ta.clamp_min(1e-6)).cpu().numpy()
+
+
+def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, bound: float = 0.02,
+              batch: int = 16, seed: int = 0, force_error=None):
+    """Per-tile total viewshed of a large DEM cut into 256 x 256 tiles (edge tiles
+    padded by replicating the last row / column).  The network predicts every
+    tile; the engine recomputes a random check_fraction of them, and any checked
+    tile whose total visible area is off by more than `bound` (relative) is
+    replaced by the engine's result.  `force_error` (tile index -> error) injects
+    errors on the host to exercise the fallback.
+
+    Returns (area map of the DEM, stats dict)."""
+    import torch
+    from .engine import SkewEngine
+    H, W = dem.shape
+    ty, tx = -(-H // TILE), -(-W // TILE)
+    padded = np.pad(dem, ((0, ty * TILE - H), (0, tx * TILE - W)), mode="edge")
+    tiles = padded.reshape(ty, TILE, tx, TILE).transpose(0, 2, 1, 3).reshape(ty * tx, TILE, TILE)
+    x = encode_tiles(tiles)
+    out = torch.empty((len(tiles), TILE, TILE), dtype=torch.float32, device="cuda")
+    with torch.no_grad():
+        for i in range(0, len(tiles), batch):
+            out[i:i + batch] = net(x[i:i + batch])
+    rng = np.random.default_rng(seed)
+    n_check = max(1, int(round(check_fraction * len(tiles))))
+    checked = np.sort(rng.choice(len(tiles), n_check, replace=False))
+    eng = engine or SkewEngine(TILE, TILE)
+    truth = label_tiles(tiles[checked], eng)
+    errs = tile_area_error(out[checked], truth)
+    if force_error:
+        for j, t in enumerate(checked):
+            if int(t) in force_error:
+                errs[j] = force_error[int(t)]
+    fell_back = [int(t) for t, e in zip(checked, errs) if e > bound]
+    for j, t in enumerate(checked):
+        if errs[j] > bound:
+            out[t] = truth[j]
+    if engine is None:
+        eng.close()
+    area = torch.expm1(out).clamp_min(0).cpu().numpy()
+    area = area.reshape(ty, tx, TILE, TILE).transpose(0, 2, 1, 3).reshape(ty * TILE, tx * TILE)[:H, :W]
+    stats = {"tiles": int(len(tiles)), "checked": [int(t) for t in checked], "errors": [float(e) for e in errs],
+             "fell_back": fell_back}
+    return area, stats

@@ -1,0 +1,121 @@
+"""The learned total-viewshed surrogate: its convolution kernels against a float64
+NumPy convolution (forward, data and weight gradients), training, and the
+engine-checked tiled inference with fallback."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from skewengine_gb300 import synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def _conv_ref(x, w, b, relu):
+    """NumPy conv3x3 (NHWC, zero padding) in float64; w: (Cout, 9*Cin)."""
+    n, h, wd, cin = x.shape
+    xp = np.pad(x, ((0, 0), (1, 1), (1, 1), (0, 0)))
+    cols = np.stack([xp[:, ky:ky + h, kx:kx + wd, :] for ky in range(3) for kx in range(3)], axis=3)
+    cols = cols.reshape(n, h, wd, 9 * cin)
+    pre = cols @ w.T + (b if b is not None else 0.0)
+    return (np.maximum(pre, 0.0) if relu else pre), pre, cols
+
+
+def _bf16(a):
+    import torch
+    return torch.as_tensor(a, dtype=torch.float32).to(torch.bfloat16)
+
+
+@pytest.fixture(scope="module")
+def sur():
+    from skewengine_gb300 import build
+    build.build()
+    from skewengine_gb300 import surrogate
+    return surrogate
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout,relu", [(2, 19, 23, 8, 32, True), (1, 37, 5, 32, 64, False),
+                                                  (3, 16, 16, 96, 72, True), (1, 130, 3, 64, 8, True)])
+def test_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
+    import torch
+    rng = np.random.default_rng(cin * 7 + cout)
+    xb = _bf16(rng.normal(0, 1, (n, h, w, cin)))
+    wb = _bf16(rng.normal(0, 0.2, (cout, 9 * cin)))
+    b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32)
+    wpad = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
+    wpad[:, : 9 * cin] = wb
+    y = sur.conv3x3(xb.cuda().contiguous(), wpad.cuda(), b.cuda(), relu).float().cpu().numpy()
+    ref, _, _ = _conv_ref(xb.double().numpy(), wb.double().numpy(), b.double().numpy(), relu)
+    # float32 accumulation of exact bfloat16 products, then one bfloat16 rounding
+    assert np.all(np.abs(y - ref) <= 2 ** -7 * np.abs(ref) + 1e-3), np.abs(y - ref).max()
+
+
+def test_conv_gradients_match_numpy(sur):
+    """d(sum(g * y))/dx, /dw, /db through the autograd function against NumPy."""
+    import torch
+    rng = np.random.default_rng(5)
+    n, h, w, cin, cout = 2, 21, 18, 32, 64
+    xb = _bf16(rng.normal(0, 1, (n, h, w, cin)))
+    w32 = torch.zeros((cout, sur.kpad(cin)))
+    w32[:, : 9 * cin] = torch.as_tensor(rng.normal(0, 0.1, (cout, 9 * cin)), dtype=torch.float32)
+    b32 = torch.as_tensor(rng.normal(0, 0.1, cout), dtype=torch.float32)
+    g = _bf16(rng.normal(0, 1, (n, h, w, cout)))
+    x = xb.cuda().contiguous().requires_grad_(True)
+    wp = w32.cuda().requires_grad_(True)
+    bp = b32.cuda().requires_grad_(True)
+    y = sur.conv_op(x, wp, bp, True)
+    (y.float() * g.cuda().float()).sum().backward()
+    wq = w32[:, : 9 * cin].to(torch.bfloat16).double().numpy()
+    _, pre, cols = _conv_ref(xb.double().numpy(), wq, b32.double().numpy(), True)
+    # the kernel's output is bfloat16: its ReLU mask is that of the rounded output
+    ybf = _bf16(np.maximum(pre, 0)).double().numpy()
+    dpre = _bf16(g.double().numpy() * (ybf > 0)).double().numpy()
+    dw_ref = dpre.reshape(-1, cout).T @ cols.reshape(-1, 9 * cin)
+    db_ref = dpre.reshape(-1, cout).sum(0)
+    dcols = (dpre @ wq).reshape(n, h, w, 9, cin)
+    dxp = np.zeros((n, h + 2, w + 2, cin))
+    for t in range(9):
+        ky, kx = divmod(t, 3)
+        dxp[:, ky:ky + h, kx:kx + w, :] += dcols[:, :, :, t, :]
+    dx_ref = dxp[:, 1:-1, 1:-1, :]
+    dw = wp.grad[:, : 9 * cin].cpu().double().numpy()
+    if wp.grad.shape[1] > 9 * cin:  # padding columns of the reduction get no gradient
+        assert wp.grad[:, 9 * cin:].abs().max().item() == 0
+    assert np.abs(dw - dw_ref).max() <= 1e-3 * np.abs(dw_ref).max()
+    assert np.abs(bp.grad.cpu().double().numpy() - db_ref).max() <= 1e-3 * np.abs(db_ref).max()
+    dx = x.grad.float().cpu().double().numpy()
+    assert np.all(np.abs(dx - dx_ref) <= 2 ** -7 * np.abs(dx_ref) + 2e-2 * np.abs(dx_ref).max() / 64)
+
+
+def test_training_reduces_loss(sur):
+    """A few hundred Adam steps on engine-labelled tiles reduce the loss several-fold."""
+    tiles = sur.make_tiles(24, 11)
+    x = sur.encode_tiles(tiles)
+    y = sur.label_tiles(tiles)
+    net = sur.make_net(seed=1)
+    losses = sur.train(net, x, y, steps=150, batch=8, lr=2e-3)
+    first, last = np.mean(losses[:10]), np.mean(losses[-10:])
+    assert last < first / 3, (first, last)
+
+
+def test_inference_falls_back_to_the_engine(sur):
+    """Tiles whose checked error exceeds the bound are replaced by the engine's
+    result (errors injected on the host); the others keep the network's."""
+    import torch
+    dem = synthetic.fractal_dem(520, 3, side_y=600)
+    net = sur.make_net(seed=2)
+    area, st = sur.infer_dem(net, dem, check_fraction=0.25, bound=0.02,
+                             force_error={t: 0.5 for t in range(9)})
+    assert st["tiles"] == 9 and len(st["checked"]) == 2
+    assert sorted(st["fell_back"]) == sorted(st["checked"])  # untrained net and injected errors
+    # a fallen-back tile equals the engine's own result for that tile
+    t = st["checked"][0]
+    ty, tx = divmod(t, 3)
+    tile = np.pad(dem, ((0, 768 - 600), (0, 768 - 520)), mode="edge")[ty * 256:(ty + 1) * 256, tx * 256:(tx + 1) * 256]
+    from skewengine_gb300 import SkewEngine
+    with SkewEngine(256, 256) as eng:
+        want = eng.run(0, np.ascontiguousarray(tile, np.float32))
+    got = np.pad(area, ((0, 768 - 600), (0, 768 - 520)))[ty * 256:(ty + 1) * 256, tx * 256:(tx + 1) * 256]
+    h, w = min(256, 600 - ty * 256), min(256, 520 - tx * 256)
+    want_log = torch.log1p(torch.as_tensor(want)).numpy()
+    np.testing.assert_allclose(got[:h, :w], np.expm1(want_log)[:h, :w], rtol=1e-5, atol=1e-3)
