@@ -203,15 +203,36 @@ def label_tiles(tiles: np.ndarray, engine=None):
     return torch.log1p(out)
 
 
-def make_tiles(count: int, seed: int) -> np.ndarray:
-    """Seeded fractal DEM tiles (roughness 0.6-0.9, 0-1500 m relief, 10 m cells)."""
+def _tile(args):
+    s, h = args
+    return synthetic.fractal_dem(TILE, s, roughness=h)
+
+
+def make_tiles(count: int, seed: int, workers: int | None = None) -> np.ndarray:
+    """Seeded fractal DEM tiles (roughness 0.6-0.9, 0-1500 m relief, 10 m cells).
+    Large counts are generated by a pool of spawned processes (spawned, so that
+    no CUDA context is forked)."""
     rng = np.random.default_rng(seed)
-    return np.stack([synthetic.fractal_dem(TILE, int(rng.integers(1 << 30)), roughness=float(rng.uniform(0.6, 0.9)))
-                     for _ in range(count)])
+    spec = [(int(rng.integers(1 << 30)), float(rng.uniform(0.6, 0.9))) for _ in range(count)]
+    if count < 256:
+        return np.stack([_tile(a) for a in spec])
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(workers or os.cpu_count()) as pool:
+        return np.stack(pool.map(_tile, spec, chunksize=64))
 
 
-def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 0, log=None):
-    """Adam on the mean squared error of log area; returns the per-step losses."""
+def _log_total(logarea):
+    """log of a tile's total visible area from per-cell log(1 + area)."""
+    import torch
+    return torch.logsumexp(logarea.flatten(1), 1)
+
+
+def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 0, log=None,
+          tile_weight: float = 1.0):
+    """Adam on the mean squared error of per-cell log area plus `tile_weight`
+    times the squared error of the log of each tile's total area (per-cell log
+    errors alone leave tile totals biased low: the totals are dominated by the
+    few cells that see far).  Returns the per-step losses."""
     import torch
     opt = torch.optim.Adam(net.parameters(), lr=lr)
     sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, max(steps, 1))
@@ -220,7 +241,8 @@ def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 
     for step in range(steps):
         idx = torch.randint(0, x.shape[0], (batch,), generator=g).to(x.device)
         pred = net(x[idx])
-        loss = torch.mean((pred - y[idx]) ** 2)
+        yt = y[idx]
+        loss = torch.mean((pred - yt) ** 2) + tile_weight * torch.mean((_log_total(pred) - _log_total(yt)) ** 2)
         opt.zero_grad(set_to_none=True)
         loss.backward()
         opt.step()
@@ -253,6 +275,15 @@ def tile_area_error(pred_log, true_log):
     return ((pa - ta).abs() / ta.clamp_min(1e-6)).cpu().numpy()
 
 
+def cut_tiles(dem: np.ndarray):
+    """256 x 256 tiles of a DEM in row-major tile order (edge tiles padded by
+    replicating the last row / column) and the tile grid's shape."""
+    H, W = dem.shape
+    ty, tx = -(-H // TILE), -(-W // TILE)
+    padded = np.pad(dem, ((0, ty * TILE - H), (0, tx * TILE - W)), mode="edge")
+    return padded.reshape(ty, TILE, tx, TILE).transpose(0, 2, 1, 3).reshape(ty * tx, TILE, TILE), (ty, tx)
+
+
 def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, bound: float = 0.02,
               batch: int = 16, seed: int = 0, force_error=None):
     """Per-tile total viewshed of a large DEM cut into 256 x 256 tiles (edge tiles
@@ -266,9 +297,7 @@ def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, b
     import torch
     from .engine import SkewEngine
     H, W = dem.shape
-    ty, tx = -(-H // TILE), -(-W // TILE)
-    padded = np.pad(dem, ((0, ty * TILE - H), (0, tx * TILE - W)), mode="edge")
-    tiles = padded.reshape(ty, TILE, tx, TILE).transpose(0, 2, 1, 3).reshape(ty * tx, TILE, TILE)
+    tiles, (ty, tx) = cut_tiles(dem)
     x = encode_tiles(tiles)
     out = torch.empty((len(tiles), TILE, TILE), dtype=torch.float32, device="cuda")
     with torch.no_grad():
@@ -295,3 +324,49 @@ def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, b
     stats = {"tiles": int(len(tiles)), "checked": [int(t) for t in checked], "errors": [float(e) for e in errs],
              "fell_back": fell_back}
     return area, stats
+
+
+def main(argv=None) -> int:
+    """Train the surrogate on engine-labelled tiles and save its weights:
+    python -m skewengine_gb300.surrogate --tiles 20000 --steps 4000."""
+    import argparse
+    import json
+    import time
+    import torch
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--tiles", type=int, default=20000)
+    ap.add_argument("--val", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--out", default=WEIGHTS)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    tiles = make_tiles(a.tiles, 1)
+    val = make_tiles(a.val, 2)
+    t1 = time.time()
+    x, y = encode_tiles(tiles), label_tiles(tiles)
+    xv, yv = encode_tiles(val), label_tiles(val)
+    torch.cuda.synchronize()
+    t2 = time.time()
+    net = make_net(seed=0)
+    losses = train(net, x, y, a.steps, a.batch, a.lr, log=lambda m: print(m, flush=True))
+    torch.cuda.synchronize()
+    t3 = time.time()
+    with torch.no_grad():
+        pv = torch.cat([net(xv[i:i + 16]) for i in range(0, len(xv), 16)])
+    err = tile_area_error(pv, yv)
+    base = tile_area_error(torch.full_like(yv, float(y.mean())), yv)
+    save(net, a.out)
+    print(json.dumps({"tiles": a.tiles, "steps": a.steps, "batch": a.batch, "gen_s": t1 - t0, "label_s": t2 - t1,
+                      "train_s": t3 - t2, "final_loss": float(np.mean(losses[-50:])),
+                      "val_rms_log": float(torch.sqrt(torch.mean((pv - yv) ** 2))),
+                      "val_tile_area_err_median": float(np.median(err)), "val_tile_area_err_p90": float(np.quantile(err, 0.9)),
+                      "val_within_2pct": float(np.mean(err <= 0.02)),
+                      "baseline_tile_area_err_median": float(np.median(base)),
+                      "baseline_within_2pct": float(np.mean(base <= 0.02))}), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
