@@ -203,22 +203,41 @@ def label_tiles(tiles: np.ndarray, engine=None):
     return torch.log1p(out)
 
 
-def _tile(args):
-    s, h = args
-    return synthetic.fractal_dem(TILE, s, roughness=h)
+SOURCE_SIDES = (256, 512, 1024, 2048, 4096)
+
+
+def _dem_tiles(args):
+    side, seed, h = args
+    return cut_tiles(synthetic.fractal_dem(side, seed, roughness=h))[0]
 
 
 def make_tiles(count: int, seed: int, workers: int | None = None) -> np.ndarray:
-    """Seeded fractal DEM tiles (roughness 0.6-0.9, 0-1500 m relief, 10 m cells).
+    """Seeded fractal DEM tiles: the 256 x 256 tiles of diamond-square DEMs of
+    sides 256 to 4096 (roughness 0.6-0.9, 0-1500 m relief, 10 m cells), an equal
+    share of the tiles from each side, shuffled.  A tile of a larger DEM has less
+    relief than a whole small DEM, as the tiles of a large DEM at inference do.
     Large counts are generated by a pool of spawned processes (spawned, so that
     no CUDA context is forked)."""
     rng = np.random.default_rng(seed)
-    spec = [(int(rng.integers(1 << 30)), float(rng.uniform(0.6, 0.9))) for _ in range(count)]
+    share = [count // len(SOURCE_SIDES) + (i < count % len(SOURCE_SIDES)) for i in range(len(SOURCE_SIDES))]
+    spec, cls = [], []
+    for c, side in enumerate(SOURCE_SIDES):
+        per_dem = (side // TILE) ** 2
+        for _ in range(-(-share[c] // per_dem)):
+            spec.append((side, int(rng.integers(1 << 30)), float(rng.uniform(0.6, 0.9))))
+            cls.append(c)
     if count < 256:
-        return np.stack([_tile(a) for a in spec])
-    import multiprocessing as mp
-    with mp.get_context("spawn").Pool(workers or os.cpu_count()) as pool:
-        return np.stack(pool.map(_tile, spec, chunksize=64))
+        parts = [_dem_tiles(a) for a in spec]
+    else:
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(workers or os.cpu_count()) as pool:
+            parts = pool.map(_dem_tiles, spec, chunksize=1)
+    picked = []
+    for c in range(len(SOURCE_SIDES)):
+        pool_c = np.concatenate([p for p, k in zip(parts, cls) if k == c]) if share[c] else np.zeros((0, TILE, TILE))
+        picked.append(pool_c[rng.permutation(len(pool_c))[: share[c]]])
+    tiles = np.concatenate(picked).astype(np.float32)
+    return tiles[rng.permutation(len(tiles))]
 
 
 def _log_total(logarea):
