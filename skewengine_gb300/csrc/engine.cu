@@ -120,6 +120,11 @@ struct ske_engine_s {
     int64_t lr_gauss_off = 0, lr_taper_off = 0;  // local Radon tables inside d_tw
     unsigned* d_counter = nullptr;
     int* d_status = nullptr;
+    // Tensor maps of d_SO for the TMA-staged deskew, for the buffer they were
+    // encoded for.
+    DeskewMaps maps;
+    const float* maps_so = nullptr;
+    int maps_slots = 0;
     int4* d_lists = nullptr;  // survivor lists of the viewshed sweep
     size_t list_bytes = 0;
     float* h_pin = nullptr;
@@ -406,11 +411,16 @@ int run_deskew(ske_engine e, const Batch& b, int is_max, int accum, bool rows_fr
         tl.count[t]++;
         e->used |= 1u << t;
     }
+    if (e->maps_so != e->d_SO || e->maps_slots != e->slots) {
+        encode_band_maps(&e->maps, e->d_SO, e->stride, e->slots, e->dimx, e->dimy);  // ok = false: plain staging
+        e->maps_so = e->d_SO;
+        e->maps_slots = e->slots;
+    }
     LaunchScope ls(e, "deskew", 1);
     if (is_max) return ls.done(launch_deskew_max(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->dimx, e->dimy, e->stream));
     return ls.done(launch_deskew_add(e->dg, tl, e->d_SO, e->stride, e->d_acc, e->d_comp, e->dimx, e->dimy, accum,
                                      e->stream, rows_from_p ? reinterpret_cast<const cd*>(e->d_P) : nullptr,
-                                     e->pstride, so_masked));
+                                     e->pstride, so_masked, &e->maps, e->d_status));
 }
 
 int run_prepare(ske_engine e, const float* input, int on_device) {

@@ -6,6 +6,8 @@
 // intrinsics (no contraction).
 #include <vector>
 
+#include <cuda.h>
+
 #include "kernels.h"
 
 namespace ske {
@@ -288,6 +290,184 @@ __global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4) k_deskew(D
     }
 }
 
+// ---- TMA-staged deskew ------------------------------------------------------
+// The same deskew (add / Kahan, plain or masked) with each sector's band of
+// kDeskewBand skewed rows x 32 columns brought into shared memory by the tensor
+// memory accelerator: the skewed output is a 3-D tensor (columns dim_i, rows,
+// slots; row pitch dim_i*4 bytes, a multiple of 16), thread 0 issues one
+// cp.async.bulk.tensor per sector (x = j0, a multiple of 32 floats) and the
+// copies complete on mbarriers.  Two buffers: the next staged sector's band is
+// in flight while the CTA accumulates the current one.  Columns past dim_i and
+// rows past the tensor read as zero.  Every wait is bounded; a wait that runs
+// out sets the engine's status word (the host reports SKE_ERR_DEVICE).
+constexpr int kTmaBoxBytes = kDeskewBand * kTile * 4;
+constexpr long long kTmaWaitLimit = 1ll << 20;
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, int bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, int parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the completion of phase `parity`; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, int parity) {
+    for (long long i = 0; i < kTmaWaitLimit; i++)
+        if (mbar_try(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_band(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of dst come first
+    mbar_expect(bar, kTmaBoxBytes);
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+            "r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+        : "memory");
+}
+
+template <int kMode, bool kMasked>
+__global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4)
+    k_deskew_tma(const __grid_constant__ CUtensorMap map_x, const __grid_constant__ CUtensorMap map_y, DevGeometry g,
+                 TypeLists tl, const float* __restrict__ SO, int64_t stride, float* __restrict__ acc,
+                 float* __restrict__ comp, int dimx, int dimy, int* __restrict__ status) {
+    __shared__ __align__(128) float band[2][kDeskewBand][kTile];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ unsigned bmask[kMasked ? kDeskewBand : 1];
+    constexpr int kPer = kDeskewRows / 8;
+    const int t = blockIdx.z;
+    const int cnt = tl.count[t];
+    if (cnt == 0) return;
+    const int64_t n = (int64_t)dimx * dimy;
+    const int dim_i = (t == 1 || t == 2) ? dimy : dimx;
+    const int dim_o = (t == 1 || t == 2) ? dimx : dimy;
+    const CUtensorMap* map = (t == 1 || t == 2) ? &map_y : &map_x;
+    const int j0 = blockIdx.x * kTile, i0 = blockIdx.y * kDeskewRows;
+    if (j0 >= dim_i || i0 >= dim_o) return;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTile + tx;
+    const int j = j0 + tx;
+    const bool col_ok = j < dim_i;
+    const int jlast = min(j0 + kTile, dim_i) - 1;
+    const int i_end = min(i0 + kDeskewRows, dim_o);
+    const int ib = ty * kPer;
+    const int nv = min(kPer, i_end - i0 - ib);
+    float* A = acc + t * n;
+    float s[kPer], c[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int i = i0 + ib + k;
+        s[k] = (col_ok && i < i_end) ? A[(int64_t)i * dim_i + j] : 0.0f;
+        c[k] = (kMode == kDeskewKahan && col_ok && i < i_end) ? comp[t * n + (int64_t)i * dim_i + j] : 0.0f;
+    }
+    // Band origin of sector q and whether it fits the staged band.
+    auto band_of = [&](int q, int* r0, int* nrows) {
+        const SectorDesc& d = g.desc[tl.angle[t][q]];
+        const int32_t* tg = g.target + d.col_off;
+        *r0 = i0 + tg[j0];
+        *nrows = (i_end - i0) + 1 + (tg[jlast] - tg[j0]);
+        return *nrows <= kDeskewBand;
+    };
+    if (tid == 0) {
+        mbar_init(&bar[0]);
+        mbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int r0n, nrn;
+    if (tid == 0 && band_of(0, &r0n, &nrn)) tma_band(&band[0][0][0], map, j0, r0n, tl.slot[t][0], &bar[0]);
+    int uses[2] = {0, 0};
+    bool ok_all = true;
+    for (int q = 0; q < cnt; q++) {
+        const int buf = q & 1;
+        // Prefetch the next sector's band into the other buffer (freed by the
+        // barrier that ended the previous sector).
+        if (tid == 0 && q + 1 < cnt && band_of(q + 1, &r0n, &nrn))
+            tma_band(&band[buf ^ 1][0][0], map, j0, r0n, tl.slot[t][q + 1], &bar[buf ^ 1]);
+        const SectorDesc& d = g.desc[tl.angle[t][q]];
+        const int32_t* tg = g.target + d.col_off;
+        const int tmin = tg[j0];
+        const int tj = col_ok ? tg[j] : tmin;
+        const float w = col_ok ? g.weight[d.col_off + j] : 0.0f;
+        int r0, nrows;
+        const bool staged = band_of(q, &r0, &nrows);
+        const float* so = SO + tl.slot[t][q] * stride;
+        const int32_t* rfirst = g.first + d.row_off;
+        const int32_t* rlast = g.last + d.row_off;
+        bool full = false;
+        if (staged) {
+            unsigned m = 0;
+            if (kMasked && tid < nrows) {
+                const int r = r0 + tid;
+                if (r < d.H) {
+                    const int lo_c = max(rfirst[r] - j0, 0), hi_c = min(rlast[r] - j0, kTile);
+                    if (hi_c > lo_c) m = (hi_c >= 32 ? 0xffffffffu : (1u << hi_c) - 1u) & ~((1u << lo_c) - 1u);
+                }
+                bmask[tid] = m;
+            }
+            ok_all = mbar_wait(&bar[buf], uses[buf] & 1) && ok_all;
+            uses[buf]++;
+            if (kMasked) full = __syncthreads_and(tid >= nrows || m == 0xffffffffu);
+            else __syncthreads();
+        }
+        if (col_ok && nv > 0) {
+            const int off = tj - tmin;
+            float cell[kPer + 1];
+#pragma unroll
+            for (int kk = 0; kk <= kPer; kk++) {
+                cell[kk] = 0.0f;
+                if (kk > nv) continue;
+                const int br = ib + kk + off;
+                const int r = i0 + ib + kk + tj;
+                if (kMasked && !full) {
+                    const bool okc = staged ? ((bmask[br] >> tx) & 1u) != 0
+                                            : (r < d.H && j >= rfirst[r] && j < rlast[r]);
+                    cell[kk] = okc ? (staged ? band[buf][br][tx] : so[(int64_t)r * dim_i + j]) : 0.0f;
+                } else {
+                    cell[kk] = staged ? band[buf][br][tx] : so[(int64_t)r * dim_i + j];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kPer; k++) {
+                if (k >= nv) continue;
+                const float v = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), cell[k]), __fmul_rn(w, cell[k + 1]));
+                if (kMode == kDeskewKahan) {
+                    const float y = __fsub_rn(v, c[k]);
+                    const float ts = __fadd_rn(s[k], y);
+                    c[k] = __fsub_rn(__fsub_rn(ts, s[k]), y);
+                    s[k] = ts;
+                } else {
+                    s[k] = __fadd_rn(s[k], v);
+                }
+            }
+        }
+        __syncthreads();  // this buffer and the masks are free for the next sectors
+    }
+    if (!ok_all) atomicExch(status, 7);  // a band copy never arrived
+    if (!col_ok) return;
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int i = i0 + ib + k;
+        if (i >= i_end) continue;
+        A[(int64_t)i * dim_i + j] = s[k];
+        if (kMode == kDeskewKahan) comp[t * n + (int64_t)i * dim_i + j] = c[k];
+    }
+}
+
 __global__ void k_reduce(const float* __restrict__ acc, const float* __restrict__ comp, unsigned used,
                          float* __restrict__ out, int dimx, int dimy, int is_max, int kahan) {
     const int64_t n = (int64_t)dimx * dimy;
@@ -347,10 +527,70 @@ static dim3 deskew_grid(int dimx, int dimy) {
     return dim3((dl + kTile - 1) / kTile, (dl + kDeskewRows - 1) / kDeskewRows, 4);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+bool encode_band_maps(DeskewMaps* m, const float* SO, int64_t stride, int slots, int dimx, int dimy) {
+    m->ok = false;
+    const EncodeTiledFn fn = encode_fn();
+    if (!fn || !SO || slots < 1 || stride % 4 || ((uintptr_t)SO & 15)) return false;
+    const int widths[2] = {dimx, dimy};
+    for (int k = 0; k < 2; k++) {
+        const int w = widths[k];
+        const int64_t rows = stride / w;
+        // Row pitch a multiple of 16 bytes; box no wider or taller than the tensor.
+        if (w % 4 || w < kTile || rows < kDeskewBand) return false;
+        const cuuint64_t dims[3] = {(cuuint64_t)w, (cuuint64_t)rows, (cuuint64_t)slots};
+        const cuuint64_t strides[2] = {(cuuint64_t)w * 4, (cuuint64_t)stride * 4};
+        const cuuint32_t box[3] = {(cuuint32_t)kTile, (cuuint32_t)kDeskewBand, 1};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        if (fn(k == 0 ? &m->x : &m->y, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)SO, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    m->ok = true;
+    return true;
+}
+
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO, int64_t stride,
                               float* acc, float* comp, int dimx, int dimy, int accum_mode, cudaStream_t st,
-                              const cd* Q, int64_t pstride, bool masked) {
+                              const cd* Q, int64_t pstride, bool masked, const DeskewMaps* maps, int* status) {
     const dim3 grid = deskew_grid(dimx, dimy), block(kTile, 8);
+    if (!Q && maps && maps->ok && status) {
+        if (accum_mode == kAccumKahan) {
+            if (masked)
+                k_deskew_tma<kDeskewKahan, true><<<grid, block, 0, st>>>(maps->x, maps->y, g, tl, SO, stride, acc, comp,
+                                                                        dimx, dimy, status);
+            else
+                k_deskew_tma<kDeskewKahan, false><<<grid, block, 0, st>>>(maps->x, maps->y, g, tl, SO, stride, acc,
+                                                                         comp, dimx, dimy, status);
+        } else {
+            if (masked)
+                k_deskew_tma<kDeskewAdd, true><<<grid, block, 0, st>>>(maps->x, maps->y, g, tl, SO, stride, acc,
+                                                                      nullptr, dimx, dimy, status);
+            else
+                k_deskew_tma<kDeskewAdd, false><<<grid, block, 0, st>>>(maps->x, maps->y, g, tl, SO, stride, acc,
+                                                                       nullptr, dimx, dimy, status);
+        }
+        return cudaGetLastError();
+    }
     if (masked && !Q) {
         if (accum_mode == kAccumKahan)
             k_deskew<kDeskewKahan, false, true><<<grid, block, 0, st>>>(g, tl, SO, stride, acc, comp, dimx, dimy);

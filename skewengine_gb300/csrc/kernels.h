@@ -4,6 +4,8 @@
 
 #include <cstdint>
 
+#include <cuda.h>
+
 #include "ske_device.cuh"
 
 namespace ske {
@@ -42,12 +44,24 @@ cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* S
 // With Q set, the slots are Radon sectors whose rows stay within dim_i, read
 // from their filtered row values (Q: pstride complex doubles per slot) instead
 // of SO: what the back-projection would write, without writing it.
+// Tensor maps of the skewed-output buffer for the TMA-staged deskew: 3-D
+// (columns, rows, slots) float32 views with rows of dimx (x) and dimy (y) cells.
+struct DeskewMaps {
+    CUtensorMap x, y;
+    bool ok = false;
+};
+// Encodes both maps; false (and maps unusable) where the layout does not allow
+// TMA (a row width not a multiple of 4 cells or under 32, no driver entry point).
+bool encode_band_maps(DeskewMaps* m, const float* SO, int64_t stride, int slots, int dimx, int dimy);
+
 // masked: SO holds defined values only on its sectors' valid cells (rows within
-// dim_i, SO not zeroed first); every other cell is read as zero.
+// dim_i, SO not zeroed first); every other cell is read as zero.  With maps
+// (ok) and a status word, the bands are staged by TMA (k_deskew_tma); a copy
+// that never completes sets *status.
 cudaError_t launch_deskew_add(const DevGeometry& g, const TypeLists& tl, const float* SO,
                               int64_t stride, float* acc, float* comp, int dimx, int dimy,
                               int accum_mode, cudaStream_t st, const cd* Q = nullptr, int64_t pstride = 0,
-                              bool masked = false);
+                              bool masked = false, const DeskewMaps* maps = nullptr, int* status = nullptr);
 // Max mode with angle encoding (skewEngine.cuh:774-785).
 cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const float* SO,
                               int64_t stride, float* acc, int dimx, int dimy, cudaStream_t st);
