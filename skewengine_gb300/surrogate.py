@@ -176,16 +176,17 @@ def make_net(seed: int = 0, device="cuda"):
     return UNet().to(device)
 
 
-def encode_tiles(tiles: np.ndarray):
-    """(N, 256, 256) float32 heights -> (N, 256, 256, 8) bfloat16 network input (CUDA)."""
+def encode_tiles(tiles):
+    """(N, 256, 256) float32 heights (NumPy or CUDA tensor) -> (N, 256, 256, 8)
+    bfloat16 network input (CUDA)."""
     import torch
-    t = torch.as_tensor(np.ascontiguousarray(tiles, np.float32), device="cuda")
+    t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda")
     mean = t.mean((1, 2), keepdim=True)
     rng = (t.amax((1, 2), keepdim=True) - t.amin((1, 2), keepdim=True))
-    x = torch.zeros(t.shape + (IN_CH,), dtype=torch.float32, device="cuda")
-    x[..., 0] = (t - mean) / torch.where(rng > 0, rng, torch.ones_like(rng))
-    x[..., 1] = torch.log1p(rng).expand_as(t)
-    return x.to(torch.bfloat16).contiguous()
+    x = torch.zeros(t.shape + (IN_CH,), dtype=torch.bfloat16, device="cuda")
+    x[..., 0] = ((t - mean) / torch.where(rng > 0, rng, torch.ones_like(rng))).to(torch.bfloat16)
+    x[..., 1] = torch.log1p(rng).expand_as(t).to(torch.bfloat16)
+    return x
 
 
 def label_tiles(tiles: np.ndarray, engine=None):
@@ -303,7 +304,16 @@ def cut_tiles(dem: np.ndarray):
     return padded.reshape(ty, TILE, tx, TILE).transpose(0, 2, 1, 3).reshape(ty * tx, TILE, TILE), (ty, tx)
 
 
-def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, bound: float = 0.02,
+def _cut_tiles_dev(dem):
+    """cut_tiles on a CUDA tensor, on the device."""
+    import torch.nn.functional as F
+    H, W = dem.shape
+    ty, tx = -(-H // TILE), -(-W // TILE)
+    padded = F.pad(dem[None, None], (0, tx * TILE - W, 0, ty * TILE - H), mode="replicate")[0, 0]
+    return padded.reshape(ty, TILE, tx, TILE).permute(0, 2, 1, 3).reshape(ty * tx, TILE, TILE).contiguous(), (ty, tx)
+
+
+def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float = 0.02,
               batch: int = 16, seed: int = 0, force_error=None):
     """Per-tile total viewshed of a large DEM cut into 256 x 256 tiles (edge tiles
     padded by replicating the last row / column).  The network predicts every
@@ -312,11 +322,15 @@ def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, b
     replaced by the engine's result.  `force_error` (tile index -> error) injects
     errors on the host to exercise the fallback.
 
-    Returns (area map of the DEM, stats dict)."""
+    `dem` is a NumPy array or a CUDA tensor; the area map comes back the same way
+    (a CUDA tensor stays on the device throughout).  Returns (area map, stats)."""
     import torch
     from .engine import SkewEngine
-    H, W = dem.shape
-    tiles, (ty, tx) = cut_tiles(dem)
+    on_host = not torch.is_tensor(dem)
+    d = torch.as_tensor(np.ascontiguousarray(dem, np.float32) if on_host else dem, dtype=torch.float32,
+                        device="cuda")
+    H, W = d.shape
+    tiles, (ty, tx) = _cut_tiles_dev(d)
     x = encode_tiles(tiles)
     out = torch.empty((len(tiles), TILE, TILE), dtype=torch.float32, device="cuda")
     with torch.no_grad():
@@ -326,8 +340,11 @@ def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, b
     n_check = max(1, int(round(check_fraction * len(tiles))))
     checked = np.sort(rng.choice(len(tiles), n_check, replace=False))
     eng = engine or SkewEngine(TILE, TILE)
-    truth = label_tiles(tiles[checked], eng)
-    errs = tile_area_error(out[checked], truth)
+    truth = torch.empty((n_check, TILE, TILE), dtype=torch.float32, device="cuda")
+    for j, t in enumerate(checked):
+        eng.run(0, tiles[int(t)], truth[j])
+    truth = torch.log1p(truth)
+    errs = tile_area_error(out[torch.as_tensor(checked, device="cuda")], truth)
     if force_error:
         for j, t in enumerate(checked):
             if int(t) in force_error:
@@ -335,14 +352,14 @@ def infer_dem(net, dem: np.ndarray, engine=None, check_fraction: float = 0.05, b
     fell_back = [int(t) for t, e in zip(checked, errs) if e > bound]
     for j, t in enumerate(checked):
         if errs[j] > bound:
-            out[t] = truth[j]
+            out[int(t)] = truth[j]
     if engine is None:
         eng.close()
-    area = torch.expm1(out).clamp_min(0).cpu().numpy()
-    area = area.reshape(ty, tx, TILE, TILE).transpose(0, 2, 1, 3).reshape(ty * TILE, tx * TILE)[:H, :W]
+    area = torch.expm1(out).clamp_min_(0)
+    area = area.reshape(ty, tx, TILE, TILE).permute(0, 2, 1, 3).reshape(ty * TILE, tx * TILE)[:H, :W]
     stats = {"tiles": int(len(tiles)), "checked": [int(t) for t in checked], "errors": [float(e) for e in errs],
              "fell_back": fell_back}
-    return area, stats
+    return (area.cpu().numpy() if on_host else area), stats
 
 
 def main(argv=None) -> int:
