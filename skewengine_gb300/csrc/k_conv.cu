@@ -95,7 +95,7 @@ __device__ __forceinline__ const bf16* a_src(const bf16* __restrict__ X, const P
     return X + ((int64_t)(p.base + iy * W + ix) * Cin + ci);
 }
 
-__global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
+__global__ void __launch_bounds__(kThreads, 5) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
                                                       const float* __restrict__ bias, bf16* __restrict__ Y, int M,
                                                       int H, int W, int Cin, int Cout, int Kpad, int relu) {
     __shared__ __align__(16) bf16 As[2][kBM][kPitch];
