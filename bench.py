@@ -419,6 +419,10 @@ def surrogate_workload(args):
         torch.cuda.synchronize()
     fwd_ms = t0.elapsed_time(t1)
     err = sur.tile_area_error(pred, torch.log1p(truth))
+    # the whole DEM's visible area (the sum over its tiles), network alone
+    net_total = float(torch.expm1(pred).clamp_min(0).sum())
+    true_total = float(truth.sum())
+    dem_err = abs(net_total - true_total) / true_total
     flops = sur.conv_flops_per_tile() * len(tiles)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
@@ -434,7 +438,8 @@ def surrogate_workload(args):
                        "checked_tiles": len(stats["checked"]), "fell_back": len(stats["fell_back"]),
                        "tile_area_error_median": float(np.median(err)),
                        "tile_area_error_p90": float(np.quantile(err, 0.9)),
-                       "tiles_within_2pct": float(np.mean(err <= 0.02))},
+                       "tiles_within_2pct": float(np.mean(err <= 0.02)),
+                       "dem_total_area_error_network": dem_err},
             "roofline": {"bound": "tensor", "kernel": "k_conv3x3 (network forward, all tiles)",
                          "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["bf16_tflops"],
