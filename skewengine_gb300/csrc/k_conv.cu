@@ -95,7 +95,7 @@ __device__ __forceinline__ const bf16* a_src(const bf16* __restrict__ X, const P
     return X + ((int64_t)(p.base + iy * W + ix) * Cin + ci);
 }
 
-__global__ void __launch_bounds__(kThreads, 5) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
+__global__ void __launch_bounds__(kThreads, 4) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
                                                       const float* __restrict__ bias, bf16* __restrict__ Y, int M,
                                                       int H, int W, int Cin, int Cout, int Kpad, int relu) {
     __shared__ __align__(16) bf16 As[2][kBM][kPitch];
@@ -104,22 +104,30 @@ __global__ void __launch_bounds__(kThreads, 5) k_conv3x3(const bf16* __restrict_
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
     const int wm = (warp >> 1) * 64, wn = (warp & 1) * 32;
 
-    // This thread's A rows (4) and B rows (2) and their 8-wide k offsets.
-    Pix pa[4];
-    int ka[4];
+    // This thread's 4 A rows (pixels) share one 8-wide k offset kc: their
+    // (tap, channel) pair is tracked incrementally as k advances by kBK, so each
+    // chunk costs a bounds test and an add (no division per chunk and slice).
+    const int kc = (tid & 3) * 8;
+    const bf16* prow[4];
+    int py[4], px[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        const int c = tid + i * kThreads;
-        pa[i] = pixel_of(m0 + (c >> 2), M, H, W);
-        ka[i] = (c & 3) * 8;
+        const Pix p = pixel_of(m0 + ((tid + i * kThreads) >> 2), M, H, W);
+        py[i] = p.y;
+        px[i] = p.x;
+        prow[i] = p.y >= 0 ? X + (int64_t)(p.base + p.y * W + p.x) * Cin : X;
     }
-    auto load = [&](int stage, int k0) {
+    int tap = kc / Cin, ci = kc - (kc / Cin) * Cin;  // k = k0 + kc at the next load
+    auto load = [&](int stage, int k0) {  // called with k0 = 0, kBK, 2*kBK, ... in order
+        const int ky = tap / 3, kx = tap - 3 * (tap / 3);
+        const int64_t toff = ((int64_t)(ky - 1) * W + (kx - 1)) * Cin + ci;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int c = tid + i * kThreads;
-            const bf16* src = a_src(X, pa[i], k0 + ka[i], Cin, H, W);
-            cp_async16(&As[stage][c >> 2][ka[i]], src ? src : X, src ? 16 : 0);
+            const int iy = py[i] + ky - 1, ix = px[i] + kx - 1;
+            const bool ok = tap < 9 && iy >= 0 && iy < H && ix >= 0 && ix < W;
+            cp_async16(&As[stage][(tid + i * kThreads) >> 2][kc], ok ? prow[i] + toff : X, ok ? 16 : 0);
         }
+        for (ci += kBK; ci >= Cin; ci -= Cin) tap++;
 #pragma unroll
         for (int i = 0; i < 2; i++) {
             const int c = tid + i * kThreads;
