@@ -346,6 +346,12 @@ int ske_render_input(const float* image, int count, uint8_t* grey);
  * cin a multiple of 8, cout even. */
 int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
                      int cin, int cout, int relu, void* stream);
+/* ske_conv3x3_bf16 of the channel concatenation [nearest-upsampled xlow, xskip]
+ * without materialising it: xlow is n x h/2 x w/2 x c1, xskip n x h x w x c2
+ * (h, w even; c1, c2 multiples of 8); w has cin = c1 + c2.  Same results as the
+ * convolution of the concatenated tensor. */
+int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
+                           int n, int h, int w_, int c1, int c2, int cout, int relu, void* stream);
 /* Weight gradient of ske_conv3x3_bf16, added into dw (cout x kpad float32):
  * dw[co][k] += sum over pixels of dy[pixel][co] * (im2col x)[pixel][k].
  * cout a multiple of 8. */

@@ -95,9 +95,16 @@ __device__ __forceinline__ const bf16* a_src(const bf16* __restrict__ X, const P
     return X + ((int64_t)(p.base + iy * W + ix) * Cin + ci);
 }
 
+// kUpCat: the input is the channel concatenation of X (C1 channels at half the
+// resolution, nearest-upsampled) and X2 (C2 channels at full resolution), read
+// in place: A's 8-channel chunk at (y, x) comes from X at (y/2, x/2) for
+// channels below C1, else from X2.  The same products in the same order as on
+// the materialised concatenation.
+template <bool kUpCat>
 __global__ void __launch_bounds__(kThreads, 4) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
                                                       const float* __restrict__ bias, bf16* __restrict__ Y, int M,
-                                                      int H, int W, int Cin, int Cout, int Kpad, int relu) {
+                                                      int H, int W, int Cin, int Cout, int Kpad, int relu,
+                                                      const bf16* __restrict__ X2, int C1) {
     __shared__ __align__(16) bf16 As[2][kBM][kPitch];
     __shared__ __align__(16) bf16 Bs[2][kBN][kPitch];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -109,13 +116,14 @@ __global__ void __launch_bounds__(kThreads, 4) k_conv3x3(const bf16* __restrict_
     // chunk costs a bounds test and an add (no division per chunk and slice).
     const int kc = (tid & 3) * 8;
     const bf16* prow[4];
-    int py[4], px[4];
+    int py[4], px[4], pn[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
         const Pix p = pixel_of(m0 + ((tid + i * kThreads) >> 2), M, H, W);
         py[i] = p.y;
         px[i] = p.x;
-        prow[i] = p.y >= 0 ? X + (int64_t)(p.base + p.y * W + p.x) * Cin : X;
+        pn[i] = p.y >= 0 ? p.base / (H * W) : 0;
+        prow[i] = (!kUpCat && p.y >= 0) ? X + (int64_t)(p.base + p.y * W + p.x) * Cin : X;
     }
     int tap = kc / Cin, ci = kc - (kc / Cin) * Cin;  // k = k0 + kc at the next load
     auto load = [&](int stage, int k0) {  // called with k0 = 0, kBK, 2*kBK, ... in order
@@ -125,7 +133,16 @@ __global__ void __launch_bounds__(kThreads, 4) k_conv3x3(const bf16* __restrict_
         for (int i = 0; i < 4; i++) {
             const int iy = py[i] + ky - 1, ix = px[i] + kx - 1;
             const bool ok = tap < 9 && iy >= 0 && iy < H && ix >= 0 && ix < W;
-            cp_async16(&As[stage][(tid + i * kThreads) >> 2][kc], ok ? prow[i] + toff : X, ok ? 16 : 0);
+            const bf16* src = X;
+            if (ok) {
+                if (!kUpCat)
+                    src = prow[i] + toff;
+                else if (ci < C1)
+                    src = X + ((int64_t)(pn[i] * (H >> 1) + (iy >> 1)) * (W >> 1) + (ix >> 1)) * C1 + ci;
+                else
+                    src = X2 + ((int64_t)(pn[i] * H + iy) * W + ix) * (Cin - C1) + (ci - C1);
+            }
+            cp_async16(&As[stage][(tid + i * kThreads) >> 2][kc], src, ok ? 16 : 0);
         }
         for (ci += kBK; ci >= Cin; ci -= Cin) tap++;
 #pragma unroll
@@ -284,8 +301,24 @@ extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias,
     if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
     const int kpad = (9 * cin + kBK - 1) / kBK * kBK;
     const dim3 grid((unsigned)((m + kBM - 1) / kBM), (unsigned)((cout + kBN - 1) / kBN));
-    k_conv3x3<<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)w, bias, (bf16*)y, (int)m,
-                                                           h, w_, cin, cout, kpad, relu);
+    k_conv3x3<false><<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)w, bias, (bf16*)y,
+                                                                  (int)m, h, w_, cin, cout, kpad, relu, nullptr, 0);
+    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
+extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
+                                      int n, int h, int w_, int c1, int c2, int cout, int relu, void* stream) {
+    if (!xlow || !xskip || !w || !y || n < 1 || h < 2 || w_ < 2 || h % 2 || w_ % 2 || c1 < 8 || c1 % 8 ||
+        c2 < 8 || c2 % 8 || cout < 2 || cout % 2)
+        return SKE_ERR_INVALID;
+    const int64_t m = (int64_t)n * h * w_;
+    const int cin = c1 + c2;
+    if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
+    const int kpad = (9 * cin + kBK - 1) / kBK * kBK;
+    const dim3 grid((unsigned)((m + kBM - 1) / kBM), (unsigned)((cout + kBN - 1) / kBN));
+    k_conv3x3<true><<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)xlow, (const bf16*)w, bias, (bf16*)y,
+                                                                 (int)m, h, w_, cin, cout, kpad, relu,
+                                                                 (const bf16*)xskip, c1);
     return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
 }
 

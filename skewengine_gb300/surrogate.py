@@ -59,6 +59,23 @@ def conv3x3(x, w, bias=None, relu: bool = False):
     return y
 
 
+def conv3x3_upcat(xlow, skip, w, bias=None, relu: bool = False):
+    """conv3x3(cat([nearest-upsampled xlow, skip], channels)) without building the
+    concatenation; the same values as conv3x3 on it."""
+    import torch
+    n, h, wd, c2 = skip.shape
+    c1 = xlow.shape[3]
+    cout = w.shape[0]
+    assert xlow.shape[:3] == (n, h // 2, wd // 2) and xlow.is_contiguous() and skip.is_contiguous()
+    assert w.shape[1] == kpad(c1 + c2) and w.dtype == torch.bfloat16
+    y = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=skip.device)
+    check(load().ske_conv3x3_upcat_bf16(C.c_void_p(xlow.data_ptr()), C.c_void_p(skip.data_ptr()),
+                                        C.c_void_p(w.data_ptr()),
+                                        C.c_void_p(bias.data_ptr()) if bias is not None else None,
+                                        C.c_void_p(y.data_ptr()), n, h, wd, c1, c2, cout, int(relu), _stream(skip)))
+    return y
+
+
 def conv3x3_wgrad(x, dy, cout: int):
     """dW (Cout, kpad(Cin)) float32 of conv3x3 for input x and output gradient dy."""
     import torch
@@ -162,14 +179,21 @@ def make_net(seed: int = 0, device="cuda"):
             import torch.nn.functional as F
             return F.interpolate(x.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
 
+        def upcat(self, low, skip, name):
+            # Without gradients the decoder reads the upsampled low-resolution
+            # input and the skip connection in place (same values).
+            if not torch.is_grad_enabled():
+                return conv3x3_upcat(low, skip, self.w[name].to(torch.bfloat16), self.b[name], True)
+            return self.c(torch.cat([self.up(low), skip], 3).contiguous(), name)
+
         def forward(self, x):
             e1 = self.c(self.c(x, "e1a"), "e1b")
             e2 = self.c(self.c(self.pool(e1), "e2a"), "e2b")
             e3 = self.c(self.c(self.pool(e2), "e3a"), "e3b")
             b4 = self.c(self.c(self.pool(e3), "b4a"), "b4b")
-            d3 = self.c(self.c(torch.cat([self.up(b4), e3], 3).contiguous(), "d3a"), "d3b")
-            d2 = self.c(self.c(torch.cat([self.up(d3), e2], 3).contiguous(), "d2a"), "d2b")
-            d1 = self.c(self.c(torch.cat([self.up(d2), e1], 3).contiguous(), "d1a"), "d1b")
+            d3 = self.c(self.upcat(b4, e3, "d3a"), "d3b")
+            d2 = self.c(self.upcat(d3, e2, "d2a"), "d2b")
+            d1 = self.c(self.upcat(d2, e1, "d1a"), "d1b")
             return (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log area
 
     import torch  # noqa: F811  (used inside forward)

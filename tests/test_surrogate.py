@@ -50,6 +50,24 @@ def test_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
     assert np.all(np.abs(y - ref) <= 2 ** -7 * np.abs(ref) + 1e-3), np.abs(y - ref).max()
 
 
+def test_upcat_conv_equals_conv_of_the_concatenation(sur):
+    """The fused upsample + concatenate convolution gives the bits of the
+    convolution of the materialised concatenation."""
+    import torch
+    import torch.nn.functional as F
+    rng = np.random.default_rng(3)
+    low = _bf16(rng.normal(0, 1, (2, 9, 13, 64))).cuda().contiguous()
+    skip = _bf16(rng.normal(0, 1, (2, 18, 26, 32))).cuda().contiguous()
+    w = torch.zeros((48, sur.kpad(96)), dtype=torch.bfloat16)
+    w[:, : 9 * 96] = _bf16(rng.normal(0, 0.1, (48, 9 * 96)))
+    w = w.cuda()
+    b = torch.as_tensor(rng.normal(0, 0.5, 48), dtype=torch.float32).cuda()
+    up = F.interpolate(low.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
+    want = sur.conv3x3(torch.cat([up, skip], 3).contiguous(), w, b, True)
+    got = sur.conv3x3_upcat(low, skip, w, b, True)
+    assert torch.equal(got.view(torch.int16), want.view(torch.int16))
+
+
 def test_conv_gradients_match_numpy(sur):
     """d(sum(g * y))/dx, /dw, /db through the autograd function against NumPy."""
     import torch
