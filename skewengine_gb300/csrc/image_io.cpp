@@ -136,11 +136,12 @@ const uint16_t kDistBase[30] = {1, 2, 3, 4, 5, 7, 9, 13, 17, 25, 33, 49, 65, 97,
                                 1025, 1537, 2049, 3073, 4097, 6145, 8193, 12289, 16385, 24577};
 const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
 
-bool inflate_codes(BitReader& br, std::vector<uint8_t>& out, const Huffman& lit, const Huffman& dist) {
+bool inflate_codes(BitReader& br, std::vector<uint8_t>& out, const Huffman& lit, const Huffman& dist, size_t limit) {
     for (;;) {
         int sym = decode_symbol(br, lit);
         if (sym < 0) return false;
         if (sym < 256) {
+            if (out.size() >= limit) return false;
             out.push_back((uint8_t)sym);
         } else if (sym == 256) {
             return true;
@@ -152,13 +153,15 @@ bool inflate_codes(BitReader& br, std::vector<uint8_t>& out, const Huffman& lit,
             if (ds < 0 || ds >= 30) return false;
             const size_t d = (size_t)kDistBase[ds] + (size_t)br.bits(kDistExtra[ds]);
             if (br.overrun || d > out.size()) return false;
+            if (out.size() + len > limit) return false;
             const size_t from = out.size() - d;
             for (int i = 0; i < len; i++) out.push_back(out[from + i]);
         }
     }
 }
 
-bool inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out) {
+// Stops (false) once the output would exceed `limit` bytes.
+bool inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out, size_t limit) {
     BitReader br{in, n};
     int last;
     do {
@@ -173,6 +176,7 @@ bool inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out) {
             const unsigned nlen = in[br.pos + 2] | in[br.pos + 3] << 8;
             br.pos += 4;
             if ((len ^ 0xffffu) != nlen || br.pos + len > n) return false;
+            if (out.size() + len > limit) return false;
             out.insert(out.end(), in + br.pos, in + br.pos + len);
             br.pos += len;
         } else if (type == 1) {  // fixed codes (RFC 1951 section 3.2.6)
@@ -185,7 +189,7 @@ bool inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out) {
             Huffman lit, dist;
             build_huffman(lit, l, 288);
             build_huffman(dist, l + 288, 30);
-            if (!inflate_codes(br, out, lit, dist)) return false;
+            if (!inflate_codes(br, out, lit, dist, limit)) return false;
         } else if (type == 2) {  // dynamic codes (RFC 1951 section 3.2.7)
             const int hlit = br.bits(5) + 257, hdist = br.bits(5) + 1, hclen = br.bits(4) + 4;
             static const uint8_t order[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
@@ -219,7 +223,7 @@ bool inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out) {
             if (l[256] == 0) return false;  // no end-of-block code
             Huffman lit, dist;
             if (!build_huffman(lit, l, hlit) || !build_huffman(dist, l + hlit, hdist)) return false;
-            if (!inflate_codes(br, out, lit, dist)) return false;
+            if (!inflate_codes(br, out, lit, dist, limit)) return false;
         } else {
             return false;
         }
@@ -227,11 +231,11 @@ bool inflate(const uint8_t* in, size_t n, std::vector<uint8_t>& out) {
     return true;
 }
 
-bool zlib_decompress(const std::vector<uint8_t>& z, std::vector<uint8_t>& out) {
+bool zlib_decompress(const std::vector<uint8_t>& z, std::vector<uint8_t>& out, size_t limit) {
     if (z.size() < 6) return false;
     const unsigned cmf = z[0], flg = z[1];
     if ((cmf & 0x0fu) != 8 || (cmf >> 4) > 7 || ((cmf << 8) | flg) % 31 != 0 || (flg & 0x20u)) return false;
-    if (!inflate(z.data() + 2, z.size() - 6, out)) return false;
+    if (!inflate(z.data() + 2, z.size() - 6, out, limit)) return false;
     return adler32(out.data(), out.size()) == be32(z.data() + z.size() - 4);
 }
 
@@ -414,10 +418,21 @@ int png_decode(const std::vector<uint8_t>& f, PngImage& im, std::vector<uint8_t>
     if (!rgba) return SKE_OK;
     if ((uint64_t)im.w * im.h > ((uint64_t)1 << 31)) return SKE_ERR_INVALID;
 
-    std::vector<uint8_t> raw;
-    if (!zlib_decompress(idat, raw)) return SKE_ERR_INVALID;
     const int bits_pp = channels_of(im.ctype) * im.depth;
     const int bpp = bits_pp < 8 ? 1 : bits_pp / 8;
+    // The filtered scanlines' size follows from the header: decompress no more.
+    size_t expect = 0;
+    for (int p = 0; p < (im.interlace ? 7 : 1); p++) {
+        static const int sx0[7] = {0, 4, 0, 2, 0, 1, 0}, sy0[7] = {0, 0, 4, 0, 2, 0, 1};
+        static const int sdx[7] = {8, 8, 4, 4, 2, 2, 1}, sdy[7] = {8, 8, 8, 4, 4, 2, 2};
+        const uint32_t x0 = im.interlace ? sx0[p] : 0, y0 = im.interlace ? sy0[p] : 0;
+        const uint32_t dx = im.interlace ? sdx[p] : 1, dy = im.interlace ? sdy[p] : 1;
+        if (im.w <= x0 || im.h <= y0) continue;
+        const uint64_t pw = (im.w - x0 + dx - 1) / dx, ph = (im.h - y0 + dy - 1) / dy;
+        expect += (size_t)((pw * bits_pp + 7) / 8 + 1) * ph;
+    }
+    std::vector<uint8_t> raw;
+    if (!zlib_decompress(idat, raw, expect)) return SKE_ERR_INVALID;
     rgba->assign((size_t)im.w * im.h * 4, 0);
     // Adam7 passes (PNG specification 8.2): start and step in x and y.
     static const int ax0[7] = {0, 4, 0, 2, 0, 1, 0}, ay0[7] = {0, 0, 4, 0, 2, 0, 1};

@@ -291,12 +291,17 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_wgrad(const bf16* __restri
         }
 }
 
+// cp.async copies 16 bytes: tensors must start on 16-byte boundaries (outputs:
+// 4 bytes, for the bf16 pairs of the epilogue).
+bool aligned(const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
+
 }  // namespace
 
 extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
                                 int cin, int cout, int relu, void* stream) {
     if (!x || !w || !y || n < 1 || h < 1 || w_ < 1 || cin < 8 || cin % 8 || cout < 2 || cout % 2)
         return SKE_ERR_INVALID;
+    if (!aligned(x, 16) || !aligned(w, 16) || !aligned(y, 4) || !aligned(bias, 4)) return SKE_ERR_INVALID;
     const int64_t m = (int64_t)n * h * w_;
     if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
     const int kpad = (9 * cin + kBK - 1) / kBK * kBK;
@@ -310,6 +315,8 @@ extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const
                                       int n, int h, int w_, int c1, int c2, int cout, int relu, void* stream) {
     if (!xlow || !xskip || !w || !y || n < 1 || h < 2 || w_ < 2 || h % 2 || w_ % 2 || c1 < 8 || c1 % 8 ||
         c2 < 8 || c2 % 8 || cout < 2 || cout % 2)
+        return SKE_ERR_INVALID;
+    if (!aligned(xlow, 16) || !aligned(xskip, 16) || !aligned(w, 16) || !aligned(y, 4) || !aligned(bias, 4))
         return SKE_ERR_INVALID;
     const int64_t m = (int64_t)n * h * w_;
     const int cin = c1 + c2;
@@ -326,6 +333,7 @@ extern "C" int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, 
                                       int cout, void* stream) {
     if (!x || !dy || !dw || n < 1 || h < 1 || w_ < 1 || cin < 8 || cin % 8 || cout < 8 || cout % 8)
         return SKE_ERR_INVALID;
+    if (!aligned(x, 16) || !aligned(dy, 16) || !aligned(dw, 4)) return SKE_ERR_INVALID;
     const int64_t m = (int64_t)n * h * w_;
     if (m > 0x7fffffff / 2) return SKE_ERR_INVALID;
     const int kpad = (9 * cin + kBK - 1) / kBK * kBK;

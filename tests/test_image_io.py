@@ -84,6 +84,28 @@ def test_png_rejects_damaged_files(ske, images, tmp_path):
         ske.read_png_rgba(tmp_path / "missing.png")
 
 
+def test_png_decompression_is_bounded_by_the_header(ske, tmp_path):
+    """An IDAT that inflates to far more than the header's image needs is refused
+    (decompression stops at the expected size)."""
+    import struct
+    import zlib
+    from skewengine_gb300 import SkeError
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xffffffff)
+
+    ihdr = struct.pack(">IIBBBBB", 4, 4, 8, 0, 0, 0, 0)  # 4 x 4 grey: 20 bytes of scanlines
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", ihdr) + chunk(b"IDAT", zlib.compress(b"\0" * 20_000_000)) + \
+        chunk(b"IEND", b"")
+    (tmp_path / "bomb.png").write_bytes(png)
+    with pytest.raises(SkeError):
+        ske.read_png_rgba(tmp_path / "bomb.png")
+    good = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", ihdr) + chunk(b"IDAT", zlib.compress(b"\0\x07\x07\x07\x07" * 4)) + \
+        chunk(b"IEND", b"")
+    (tmp_path / "ok.png").write_bytes(good)
+    assert (ske.read_png_rgba(tmp_path / "ok.png")[..., 0] == 7).all()
+
+
 def test_min_max_of_renderer_matches_reference(ske, images):
     """The Radon colouring's scale comes from getMinMax; an all-negative grid
     reports FLT_MIN as its maximum in the reference."""

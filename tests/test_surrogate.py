@@ -68,6 +68,18 @@ def test_upcat_conv_equals_conv_of_the_concatenation(sur):
     assert torch.equal(got.view(torch.int16), want.view(torch.int16))
 
 
+def test_conv_rejects_misaligned_tensors(sur):
+    """16-byte copies need 16-byte aligned inputs: a view starting 2 bytes into a
+    buffer is refused before anything is launched."""
+    import torch
+    from skewengine_gb300 import SkeError
+    buf = torch.zeros(8 * 8 * 8 + 8, dtype=torch.bfloat16, device="cuda")
+    x = buf[1:1 + 8 * 8 * 8].view(1, 8, 8, 8)
+    w = torch.zeros((16, sur.kpad(8)), dtype=torch.bfloat16, device="cuda")
+    with pytest.raises(SkeError):
+        sur.conv3x3(x, w)
+
+
 def test_conv_gradients_match_numpy(sur):
     """d(sum(g * y))/dx, /dw, /db through the autograd function against NumPy."""
     import torch
