@@ -68,10 +68,11 @@
 //    every remaining slope fl(fl(S[k]-h)/d') is at most fl(a/d'), and a/d' is
 //    largest at d' = d+1 when a >= 0 and at d' = n when a < 0.  An observer that
 //    passes is finished: every later step would be invisible, so cv = 1 + sum
-//    (its last run closes at the next step).  Smax comes from per-8-cell block
-//    maxima of the row (suffix maxima forward, prefix maxima backward).  The
-//    chunked sweep tests every kCheck steps with the a >= 0 bound and stops a
-//    warp when all its observers are finished.
+//    (its last run closes at the next step).  The chunked sweep takes Smax
+//    from per-8-cell suffix (forward) and prefix (backward) maxima, tests every
+//    kCheck steps with the a >= 0 bound and stops a warp when all its observers
+//    are finished.  The compacting sweep tests each observer after every level
+//    against 16-cell, 128-cell and suffix (prefix) maxima (see retire).
 #include <algorithm>
 #include <vector>
 
@@ -418,16 +419,18 @@ __host__ __device__ inline int lrow_pad(int max_row) { return kLPad + ((max_row 
 __host__ __device__ inline int nblk(int max_row, int size) { return (max_row + size - 1) / size; }
 
 // Per-warp shared memory of the compacting sweep, in floats from the warp's base:
-// the padded row; suffix maxima of kBlk-cell blocks (one -inf entry after);
-// prefix maxima (one -inf entry before); kB1-cell and kB2-cell block maxima
-// (kMPad -inf entries on both sides).
+// the padded row; suffix maxima of kB2-cell blocks (one -inf entry after);
+// prefix maxima of kB2-cell blocks (one -inf entry before); kB1-cell and
+// kB2-cell block maxima (kMPad -inf entries on both sides).  About 1.17 floats
+// per cell of the longest row: 2335 per warp at 2000 cells, so six 4-warp CTAs
+// share an SM's 228 KB.
 struct LLayout {
-    int suf, pre, b16, b128, total;
+    int s128, p128, b16, b128, total;
     __host__ __device__ explicit LLayout(int max_row) {
-        const int n8 = nblk(max_row, kBlk), n16 = nblk(max_row, kB1), n128 = nblk(max_row, kB2);
-        suf = lrow_pad(max_row);
-        pre = suf + n8 + 2;
-        b16 = pre + n8 + kMPad;
+        const int n16 = nblk(max_row, kB1), n128 = nblk(max_row, kB2);
+        s128 = lrow_pad(max_row);
+        p128 = s128 + n128 + 2;
+        b16 = p128 + n128 + kMPad;
         b128 = b16 + n16 + 2 * kMPad;
         total = b128 + n128 + kMPad;
     }
@@ -435,8 +438,8 @@ struct LLayout {
 
 // The block maxima of the row being swept.
 struct RowMax {
-    const float *suf, *pre, *b16, *b128;
-    int n8;
+    const float *s128, *p128, *b16, *b128;
+    int n128;
 };
 
 // One lane's two observers of a batch.  Slot q scans forward when the batch's
@@ -504,16 +507,21 @@ __device__ __forceinline__ bool owns(const RowOut& o, int x) {
     return o.first + x < o.sd->dim_i || owner_row(*o.sd, o.rfirst, o.rlast, o.rowbase + x) == o.row;
 }
 
-// kB1- and kB2-cell block maxima of the row, the -inf padding of every maxima
-// array, after block_maxima has filled suf and pre.
-__device__ void coarse_maxima(const float* __restrict__ A, int L, float* suf, float* pre, float* b16, float* b128,
-                              int lane) {
+// The maxima arrays of a fast-path row (finite, at most 32 * kB2 cells, so one
+// kB2 block per lane): kB1- and kB2-cell block maxima with their -inf padding,
+// s128[b] = max A[kB2*b ..] to the row end (s128[n128] = -inf) and
+// p128[b] = max A[.. kB2*b + kB2-1] from the row start (p128[-1] = -inf).
+__device__ void row_maxima(const float* __restrict__ A, int L, float* s128, float* p128, float* b16, float* b128,
+                           int lane) {
     const float ninf = __int_as_float(0xff800000);
-    const int n8 = nblk(L, kBlk), n16 = nblk(L, kB1), n128 = nblk(L, kB2);
-    for (int b = lane; b < n16; b += 32) {
-        float m = ninf;
-        for (int c = b * kB1; c < min(b * kB1 + kB1, L); c++) m = fmaxf(m, A[c]);
-        b16[b] = m;
+    const int n16 = nblk(L, kB1), n128 = nblk(L, kB2);
+    // kB1 = 16 cells: half a warp per block, a row segment of 32 cells per pass.
+    for (int c0 = 0; c0 < n16 * kB1; c0 += 32) {
+        float m = c0 + lane < L ? A[c0 + lane] : ninf;
+#pragma unroll
+        for (int off = kB1 / 2; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+        const int b = (c0 + lane) >> kB1Log;
+        if ((lane & (kB1 - 1)) == 0 && b < n16) b16[b] = m;
     }
     if (lane < kMPad) {
         b16[-1 - lane] = ninf;
@@ -521,63 +529,82 @@ __device__ void coarse_maxima(const float* __restrict__ A, int L, float* suf, fl
         b128[-1 - lane] = ninf;
         b128[n128 + lane] = ninf;
     }
-    if (lane == 0) {
-        suf[n8] = ninf;
-        pre[-1] = ninf;
-    }
     __syncwarp();
     constexpr int kPer = kB2 / kB1;
-    for (int b = lane; b < n128; b += 32) {
-        float m = ninf;
-        for (int c = b * kPer; c < min(b * kPer + kPer, n16); c++) m = fmaxf(m, b16[c]);
-        b128[b] = m;
+    float m = ninf;  // this lane's kB2 block
+    if (lane < n128) {
+        for (int c = lane * kPer; c < min(lane * kPer + kPer, n16); c++) m = fmaxf(m, b16[c]);
+        b128[lane] = m;
+    }
+    // Inclusive prefix and suffix maxima over the lanes (Hillis-Steele).
+    float inc_p = m, inc_s = m;
+    for (int off = 1; off < 32; off <<= 1) {
+        const float up = __shfl_up_sync(0xffffffffu, inc_p, off);
+        const float dn = __shfl_down_sync(0xffffffffu, inc_s, off);
+        if (lane >= off) inc_p = fmaxf(inc_p, up);
+        if (lane + off < 32) inc_s = fmaxf(inc_s, dn);
+    }
+    if (lane < n128) {
+        s128[lane] = inc_s;
+        p128[lane] = inc_p;
+    }
+    if (lane == 0) {
+        s128[n128] = ninf;
+        p128[-1] = ninf;
     }
 }
 
 // Retirement test after step dc: true when no target beyond distance dc can be
 // visible from observer x (n steps in this direction, height h, horizon mx).
+// The remaining targets are covered by kT blocks of kB1 cells from the one
+// holding the nearest target, kT blocks of kB2 cells from the next uncovered
+// cell, and the suffix (prefix) maximum beyond; blocks past the row end read
+// -inf.  The first block may also hold up to kB1-1 passed targets, which only
+// raises the bound.
 //  * mx < 0: every remaining slope is at most fl(a/n), a = fl(Smax - h) < 0
-//    (Smax the suffix or prefix maximum), as in the header.
+//    with Smax the maximum over all those blocks, as in the header.
 //  * mx >= 0: a block of remaining targets with maximum M and nearest
 //    remaining distance ds holds no visible target when
 //    M - h <= fl(fl(mx * kShrink) * ds): that product is below mx * ds, so
 //    every target u = fl(z - h) <= M - h at distance d' >= ds has
 //    u / d' <= mx (u >= 0) or u / d' < 0 <= mx (u < 0), and fl(u / d') <= mx.
-//    The blocks: kT of kB1 cells from the one holding the nearest target, kT
-//    of kB2 cells from the next uncovered cell, and the suffix (prefix) maximum
-//    beyond.  Blocks past the row end read -inf.
 template <bool kFwd>
 __device__ __forceinline__ bool retire(const RowMax& rm, int x, int n, int dc, float h, float mx) {
     const int k = kFwd ? x + dc + 1 : x - dc - 1;  // nearest remaining target
+    const int b = k >> kB1Log;
+    float m1[kT], m2[kT];
+#pragma unroll
+    for (int j = 0; j < kT; j++) m1[j] = rm.b16[kFwd ? b + j : b - j];
+    const int c = kFwd ? (b + kT) * kB1 : (b - kT + 1) * kB1 - 1;  // first uncovered cell
+    const int b2 = c >> kB2Log;                                     // arithmetic shift: floor
+#pragma unroll
+    for (int j = 0; j < kT; j++) m2[j] = rm.b128[kFwd ? b2 + j : b2 - j];
+    const float tail = kFwd ? rm.s128[min(b2 + kT, rm.n128)] : rm.p128[max(b2 - kT, -1)];
     if (mx < 0.0f) {
-        const float a = __fsub_rn(kFwd ? rm.suf[k >> 3] : rm.pre[k >> 3], h);
+        float m = tail;
+#pragma unroll
+        for (int j = 0; j < kT; j++) m = fmaxf(m, fmaxf(m1[j], m2[j]));
+        const float a = __fsub_rn(m, h);
         if (!(a < 0.0f)) return false;
         const float2 t = g_recip[n];
         return div_fast(a, t.x, t.y) <= mx;
     }
     const float mxc = __fmul_rn(mx, kShrink);
-    int b = k >> kB1Log;
-    bool ok = __fsub_rn(rm.b16[b], h) <= __fmul_rn(mxc, __int2float_rn(dc + 1));
+    bool ok = __fsub_rn(m1[0], h) <= __fmul_rn(mxc, __int2float_rn(dc + 1));
     float ds = __int2float_rn(kFwd ? (b + 1) * kB1 - x : x - (b * kB1 - 1));
 #pragma unroll
     for (int j = 1; j < kT; j++) {
-        b += kFwd ? 1 : -1;
-        ok &= __fsub_rn(rm.b16[b], h) <= __fmul_rn(mxc, ds);
+        ok &= __fsub_rn(m1[j], h) <= __fmul_rn(mxc, ds);
         ds = __fadd_rn(ds, (float)kB1);
     }
-    int c = kFwd ? (b + 1) * kB1 : b * kB1 - 1;  // first uncovered cell
-    int b2 = c >> kB2Log;                          // arithmetic shift: floor
-    ok &= __fsub_rn(rm.b128[b2], h) <= __fmul_rn(mxc, __int2float_rn(kFwd ? c - x : x - c));
+    ok &= __fsub_rn(m2[0], h) <= __fmul_rn(mxc, __int2float_rn(kFwd ? c - x : x - c));
     ds = __int2float_rn(kFwd ? (b2 + 1) * kB2 - x : x - (b2 * kB2 - 1));
 #pragma unroll
     for (int j = 1; j < kT; j++) {
-        b2 += kFwd ? 1 : -1;
-        ok &= __fsub_rn(rm.b128[b2], h) <= __fmul_rn(mxc, ds);
+        ok &= __fsub_rn(m2[j], h) <= __fmul_rn(mxc, ds);
         ds = __fadd_rn(ds, (float)kB2);
     }
-    c = kFwd ? (b2 + 1) * kB2 : b2 * kB2 - 1;
-    const int i8 = kFwd ? min(c >> 3, rm.n8) : max(c >> 3, -1);
-    ok &= __fsub_rn(kFwd ? rm.suf[i8] : rm.pre[i8], h) <= __fmul_rn(mxc, ds);
+    ok &= __fsub_rn(tail, h) <= __fmul_rn(mxc, ds);
     return ok;
 }
 
@@ -698,8 +725,8 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
     const LLayout lay(a.max_row);
     float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * lay.total;
     float* A = buf + kLPad;
-    float* suf = buf + lay.suf;
-    float* pre = buf + lay.pre;
+    float* s128 = buf + lay.s128;
+    float* p128 = buf + lay.p128;
     float* b16 = buf + lay.b16;
     float* b128 = buf + lay.b128;
     const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
@@ -744,11 +771,9 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
         const bool fast = __all_sync(0xffffffffu, ok) && L <= kLFastMaxRow && div_safe(a.povh);
         __syncwarp();
         if (fast) {
-            block_maxima(A, L, suf, pre, lane);
+            row_maxima(A, L, s128, p128, b16, b128, lane);
             __syncwarp();
-            coarse_maxima(A, L, suf, pre, b16, b128, lane);
-            __syncwarp();
-            const RowMax rm{suf, pre, b16, b128, nblk(L, kBlk)};
+            const RowMax rm{s128, p128, b16, b128, nblk(L, kB2)};
             sweep_row(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane);
         } else {
             for (int x = lane; x < L; x += 32) {
