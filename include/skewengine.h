@@ -357,6 +357,10 @@ int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, c
  * cout a multiple of 8. */
 int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
                            int cout, void* stream);
+/* Synchronises `stream`, then sets *failed to 1 if a forward convolution since
+ * the previous call gave up waiting for its tensor-core operations (its output
+ * is then not written), else 0, and clears the flag. */
+int ske_conv_status(int* failed, void* stream);
 
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
  * a raw float32 file or a synthetic input and writes the result.  See

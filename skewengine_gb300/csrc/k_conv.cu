@@ -8,18 +8,16 @@
 //   Y[m][co] = bias[co] + sum_k A[m][k] * Wt[co][k],  m = (n, y, x), k = (ky, kx, ci)
 //   A[m][k]  = X[n][y+ky-1][x+kx-1][ci] (zero outside the image)
 // Cin is a multiple of 8, so every 8 consecutive k of a row of A are 16
-// contiguous bytes of X (or all zero).  A CTA of 4 warps computes a 128 x 64
-// tile of Y; k advances in slices of 32 that cp.async copies into a double
-// buffer in shared memory (zero-filled where A is padding), ldmatrix feeds
-// mma.sync m16n8k16 (bf16 in, f32 accumulate), and the epilogue adds the bias,
-// optionally applies ReLU and stores bf16 pairs.
+// contiguous bytes of X (or all zero).  It runs on the 5th-generation tensor
+// cores (tcgen05.mma with the accumulator in tensor memory; k_conv3x3 below).
 //
 // The weight gradient dW[co][k] = sum_m dY[m][co] * A[m][k] runs over a chunk of
-// pixels per CTA with the same tiles (A and dY staged in shared memory, read
-// with transposing ldmatrix), and the chunks' partial sums are added into a
-// float32 dW with atomics.
+// pixels per CTA (A and dY staged in shared memory, read with transposing
+// ldmatrix into mma.sync m16n8k16), and the chunks' partial sums are added into
+// a float32 dW with atomics.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "../../include/skewengine.h"
@@ -28,8 +26,7 @@ namespace {
 
 typedef __nv_bfloat16 bf16;
 
-constexpr int kBM = 128, kBN = 64, kBK = 32, kThreads = 128;
-constexpr int kPitch = kBK + 8;  // shared row pitch in bf16: 80 bytes, ldmatrix conflict-free
+constexpr int kBK = 32, kThreads = 128;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -43,11 +40,6 @@ __device__ __forceinline__ void cp_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(kN));
 }
 
-__device__ __forceinline__ void ldsm_x4(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(smem_u32(p)));
-}
 __device__ __forceinline__ void ldsm_x4_t(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
                  : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
@@ -95,119 +87,261 @@ __device__ __forceinline__ const bf16* a_src(const bf16* __restrict__ X, const P
     return X + ((int64_t)(p.base + iy * W + ix) * Cin + ci);
 }
 
+// ---- forward convolution on the tensor cores (tcgen05) ----------------------
+//
+// A CTA of 4 warps computes a 128 x BN tile of Y (BN = Cout rounded up to a
+// multiple of 16, at most 128) with tcgen05.mma kind::f16 (bfloat16 A and B,
+// float32 accumulator in tensor memory, BN columns of its 128 lanes).  K
+// advances in slices of 32, two MMAs of K = 16 each.  Every thread copies its
+// share of a slice's A rows (the im2col gather, zero where A is padding) and B
+// rows (weights) with cp.async into a kTcStages-deep ring in shared memory, in
+// the canonical K-major layout without swizzle: core matrices of 8 rows x 16
+// bytes (128 contiguous bytes), the 4 core matrices of a row group's slice
+// adjacent (leading byte offset 128), row groups 512 bytes apart (stride byte
+// offset).  Slices are fetched
+// kTcPrefetch ahead.  Once every thread's copies of a slice have landed
+// (wait_group, proxy fence, barrier) thread 0 issues its MMAs and commits them
+// to the stage's mbarrier.  A stage is refilled with the slice kTcStages after
+// the one it held, which was issued kTcStages - kTcPrefetch = 2 slices earlier,
+// so the tensor pipe keeps a slice queued while the next one's barrier passes.
+// The epilogue reads the accumulator with tcgen05.ld (warp w owns lanes
+// 32w..32w+31, i.e. output rows), adds the bias, applies ReLU and stores
+// bfloat16.  Every wait is bounded: one that runs out sets g_conv_status,
+// skips the remaining MMAs and the epilogue, and the CTA still releases its
+// tensor memory.
+//
 // kUpCat: the input is the channel concatenation of X (C1 channels at half the
 // resolution, nearest-upsampled) and X2 (C2 channels at full resolution), read
 // in place: A's 8-channel chunk at (y, x) comes from X at (y/2, x/2) for
 // channels below C1, else from X2.  The same products in the same order as on
 // the materialised concatenation.
+constexpr int kTcBM = 128, kTcBK = 32, kTcStages = 4, kTcPrefetch = 2, kTcMaxBN = 128;
+constexpr int kTcABytes = kTcBM * kTcBK * 2;  // 8 KB of A per stage
+constexpr int kTcSBO = (kTcBK / 8) * 128;     // bytes between row groups
+constexpr long long kTcWaitLimit = 1ll << 22;
+
+__device__ int g_conv_status;  // 1: a tensor-core wait ran out
+
+__host__ __device__ constexpr int tc_smem_bytes(int bn) {
+    return kTcStages * (kTcABytes + bn * kTcBK * 2) + kTcStages * 8 + 16;
+}
+
+__device__ __forceinline__ void tc_mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool tc_mbar_wait(uint64_t* bar, int parity) {
+    for (long long i = 0; i < kTcWaitLimit; i++) {
+        unsigned ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor: start address, leading byte offset 128,
+// stride byte offset kTcSBO (all in 16-byte units), descriptor version 1, no
+// swizzle.
+__device__ __forceinline__ uint64_t tc_desc(unsigned saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(kTcSBO >> 4) << 32) |
+           (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: f32 accumulator (bits 4-5 = 1), A and B
+// bfloat16 (bits 7-9 = 1, 10-12 = 1), both K-major, N >> 3 at bit 17,
+// M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t tc_idesc(int bn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kTcBM >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(unsigned dtmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::
+            "r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 16 consecutive f32 columns of this warp's 32 lanes (lane = row) from tensor memory.
+__device__ __forceinline__ void tc_ld16(unsigned taddr, float* v) {
+    unsigned r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
 template <bool kUpCat>
-__global__ void __launch_bounds__(kThreads, 4) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
+__global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
                                                       const float* __restrict__ bias, bf16* __restrict__ Y, int M,
                                                       int H, int W, int Cin, int Cout, int Kpad, int relu,
-                                                      const bf16* __restrict__ X2, int C1) {
-    __shared__ __align__(16) bf16 As[2][kBM][kPitch];
-    __shared__ __align__(16) bf16 Bs[2][kBN][kPitch];
+                                                      const bf16* __restrict__ X2, int C1, int BN, int vec16) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * kBN;
-    const int wm = (warp >> 1) * 64, wn = (warp & 1) * 32;
+    const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * BN;
+    const int bbytes = BN * kTcBK * 2;
+    unsigned char* As = tc_smem;                           // [kTcStages][kTcABytes]
+    unsigned char* Bs = tc_smem + kTcStages * kTcABytes;   // [kTcStages][bbytes]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(Bs + kTcStages * bbytes);
+    unsigned* tslot = reinterpret_cast<unsigned*>(bar + kTcStages);
+    const unsigned ncols = BN <= 32 ? 32u : BN <= 64 ? 64u : 128u;
 
-    // This thread's 4 A rows (pixels) share one 8-wide k offset kc: their
-    // (tap, channel) pair is tracked incrementally as k advances by kBK, so each
-    // chunk costs a bounds test and an add (no division per chunk and slice).
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kTcStages; s++) tc_mbar_init(&bar[s]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+
+    // This thread's 4 A rows (pixels) share one 8-wide k offset kc within each
+    // 32-wide half of a slice: their (tap, channel) pair is tracked
+    // incrementally as k advances by 32, so each chunk costs a bounds test and
+    // an add (no division per chunk).
     const int kc = (tid & 3) * 8;
     const bf16* prow[4];
     int py[4], px[4], pn[4];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        const Pix p = pixel_of(m0 + ((tid + i * kThreads) >> 2), M, H, W);
+        const Pix p = pixel_of(m0 + (tid >> 2) + 32 * i, M, H, W);
         py[i] = p.y;
         px[i] = p.x;
         pn[i] = p.y >= 0 ? p.base / (H * W) : 0;
         prow[i] = (!kUpCat && p.y >= 0) ? X + (int64_t)(p.base + p.y * W + p.x) * Cin : X;
     }
     int tap = kc / Cin, ci = kc - (kc / Cin) * Cin;  // k = k0 + kc at the next load
-    auto load = [&](int stage, int k0) {  // called with k0 = 0, kBK, 2*kBK, ... in order
-        const int ky = tap / 3, kx = tap - 3 * (tap / 3);
-        const int64_t toff = ((int64_t)(ky - 1) * W + (kx - 1)) * Cin + ci;
+    // Byte offset of (row r, 8-element chunk c) of a stage in the core-matrix layout.
+    auto cm = [](int r, int c) { return (r >> 3) * kTcSBO + c * 128 + (r & 7) * 16; };
+    auto load = [&](int stage, int k0) {  // called with k0 = 0, kTcBK, 2*kTcBK, ... in order
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const int iy = py[i] + ky - 1, ix = px[i] + kx - 1;
-            const bool ok = tap < 9 && iy >= 0 && iy < H && ix >= 0 && ix < W;
-            const bf16* src = X;
-            if (ok) {
-                if (!kUpCat)
-                    src = prow[i] + toff;
-                else if (ci < C1)
-                    src = X + ((int64_t)(pn[i] * (H >> 1) + (iy >> 1)) * (W >> 1) + (ix >> 1)) * C1 + ci;
-                else
-                    src = X2 + ((int64_t)(pn[i] * H + iy) * W + ix) * (Cin - C1) + (ci - C1);
+        for (int half = 0; half < kTcBK / 32; half++) {
+            const int ky = tap / 3, kx = tap - 3 * (tap / 3);
+            const int64_t toff = ((int64_t)(ky - 1) * W + (kx - 1)) * Cin + ci;
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const int iy = py[i] + ky - 1, ix = px[i] + kx - 1;
+                const bool ok = tap < 9 && iy >= 0 && iy < H && ix >= 0 && ix < W;
+                const bf16* src = X;
+                if (ok) {
+                    if (!kUpCat)
+                        src = prow[i] + toff;
+                    else if (ci < C1)
+                        src = X + ((int64_t)(pn[i] * (H >> 1) + (iy >> 1)) * (W >> 1) + (ix >> 1)) * C1 + ci;
+                    else
+                        src = X2 + ((int64_t)(pn[i] * H + iy) * W + ix) * (Cin - C1) + (ci - C1);
+                }
+                cp_async16(As + stage * kTcABytes + cm((tid >> 2) + 32 * i, half * 4 + (tid & 3)), src, ok ? 16 : 0);
             }
-            cp_async16(&As[stage][(tid + i * kThreads) >> 2][kc], src, ok ? 16 : 0);
+            for (ci += 32; ci >= Cin; ci -= Cin) tap++;
         }
-        for (ci += kBK; ci >= Cin; ci -= Cin) tap++;
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const int c = tid + i * kThreads;
-            const int co = n0 + (c >> 2), kc = (c & 3) * 8;
-            const bool ok = co < Cout;
-            cp_async16(&Bs[stage][c >> 2][kc], ok ? Wt + (int64_t)co * Kpad + k0 + kc : Wt, ok ? 16 : 0);
+        for (int q = tid; q < BN * (kTcBK / 8); q += kThreads) {
+            const int r = q / (kTcBK / 8), c = q % (kTcBK / 8), co = n0 + r;
+            const bool ok = co < Cout && k0 + c * 8 < Kpad;
+            cp_async16(Bs + stage * bbytes + cm(r, c), ok ? Wt + (int64_t)co * Kpad + k0 + c * 8 : Wt, ok ? 16 : 0);
         }
-        cp_commit();
     };
 
-    float acc[4][4][4];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++)
-#pragma unroll
-            for (int e = 0; e < 4; e++) acc[i][j][e] = 0.0f;
-
-    const int KT = Kpad / kBK;
-    load(0, 0);
-    for (int kt = 0; kt < KT; kt++) {
-        const int s = kt & 1;
-        if (kt + 1 < KT) {
-            load(s ^ 1, (kt + 1) * kBK);
-            cp_wait<1>();
-        } else {
-            cp_wait<0>();
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < kBK; kk += 16) {
-            unsigned af[4][4], bfr[4][2];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-                ldsm_x4(af[i][0], af[i][1], af[i][2], af[i][3], &As[s][wm + i * 16 + (lane & 15)][kk + (lane >> 4) * 8]);
-#pragma unroll
-            for (int j = 0; j < 4; j += 2)
-                ldsm_x4(bfr[j][0], bfr[j][1], bfr[j + 1][0], bfr[j + 1][1],
-                        &Bs[s][wn + j * 8 + (lane >> 4) * 8 + (lane & 7)][kk + ((lane >> 3) & 1) * 8]);
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) mma_bf16(acc[i][j], af[i], bfr[j]);
-        }
-        __syncthreads();  // the next load overwrites this stage
+    const int KT = (Kpad + kTcBK - 1) / kTcBK;
+    const uint32_t idesc = tc_idesc(BN);
+    for (int s = 0; s < kTcPrefetch; s++) {
+        if (s < KT) load(s, s * kTcBK);
+        cp_commit();
     }
-
+    bool fail = false;
+    for (int kt = 0; kt < KT; kt++) {
+        const int nxt = kt + kTcPrefetch;
+        if (nxt < KT) {
+            // The stage last held slice nxt - kTcStages: its MMAs must be done reading it.
+            const int st = nxt % kTcStages, prev = nxt - kTcStages;
+            if (prev >= 0 && !fail) fail = !tc_mbar_wait(&bar[st], (prev / kTcStages) & 1);
+            load(st, nxt * kTcBK);
+        }
+        cp_commit();
+        cp_wait<kTcPrefetch>();  // this thread's copies of slice kt have landed
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (__syncthreads_or(fail)) {
+            fail = true;
+            break;
+        }
+        if (tid == 0) {
+            tc_fence_after();
+            const int s = kt % kTcStages;
+            const unsigned a0 = smem_u32(As + s * kTcABytes), b0 = smem_u32(Bs + s * bbytes);
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+            for (int kk = 0; kk < kTcBK / 16; kk++)
+                tc_mma(tmem, tc_desc(a0 + kk * 256), tc_desc(b0 + kk * 256), idesc, (kt | kk) != 0);
+            tc_commit(&bar[s]);
+        }
+    }
+    cp_wait<0>();
+    // The last slice's commit completes after every earlier MMA.
+    if (!fail && KT > 0) fail = !tc_mbar_wait(&bar[(KT - 1) % kTcStages], ((KT - 1) / kTcStages) & 1);
+    fail = __syncthreads_or(fail);
+    tc_fence_after();
+    if (!fail) {
+        const int m = m0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            float v[16];
+            tc_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0, v);
+            if (m >= M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int co = n0 + wn + j * 8 + (lane & 3) * 2;
-            if (co >= Cout) continue;
-            const float b0 = bias ? bias[co] : 0.0f, b1 = bias ? bias[co + 1] : 0.0f;
+            for (int g = 0; g < 16; g += 8) {
+                const int co = n0 + c0 + g;
+                if (co >= Cout) break;
+                float o[8];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int m = m0 + wm + i * 16 + (lane >> 2) + h * 8;
-                if (m >= M) continue;
-                float v0 = acc[i][j][2 * h] + b0, v1 = acc[i][j][2 * h + 1] + b1;
-                if (relu) v0 = fmaxf(v0, 0.0f), v1 = fmaxf(v1, 0.0f);
-                *reinterpret_cast<__nv_bfloat162*>(Y + (int64_t)m * Cout + co) = __floats2bfloat162_rn(v0, v1);
+                for (int e = 0; e < 8; e++) {
+                    const float b = (bias && co + e < Cout) ? bias[co + e] : 0.0f;
+                    o[e] = __fadd_rn(v[g + e], b);
+                    if (relu) o[e] = fmaxf(o[e], 0.0f);
+                }
+                bf16* dst = Y + (int64_t)m * Cout + co;
+                if (vec16 && co + 8 <= Cout) {
+                    __nv_bfloat162 h[4];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) h[e] = __floats2bfloat162_rn(o[2 * e], o[2 * e + 1]);
+                    *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<const uint4*>(h);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < 8; e += 2)
+                        if (co + e < Cout)
+                            *reinterpret_cast<__nv_bfloat162*>(dst + e) = __floats2bfloat162_rn(o[e], o[e + 1]);
+                }
             }
         }
+    } else if (tid == 0) {
+        atomicExch(&g_conv_status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
 }
 
 // Weight gradient: a CTA owns a 64 (co) x 64 (k) tile of dW and a chunk of
@@ -295,6 +429,27 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_wgrad(const bf16* __restri
 // 4 bytes, for the bf16 pairs of the epilogue).
 bool aligned(const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
 
+// Launch of the tensor-core forward convolution: BN = Cout rounded up to 16,
+// at most kTcMaxBN, and Cout / BN column tiles.  With 4 stages a CTA holds
+// 36-64 KB of shared memory, so at most 6 (BN 16) down to 3 (BN 128) CTAs share
+// an SM and their tensor-memory columns (32, 64 or 128 each) stay within the
+// SM's 512.
+template <bool kUpCat>
+int launch_conv_tc(const bf16* x, const bf16* w, const float* bias, bf16* y, int64_t m, int h, int w_, int cin,
+                   int cout, int relu, const bf16* x2, int c1, cudaStream_t st) {
+    const int kpad = (9 * cin + kTcBK - 1) / kTcBK * kTcBK;
+    const int bn = std::min(kTcMaxBN, (cout + 15) / 16 * 16);
+    const int smem = tc_smem_bytes(bn);
+    if (cudaFuncSetAttribute(k_conv3x3<kUpCat>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             tc_smem_bytes(kTcMaxBN)) != cudaSuccess)
+        return SKE_ERR_CUDA;
+    const dim3 grid((unsigned)((m + kTcBM - 1) / kTcBM), (unsigned)((cout + bn - 1) / bn));
+    const int vec16 = cout % 8 == 0 && aligned(y, 16);
+    k_conv3x3<kUpCat><<<grid, kThreads, smem, st>>>(x, w, bias, y, (int)m, h, w_, cin, cout, kpad, relu, x2, c1, bn,
+                                                     vec16);
+    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
 }  // namespace
 
 extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
@@ -304,11 +459,8 @@ extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias,
     if (!aligned(x, 16) || !aligned(w, 16) || !aligned(y, 4) || !aligned(bias, 4)) return SKE_ERR_INVALID;
     const int64_t m = (int64_t)n * h * w_;
     if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
-    const int kpad = (9 * cin + kBK - 1) / kBK * kBK;
-    const dim3 grid((unsigned)((m + kBM - 1) / kBM), (unsigned)((cout + kBN - 1) / kBN));
-    k_conv3x3<false><<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)w, bias, (bf16*)y,
-                                                                  (int)m, h, w_, cin, cout, kpad, relu, nullptr, 0);
-    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+    return launch_conv_tc<false>((const bf16*)x, (const bf16*)w, bias, (bf16*)y, m, h, w_, cin, cout, relu, nullptr,
+                                 0, (cudaStream_t)stream);
 }
 
 extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
@@ -321,12 +473,21 @@ extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const
     const int64_t m = (int64_t)n * h * w_;
     const int cin = c1 + c2;
     if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
-    const int kpad = (9 * cin + kBK - 1) / kBK * kBK;
-    const dim3 grid((unsigned)((m + kBM - 1) / kBM), (unsigned)((cout + kBN - 1) / kBN));
-    k_conv3x3<true><<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)xlow, (const bf16*)w, bias, (bf16*)y,
-                                                                 (int)m, h, w_, cin, cout, kpad, relu,
-                                                                 (const bf16*)xskip, c1);
-    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+    return launch_conv_tc<true>((const bf16*)xlow, (const bf16*)w, bias, (bf16*)y, m, h, w_, cin, cout, relu,
+                                (const bf16*)xskip, c1, (cudaStream_t)stream);
+}
+
+extern "C" int ske_conv_status(int* failed, void* stream) {
+    if (!failed) return SKE_ERR_INVALID;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return SKE_ERR_CUDA;
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_conv_status, sizeof(int)) != cudaSuccess) return SKE_ERR_CUDA;
+    if (v) {
+        const int zero = 0;
+        if (cudaMemcpyToSymbol(g_conv_status, &zero, sizeof(int)) != cudaSuccess) return SKE_ERR_CUDA;
+    }
+    *failed = v;
+    return SKE_OK;
 }
 
 extern "C" int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,

@@ -8,8 +8,9 @@ trained on the engine's own outputs, and at inference the engine itself checks
 a sample of tiles and recomputes every tile whose error exceeds the bound.
 
 The convolutions are the engine's hand-written implicit-GEMM kernels
-(``ske_conv3x3_bf16`` forward and data gradient, ``ske_conv3x3_wgrad_bf16``
-weight gradient, tensor-core mma.sync with bfloat16 operands); pooling,
+(``ske_conv3x3_bf16`` forward and data gradient on tcgen05 with the accumulator
+in tensor memory, ``ske_conv3x3_wgrad_bf16`` weight gradient on mma.sync, both
+with bfloat16 operands and float32 accumulation); pooling,
 upsampling, concatenation, the 1x1 output layer, the loss and the optimiser are
 PyTorch operations around them.
 
@@ -27,7 +28,7 @@ import os
 import numpy as np
 
 from . import synthetic
-from ._lib import check, load
+from ._lib import SkeError, check, load
 
 TILE = 256
 IN_CH = 8
@@ -74,6 +75,16 @@ def conv3x3_upcat(xlow, skip, w, bias=None, relu: bool = False):
                                         C.c_void_p(bias.data_ptr()) if bias is not None else None,
                                         C.c_void_p(y.data_ptr()), n, h, wd, c1, c2, cout, int(relu), _stream(skip)))
     return y
+
+
+def conv_check(device=None) -> None:
+    """Synchronise the current stream and raise SkeError if a forward convolution
+    since the previous check gave up waiting for its tensor-core operations."""
+    import torch
+    failed = C.c_int(0)
+    check(load().ske_conv_status(C.byref(failed), C.c_void_p(torch.cuda.current_stream(device).cuda_stream)))
+    if failed.value:
+        raise SkeError(6, "a tensor-core convolution gave up waiting for its MMAs; its output is not valid")
 
 
 def conv3x3_wgrad(x, dy, cout: int):
@@ -292,6 +303,8 @@ def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 
         opt.step()
         sched.step()
         losses.append(float(loss.detach()))
+        if step % 200 == 0 or step == steps - 1:
+            conv_check()
         if log and (step % 200 == 0 or step == steps - 1):
             log(f"step {step} loss {losses[-1]:.4f}")
     return losses
@@ -360,6 +373,7 @@ def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float 
     with torch.no_grad():
         for i in range(0, len(tiles), batch):
             out[i:i + batch] = net(x[i:i + batch])
+    conv_check()
     rng = np.random.default_rng(seed)
     n_check = max(1, int(round(check_fraction * len(tiles))))
     checked = np.sort(rng.choice(len(tiles), n_check, replace=False))

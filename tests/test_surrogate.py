@@ -35,7 +35,8 @@ def sur():
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout,relu", [(2, 19, 23, 8, 32, True), (1, 37, 5, 32, 64, False),
-                                                  (3, 16, 16, 96, 72, True), (1, 130, 3, 64, 8, True)])
+                                                  (3, 16, 16, 96, 72, True), (1, 130, 3, 64, 8, True),
+                                                  (1, 24, 20, 64, 256, True), (2, 9, 11, 16, 130, False)])
 def test_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
     import torch
     rng = np.random.default_rng(cin * 7 + cout)
@@ -44,7 +45,9 @@ def test_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
     b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32)
     wpad = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
     wpad[:, : 9 * cin] = wb
-    y = sur.conv3x3(xb.cuda().contiguous(), wpad.cuda(), b.cuda(), relu).float().cpu().numpy()
+    y = sur.conv3x3(xb.cuda().contiguous(), wpad.cuda(), b.cuda(), relu)
+    sur.conv_check()  # no tensor-core wait ran out
+    y = y.float().cpu().numpy()
     ref, _, _ = _conv_ref(xb.double().numpy(), wb.double().numpy(), b.double().numpy(), relu)
     # float32 accumulation of exact bfloat16 products, then one bfloat16 rounding
     assert np.all(np.abs(y - ref) <= 2 ** -7 * np.abs(ref) + 1e-3), np.abs(y - ref).max()
