@@ -444,8 +444,8 @@ def surrogate_workload(args):
                          "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                          "frac": achieved / peaks["bf16_tflops"],
                          "work": f"{sur.conv_flops_per_tile() / 1e9:.2f} GFLOP of 3x3 convolutions per tile",
-                         "note": "mma.sync bf16 tensor-core kernels; pooling, upsampling and concatenation time "
-                                 "included", "traffic": None}}
+                         "note": "forward convolutions on tcgen05 (bf16, f32 accumulator in tensor memory); "
+                                 "pooling, upsampling and the head included", "traffic": None}}
     print(json.dumps(line), flush=True)
     eng.close()
     return 0

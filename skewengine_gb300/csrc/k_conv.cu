@@ -34,6 +34,11 @@ __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)_
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, int nbytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes));
 }
+// The same through L1 (.ca): the nine taps of a 3x3 window re-read each input
+// pixel, mostly within one CTA or its neighbours on the SM.
+__device__ __forceinline__ void cp_async16_ca(void* dst, const void* src, int nbytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(nbytes));
+}
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;"); }
 template <int kN>
 __device__ __forceinline__ void cp_wait() {
@@ -254,14 +259,15 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
                     else
                         src = X2 + ((int64_t)(pn[i] * H + iy) * W + ix) * (Cin - C1) + (ci - C1);
                 }
-                cp_async16(As + stage * kTcABytes + cm((tid >> 2) + 32 * i, half * 4 + (tid & 3)), src, ok ? 16 : 0);
+                cp_async16_ca(As + stage * kTcABytes + cm((tid >> 2) + 32 * i, half * 4 + (tid & 3)), src,
+                              ok ? 16 : 0);
             }
             for (ci += 32; ci >= Cin; ci -= Cin) tap++;
         }
         for (int q = tid; q < BN * (kTcBK / 8); q += kThreads) {
             const int r = q / (kTcBK / 8), c = q % (kTcBK / 8), co = n0 + r;
             const bool ok = co < Cout && k0 + c * 8 < Kpad;
-            cp_async16(Bs + stage * bbytes + cm(r, c), ok ? Wt + (int64_t)co * Kpad + k0 + c * 8 : Wt, ok ? 16 : 0);
+            cp_async16_ca(Bs + stage * bbytes + cm(r, c), ok ? Wt + (int64_t)co * Kpad + k0 + c * 8 : Wt, ok ? 16 : 0);
         }
     };
 
