@@ -99,14 +99,13 @@ __device__ __forceinline__ const bf16* a_src(const bf16* __restrict__ X, const P
 // float32 accumulator in tensor memory, BN columns of its 128 lanes).  K
 // advances in slices of 32, two MMAs of K = 16 each.  Every thread copies its
 // share of a slice's A rows (the im2col gather, zero where A is padding) and B
-// rows (weights) with cp.async into a kTcStages-deep ring in shared memory, in
-// the canonical K-major layout without swizzle: core matrices of 8 rows x 16
-// bytes (128 contiguous bytes), the 4 core matrices of a row group's slice
-// adjacent (leading byte offset 128), row groups 512 bytes apart (stride byte
-// offset).  Slices are fetched
-// kTcPrefetch ahead.  Once every thread's copies of a slice have landed
-// (wait_group, proxy fence, barrier) thread 0 issues its MMAs and commits them
-// to the stage's mbarrier.  A stage is refilled with the slice kTcStages after
+// rows (weights) with cp.async through L1 into a kTcStages-deep ring in shared
+// memory, in the canonical K-major layout without swizzle: core matrices of 8
+// rows x 16 bytes (128 contiguous bytes), the 4 core matrices of a row group's
+// slice adjacent (leading byte offset 128), row groups 512 bytes apart (stride
+// byte offset).  Slices are fetched kTcPrefetch ahead.  Once every thread's
+// copies of a slice have landed (wait_group, proxy fence, barrier) thread 0
+// issues its MMAs and commits them to the stage's mbarrier.  A stage is refilled with the slice kTcStages after
 // the one it held, which was issued kTcStages - kTcPrefetch = 2 slices earlier,
 // so the tensor pipe keeps a slice queued while the next one's barrier passes.
 // The epilogue reads the accumulator with tcgen05.ld (warp w owns lanes
@@ -224,7 +223,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
     const unsigned tmem = *tslot;
 
     // This thread's 4 A rows (pixels) share one 8-wide k offset kc within each
-    // 32-wide half of a slice: their (tap, channel) pair is tracked
+    // 32-wide part of a slice: their (tap, channel) pair is tracked
     // incrementally as k advances by 32, so each chunk costs a bounds test and
     // an add (no division per chunk).
     const int kc = (tid & 3) * 8;
