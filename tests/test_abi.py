@@ -119,6 +119,29 @@ def test_null_engine_is_rejected(lib):
     assert lib.ske_destroy(None) == 0
 
 
+def test_convolutions_validate_arguments_before_launching(lib):
+    """Shapes and alignments the surrogate's convolution kernels cannot take are
+    refused before any device work.  The pointers are stand-ins that are never
+    dereferenced: every call below fails its argument checks."""
+    a = C.c_void_p(0x10000)  # 16-byte aligned
+    odd = C.c_void_p(0x10002)
+    s = None
+    conv = lib.ske_conv3x3_bf16
+    assert conv(a, a, None, a, 1, 8, 8, 12, 16, 1, s) == 1  # cin not a multiple of 8
+    assert conv(a, a, None, a, 1, 8, 8, 16, 15, 1, s) == 1  # odd cout
+    assert conv(a, a, None, a, 0, 8, 8, 16, 16, 1, s) == 1  # empty batch
+    assert conv(odd, a, None, a, 1, 8, 8, 16, 16, 1, s) == 1  # misaligned input
+    assert conv(a, odd, None, a, 1, 8, 8, 16, 16, 1, s) == 1  # misaligned weights
+    assert conv(a, a, None, None, 1, 8, 8, 16, 16, 1, s) == 1  # no output
+    upcat = lib.ske_conv3x3_upcat_bf16
+    assert upcat(a, a, a, None, a, 1, 7, 8, 16, 16, 16, 1, s) == 1  # odd height
+    assert upcat(a, a, a, None, a, 1, 8, 8, 16, 12, 16, 1, s) == 1  # skip channels not a multiple of 8
+    wgrad = lib.ske_conv3x3_wgrad_bf16
+    assert wgrad(a, a, a, 1, 8, 8, 16, 12, s) == 1  # cout not a multiple of 8
+    assert wgrad(a, a, odd, 1, 8, 8, 16, 16, s) == 1  # misaligned float32 gradient
+    assert lib.ske_conv_status(None, s) == 1
+
+
 def test_cli_usage_errors():
     from skewengine_gb300 import cli_run
     assert cli_run([]) == 1
