@@ -203,6 +203,12 @@ int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, cons
                   const float* const* inputs, int inputs_on_device, float* const* outputs,
                   int outputs_on_device, const ske_params* p);
 
+/* ske_run_batch over the listed angles (each in [0,180), accumulated in list
+ * order) for every DEM, as ske_run_angles is ske_run over a list. */
+int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
+                         const float* const* inputs, int inputs_on_device, float* const* outputs,
+                         int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p);
+
 /* Per-sector API (drop-in for the reference's skew/kernel/deskew/reduce
  * methods driven from main.cu:147-164) ----------------------------------------*/
 
@@ -250,12 +256,15 @@ int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_d
  * memory budget, inside another framework's allocator, or on a path where
  * allocation is forbidden -- this runs the viewshed sweep (its chunked form,
  * whose only scratch is its work list) over a skewed sector the caller already
- * holds in device memory: `skew_in` (row stride dim_i;
- * every row segment r*dim_i + [first[r], last[r]) must lie inside it),
- * `first`/`last` (skew_height int32 entries, device), and writes cv*scale2 to
- * every valid cell of `skew_out` (other cells are left as they are: zero the
- * buffer first, as resetSkew does, skewEngine.cuh:542-570).  Results equal the
- * built-in SDEM operator's on the same sector bit for bit.
+ * holds in device memory: `skew_in` (row stride dim_i), `first`/`last`
+ * (skew_height int32 entries, device, every row with 0 <= first <= last <=
+ * dim_l like the engine's own geometry; any other row is rejected with
+ * SKE_ERR_INVALID), and writes cv*scale2 to every valid cell of `skew_out`
+ * (other cells are left as they are: zero the buffer first, as resetSkew
+ * does, skewEngine.cuh:542-570).  `skew_in` and `skew_out` must each hold at
+ * least (skew_height-1)*dim_i + dim_l floats, the last cell a row can reach;
+ * the engine's own skew buffers hold 2*dimx*dimy + dim_l (skewEngine.cuh:425-426).
+ * Results equal the built-in SDEM operator's on the same sector bit for bit.
  *
  * Its scratch (sector descriptor, work-queue head, status word, work items) is
  * a file-scope device array of about 8 MiB that every GPU loading this library
@@ -267,7 +276,10 @@ int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_d
  * any stream capture.  Every call shares the array and keeps the last call's
  * contents (the queue head and status are cleared on each call); calls that
  * overlap on the GPU race, calls from several host threads are serialised.
- * Synchronous with respect to `stream` (a cudaStream_t, NULL = default). */
+ * Every call copies the row limits and, at the end, a status word to the host
+ * and waits for `stream` (a cudaStream_t, NULL = default) each time, so it
+ * returns with the sweep finished.  The calling thread's current device is
+ * restored before the call returns. */
 int ske_sdem_sector_noalloc(int device, const float* skew_in, float* skew_out, int dim_i,
                             int skew_height, int dim_l, const int32_t* first, const int32_t* last,
                             float scale2, float povh, void* stream);
@@ -363,8 +375,16 @@ int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int 
 int ske_conv_status(int* failed, void* stream);
 
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
- * a raw float32 file or a synthetic input and writes the result.  See
- * INTEGRATION.md for the argument list. */
+ * an input file and writes the result.
+ *   argv: run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]
+ *   kernel: sdem | identitydem | radon | identityimg | cepstrum | localradon, or
+ *           0..5 (the reference's KERNELS enum, src/global.h:77; 5 = radon with
+ *           its local-transform switch set);
+ *   input:  raw float32 grid, ESRI .bil int16 DEM (with its .hdr; dimx/dimy 0
+ *           take NCOLS/NROWS) or .png image;
+ *   output: raw float32 grid (.flt) or, for a name ending in .png, the
+ *           reference's coloured result image.
+ * Returns 0 or a SKE_* status; messages go to stderr. */
 int run(int argc, char** argv);
 
 #ifdef __cplusplus

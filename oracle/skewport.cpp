@@ -437,6 +437,65 @@ int port_run_angles(int op, const float* input, float* output, int dimx, int dim
     return 0;
 }
 
+int port_run_angles_ordered(int op, const float* input, float* output, int dimx, int dimy, const int* angles,
+                            int nangles, float povh, int nthreads) {
+    if (dimx <= 0 || dimy <= 0 || nangles <= 0) return 1;
+    for (int i = 0; i < nangles; i++)
+        if (angles[i] < 0 || angles[i] >= 180) return 1;
+    std::vector<float> src[4];
+    orientations(input, dimx, dimy, src);
+    const size_t n = (size_t)dimx * dimy;
+    const int diml = std::max(dimx, dimy);
+    const int nt = nthreads > 0 ? nthreads : 1;
+    const bool max_mode = op == PORT_CEPSTRUM;
+    // Per sector of a chunk: its geometry and the value its deskew folds into
+    // every accumulator cell, (1-w)*lo + w*hi (add) or max(lo, hi) (max), the
+    // same float expressions deskew_rows evaluates.
+    const int chunk = 2 * nt;
+    std::vector<Sector> sec(chunk);
+    std::vector<std::vector<float>> val(chunk, std::vector<float>(n));
+    std::vector<std::vector<float>> S(nt, std::vector<float>(2 * n + diml)), O(nt, std::vector<float>(2 * n + diml));
+    std::vector<float> acc[4];
+    for (int c0 = 0; c0 < nangles; c0 += chunk) {
+        const int cn = std::min(chunk, nangles - c0);
+#pragma omp parallel for num_threads(nt) schedule(dynamic)
+        for (int k = 0; k < cn; k++) {
+            const int th = omp_get_thread_num();
+            Sector& s = sec[k];
+            make_sector(dimx, dimy, angles[c0 + k], s);
+            std::fill(S[th].begin(), S[th].end(), 0.0f);
+            std::fill(O[th].begin(), O[th].end(), 0.0f);
+            skew_rows(s, src[s.type].data(), S[th].data());
+            run_operator(op, s, S[th].data(), O[th].data(), povh);
+            const float* Ot = O[th].data();
+            for (int i = 0; i < s.dim_o; i++)
+                for (int j = 0; j < s.dim_i; j++) {
+                    const float lo = Ot[(size_t)(i + s.target[j]) * s.dim_i + j];
+                    const float hi = Ot[(size_t)(i + s.target[j] + 1) * s.dim_i + j];
+                    val[k][(size_t)i * s.dim_i + j] =
+                        max_mode ? std::max(lo, hi) : (1.0f - s.weight[j]) * lo + s.weight[j] * hi;
+                }
+        }
+        for (int k = 0; k < cn; k++) {  // fold in list order, as one reference thread does
+            const Sector& s = sec[k];
+            std::vector<float>& a = acc[s.type];
+            if (a.empty()) a.assign(n, 0.0f);
+            const float* v = val[k].data();
+            for (size_t q = 0; q < (size_t)s.dim_o * s.dim_i; q++) {
+                if (max_mode) {
+                    a[q] = std::max(a[q], v[q]);
+                    a[q] = s.a + 1000 * (int)(a[q] / 1000);
+                } else {
+                    a[q] += v[q];
+                }
+            }
+        }
+    }
+    memset(output, 0, sizeof(float) * n);
+    reduce_types(output, dimx, dimy, acc, max_mode);
+    return 0;
+}
+
 int port_run(int op, const float* input, float* output, int dimx, int dimy, int nsect, float povh,
              int nthreads) {
     if (nsect <= 0 || nsect > 180) return 1;

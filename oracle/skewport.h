@@ -34,6 +34,13 @@ int port_geometry(int dimx, int dimy, int angle, int* iinfo, double* dinfo,
 int port_run_angles(int op, const float* input, float* output, int dimx, int dimy,
                     const int* angles, int nangles, float povh, int nthreads);
 
+// The result port_run_angles gives with one thread (the reference's
+// single-thread accumulation order, in list order), computed on nthreads: each
+// sector's deskewed values are formed in parallel, then folded into the
+// per-type accumulators in list order.  Bit-identical to nthreads == 1.
+int port_run_angles_ordered(int op, const float* input, float* output, int dimx, int dimy,
+                            const int* angles, int nangles, float povh, int nthreads);
+
 // Whole run over angles 0..nsect-1.
 int port_run(int op, const float* input, float* output, int dimx, int dimy, int nsect,
              float povh, int nthreads);

@@ -60,6 +60,8 @@ SIGNATURES = [
                                  C.POINTER(Params), C.c_void_p, C.c_int, C.POINTER(C.c_uint32)]),
     ("ske_run_batch", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                 C.c_void_p, C.c_int, C.POINTER(Params)]),
+    ("ske_run_batch_angles", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(Params)]),
     ("ske_prepare", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("ske_skew", C.c_int, [C.c_void_p, C.c_int]),
     ("ske_kernel", C.c_int, [C.c_void_p, C.c_int, C.c_float]),

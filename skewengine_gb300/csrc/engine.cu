@@ -818,9 +818,21 @@ int ske_fold(ske_engine e, int kernel, const float* acc, const float* comp, int 
 int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
                   const float* const* inputs, int inputs_on_device, float* const* outputs, int outputs_on_device,
                   const ske_params* p) {
+    ske_params prm;
+    SKE_TRY(validate_params(p, &prm));
+    std::vector<int32_t> angles(prm.max_sector);
+    for (int i = 0; i < prm.max_sector; i++) angles[i] = i;
+    return ske_run_batch_angles(e, kernel, count, dimx, dimy, inputs, inputs_on_device, outputs, outputs_on_device,
+                                angles.data(), prm.max_sector, &prm);
+}
+
+int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
+                         const float* const* inputs, int inputs_on_device, float* const* outputs,
+                         int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p) {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (count < 0 || (count > 0 && (!dimx || !dimy || !inputs || !outputs)))
         return fail(SKE_ERR_INVALID, "bad batch arguments");
+    if (nangles < 1 || !angles) return fail(SKE_ERR_INVALID, "empty angle list");
     // One child engine per other grid size, created on first use and kept with
     // the parent (geometry, work lists and buffers are reused by later batches).
     int rc = SKE_OK;
@@ -838,7 +850,8 @@ int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, cons
             }
         }
         const int64_t before = sub->launches;
-        rc = ske_run(sub, kernel, inputs[i], inputs_on_device, outputs[i], outputs_on_device, p);
+        rc = ske_run_angles(sub, kernel, inputs[i], inputs_on_device, outputs[i], outputs_on_device, angles, nangles,
+                            p);
         if (sub != e) e->launches += sub->launches - before;
     }
     return rc;

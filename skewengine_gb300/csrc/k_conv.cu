@@ -277,6 +277,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
         cp_commit();
     }
     bool fail = false;
+    int last_commit = -1;  // thread 0: the last slice whose MMAs were committed
     for (int kt = 0; kt < KT; kt++) {
         const int nxt = kt + kTcPrefetch;
         if (nxt < KT) {
@@ -300,12 +301,20 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
             for (int kk = 0; kk < kTcBK / 16; kk++)
                 tc_mma(tmem, tc_desc(a0 + kk * 256), tc_desc(b0 + kk * 256), idesc, (kt | kk) != 0);
             tc_commit(&bar[s]);
+            last_commit = kt;
         }
     }
     cp_wait<0>();
     // The last slice's commit completes after every earlier MMA.
     if (!fail && KT > 0) fail = !tc_mbar_wait(&bar[(KT - 1) % kTcStages], ((KT - 1) / kTcStages) & 1);
     fail = __syncthreads_or(fail);
+    // Giving up: before the tensor memory is freed below, thread 0 waits once
+    // more (bounded) for the last commit it issued, which arrives after all of
+    // its MMAs, so that none is still writing the accumulator when it is freed.
+    // If that wait runs out too the memory is freed regardless (the output is
+    // not written and the status flag tells the host).
+    if (fail && tid == 0 && last_commit >= 0)
+        tc_mbar_wait(&bar[last_commit % kTcStages], (last_commit / kTcStages) & 1);
     tc_fence_after();
     if (!fail) {
         const int m = m0 + warp * 32 + lane;

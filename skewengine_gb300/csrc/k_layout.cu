@@ -349,6 +349,7 @@ __global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4)
     __shared__ __align__(128) float band[2][kDeskewBand][kTile];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ unsigned bmask[kMasked ? kDeskewBand : 1];
+    __shared__ int s_abort;  // a band wait ran out: stop issuing and reading bands
     constexpr int kPer = kDeskewRows / 8;
     const int t = blockIdx.z;
     const int cnt = tl.count[t];
@@ -385,19 +386,28 @@ __global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4)
     if (tid == 0) {
         mbar_init(&bar[0]);
         mbar_init(&bar[1]);
+        s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     int r0n, nrn;
-    if (tid == 0 && band_of(0, &r0n, &nrn)) tma_band(&band[0][0][0], map, j0, r0n, tl.slot[t][0], &bar[0]);
-    int uses[2] = {0, 0};
-    bool ok_all = true;
+    // uses[b]: phases of bar[b] this thread has seen complete; issued[b]: copies
+    // thread 0 has started into buffer b.  issued - uses (thread 0) is what is
+    // still in flight if the CTA has to give up.
+    int uses[2] = {0, 0}, issued[2] = {0, 0};
+    if (tid == 0 && band_of(0, &r0n, &nrn)) {
+        tma_band(&band[0][0][0], map, j0, r0n, tl.slot[t][0], &bar[0]);
+        issued[0]++;
+    }
+    volatile int* abort_flag = &s_abort;
     for (int q = 0; q < cnt; q++) {
         const int buf = q & 1;
         // Prefetch the next sector's band into the other buffer (freed by the
-        // barrier that ended the previous sector).
-        if (tid == 0 && q + 1 < cnt && band_of(q + 1, &r0n, &nrn))
+        // barrier that ended the previous sector), unless the CTA is giving up.
+        if (tid == 0 && q + 1 < cnt && !*abort_flag && band_of(q + 1, &r0n, &nrn)) {
             tma_band(&band[buf ^ 1][0][0], map, j0, r0n, tl.slot[t][q + 1], &bar[buf ^ 1]);
+            issued[buf ^ 1]++;
+        }
         const SectorDesc& d = g.desc[tl.angle[t][q]];
         const int32_t* tg = g.target + d.col_off;
         const int tmin = tg[j0];
@@ -419,10 +429,11 @@ __global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4)
                 }
                 bmask[tid] = m;
             }
-            ok_all = mbar_wait(&bar[buf], uses[buf] & 1) && ok_all;
-            uses[buf]++;
+            if (mbar_wait(&bar[buf], uses[buf] & 1)) uses[buf]++;
+            else *abort_flag = 1;  // written before the barrier, read by every thread after it
             if (kMasked) full = __syncthreads_and(tid >= nrows || m == 0xffffffffu);
             else __syncthreads();
+            if (*abort_flag) break;  // CTA-uniform: the band is not read
         }
         if (col_ok && nv > 0) {
             const int off = tj - tmin;
@@ -457,7 +468,17 @@ __global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4)
         }
         __syncthreads();  // this buffer and the masks are free for the next sectors
     }
-    if (!ok_all) atomicExch(status, 7);  // a band copy never arrived
+    if (*abort_flag) {
+        // A band copy did not arrive in time.  Report it, leave the accumulators
+        // as they were, and keep the CTA (and so its shared memory) alive until
+        // every copy thread 0 started has landed, each wait again bounded.
+        if (tid == 0) {
+            atomicExch(status, 7);
+            for (int b = 0; b < 2; b++)
+                if (issued[b] > uses[b]) mbar_wait(&bar[b], uses[b] & 1);
+        }
+        return;
+    }
     if (!col_ok) return;
 #pragma unroll
     for (int k = 0; k < kPer; k++) {

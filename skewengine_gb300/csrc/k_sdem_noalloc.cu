@@ -21,7 +21,10 @@
 // capture.  All calls share the array (and the host arrays), which keep the
 // last call's contents: the queue head and status are cleared on every call,
 // the item list and descriptor are rewritten.  Calls that overlap on the GPU
-// race; calls from several host threads are serialised by a mutex.
+// race; calls from several host threads are serialised by a mutex.  Each call
+// reads the row limits and, at the end, a status word back to the host and
+// waits for `stream` to drain both times; the calling thread's current device
+// is restored before it returns.
 #include <algorithm>
 #include <mutex>
 
@@ -62,6 +65,21 @@ int setup(int device) {
 
 int cuda_fail(cudaError_t e) { return set_last_error(SKE_ERR_CUDA, cudaGetErrorString(e)); }
 
+// Restores the calling thread's current device on every return path, so a
+// caller working on another device keeps it.
+struct DeviceGuard {
+    int saved = -1;
+    DeviceGuard() {
+        if (cudaGetDevice(&saved) != cudaSuccess) {
+            cudaGetLastError();
+            saved = -1;
+        }
+    }
+    ~DeviceGuard() {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
+
 }  // namespace
 }  // namespace ske
 
@@ -85,6 +103,7 @@ extern "C" int ske_sdem_sector_noalloc(int device, const float* skew_in, float* 
         return set_last_error(SKE_ERR_NO_DEVICE, "sdem_sector_noalloc: device not available");
     }
     std::lock_guard<std::mutex> lock(g_mutex);
+    DeviceGuard restore;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return cuda_fail(e);
@@ -97,13 +116,17 @@ extern "C" int ske_sdem_sector_noalloc(int device, const float* skew_in, float* 
     if (e == cudaSuccess) e = cudaMemcpyAsync(h_last, last, sizeof(int32_t) * skew_height, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e);
+    // Every row must satisfy 0 <= first <= last <= dim_l, as the engine's own
+    // geometry does (skewShape, skewEngine.cuh:573-596): the sweep then reads
+    // and writes flat cells r*dim_i + [first, last) only, all below
+    // (skew_height-1)*dim_i + dim_l, and owner_row's early exit stays exact.
     const int chunk = sdem_chunk();
     int lmax = 0;
     for (int r = 0; r < skew_height; r++) {
-        const int L = h_last[r] - h_first[r];
-        if (h_first[r] < 0 || L > dim_l)
-            return set_last_error(SKE_ERR_INVALID, "sdem_sector_noalloc: first/last outside the skewed grid");
-        lmax = std::max(lmax, L);
+        if (h_first[r] < 0 || h_last[r] > dim_l || h_first[r] > h_last[r])
+            return set_last_error(SKE_ERR_INVALID,
+                                  "sdem_sector_noalloc: a row's first/last is outside 0 <= first <= last <= dim_l");
+        lmax = std::max(lmax, h_last[r] - h_first[r]);
     }
     std::fill(h_bucket, h_bucket + lmax + 2, (int64_t)0);
     int64_t total = 0;

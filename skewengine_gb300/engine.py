@@ -304,8 +304,11 @@ def execute(kernel, data, max_sector: int = 180, povh: float = DEFAULT_POVH, acc
 
 
 def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference",
-              device: int = 0, outs=None):
-    """Run one operator over many grids of uneven size (``ske_run_batch``)."""
+              device: int = 0, outs=None, angles=None, engine=None):
+    """Run one operator over many grids of uneven size (``ske_run_batch``, or
+    ``ske_run_batch_angles`` with an angle list).  ``engine``: an existing
+    SkewEngine to run on (it keeps the batch's plan and buffers for later calls);
+    by default one is made for the largest grid and closed afterwards."""
     grids = list(grids)
     if not grids:
         return []
@@ -323,9 +326,19 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
     dx = np.array([d[0] for d in dims], np.int32)
     dy = np.array([d[1] for d in dims], np.int32)
     prm = params(max_sector, povh, accum)
-    with SkewEngine(big[0], big[1], device) as eng:
-        check(eng._lib.ske_run_batch(eng._h, _kernel_id(kernel), len(grids), dx.ctypes.data, dy.ctypes.data,
-                                     ins, int(on_dev), ous, int(on_dev), C.byref(prm)))
+    eng = engine if engine is not None else SkewEngine(big[0], big[1], device)
+    try:
+        if angles is None:
+            check(eng._lib.ske_run_batch(eng._h, _kernel_id(kernel), len(grids), dx.ctypes.data, dy.ctypes.data,
+                                         ins, int(on_dev), ous, int(on_dev), C.byref(prm)))
+        else:
+            a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
+            check(eng._lib.ske_run_batch_angles(eng._h, _kernel_id(kernel), len(grids), dx.ctypes.data,
+                                                dy.ctypes.data, ins, int(on_dev), ous, int(on_dev), a.ctypes.data,
+                                                len(a), C.byref(prm)))
+    finally:
+        if engine is None:
+            eng.close()
     return outs
 
 

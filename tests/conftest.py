@@ -39,6 +39,7 @@ def port():
     up = np.ctypeslib.ndpointer(np.uint16, flags="C")
     lib.port_run.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int]
     lib.port_run_angles.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, C.c_int]
+    lib.port_run_angles_ordered.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, C.c_int]
     lib.port_sector.argtypes = [C.c_int, fp, C.c_int, C.c_int, C.c_int, C.c_float, fp, fp, fp]
     lib.port_geometry.argtypes = [C.c_int, C.c_int, C.c_int, ip, dp, up, up, ip, fp]
     lib.port_sdem_counts.argtypes = [fp, C.c_int, C.c_int, C.c_int, C.c_float, fp]
@@ -73,6 +74,23 @@ class PortOracle:
         assert self.lib.port_run_angles(op, np.ascontiguousarray(x, np.float32), out, dx, dy, a, len(a), povh,
                                         threads) == 0
         return out
+
+    def run_ordered(self, op, x, angles=None, povh=0.15, threads=None):
+        """The single-thread result (reference accumulation order) computed on
+        all host cores: sectors in parallel, folded in list order."""
+        dy, dx = x.shape
+        out = np.zeros_like(x)
+        a = np.ascontiguousarray(range(180) if angles is None else angles, np.int32)
+        nt = threads or os.cpu_count() or 1
+        assert self.lib.port_run_angles_ordered(op, np.ascontiguousarray(x, np.float32), out, dx, dy, a, len(a),
+                                                povh, nt) == 0
+        return out
+
+    def counts_many(self, x, angles, povh=0.15, threads=None):
+        """port_sdem_counts of several sectors, one host thread per sector."""
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+            return list(ex.map(lambda a: self.counts(x, a, povh), angles))
 
     def sector(self, op, x, angle, povh=0.15):
         dy, dx = x.shape

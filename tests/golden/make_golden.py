@@ -3,7 +3,7 @@
 Run where the reference sources are present (it builds ``oracle/_ref`` from them
 through ``oracle/Makefile``)::
 
-    python tests/golden/make_golden.py [--ref /path/to/skewEngine]
+    python tests/golden/make_golden.py --ref /path/to/skewEngine
 
 Outputs, all in this folder:
 
@@ -133,7 +133,7 @@ def geometry_digest(lib, dx: int, dy: int) -> list[str]:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="reference project root")
     args = ap.parse_args()
     lib = load_ref(args.ref)
 

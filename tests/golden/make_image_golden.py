@@ -3,7 +3,7 @@
 Run where the reference sources are present (it builds ``oracle/_ref`` from them
 through ``oracle/Makefile``)::
 
-    python tests/golden/make_image_golden.py [--ref /path/to/skewEngine]
+    python tests/golden/make_image_golden.py --ref /path/to/skewEngine
 
 Output ``images.npz`` in this folder:
 
@@ -41,7 +41,7 @@ def build_ref(ref: str) -> C.CDLL:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="reference project root")
     args = ap.parse_args()
     lib = build_ref(args.ref)
     rng = np.random.default_rng(20240)

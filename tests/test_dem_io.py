@@ -1,0 +1,85 @@
+"""DEM file input and output of run(argc, argv): the ESRI .bil int16 grid with
+its .hdr (readBilData / parse_hdr / check_dem, src/kernelSDEM.h:31-142) and the
+raw float32 .flt result dump (showResultsSDEM, src/kernelSDEM.h:433-439).
+
+The reference reads a .bil as little-endian int16 metres, row after row, and
+divides each value by 10 in binary64 before storing it as float (cell units of
+a 10 m grid, kernelSDEM.h:43-50).  Without a header the grid is square with the
+side taken from the file size (check_dem, :132-135).  The GPU tests write such
+files, run the total viewshed through run(), and compare the .flt bit for bit
+with the oracle on the same divided grid.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from skewengine_gb300 import synthetic
+
+
+def _bil_grid(raw: np.ndarray) -> np.ndarray:
+    """The float grid readBilData makes of int16 metres: (float)((float)v / 10.0)."""
+    return (raw.astype(np.float32).astype(np.float64) / 10.0).astype(np.float32)
+
+
+def _fractal_int16(side_x: int, side_y: int, seed: int) -> np.ndarray:
+    # Heights in metres (0-1500 m, the fractal DEM of the benchmark configs).
+    m = synthetic.fractal_dem(side_x, seed, side_y=side_y) * np.float32(synthetic.CELL_SIZE_M)
+    return np.round(m).astype("<i2")
+
+
+def _write_hdr(path, ncols, nrows):
+    path.write_text(f"BYTEORDER      I\nLAYOUT         BIL\nNROWS         {nrows}\nNCOLS         {ncols}\n"
+                    f"NBANDS        1\nNBITS         16\nCELLSIZE      10\nXLLCORNER     310000\n"
+                    f"YLLCORNER     4070000\n")
+
+
+def test_bil_reader_rejects_short_files(tmp_path):
+    """A .bil with fewer bytes than its header's grid is refused before any
+    device work (so this runs without a GPU)."""
+    from skewengine_gb300 import cli_run
+    raw = np.zeros((10, 12), "<i2")
+    (tmp_path / "dem.bil").write_bytes(raw.tobytes())
+    _write_hdr(tmp_path / "dem.hdr", 40, 40)
+    assert cli_run(["sdem", str(tmp_path / "dem.bil"), 0, 0, str(tmp_path / "out.flt")]) == 1
+
+
+@pytest.mark.gpu
+def test_bil_square_without_header(gpu_lib, oracle, tmp_path):
+    """No .hdr: the side comes from the file size, as check_dem does."""
+    from skewengine_gb300 import cli_run
+    raw = _fractal_int16(96, 96, 311)
+    (tmp_path / "dem.bil").write_bytes(raw.tobytes())
+    assert cli_run(["sdem", str(tmp_path / "dem.bil"), 0, 0, str(tmp_path / "out.flt")]) == 0
+    got = np.fromfile(tmp_path / "out.flt", "<f4").reshape(96, 96)
+    want = oracle.run(0, _bil_grid(raw), povh=synthetic.POVH)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_bil_with_esri_header_non_square(gpu_lib, oracle, tmp_path):
+    """An ESRI header's NCOLS/NROWS give a non-square grid (dimx/dimy 0)."""
+    from skewengine_gb300 import cli_run
+    raw = _fractal_int16(80, 56, 312)  # 56 rows of 80 columns
+    (tmp_path / "dem.bil").write_bytes(raw.tobytes())
+    _write_hdr(tmp_path / "dem.hdr", 80, 56)
+    assert cli_run(["sdem", str(tmp_path / "dem.bil"), 0, 0, str(tmp_path / "out.flt"), 180, 0.15]) == 0
+    got = np.fromfile(tmp_path / "out.flt", "<f4")
+    assert got.size == 80 * 56
+    want = oracle.run(0, _bil_grid(raw), povh=np.float32(0.15))
+    assert np.array_equal(got.reshape(56, 80).view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_bil_explicit_dims_and_angle_count(gpu_lib, oracle, tmp_path):
+    """Explicit dimx/dimy take precedence over the header; max_sector limits the
+    angles 0..max_sector-1; the division by 10 reaches negative and large values."""
+    from skewengine_gb300 import cli_run
+    rng = np.random.default_rng(313)
+    raw = rng.integers(-400, 8000, size=(48, 64)).astype("<i2")
+    (tmp_path / "dem.bil").write_bytes(raw.tobytes())
+    _write_hdr(tmp_path / "dem.hdr", 10, 10)  # ignored: dims given
+    assert cli_run(["sdem", str(tmp_path / "dem.bil"), 64, 48, str(tmp_path / "out.flt"), 45]) == 0
+    got = np.fromfile(tmp_path / "out.flt", "<f4").reshape(48, 64)
+    want = oracle.run(0, _bil_grid(raw), nsect=45, povh=np.float32(0.15))
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

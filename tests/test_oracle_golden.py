@@ -107,3 +107,18 @@ def test_los_step_counts(port, dims):
     steps = port.port_los_steps(dims[0], dims[1], 180)
     expect = {500: 1.918e10, 2000: 1.228e12}[dims[0]]
     assert abs(steps - expect) / expect < 0.01
+
+
+@pytest.mark.parametrize("op", [0, 1, 2, 4, 5])
+def test_ordered_parallel_oracle_equals_single_thread(oracle, op):
+    """The all-cores oracle mode reproduces the one-thread accumulation order
+    bit for bit (square and non-square grids, a scrambled angle list)."""
+    from skewengine_gb300 import synthetic
+    rng = np.random.default_rng(op)
+    for dx, dy in ((40, 40), (37, 23)):
+        x = synthetic.fractal_dem(dx, 5 + op, side_y=dy) if op in (0, 1) else \
+            synthetic.blurred_texture(dx, 5 + op, side_y=dy)[0]
+        angles = rng.permutation(180)[:70] if op != 5 else rng.permutation(180)[:12]
+        want = oracle.run_angles(op, x, angles, povh=0.15, threads=1)
+        got = oracle.run_ordered(op, x, angles, povh=0.15, threads=5)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (op, dx, dy)

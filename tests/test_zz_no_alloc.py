@@ -50,3 +50,76 @@ def test_noalloc_rejects_oversized_sector(gpu_lib):
     rc = gpu_lib.ske_sdem_sector_noalloc(0, p, p, 5000, 10, 5000, p, p, 1.0, 0.15, None)
     assert rc == 1
     assert b"4096" in gpu_lib.ske_last_error()
+
+
+def _call(gpu_lib, skew, first, last, dim_i, h, dim_l, device=0):
+    return gpu_lib.ske_sdem_sector_noalloc(device, C.c_void_p(skew.data_ptr()), C.c_void_p(skew.data_ptr()), dim_i,
+                                           h, dim_l, C.c_void_p(first.data_ptr()), C.c_void_p(last.data_ptr()),
+                                           1.0, float(POVH), None)
+
+
+def test_noalloc_rejects_rows_outside_the_grid(gpu_lib):
+    """A row whose last passes dim_l, or whose first lies far beyond the grid
+    with a short length, is refused before any device work; the caller's
+    buffers (sized for the valid rows) are never touched."""
+    torch = pytest.importorskip("torch")
+    dim_i, h, dim_l = 64, 8, 64
+    skew = torch.zeros((h - 1) * dim_i + dim_l, dtype=torch.float32, device="cuda")
+    first = torch.zeros(h, dtype=torch.int32, device="cuda")
+    good = torch.full((h,), dim_l, dtype=torch.int32, device="cuda")
+    assert _call(gpu_lib, skew, first, good, dim_i, h, dim_l) == 0, gpu_lib.ske_last_error().decode()
+    cases = []
+    last = good.clone()
+    last[3] = dim_l + 1
+    cases.append((first, last))
+    far_first = first.clone()
+    far_last = good.clone()
+    far_first[5] = 1 << 30
+    far_last[5] = (1 << 30) + 10
+    cases.append((far_first, far_last))
+    neg = first.clone()
+    neg[0] = -1
+    cases.append((neg, good))
+    crossed = first.clone()
+    crossed[2] = 10
+    crossed_last = good.clone()
+    crossed_last[2] = 5
+    cases.append((crossed, crossed_last))
+    for f, l in cases:
+        torch.cuda.synchronize()
+        assert _call(gpu_lib, skew, f, l, dim_i, h, dim_l) == 1
+        assert b"first/last" in gpu_lib.ske_last_error()
+
+
+def test_noalloc_rejects_too_many_rows_and_items(gpu_lib):
+    torch = pytest.importorskip("torch")
+    # More skewed rows than the static row arrays hold: refused before reading them.
+    p = C.c_void_p(16)  # never dereferenced
+    rc = gpu_lib.ske_sdem_sector_noalloc(0, p, p, 64, (1 << 17) + 1, 64, p, p, 1.0, 0.15, None)
+    assert rc == 1 and b"131072" in gpu_lib.ske_last_error()
+    # 131072 rows of 4096 cells at row stride 1 need 2^22 work items of 128
+    # observers (the static item list holds 2^20).  Every row reads cells
+    # r + [0, 4096) only, all inside the buffer, had it run.
+    h, dim_l = 1 << 17, 4096
+    skew = torch.zeros(h - 1 + dim_l, dtype=torch.float32, device="cuda")
+    first = torch.zeros(h, dtype=torch.int32, device="cuda")
+    last = torch.full((h,), dim_l, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    assert _call(gpu_lib, skew, first, last, 1, h, dim_l) == 1
+    assert b"2^20" in gpu_lib.ske_last_error()
+
+
+def test_noalloc_rejects_missing_device_and_keeps_current_device(gpu_lib):
+    torch = pytest.importorskip("torch")
+    p = C.c_void_p(16)  # never dereferenced: the device check comes first
+    n = torch.cuda.device_count()
+    rc = gpu_lib.ske_sdem_sector_noalloc(n, p, p, 64, 8, 64, p, p, 1.0, 0.15, None)
+    assert rc == 3 and b"device" in gpu_lib.ske_last_error()
+    # A successful call leaves the calling thread's current device as it was.
+    skew = torch.zeros(7 * 64 + 64, dtype=torch.float32, device="cuda:0")
+    first = torch.zeros(8, dtype=torch.int32, device="cuda:0")
+    last = torch.full((8,), 64, dtype=torch.int32, device="cuda:0")
+    before = torch.cuda.current_device()
+    torch.cuda.synchronize()
+    assert _call(gpu_lib, skew, first, last, 64, 8, 64) == 0
+    assert torch.cuda.current_device() == before
