@@ -67,8 +67,15 @@ typedef struct ske_params {
     int32_t max_sector; /* angles 0..max_sector-1, 1..180 (global.cpp:69, default 180) */
     float povh;         /* observer height in cell units (kernelSDEM.h:159, 1.5/10)    */
     int32_t accum;      /* SKE_ACCUM_*                                                  */
-    int32_t flags;      /* reserved, 0                                                  */
+    int32_t flags;      /* SKE_FLAG_* bits, 0 by default                                */
 } ske_params;
+
+/* ske_params.flags (no counterpart in the reference). */
+#define SKE_FLAG_NO_TUNE 1  /* keep the viewshed sweep's built-in shape: skip the
+                               autotuner that times a few level schedules and CTA
+                               counts on the first run (results are identical)   */
+#define SKE_FLAG_NO_GRAPH 2 /* batched runs: launch the kernels of every call
+                               directly instead of replaying a captured CUDA graph */
 
 /* Geometry of one sector, computeParams + skewShape (skewEngine.cuh:504-596). */
 typedef struct ske_sector_geometry {
@@ -204,10 +211,26 @@ int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, cons
                   int outputs_on_device, const ske_params* p);
 
 /* ske_run_batch over the listed angles (each in [0,180), accumulated in list
- * order) for every DEM, as ske_run_angles is ske_run over a list. */
+ * order) for every DEM, as ske_run_angles is ske_run over a list.
+ *
+ * Total viewshed (SKE_KERNEL_SDEM): the grids whose sectors' rows stay within
+ * their width (every square grid) run together.  The engine keeps a plan of
+ * the batch (geometry per grid size, buffers, work lists) while later calls
+ * bring the same grid sizes and angles; its memory budget splits the batch into
+ * waves, and each wave is five kernel launches over all of its grids and
+ * sectors (orientations, skew, viewshed sweep, deskew, fold; the main loop of
+ * src/main.cu:86-168 for every grid at once), replayed as a captured CUDA graph
+ * from the second call on (SKE_FLAG_NO_GRAPH: plain launches).  Results are the
+ * same as ske_run_angles on each grid, bit for bit in both accumulation modes.
+ * Other grids and other operators run one grid at a time. */
 int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
                          const float* const* inputs, int inputs_on_device, float* const* outputs,
                          int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p);
+
+/* Shape of the last viewshed sweep the engine launched: level schedule (lvl0
+ * steps, then lvl1 when non-zero, then 64-step levels) and resident CTAs per SM
+ * (0 = as many as fit), as chosen by the autotuner.  No reference counterpart. */
+int ske_sweep_shape(ske_engine e, int* lvl0, int* lvl1, int* ctas_per_sm);
 
 /* Per-sector API (drop-in for the reference's skew/kernel/deskew/reduce
  * methods driven from main.cu:147-164) ----------------------------------------*/

@@ -87,7 +87,19 @@ struct ItemPlan {
     uint64_t* d_items = nullptr;
     int64_t n_items = 0;
     int max_row = 0;
+    std::vector<uint64_t> h_items;  // host copy: the autotuner samples it
 };
+
+// Shape of the compacting sweep the autotuner chooses: level schedule
+// (lvl0, then lvl1, then 64-step levels) and resident CTAs per SM (0 = all
+// that fit).  Every shape gives the same results bit for bit; only the time
+// differs.
+struct SweepShape {
+    int lvl0 = 64, lvl1 = 0, ctas = 0;
+};
+
+struct BatchPlan;
+void destroy_batch_plan(BatchPlan* p);
 
 struct ProfEntry {
     double ms = 0;
@@ -153,6 +165,13 @@ struct ske_engine_s {
     // lists (the parent's stride holds the child's skewed grids) and owns the rest.
     ske_engine parent = nullptr;
     std::map<std::pair<int, int>, ske_engine> children;
+    // Batched total-viewshed runs: the plan of the last batch (grids, angles,
+    // waves, work lists, captured graphs), reused while the batch keeps its shape.
+    BatchPlan* batch_plan = nullptr;
+    int flags = 0;           // ske_params.flags of the current run
+    SweepShape last_shape;   // shape of the last compacting sweep launched
+    uint64_t* d_tune_items = nullptr;  // the autotuner's sample of a work list
+    size_t tune_items_cap = 0;
 };
 
 namespace {
@@ -322,15 +341,96 @@ int get_items(ske_engine e, const Batch& b, ItemPlan** out) {
         *out = &it->second;
         return SKE_OK;
     }
-    std::vector<uint64_t> items;
     ItemPlan plan;
-    sdem_items(e->geo, b, items, &plan.max_row);
-    plan.n_items = (int64_t)items.size();
-    SKE_TRY(dev_alloc(&plan.d_items, items.size()));
-    if (!items.empty())
-        SKE_CK(cudaMemcpy(plan.d_items, items.data(), sizeof(uint64_t) * items.size(), cudaMemcpyHostToDevice));
-    auto ins = e->item_plans.emplace(key, plan);
+    sdem_items(e->geo, b, plan.h_items, &plan.max_row);
+    plan.n_items = (int64_t)plan.h_items.size();
+    SKE_TRY(dev_alloc(&plan.d_items, plan.h_items.size()));
+    if (!plan.h_items.empty())
+        SKE_CK(cudaMemcpy(plan.d_items, plan.h_items.data(), sizeof(uint64_t) * plan.h_items.size(),
+                          cudaMemcpyHostToDevice));
+    auto ins = e->item_plans.emplace(key, std::move(plan));
     *out = &ins.first->second;
+    return SKE_OK;
+}
+
+// ---- sweep autotuner --------------------------------------------------------
+// The compacting sweep's speed depends on its level schedule (a short first
+// level retires the many observers that see nothing far away sooner, for more
+// retirement tests) and on how many CTAs share an SM (more warps hide latency,
+// fewer leave each warp more L1).  The tuner times a few shapes on a sample of
+// the actual work list (every 8th row, which keeps the longest-first length
+// distribution) the first time a device meets rows of a given length class,
+// and keeps the fastest for the process.  Every shape writes the same bits.
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, SweepShape> g_tuned;  // (device, max_row / 256) -> shape
+
+int tune_sweep(ske_engine e, const SdemLaunch& base, const std::vector<uint64_t>& items, SweepShape* out) {
+    *out = SweepShape();
+    if (e->flags & SKE_FLAG_NO_TUNE) return SKE_OK;
+    const auto key = std::make_pair(e->device, (base.max_row + 255) / 256);
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+        *out = it->second;
+        return SKE_OK;
+    }
+    constexpr int kStride = 8;
+    if (items.size() < (size_t)64 * e->num_sms) return SKE_OK;  // too little work to time; keep the default
+    std::vector<uint64_t> sample;
+    sample.reserve(items.size() / kStride + 1);
+    for (size_t i = 0; i < items.size(); i += kStride) sample.push_back(items[i]);
+    if (sample.size() > e->tune_items_cap) {
+        cudaFree(e->d_tune_items);
+        e->d_tune_items = nullptr;
+        e->tune_items_cap = 0;
+        SKE_TRY(dev_alloc(&e->d_tune_items, sample.size()));
+        e->tune_items_cap = sample.size();
+    }
+    SKE_CK(cudaMemcpyAsync(e->d_tune_items, sample.data(), sizeof(uint64_t) * sample.size(), cudaMemcpyHostToDevice,
+                           e->stream));
+    const int max_ctas = sdem_max_ctas_per_sm(base);
+    const SweepShape sched[] = {{64, 0, 0}, {32, 0, 0}, {16, 48, 0}, {32, 32, 0}};
+    std::vector<SweepShape> cands;
+    for (const SweepShape& c : sched) {
+        cands.push_back(c);
+        if (max_ctas > 1) cands.push_back({c.lvl0, c.lvl1, max_ctas - 1});
+    }
+    cudaEvent_t ev[2];
+    SKE_CK(cudaEventCreate(&ev[0]));
+    SKE_CK(cudaEventCreate(&ev[1]));
+    float best = 0.0f;
+    SweepShape pick;
+    int rc = SKE_OK;
+    for (int rep = 0; rep < 2 && rc == SKE_OK; rep++) {  // the second pass is the one compared
+        for (const SweepShape& c : cands) {
+            SdemLaunch a = base;
+            a.items = e->d_tune_items;
+            a.n_items = (int64_t)sample.size();
+            a.lvl0 = c.lvl0;
+            a.lvl1 = c.lvl1;
+            a.ctas_per_sm = c.ctas;
+            cudaError_t err = cudaEventRecord(ev[0], e->stream);
+            if (err == cudaSuccess) err = launch_sdem(a, e->num_sms, e->stream);
+            if (err == cudaSuccess) err = cudaEventRecord(ev[1], e->stream);
+            if (err == cudaSuccess) err = cudaEventSynchronize(ev[1]);
+            float ms = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, ev[0], ev[1]);
+            if (err != cudaSuccess) {
+                rc = fail(SKE_ERR_CUDA, "sweep autotuner: %s", cudaGetErrorString(err));
+                break;
+            }
+            e->launches += 1;
+            if (rep == 1 && (best == 0.0f || ms < best)) {
+                best = ms;
+                pick = c;
+            }
+        }
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (rc != SKE_OK) return rc;
+    g_tuned[key] = pick;
+    *out = pick;
     return SKE_OK;
 }
 
@@ -363,6 +463,12 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             a.status = e->d_status;
             a.lists = e->d_lists;
             a.list_bytes = e->list_bytes;
+            SweepShape shape;
+            SKE_TRY(tune_sweep(e, a, plan->h_items, &shape));
+            a.lvl0 = shape.lvl0;
+            a.lvl1 = shape.lvl1;
+            a.ctas_per_sm = shape.ctas;
+            e->last_shape = shape;
             LaunchScope ls(e, "sdem_sweep", plan->n_items > 0 ? 1 : 0);
             return ls.done(launch_sdem(a, e->num_sms, e->stream));
         }
@@ -500,6 +606,7 @@ int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on
         if (angles[i] < 0 || angles[i] >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angles[i]);
     SKE_TRY(validate_params(p, prm));
     SKE_TRY(set_device(e));
+    e->flags = prm->flags;
     const int is_max = kernel == SKE_KERNEL_CEPSTRUM;
     SKE_TRY(run_prepare(e, input, input_on_device));
     if (start) {
@@ -538,6 +645,434 @@ int run_angle_list(ske_engine e, int kernel, const float* input, int input_on_de
     SKE_TRY(accumulate_angles(e, kernel, input, input_on_device, angles, nangles, p, &prm));
     SKE_TRY(run_reduce(e, output, output_on_device, kernel == SKE_KERNEL_CEPSTRUM, prm.accum));
     e->prepared = false;  // the accumulators now hold this run
+    return SKE_OK;
+}
+
+// ---- batched total viewshed over grids of uneven size -------------------------
+// A batch plan holds, per grid size, the device geometry and the compact-row
+// offsets; per grid, its orientation, accumulator and staging buffers; and the
+// batch split into waves whose skewed rows (compact) fit the device memory
+// budget.  Each wave runs as five launches over all of its grids and sectors:
+// orientations, skew, sweep, deskew, fold (captured as a CUDA graph after its
+// first run).  Grids too large for a wave of their own, or with sectors whose
+// rows leave dim_i, run through the per-grid engine path instead.
+
+struct GridGeo {
+    int dimx = 0, dimy = 0;
+    Geometry geo;
+    std::vector<int32_t> rowoff;  // per skewed row: start within its sector's compact rows
+    std::vector<int64_t> cells;   // per angle: valid cells (compact size)
+    SectorDesc* d_desc = nullptr;
+    int32_t *d_target = nullptr, *d_first = nullptr, *d_last = nullptr, *d_rowoff = nullptr;
+    float* d_weight = nullptr;
+};
+
+struct BatchWave {
+    std::vector<int> grids;         // plan grid indices
+    std::vector<BatchGrid> h_grids; // host copies of the wave's grid table (in/out set per call)
+    BatchGrid* d_grids = nullptr;
+    BatchSector* d_sectors = nullptr;
+    int* d_order = nullptr;
+    int64_t* d_prep = nullptr;
+    int64_t* d_tiles = nullptr;
+    uint64_t* d_items = nullptr;
+    std::vector<uint64_t> items;
+    int64_t n_items = 0, prep_blocks = 0, tiles = 0, cells = 0;
+    int max_row = 0;
+    BatchTables tables{};
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+    const void* graph_lists = nullptr;  // survivor-list scratch the graph was captured with
+};
+
+struct BatchPlan {
+    std::vector<int> dimx, dimy, angles;
+    int accum = 0;
+    std::map<std::pair<int, int>, GridGeo*> geos;
+    std::vector<GridGeo*> grid_geo;
+    std::vector<int64_t> grid_off, io_off;  // per grid: offsets in d_grid_pool (12 n) and d_io_pool (2 n)
+    float* d_grid_pool = nullptr;
+    float* d_io_pool = nullptr;
+    float *d_SI = nullptr, *d_SO = nullptr;
+    std::vector<BatchWave> waves;
+    std::vector<int> fallback;  // grids run through the per-grid engine path
+    bool tuned = false;
+    SweepShape shape;
+};
+
+void free_wave(BatchWave& w) {
+    if (w.graph) cudaGraphExecDestroy(w.graph);
+    void* bufs[] = {w.d_grids, w.d_sectors, w.d_order, w.d_prep, w.d_tiles, w.d_items};
+    for (void* b : bufs) cudaFree(b);
+    w = BatchWave();
+}
+
+void destroy_batch_plan(BatchPlan* p) {
+    if (!p) return;
+    for (BatchWave& w : p->waves) free_wave(w);
+    for (auto& kv : p->geos) {
+        GridGeo* g = kv.second;
+        void* bufs[] = {g->d_desc, g->d_target, g->d_first, g->d_last, g->d_rowoff, g->d_weight};
+        for (void* b : bufs) cudaFree(b);
+        delete g;
+    }
+    cudaFree(p->d_grid_pool);
+    cudaFree(p->d_io_pool);
+    cudaFree(p->d_SI);
+    cudaFree(p->d_SO);
+    delete p;
+}
+
+template <typename T>
+int upload_vec(T** d, const std::vector<T>& h) {
+    SKE_TRY(dev_alloc(d, h.size()));
+    if (!h.empty()) SKE_CK(cudaMemcpy(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+    return SKE_OK;
+}
+
+int make_grid_geo(int dimx, int dimy, GridGeo** out) {
+    GridGeo* g = new GridGeo();
+    *out = g;
+    g->dimx = dimx;
+    g->dimy = dimy;
+    build_geometry(dimx, dimy, g->geo);
+    g->rowoff.assign(g->geo.first.size(), 0);
+    g->cells.assign(g->geo.desc.size(), 0);
+    for (size_t a = 0; a < g->geo.desc.size(); a++) {
+        SectorDesc& d = g->geo.desc[a];
+        int64_t c = 0;
+        d.in_width = 1;
+        for (int r = 0; r < d.H; r++) {
+            const int64_t k = d.row_off + r;
+            g->rowoff[k] = (int32_t)c;
+            const int L = g->geo.last[k] - g->geo.first[k];
+            if (L > 0) c += L;
+            if (g->geo.last[k] > d.dim_i) d.in_width = 0;
+        }
+        g->cells[a] = c;
+    }
+    SKE_TRY(upload_vec(&g->d_desc, g->geo.desc));
+    SKE_TRY(upload_vec(&g->d_target, g->geo.target));
+    SKE_TRY(upload_vec(&g->d_weight, g->geo.weight));
+    SKE_TRY(upload_vec(&g->d_first, g->geo.first));
+    SKE_TRY(upload_vec(&g->d_last, g->geo.last));
+    SKE_TRY(upload_vec(&g->d_rowoff, g->rowoff));
+    return SKE_OK;
+}
+
+// Tables of one wave: its sectors in (grid, angle-list) order, the per-(grid,
+// type) accumulation order, the prepare/fold and deskew block ranges, and the
+// work list (every valid row, longest first).
+int build_wave(BatchPlan* p, BatchWave& w) {
+    std::vector<BatchSector> secs;
+    std::vector<int> order;
+    std::vector<int64_t> prep(1, 0), tiles(1, 0);
+    int64_t cells = 0;
+    int lmax = 0;
+    w.h_grids.clear();
+    for (size_t li = 0; li < w.grids.size(); li++) {
+        const int gi = w.grids[li];
+        const GridGeo* gg = p->grid_geo[gi];
+        BatchGrid G{};
+        G.dimx = gg->dimx;
+        G.dimy = gg->dimy;
+        G.n = (int64_t)gg->dimx * gg->dimy;
+        float* base = p->d_grid_pool + p->grid_off[gi];
+        G.orient = base;
+        G.acc = base + 4 * G.n;
+        G.comp = base + 8 * G.n;
+        G.desc = gg->d_desc;
+        G.target = gg->d_target;
+        G.weight = gg->d_weight;
+        G.first = gg->d_first;
+        G.last = gg->d_last;
+        G.rowoff = gg->d_rowoff;
+        const int s0 = (int)secs.size();
+        for (int a : p->angles) {
+            secs.push_back(BatchSector{(int)li, a, cells});
+            cells += gg->cells[a];
+            const SectorDesc& d = gg->geo.desc[a];
+            for (int r = 0; r < d.H; r++)
+                lmax = std::max(lmax, gg->geo.last[d.row_off + r] - gg->geo.first[d.row_off + r]);
+        }
+        for (int t = 0; t < 4; t++) {
+            G.ts_start[t] = (int)order.size();
+            for (int s = s0; s < (int)secs.size(); s++)
+                if (gg->geo.desc[secs[s].angle].type == t) order.push_back(s);
+            G.ts_count[t] = (int)order.size() - G.ts_start[t];
+            if (G.ts_count[t] > 0) G.used |= 1u << t;
+            tiles.push_back(tiles.back() + (G.ts_count[t] > 0 ? batch_deskew_tiles(G.dimx, G.dimy, t) : 0));
+        }
+        prep.push_back(prep.back() + batch_prep_blocks(G.dimx, G.dimy));
+        w.h_grids.push_back(G);
+    }
+    // Work list: counting sort of rows by length, longest first.
+    std::vector<int64_t> start(lmax + 2, 0);
+    for (const BatchSector& bs : secs) {
+        const GridGeo* gg = p->grid_geo[w.grids[bs.grid]];
+        const SectorDesc& d = gg->geo.desc[bs.angle];
+        for (int r = 0; r < d.H; r++) {
+            const int L = gg->geo.last[d.row_off + r] - gg->geo.first[d.row_off + r];
+            if (L > 0) start[L]++;
+        }
+    }
+    int64_t total = 0;
+    for (int L = lmax; L >= 1; L--) {
+        const int64_t c = start[L];
+        start[L] = total;
+        total += c;
+    }
+    w.items.assign(total, 0);
+    for (size_t si = 0; si < secs.size(); si++) {
+        const GridGeo* gg = p->grid_geo[w.grids[secs[si].grid]];
+        const SectorDesc& d = gg->geo.desc[secs[si].angle];
+        for (int r = 0; r < d.H; r++) {
+            const int L = gg->geo.last[d.row_off + r] - gg->geo.first[d.row_off + r];
+            if (L > 0) w.items[start[L]++] = batch_item((int)si, r);
+        }
+    }
+    w.n_items = total;
+    w.max_row = lmax;
+    w.cells = cells;
+    w.prep_blocks = prep.back();
+    w.tiles = tiles.back();
+    SKE_TRY(upload_vec(&w.d_grids, w.h_grids));
+    SKE_TRY(upload_vec(&w.d_sectors, secs));
+    SKE_TRY(upload_vec(&w.d_order, order));
+    SKE_TRY(upload_vec(&w.d_prep, prep));
+    SKE_TRY(upload_vec(&w.d_tiles, tiles));
+    SKE_TRY(upload_vec(&w.d_items, w.items));
+    w.tables = BatchTables{w.d_grids, w.d_sectors, w.d_order, w.d_prep, w.d_tiles, (int)w.grids.size()};
+    return SKE_OK;
+}
+
+bool same_plan(const BatchPlan* p, int count, const int32_t* dimx, const int32_t* dimy, const int32_t* angles,
+               int nangles, int accum) {
+    if (!p || (int)p->dimx.size() != count || (int)p->angles.size() != nangles || p->accum != accum) return false;
+    for (int i = 0; i < count; i++)
+        if (p->dimx[i] != dimx[i] || p->dimy[i] != dimy[i]) return false;
+    for (int i = 0; i < nangles; i++)
+        if (p->angles[i] != angles[i]) return false;
+    return true;
+}
+
+int build_batch_plan(ske_engine e, int count, const int32_t* dimx, const int32_t* dimy, const int32_t* angles,
+                     int nangles, int accum, BatchPlan** out) {
+    BatchPlan* p = new BatchPlan();
+    *out = p;
+    p->dimx.assign(dimx, dimx + count);
+    p->dimy.assign(dimy, dimy + count);
+    p->angles.assign(angles, angles + nangles);
+    p->accum = accum;
+    int64_t grid_floats = 0, io_floats = 0;
+    std::vector<char> eligible(count, 1);
+    for (int i = 0; i < count; i++) {
+        const auto key = std::make_pair((int)dimx[i], (int)dimy[i]);
+        auto it = p->geos.find(key);
+        GridGeo* gg = nullptr;
+        if (it == p->geos.end()) {
+            const int rc = make_grid_geo(dimx[i], dimy[i], &gg);
+            p->geos[key] = gg;
+            if (rc != SKE_OK) return rc;
+        } else {
+            gg = it->second;
+        }
+        p->grid_geo.push_back(gg);
+        for (int k = 0; k < nangles; k++)
+            if (!gg->geo.desc[angles[k]].in_width) eligible[i] = 0;
+        const int64_t n = (int64_t)dimx[i] * dimy[i];
+        p->grid_off.push_back(grid_floats);
+        p->io_off.push_back(io_floats);
+        if (eligible[i]) {
+            grid_floats += 12 * n;
+            io_floats += 2 * n;
+        }
+    }
+    SKE_TRY(dev_alloc(&p->d_grid_pool, (size_t)grid_floats));
+    SKE_TRY(dev_alloc(&p->d_io_pool, (size_t)io_floats));
+    // Memory budget of a wave's compact skewed input and output (8 bytes per
+    // valid cell), after the plan's buffers, the sweep's survivor lists and a
+    // reserve for work lists and tables.
+    int lmax_all = 1;
+    for (int i = 0; i < count; i++) lmax_all = std::max(lmax_all, std::max((int)dimx[i], (int)dimy[i]));
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = (size_t)4 << 30;
+    }
+    const size_t lists = sdem_list_bytes(lmax_all, e->num_sms);
+    const size_t have_lists = e->parent ? 0 : e->list_bytes;
+    const size_t reserve = (lists > have_lists ? lists - have_lists : 0) + ((size_t)2 << 30);
+    const int64_t budget = free_b > reserve ? (int64_t)((free_b - reserve) * 0.8) : 0;
+    const int64_t cap_cells = budget / 8;
+    int64_t wave_cells = 0;
+    BatchWave cur;
+    for (int i = 0; i < count; i++) {
+        if (!eligible[i]) {
+            p->fallback.push_back(i);
+            continue;
+        }
+        int64_t c = 0;
+        for (int k = 0; k < nangles; k++) c += p->grid_geo[i]->cells[angles[k]];
+        if (c > cap_cells) {  // not even alone: the per-grid path batches its sectors itself
+            p->fallback.push_back(i);
+            continue;
+        }
+        if (!cur.grids.empty() && wave_cells + c > cap_cells) {
+            p->waves.push_back(std::move(cur));
+            cur = BatchWave();
+            wave_cells = 0;
+        }
+        cur.grids.push_back(i);
+        wave_cells += c;
+    }
+    if (!cur.grids.empty()) p->waves.push_back(std::move(cur));
+    int64_t pool = 0;
+    for (BatchWave& w : p->waves) {
+        SKE_TRY(build_wave(p, w));
+        pool = std::max(pool, w.cells);
+    }
+    SKE_TRY(dev_alloc(&p->d_SI, (size_t)pool));
+    SKE_TRY(dev_alloc(&p->d_SO, (size_t)pool));
+    return SKE_OK;
+}
+
+// The five launches of one wave, in stream order.
+int launch_wave(ske_engine e, BatchPlan* p, BatchWave& w, float povh) {
+    const BatchTables& t = w.tables;
+    {
+        LaunchScope ls(e, "prepare", 1);
+        SKE_TRY(ls.done(launch_prepare_batch(t, w.prep_blocks, e->stream)));
+    }
+    {
+        LaunchScope ls(e, "skew", 1);
+        SKE_TRY(ls.done(launch_skew_batch(t, w.d_items, w.n_items, p->d_SI, e->num_sms, e->stream)));
+    }
+    SdemLaunch a;
+    memset(&a.g, 0, sizeof(a.g));
+    a.b.count = 0;
+    a.SI = p->d_SI;
+    a.SO = p->d_SO;
+    a.stride = 0;
+    a.items = w.d_items;
+    a.n_items = w.n_items;
+    a.counter = e->d_counter;
+    a.povh = povh;
+    a.max_row = std::max(w.max_row, 1);
+    a.counts_only = 0;
+    a.status = e->d_status;
+    a.lists = e->d_lists;
+    a.list_bytes = e->list_bytes;
+    a.batched = 1;
+    a.bt = t;
+    a.lvl0 = p->shape.lvl0;
+    a.lvl1 = p->shape.lvl1;
+    a.ctas_per_sm = p->shape.ctas;
+    {
+        LaunchScope ls(e, "sdem_sweep", w.n_items > 0 ? 1 : 0);
+        SKE_TRY(ls.done(launch_sdem(a, e->num_sms, e->stream)));
+    }
+    {
+        LaunchScope ls(e, "deskew", 1);
+        SKE_TRY(ls.done(launch_deskew_batch(t, w.tiles, p->d_SO, p->accum, e->stream)));
+    }
+    LaunchScope ls(e, "reduce", 1);
+    return ls.done(launch_reduce_batch(t, w.prep_blocks, p->accum, e->stream));
+}
+
+// Tunes the sweep on the first wave (after its skew), once per plan.
+int tune_batch(ske_engine e, BatchPlan* p, BatchWave& w, float povh) {
+    if (p->tuned) return SKE_OK;
+    SdemLaunch a;
+    memset(&a.g, 0, sizeof(a.g));
+    a.b.count = 0;
+    a.SI = p->d_SI;
+    a.SO = p->d_SO;
+    a.stride = 0;
+    a.counter = e->d_counter;
+    a.povh = povh;
+    a.max_row = std::max(w.max_row, 1);
+    a.counts_only = 0;
+    a.status = e->d_status;
+    a.lists = e->d_lists;
+    a.list_bytes = e->list_bytes;
+    a.batched = 1;
+    a.bt = w.tables;
+    SKE_TRY(tune_sweep(e, a, w.items, &p->shape));
+    p->tuned = true;
+    e->last_shape = p->shape;
+    return SKE_OK;
+}
+
+int run_wave(ske_engine e, BatchPlan* p, BatchWave& w, float povh, const float* const* inputs, int in_dev,
+             float* const* outputs, int out_dev) {
+    for (size_t li = 0; li < w.grids.size(); li++) {
+        const int gi = w.grids[li];
+        BatchGrid& G = w.h_grids[li];
+        float* io = p->d_io_pool + p->io_off[gi];
+        if (in_dev) {
+            G.in = inputs[gi];
+        } else {
+            SKE_CK(cudaMemcpyAsync(io, inputs[gi], sizeof(float) * G.n, cudaMemcpyHostToDevice, e->stream));
+            G.in = io;
+        }
+        G.out = out_dev ? outputs[gi] : io + G.n;
+    }
+    SKE_CK(cudaMemcpyAsync(w.d_grids, w.h_grids.data(), sizeof(BatchGrid) * w.h_grids.size(), cudaMemcpyHostToDevice,
+                           e->stream));
+    SKE_TRY(ensure_lists(e, sdem_list_bytes(std::max(w.max_row, 1), e->num_sms)));
+    if (w.graph && w.graph_lists != (const void*)e->d_lists) {  // the lists moved: capture again
+        cudaGraphExecDestroy(w.graph);
+        w.graph = nullptr;
+    }
+    if (w.graph && !e->prof) {
+        SKE_CK(cudaGraphLaunch(w.graph, e->stream));
+        e->launches += 5;
+    } else if (!p->tuned && !(e->flags & SKE_FLAG_NO_TUNE)) {
+        // First run: orientations and skew, tune the sweep on them, then the rest.
+        const BatchTables& t = w.tables;
+        {
+            LaunchScope ls(e, "prepare", 1);
+            SKE_TRY(ls.done(launch_prepare_batch(t, w.prep_blocks, e->stream)));
+        }
+        {
+            LaunchScope ls(e, "skew", 1);
+            SKE_TRY(ls.done(launch_skew_batch(t, w.d_items, w.n_items, p->d_SI, e->num_sms, e->stream)));
+        }
+        SKE_TRY(tune_batch(e, p, w, povh));
+        SKE_TRY(launch_wave(e, p, w, povh));  // again from the orientations (the tuner wrote parts of SO)
+    } else {
+        p->tuned = true;
+        SKE_TRY(launch_wave(e, p, w, povh));
+    }
+    if (!w.graph && !w.graph_failed && !(e->flags & SKE_FLAG_NO_GRAPH) && !e->prof) {
+        // Capture the wave's launches for the next calls (nothing runs now).
+        cudaGraph_t g = nullptr;
+        const int64_t before = e->launches;
+        cudaError_t err = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeRelaxed);
+        int rc = SKE_OK;
+        if (err == cudaSuccess) {
+            rc = launch_wave(e, p, w, povh);
+            err = cudaStreamEndCapture(e->stream, &g);
+        }
+        e->launches = before;
+        if (err == cudaSuccess && rc == SKE_OK && g) err = cudaGraphInstantiate(&w.graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (err != cudaSuccess || rc != SKE_OK || !w.graph) {
+            cudaGetLastError();
+            if (w.graph) cudaGraphExecDestroy(w.graph);
+            w.graph = nullptr;
+            w.graph_failed = true;
+        } else {
+            w.graph_lists = e->d_lists;
+        }
+    }
+    if (!out_dev)
+        for (size_t li = 0; li < w.grids.size(); li++) {
+            const BatchGrid& G = w.h_grids[li];
+            SKE_CK(cudaMemcpyAsync(outputs[w.grids[li]], G.out, sizeof(float) * G.n, cudaMemcpyDeviceToHost,
+                                   e->stream));
+        }
     return SKE_OK;
 }
 
@@ -714,6 +1249,9 @@ int ske_destroy(ske_engine e) {
     e->children.clear();
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
+    destroy_batch_plan(e->batch_plan);
+    e->batch_plan = nullptr;
+    cudaFree(e->d_tune_items);
     if (e->parent) e->d_SI = e->d_SO = nullptr, e->d_P = nullptr, e->d_lists = nullptr;  // borrowed
     for (auto& kv : e->item_plans) cudaFree(kv.second.d_items);
     for (auto& p : e->pending) {
@@ -830,31 +1368,72 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
                          const float* const* inputs, int inputs_on_device, float* const* outputs,
                          int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p) {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
     if (count < 0 || (count > 0 && (!dimx || !dimy || !inputs || !outputs)))
         return fail(SKE_ERR_INVALID, "bad batch arguments");
     if (nangles < 1 || !angles) return fail(SKE_ERR_INVALID, "empty angle list");
+    for (int i = 0; i < nangles; i++)
+        if (angles[i] < 0 || angles[i] >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angles[i]);
+    for (int i = 0; i < count; i++) {
+        if (dimx[i] < 1 || dimy[i] < 1 || dimx[i] > 65535 || dimy[i] > 65535)
+            return fail(SKE_ERR_INVALID, "grid %d: %dx%d outside [1,65535]", i, dimx[i], dimy[i]);
+        if (!inputs[i] || !outputs[i]) return fail(SKE_ERR_INVALID, "grid %d: null input or output", i);
+    }
+    ske_params prm;
+    SKE_TRY(validate_params(p, &prm));
+    SKE_TRY(set_device(e));
+    e->flags = prm.flags;
+    std::vector<int> per_grid;  // grids run one at a time through an engine of their size
+    if (kernel == SKE_KERNEL_SDEM && count > 0) {
+        if (!same_plan(e->batch_plan, count, dimx, dimy, angles, nangles, prm.accum)) {
+            SKE_CK(cudaStreamSynchronize(e->stream));
+            destroy_batch_plan(e->batch_plan);
+            e->batch_plan = nullptr;
+            BatchPlan* np = nullptr;
+            const int rc = build_batch_plan(e, count, dimx, dimy, angles, nangles, prm.accum, &np);
+            if (rc != SKE_OK) {
+                destroy_batch_plan(np);
+                return rc;
+            }
+            e->batch_plan = np;
+        }
+        BatchPlan* bp = e->batch_plan;
+        for (BatchWave& w : bp->waves)
+            SKE_TRY(run_wave(e, bp, w, prm.povh, inputs, inputs_on_device, outputs, outputs_on_device));
+        SKE_TRY(check_status(e));
+        per_grid = bp->fallback;
+    } else {
+        for (int i = 0; i < count; i++) per_grid.push_back(i);
+    }
     // One child engine per other grid size, created on first use and kept with
     // the parent (geometry, work lists and buffers are reused by later batches).
-    int rc = SKE_OK;
-    for (int i = 0; i < count && rc == SKE_OK; i++) {
+    for (int i : per_grid) {
         ske_engine sub = e;
         if (dimx[i] != e->dimx || dimy[i] != e->dimy) {
             const auto key = std::make_pair((int)dimx[i], (int)dimy[i]);
             auto it = e->children.find(key);
             if (it == e->children.end()) {
-                rc = create_engine(&sub, dimx[i], dimy[i], e->device, (void*)e->stream, e);
-                if (rc != SKE_OK) break;
+                SKE_TRY(create_engine(&sub, dimx[i], dimy[i], e->device, (void*)e->stream, e));
                 e->children[key] = sub;
             } else {
                 sub = it->second;
             }
         }
         const int64_t before = sub->launches;
-        rc = ske_run_angles(sub, kernel, inputs[i], inputs_on_device, outputs[i], outputs_on_device, angles, nangles,
-                            p);
+        const int rc = ske_run_angles(sub, kernel, inputs[i], inputs_on_device, outputs[i], outputs_on_device, angles,
+                                      nangles, &prm);
         if (sub != e) e->launches += sub->launches - before;
+        if (rc != SKE_OK) return rc;
     }
-    return rc;
+    return SKE_OK;
+}
+
+int ske_sweep_shape(ske_engine e, int* lvl0, int* lvl1, int* ctas_per_sm) {
+    if (!e || !lvl0 || !lvl1 || !ctas_per_sm) return fail(SKE_ERR_INVALID, "null argument");
+    *lvl0 = e->last_shape.lvl0;
+    *lvl1 = e->last_shape.lvl1;
+    *ctas_per_sm = e->last_shape.ctas;
+    return SKE_OK;
 }
 
 int ske_prepare(ske_engine e, const float* input, int on_device) {

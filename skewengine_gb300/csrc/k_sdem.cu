@@ -467,12 +467,12 @@ __device__ __forceinline__ void visit(Slots& s, int q, float sl, float ring) {
 // row's NaN padding (see visit).  The level runs as a loop over blocks of
 // kUnroll steps: fully unrolled levels overflow the instruction cache.
 template <bool kF0, bool kF1>
-__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0) {
+__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0, int len) {
     const float* p0 = A + (kF0 ? s.x[0] + d0 : s.x[0] - d0);
     const float* p1 = A + (kF1 ? s.x[1] + d0 : s.x[1] - d0);
     const f2 hh = pk(s.h[0], s.h[1]);
 #pragma unroll 1
-    for (int k0 = 0; k0 < kLevel; k0 += kUnroll) {
+    for (int k0 = 0; k0 < len; k0 += kUnroll) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const int d = d0 + k0 + k;
@@ -499,12 +499,14 @@ struct RowOut {
     const int32_t* rfirst;
     const int32_t* rlast;
     int counts_only;
+    bool compact;         // batched run: the row's cells are its own compact row
 };
 
 // Cells that lie in the row's own span of the flat grid (column < dim_i) are
-// always the row's; cells past it may belong to a later row (owner_row).
+// always the row's; cells past it may belong to a later row (owner_row).  A
+// compact row (batched runs) owns all its cells.
 __device__ __forceinline__ bool owns(const RowOut& o, int x) {
-    return o.first + x < o.sd->dim_i || owner_row(*o.sd, o.rfirst, o.rlast, o.rowbase + x) == o.row;
+    return o.compact || o.first + x < o.sd->dim_i || owner_row(*o.sd, o.rfirst, o.rlast, o.rowbase + x) == o.row;
 }
 
 // The maxima arrays of a fast-path row (finite, at most 32 * kB2 cells, so one
@@ -622,10 +624,10 @@ struct RowLists {
 // direction's list, where qi counts the batch's earlier slots of that direction.
 template <bool kF0, bool kF1>
 __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const RowMax& rm, int L, float povh,
-                                            RowLists& rl, int d0, int lane) {
+                                            RowLists& rl, int d0, int len, int lane) {
     constexpr bool kDir[kSlots] = {kF0, kF1};
     const unsigned below = (1u << lane) - 1u;
-    const int dc = d0 + kLevel - 1;  // last step of the level
+    const int dc = d0 + len - 1;  // last step of the level
     Slots s;
 #pragma unroll
     for (int q = 0; q < kSlots; q++) {
@@ -657,7 +659,7 @@ __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const R
     }
     if (kF0 == kF1) rl.used[kF0 ? 0 : 1] += 64;
     else rl.used[0] += 32, rl.used[1] += 32;
-    level_steps<kF0, kF1>(s, A, d0);
+    level_steps<kF0, kF1>(s, A, d0, len);
 
     // Retire finished observers, keep the others for the next level.
 #pragma unroll
@@ -688,8 +690,10 @@ __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const R
 // in slot 0, a backward one in slot 1), so short lists share batches.
 // lists: four lists of L_max entries (forward in/out, backward in/out);
 // cvf, cvb: the two directions' counts, added and scaled at the end.
+// Level lengths: lvl0, then lvl1 (skipped when 0), then kLevel each; all
+// multiples of kUnroll in [kUnroll, kLevel] (lvl1 may be 0).
 __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, float povh, int4* lists,
-                          int max_row, float* cvf, float* cvb, const RowOut& o, int lane) {
+                          int max_row, float* cvf, float* cvb, const RowOut& o, int lane, int lvl0, int lvl1) {
     RowLists rl;
     rl.in[0] = rl.in[1] = nullptr;
     rl.out[0] = lists;
@@ -697,12 +701,15 @@ __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, 
     rl.n[0] = rl.n[1] = L;
     rl.cv[0] = cvf;
     rl.cv[1] = cvb;
-    for (int d0 = 1; rl.n[0] > 0 || rl.n[1] > 0; d0 += kLevel) {
+    int len = lvl0, level = 0;
+    for (int d0 = 1; rl.n[0] > 0 || rl.n[1] > 0; d0 += len, level++) {
+        len = level == 0 ? lvl0 : (level == 1 && lvl1 > 0) ? lvl1 : kLevel;
         rl.used[0] = rl.used[1] = 0;
         rl.made[0] = rl.made[1] = 0;
-        while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true>(A, rm, L, povh, rl, d0, lane);
-        while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false>(A, rm, L, povh, rl, d0, lane);
-        while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1]) sweep_batch<true, false>(A, rm, L, povh, rl, d0, lane);
+        while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true>(A, rm, L, povh, rl, d0, len, lane);
+        while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false>(A, rm, L, povh, rl, d0, len, lane);
+        while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1])
+            sweep_batch<true, false>(A, rm, L, povh, rl, d0, len, lane);
         __syncwarp();  // this level's lists and counts are visible to every lane
 #pragma unroll
         for (int dir = 0; dir < 2; dir++) {
@@ -719,6 +726,9 @@ __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, 
     }
 }
 
+// kBatch: the items are batch_item()s of a batched run over several grids,
+// whose rows are compact rows of the pools SI/SO (kernels.h, BatchGrid).
+template <bool kBatch>
 __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
     extern __shared__ float4 smem4[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -738,26 +748,46 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
         if (lane == 0) idx = atomicAdd(a.counter, 1u);
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if ((int64_t)idx >= a.n_items) break;
-        const Item it = decode(a.items[idx]);
-        const SectorDesc& d = a.g.desc[a.b.angle[it.slot]];
-        const int32_t* first = a.g.first + d.row_off;
-        const int32_t* last = a.g.last + d.row_off;
-        const int f = first[it.row];
-        const int L = last[it.row] - f;
+        const SectorDesc* dp;
+        const int32_t *first, *last;
+        int row;
+        int64_t slot_off = 0;  // the sector's slot in SI/SO (per-engine runs)
+        RowOut o;
+        if (kBatch) {
+            const uint64_t raw = a.items[idx];
+            const BatchSector bs = a.bt.sectors[(int)(raw >> 32)];
+            const BatchGrid& G = a.bt.grids[bs.grid];
+            row = (int)(raw & 0xffffffffu);
+            dp = &G.desc[bs.angle];
+            first = G.first + dp->row_off;
+            last = G.last + dp->row_off;
+            o.out = a.SO;
+            o.rowbase = bs.cells + G.rowoff[dp->row_off + row];
+        } else {
+            const Item it = decode(a.items[idx]);
+            row = it.row;
+            dp = &a.g.desc[a.b.angle[it.slot]];
+            first = a.g.first + dp->row_off;
+            last = a.g.last + dp->row_off;
+            slot_off = it.slot * a.stride;
+            o.out = a.SO + slot_off;
+            o.rowbase = (int64_t)row * dp->dim_i + first[row];
+        }
+        const SectorDesc& d = *dp;
+        const int f = first[row];
+        const int L = last[row] - f;
         if (L > a.max_row || L <= 0) {
             if (lane == 0) atomicExch(a.status, 1);
             continue;
         }
-        RowOut o;
-        o.out = a.SO + it.slot * a.stride;
-        o.rowbase = (int64_t)it.row * d.dim_i + f;
         o.first = f;
-        o.row = it.row;
+        o.row = row;
         o.sd = &d;
         o.rfirst = first;
         o.rlast = last;
         o.counts_only = a.counts_only;
-        const float* src = a.SI + it.slot * a.stride + o.rowbase;
+        o.compact = kBatch;
+        const float* src = a.SI + slot_off + o.rowbase;
         bool ok = true;
         for (int x = lane; x < L; x += 32) {
             const float v = src[x];
@@ -774,7 +804,7 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
             row_maxima(A, L, s128, p128, b16, b128, lane);
             __syncwarp();
             const RowMax rm{s128, p128, b16, b128, nblk(L, kB2)};
-            sweep_row(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane);
+            sweep_row(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane, a.lvl0, a.lvl1);
         } else {
             for (int x = lane; x < L; x += 32) {
                 if (!owns(o, x)) continue;
@@ -903,15 +933,34 @@ size_t sdem_list_bytes(int max_row, int num_sms) {
     return (size_t)num_sms * (size_t)(threads / 32) * kListsPerWarp * (size_t)std::max(max_row, 1) * sizeof(int4);
 }
 
+int sdem_max_ctas_per_sm(const SdemLaunch& a) {
+    const size_t smem = sizeof(float) * (size_t)LLayout(std::max(a.max_row, 1)).total * kLWarps;
+    auto kern = a.batched ? k_sdem<true> : k_sdem<false>;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLWarps * 32, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return per_sm;
+}
+
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (a.n_items == 0) return cudaSuccess;
+    auto level_ok = [](int v) { return v >= kUnroll && v <= kLevel && v % kUnroll == 0; };
+    if (!level_ok(a.lvl0) || (a.lvl1 != 0 && !level_ok(a.lvl1)) || a.ctas_per_sm < 0) return cudaErrorInvalidValue;
     const size_t smem = sizeof(float) * (size_t)LLayout(a.max_row).total * kLWarps;
-    cudaError_t e = cudaFuncSetAttribute(k_sdem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = a.batched ? k_sdem<true> : k_sdem<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sdem, kLWarps * 32, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kLWarps * 32, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (a.ctas_per_sm > 0 && per_sm > a.ctas_per_sm) per_sm = a.ctas_per_sm;
     int64_t blocks = (int64_t)per_sm * num_sms;
     const int64_t need = (a.n_items + kLWarps - 1) / kLWarps;
     if (blocks > need) blocks = need;
@@ -922,7 +971,7 @@ cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (blocks > fit) blocks = fit;
     e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
-    k_sdem<<<(int)blocks, kLWarps * 32, smem, st>>>(a);
+    kern<<<(int)blocks, kLWarps * 32, smem, st>>>(a);
     return cudaGetLastError();
 }
 

@@ -71,6 +71,68 @@ cudaError_t launch_deskew_max(const DevGeometry& g, const TypeLists& tl, const f
 cudaError_t launch_reduce(const float* acc, const float* comp, unsigned used, float* out, int dimx,
                           int dimy, int is_max, int accum_mode, cudaStream_t st);
 
+// --- batched runs over grids of uneven size (k_batch.cu) -------------------
+// Every sector of every grid of a batch keeps only its skewed rows' valid
+// cells, row after row ("compact rows"): row r of a sector starts at
+// cells + rowoff[row_off + r] of the batch's skewed pools and holds
+// last[r] - first[r] cells.  A batch applies only to sectors whose rows stay
+// within dim_i (every sector of a square grid), where a skewed cell belongs to
+// one row and the cells outside the rows are the zeros the reference's deskew
+// reads.
+struct BatchGrid {
+    int dimx, dimy;
+    int64_t n;                 // dimx * dimy
+    const float* in;           // the caller's input (device)
+    float* out;                // the caller's output (device)
+    float* orient;             // 4n: the four orientations
+    float* acc;                // 4n per-type accumulators
+    float* comp;               // 4n Kahan compensations
+    const SectorDesc* desc;    // the grid's 180 sector descriptors
+    const int32_t* target;
+    const float* weight;
+    const int32_t* first;
+    const int32_t* last;
+    const int32_t* rowoff;     // per angle, row r's start within the sector's compact rows
+    unsigned used;             // types that receive a sector
+    int ts_start[4];           // sectors of type t: order[ts_start[t] .. + ts_count[t]]
+    int ts_count[4];
+};
+struct BatchSector {
+    int grid, angle;
+    int64_t cells;  // start of the sector's compact rows in the skewed pools
+};
+// Tables of one wave of a batched run (device pointers).
+struct BatchTables {
+    const BatchGrid* grids;
+    const BatchSector* sectors;
+    const int* order;            // sector indices grouped by (grid, type), accumulation order inside
+    const int64_t* prep_start;   // per grid, its first block of the prepare and fold launches (+ total)
+    const int64_t* tile_start;   // per (grid, type), its first deskew tile (+ total)
+    int n_grids;
+};
+// Work items of a batch's skew and sweep: (sector index << 32) | row, longest
+// row first.
+__host__ __device__ inline uint64_t batch_item(int sector, int row) {
+    return ((uint64_t)(uint32_t)sector << 32) | (uint32_t)row;
+}
+
+// Orientations of every grid of the wave, zeroing their accumulators (and
+// compensations).  blocks: prep_start[n_grids].
+cudaError_t launch_prepare_batch(const BatchTables& t, int64_t blocks, cudaStream_t st);
+// Compact skewed rows of every item.
+cudaError_t launch_skew_batch(const BatchTables& t, const uint64_t* items, int64_t n_items, float* SI, int num_sms,
+                              cudaStream_t st);
+// Deskew + accumulate of every sector of the wave in (grid, type) order;
+// tiles: tile_start[4 * n_grids].
+cudaError_t launch_deskew_batch(const BatchTables& t, int64_t tiles, const float* SO, int accum_mode,
+                                cudaStream_t st);
+// Fold of every grid into its output.  blocks: prep_start[n_grids].
+cudaError_t launch_reduce_batch(const BatchTables& t, int64_t blocks, int accum_mode, cudaStream_t st);
+// Blocks of the prepare and fold launches for one grid.
+int64_t batch_prep_blocks(int dimx, int dimy);
+// Deskew tiles of one orientation of a grid (type t: 0..3).
+int64_t batch_deskew_tiles(int dimx, int dimy, int t);
+
 // --- operators ------------------------------------------------------------
 // Total viewshed sweep (k_sdem.cu).  items: sorted work list (see sdem_items).
 struct SdemLaunch {
@@ -88,9 +150,20 @@ struct SdemLaunch {
     int* status;        // device error word (0 = ok)
     int4* lists;        // survivor-list scratch (compacting sweep only)
     size_t list_bytes;  // its size; at least sdem_list_bytes(max_row, num_sms)
+    // Compacting sweep's level lengths: lvl0 steps, then lvl1 (none when 0),
+    // then 64 each; multiples of 8 in [8, 64] (lvl1 also 0).
+    int lvl0 = 64, lvl1 = 0;
+    int ctas_per_sm = 0;  // compacting sweep: resident CTAs per SM (0 = as many as fit)
+    // Batched runs (compacting sweep only): items are batch_item()s whose rows
+    // are read from and written to the compact pools SI/SO; g, b and stride
+    // are unused.
+    int batched = 0;
+    BatchTables bt{};
 };
 // Compacting sweep (the engine's): items are (slot, row), one per valid row.
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st);
+// Resident CTAs per SM launch_sdem uses for this launch when ctas_per_sm is 0.
+int sdem_max_ctas_per_sm(const SdemLaunch& a);
 // Bytes of survivor-list scratch launch_sdem needs for rows up to max_row cells.
 size_t sdem_list_bytes(int max_row, int num_sms);
 // Work items of a batch for launch_sdem, longest row first: (slot, row).

@@ -67,12 +67,17 @@ def _ptr(x, shape=None, writable=False):
     return C.c_void_p(x.ctypes.data), 0
 
 
-def params(max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference") -> Params:
+FLAG_NO_TUNE = 1   # keep the sweep's built-in shape (skip the autotuner)
+FLAG_NO_GRAPH = 2  # batched runs: plain launches, no captured CUDA graph
+
+
+def params(max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference", flags: int = 0) -> Params:
     p = Params()
     check(load().ske_params_default(C.byref(p)))
     p.max_sector = max_sector
     p.povh = povh
     p.accum = _accum_id(accum)
+    p.flags = int(flags)
     return p
 
 
@@ -140,7 +145,7 @@ class SkewEngine:
 
     # whole run ------------------------------------------------------------
     def run(self, kernel, data, out=None, max_sector: int = 180, povh: float = DEFAULT_POVH,
-            accum="reference", angles=None):
+            accum="reference", angles=None, flags: int = 0):
         """Full sector loop (allocate + execute + reduce of the reference)."""
         shape = (self.dimy, self.dimx)
         pin, in_dev = _ptr(data, shape)
@@ -151,7 +156,7 @@ class SkewEngine:
             else:
                 out = np.empty(shape, np.float32)
         pout, out_dev = _ptr(out, shape, writable=True)
-        prm = params(max_sector, povh, accum)
+        prm = params(max_sector, povh, accum, flags)
         if angles is None:
             check(self._lib.ske_run(self._h, _kernel_id(kernel), pin, in_dev, pout, out_dev, C.byref(prm)))
         else:
@@ -289,6 +294,12 @@ class SkewEngine:
         check(self._lib.ske_profile_get(self._h, name.encode(), C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def sweep_shape(self) -> tuple[int, int, int]:
+        """(lvl0, lvl1, CTAs per SM) of the last viewshed sweep (ske_sweep_shape)."""
+        v = [C.c_int(), C.c_int(), C.c_int()]
+        check(self._lib.ske_sweep_shape(self._h, *[C.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
     def launch_count(self) -> int:
         n = C.c_int64()
         check(self._lib.ske_launch_count(self._h, C.byref(n)))
@@ -304,7 +315,7 @@ def execute(kernel, data, max_sector: int = 180, povh: float = DEFAULT_POVH, acc
 
 
 def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference",
-              device: int = 0, outs=None, angles=None, engine=None):
+              device: int = 0, outs=None, angles=None, engine=None, flags: int = 0):
     """Run one operator over many grids of uneven size (``ske_run_batch``, or
     ``ske_run_batch_angles`` with an angle list).  ``engine``: an existing
     SkewEngine to run on (it keeps the batch's plan and buffers for later calls);
@@ -325,7 +336,7 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
     ous = (C.c_void_p * len(grids))(*[_ptr(o, writable=True)[0].value for o in outs])
     dx = np.array([d[0] for d in dims], np.int32)
     dy = np.array([d[1] for d in dims], np.int32)
-    prm = params(max_sector, povh, accum)
+    prm = params(max_sector, povh, accum, flags)
     eng = engine if engine is not None else SkewEngine(big[0], big[1], device)
     try:
         if angles is None:
