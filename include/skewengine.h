@@ -76,6 +76,13 @@ typedef struct ske_params {
                                counts on the first run (results are identical)   */
 #define SKE_FLAG_NO_GRAPH 2 /* batched runs: launch the kernels of every call
                                directly instead of replaying a captured CUDA graph */
+#define SKE_FLAG_CEPSTRUM_F32 4 /* cepstrum of square images in float32 on the FP32
+                               pipes, skew + operator + max-deskew fused in one
+                               launch per batch: outputs may fall in another
+                               1000-wide bin than the reference's binary64 where a
+                               value sits at a bin edge (a measured, stated rate);
+                               without the flag the cepstrum is the reference's,
+                               bit for bit                                         */
 
 /* Geometry of one sector, computeParams + skewShape (skewEngine.cuh:504-596). */
 typedef struct ske_sector_geometry {

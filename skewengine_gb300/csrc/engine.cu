@@ -50,6 +50,7 @@ int ensure_device_tables(int device) {
     if ((int)g_tables_ready.size() <= device) g_tables_ready.resize(device + 1, 0);
     if (g_tables_ready[device]) return SKE_OK;
     SKE_CK(sdem_init_tables());
+    SKE_CK(cepstrum_f32_init_tables());
     g_tables_ready[device] = 1;
     return SKE_OK;
 }
@@ -100,6 +101,8 @@ struct SweepShape {
 
 struct BatchPlan;
 void destroy_batch_plan(BatchPlan* p);
+struct ImagePlan;
+void destroy_image_plan(ImagePlan* p);
 
 struct ProfEntry {
     double ms = 0;
@@ -168,6 +171,7 @@ struct ske_engine_s {
     // Batched total-viewshed runs: the plan of the last batch (grids, angles,
     // waves, work lists, captured graphs), reused while the batch keeps its shape.
     BatchPlan* batch_plan = nullptr;
+    ImagePlan* image_plan = nullptr;  // float32 cepstrum over batches of square images
     int flags = 0;           // ske_params.flags of the current run
     SweepShape last_shape;   // shape of the last compacting sweep launched
     uint64_t* d_tune_items = nullptr;  // the autotuner's sample of a work list
@@ -637,10 +641,23 @@ int accumulate_angles(ske_engine e, int kernel, const float* input, int input_on
     return SKE_OK;
 }
 
+int run_images_f32(ske_engine e, int count, int dim, const float* const* inputs, int in_dev, float* const* outputs,
+                   int out_dev, const int32_t* angles, int nangles);
+
 int run_angle_list(ske_engine e, int kernel, const float* input, int input_on_device, float* output,
                    int output_on_device, const int32_t* angles, int nangles, const ske_params* p) {
     if (!output) return fail(SKE_ERR_INVALID, "null output");
     if (nangles < 1) return fail(SKE_ERR_INVALID, "empty angle list");
+    if (e && kernel == SKE_KERNEL_CEPSTRUM && p && (p->flags & SKE_FLAG_CEPSTRUM_F32) && e->dimx == e->dimy) {
+        if (!input) return fail(SKE_ERR_INVALID, "null input");
+        for (int i = 0; i < nangles; i++)
+            if (!angles || angles[i] < 0 || angles[i] >= kMaxSectors) return fail(SKE_ERR_INVALID, "bad angle list");
+        ske_params chk;
+        SKE_TRY(validate_params(p, &chk));
+        SKE_TRY(set_device(e));
+        e->flags = chk.flags;
+        return run_images_f32(e, 1, e->dimx, &input, input_on_device, &output, output_on_device, angles, nangles);
+    }
     ske_params prm;
     SKE_TRY(accumulate_angles(e, kernel, input, input_on_device, angles, nangles, p, &prm));
     SKE_TRY(run_reduce(e, output, output_on_device, kernel == SKE_KERNEL_CEPSTRUM, prm.accum));
@@ -1076,6 +1093,135 @@ int run_wave(ske_engine e, BatchPlan* p, BatchWave& w, float povh, const float* 
     return SKE_OK;
 }
 
+// ---- float32 cepstrum over batches of square images --------------------------
+// Every image of a batch has the same side; per wave of images (as many as the
+// memory budget holds) three launches: orientations, the fused float32
+// cepstrum sector loop (k_cepstrum_f32.cu) and the max fold.
+
+struct ImagePlan {
+    int dim = 0, count = 0, wave = 0;
+    std::vector<int> angles;
+    GridGeo* geo = nullptr;
+    TypeLists tl;
+    unsigned used = 0;
+    float* d_pool = nullptr;  // per wave slot: orientations 4n + accumulators 4n
+    float* d_io = nullptr;    // per wave slot: input n + output n (host buffers)
+    std::vector<BatchGrid> h_grids;
+    BatchGrid* d_grids = nullptr;
+    int64_t* d_prep = nullptr;
+};
+
+void destroy_image_plan(ImagePlan* p) {
+    if (!p) return;
+    if (p->geo) {
+        GridGeo* g = p->geo;
+        void* bufs[] = {g->d_desc, g->d_target, g->d_first, g->d_last, g->d_rowoff, g->d_weight};
+        for (void* b : bufs) cudaFree(b);
+        delete g;
+    }
+    void* bufs[] = {p->d_pool, p->d_io, p->d_grids, p->d_prep};
+    for (void* b : bufs) cudaFree(b);
+    delete p;
+}
+
+int build_image_plan(int dim, int count, const int32_t* angles, int nangles, ImagePlan** out) {
+    ImagePlan* p = new ImagePlan();
+    *out = p;
+    p->dim = dim;
+    p->count = count;
+    p->angles.assign(angles, angles + nangles);
+    SKE_TRY(make_grid_geo(dim, dim, &p->geo));
+    memset(&p->tl, 0, sizeof(p->tl));
+    for (int k = 0; k < nangles; k++) {
+        const int t = p->geo->geo.desc[angles[k]].type;
+        p->tl.angle[t][p->tl.count[t]] = angles[k];
+        p->tl.slot[t][p->tl.count[t]] = k;
+        p->tl.count[t]++;
+        p->used |= 1u << t;
+    }
+    const int64_t n = (int64_t)dim * dim;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+        cudaGetLastError();
+        free_b = (size_t)4 << 30;
+    }
+    const int64_t per = 10 * n * (int64_t)sizeof(float);
+    const int64_t budget = free_b > ((size_t)1 << 30) ? (int64_t)((free_b - ((size_t)1 << 30)) / 2) : per;
+    p->wave = (int)std::max<int64_t>(1, std::min<int64_t>(count, budget / per));
+    SKE_TRY(dev_alloc(&p->d_pool, (size_t)(8 * n) * p->wave));
+    SKE_TRY(dev_alloc(&p->d_io, (size_t)(2 * n) * p->wave));
+    SKE_TRY(dev_alloc(&p->d_grids, (size_t)p->wave));
+    std::vector<int64_t> prep(p->wave + 1);
+    for (int k = 0; k <= p->wave; k++) prep[k] = k * batch_prep_blocks(dim, dim);
+    SKE_TRY(upload_vec(&p->d_prep, prep));
+    p->h_grids.resize(p->wave);
+    for (int k = 0; k < p->wave; k++) {
+        BatchGrid& G = p->h_grids[k];
+        memset(&G, 0, sizeof(G));
+        G.dimx = G.dimy = dim;
+        G.n = n;
+        G.orient = p->d_pool + (int64_t)k * 8 * n;
+        G.acc = G.orient + 4 * n;
+        G.comp = nullptr;
+        G.used = p->used;
+    }
+    return SKE_OK;
+}
+
+int run_images_f32(ske_engine e, int count, int dim, const float* const* inputs, int in_dev, float* const* outputs,
+                   int out_dev, const int32_t* angles, int nangles) {
+    ImagePlan* p = e->image_plan;
+    if (!p || p->dim != dim || p->count != count || p->angles != std::vector<int>(angles, angles + nangles)) {
+        SKE_CK(cudaStreamSynchronize(e->stream));
+        destroy_image_plan(p);
+        e->image_plan = nullptr;
+        ImagePlan* np = nullptr;
+        const int rc = build_image_plan(dim, count, angles, nangles, &np);
+        if (rc != SKE_OK) {
+            destroy_image_plan(np);
+            return rc;
+        }
+        e->image_plan = p = np;
+    }
+    const int64_t n = (int64_t)dim * dim;
+    const DevGeometry g{p->geo->d_desc, p->geo->d_target, p->geo->d_weight, p->geo->d_first, p->geo->d_last};
+    for (int w0 = 0; w0 < count; w0 += p->wave) {
+        const int nw = std::min(p->wave, count - w0);
+        for (int k = 0; k < nw; k++) {
+            BatchGrid& G = p->h_grids[k];
+            float* io = p->d_io + (int64_t)k * 2 * n;
+            if (in_dev) {
+                G.in = inputs[w0 + k];
+            } else {
+                SKE_CK(cudaMemcpyAsync(io, inputs[w0 + k], sizeof(float) * n, cudaMemcpyHostToDevice, e->stream));
+                G.in = io;
+            }
+            G.out = out_dev ? outputs[w0 + k] : io + n;
+        }
+        SKE_CK(cudaMemcpyAsync(p->d_grids, p->h_grids.data(), sizeof(BatchGrid) * nw, cudaMemcpyHostToDevice,
+                               e->stream));
+        const BatchTables t{p->d_grids, nullptr, nullptr, p->d_prep, nullptr, nw};
+        const int64_t blocks = (int64_t)nw * batch_prep_blocks(dim, dim);
+        {
+            LaunchScope ls(e, "prepare", 1);
+            SKE_TRY(ls.done(launch_prepare_batch(t, blocks, e->stream)));
+        }
+        {
+            LaunchScope ls(e, "cepstrum", 1);
+            SKE_TRY(ls.done(launch_cepstrum_f32(t, nw, g, p->tl, dim, e->stream)));
+        }
+        {
+            LaunchScope ls(e, "reduce", 1);
+            SKE_TRY(ls.done(launch_reduce_batch(t, blocks, SKE_ACCUM_REFERENCE, e->stream, 1)));
+        }
+        if (!out_dev)
+            for (int k = 0; k < nw; k++)
+                SKE_CK(cudaMemcpyAsync(outputs[w0 + k], p->h_grids[k].out, sizeof(float) * n, cudaMemcpyDeviceToHost,
+                                       e->stream));
+    }
+    return check_status(e);
+}
+
 }  // namespace
 
 extern "C" {
@@ -1251,6 +1397,8 @@ int ske_destroy(ske_engine e) {
     if (e->stream) cudaStreamSynchronize(e->stream);
     destroy_batch_plan(e->batch_plan);
     e->batch_plan = nullptr;
+    destroy_image_plan(e->image_plan);
+    e->image_plan = nullptr;
     cudaFree(e->d_tune_items);
     if (e->parent) e->d_SI = e->d_SO = nullptr, e->d_P = nullptr, e->d_lists = nullptr;  // borrowed
     for (auto& kv : e->item_plans) cudaFree(kv.second.d_items);
@@ -1384,7 +1532,21 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
     SKE_TRY(set_device(e));
     e->flags = prm.flags;
     std::vector<int> per_grid;  // grids run one at a time through an engine of their size
-    if (kernel == SKE_KERNEL_SDEM && count > 0) {
+    if (kernel == SKE_KERNEL_CEPSTRUM && (prm.flags & SKE_FLAG_CEPSTRUM_F32) && count > 0) {
+        // Runs of consecutive square images of one side share a launch sequence.
+        int i = 0;
+        while (i < count) {
+            if (dimx[i] != dimy[i]) {
+                per_grid.push_back(i++);
+                continue;
+            }
+            int k = i + 1;
+            while (k < count && dimx[k] == dimx[i] && dimy[k] == dimx[i]) k++;
+            SKE_TRY(run_images_f32(e, k - i, dimx[i], inputs + i, inputs_on_device, outputs + i, outputs_on_device,
+                                   angles, nangles));
+            i = k;
+        }
+    } else if (kernel == SKE_KERNEL_SDEM && count > 0) {
         if (!same_plan(e->batch_plan, count, dimx, dimy, angles, nangles, prm.accum)) {
             SKE_CK(cudaStreamSynchronize(e->stream));
             destroy_batch_plan(e->batch_plan);

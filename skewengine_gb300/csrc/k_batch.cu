@@ -60,8 +60,10 @@ __global__ void __launch_bounds__(256) k_prepare_batch(BatchTables T) {
             o3[p3] = v;
             G.acc[p0] = 0.0f;
             G.acc[3 * n + p3] = 0.0f;
-            G.comp[p0] = 0.0f;
-            G.comp[3 * n + p3] = 0.0f;
+            if (G.comp) {
+                G.comp[p0] = 0.0f;
+                G.comp[3 * n + p3] = 0.0f;
+            }
         }
     }
     __syncthreads();
@@ -75,8 +77,10 @@ __global__ void __launch_bounds__(256) k_prepare_batch(BatchTables T) {
             o2[p2] = v;
             G.acc[n + p1] = 0.0f;
             G.acc[2 * n + p2] = 0.0f;
-            G.comp[n + p1] = 0.0f;
-            G.comp[2 * n + p2] = 0.0f;
+            if (G.comp) {
+                G.comp[n + p1] = 0.0f;
+                G.comp[2 * n + p2] = 0.0f;
+            }
         }
     }
 }
@@ -216,8 +220,9 @@ __global__ void __launch_bounds__(256, kMode == kKahan ? 2 : 4)
 }
 
 // Fold (skewEngine.cuh:862-914, as k_reduce) of one 32 x 32 output tile of a
-// grid: the used types in type order, compensated sums in double for Kahan.
-__global__ void __launch_bounds__(256) k_reduce_batch(BatchTables T, int kahan) {
+// grid: the used types in type order, compensated sums in double for Kahan,
+// the maximum for the cepstrum.
+__global__ void __launch_bounds__(256) k_reduce_batch(BatchTables T, int kahan, int is_max) {
     const int g = find_entry(T.prep_start, T.n_grids, blockIdx.x);
     const BatchGrid& G = T.grids[g];
     const int dimx = G.dimx, dimy = G.dimy;
@@ -232,7 +237,15 @@ __global__ void __launch_bounds__(256) k_reduce_batch(BatchTables T, int kahan) 
         const int ci = dimy - 1 - i, cj = dimx - 1 - j;
         const int64_t idx = (int64_t)i * dimx + j;
         const int64_t at[4] = {idx, (int64_t)cj * dimy + ci, (int64_t)j * dimy + ci, (int64_t)i * dimx + cj};
-        if (kahan) {
+        if (is_max) {
+            float o = 0.0f;
+            for (int t = 0; t < 4; t++)
+                if (used & (1u << t)) {
+                    const float v = G.acc[t * n + at[t]];
+                    o = o > v ? o : v;
+                }
+            G.out[idx] = o;
+        } else if (kahan) {
             double sum = 0.0;
             for (int t = 0; t < 4; t++)
                 if (used & (1u << t)) sum += (double)G.acc[t * n + at[t]] - (double)G.comp[t * n + at[t]];
@@ -283,10 +296,10 @@ cudaError_t launch_deskew_batch(const BatchTables& t, int64_t tiles, const float
     return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_batch(const BatchTables& t, int64_t blocks, int accum_mode, cudaStream_t st) {
+cudaError_t launch_reduce_batch(const BatchTables& t, int64_t blocks, int accum_mode, cudaStream_t st, int is_max) {
     if (blocks <= 0) return cudaSuccess;
     if (blocks > 0x7fffffff) return cudaErrorInvalidValue;
-    k_reduce_batch<<<(unsigned)blocks, dim3(kTile, 8), 0, st>>>(t, accum_mode == kAccumKahan);
+    k_reduce_batch<<<(unsigned)blocks, dim3(kTile, 8), 0, st>>>(t, accum_mode == kAccumKahan, is_max);
     return cudaGetLastError();
 }
 

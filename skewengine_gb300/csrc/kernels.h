@@ -117,7 +117,7 @@ __host__ __device__ inline uint64_t batch_item(int sector, int row) {
 }
 
 // Orientations of every grid of the wave, zeroing their accumulators (and
-// compensations).  blocks: prep_start[n_grids].
+// compensations, where comp is set).  blocks: prep_start[n_grids].
 cudaError_t launch_prepare_batch(const BatchTables& t, int64_t blocks, cudaStream_t st);
 // Compact skewed rows of every item.
 cudaError_t launch_skew_batch(const BatchTables& t, const uint64_t* items, int64_t n_items, float* SI, int num_sms,
@@ -126,8 +126,10 @@ cudaError_t launch_skew_batch(const BatchTables& t, const uint64_t* items, int64
 // tiles: tile_start[4 * n_grids].
 cudaError_t launch_deskew_batch(const BatchTables& t, int64_t tiles, const float* SO, int accum_mode,
                                 cudaStream_t st);
-// Fold of every grid into its output.  blocks: prep_start[n_grids].
-cudaError_t launch_reduce_batch(const BatchTables& t, int64_t blocks, int accum_mode, cudaStream_t st);
+// Fold of every grid into its output (the maximum with is_max).  blocks:
+// prep_start[n_grids].
+cudaError_t launch_reduce_batch(const BatchTables& t, int64_t blocks, int accum_mode, cudaStream_t st,
+                                int is_max = 0);
 // Blocks of the prepare and fold launches for one grid.
 int64_t batch_prep_blocks(int dimx, int dimy);
 // Deskew tiles of one orientation of a grid (type t: 0..3).
@@ -190,6 +192,14 @@ cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, 
 cudaError_t launch_local_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
                                int max_H, int max_cols, const double* gauss, const double* taper, const double* tw64,
                                cudaStream_t st);
+
+// Cepstrum blur estimation in float32, fused over the sector loop, for a batch
+// of square images of side dim (k_cepstrum_f32.cu): orientations from
+// t.grids[b].orient, max-accumulators into t.grids[b].acc (initial values
+// read), every sector of tl in its type's order.
+cudaError_t launch_cepstrum_f32(const BatchTables& t, int images, const DevGeometry& g, const TypeLists& tl, int dim,
+                                cudaStream_t st);
+cudaError_t cepstrum_f32_init_tables();
 
 // Cepstrum blur estimation (k_cepstrum.cu).
 cudaError_t launch_cepstrum(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
