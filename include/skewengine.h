@@ -239,6 +239,12 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
  * (0 = as many as fit), as chosen by the autotuner.  No reference counterpart. */
 int ske_sweep_shape(ske_engine e, int* lvl0, int* lvl1, int* ctas_per_sm);
 
+/* Fix the viewshed sweep's shape for this engine's later runs instead of the
+ * autotuner's choice: lvl0 and lvl1 of 16, 32, 48 or 64 steps (lvl1 0: none),
+ * ctas_per_sm 0 = as many as fit.  lvl0 = 0 returns the choice to the
+ * autotuner.  Results do not depend on the shape.  No reference counterpart. */
+int ske_set_sweep_shape(ske_engine e, int lvl0, int lvl1, int ctas_per_sm);
+
 /* Per-sector API (drop-in for the reference's skew/kernel/deskew/reduce
  * methods driven from main.cu:147-164) ----------------------------------------*/
 

@@ -174,6 +174,7 @@ struct ske_engine_s {
     ImagePlan* image_plan = nullptr;  // float32 cepstrum over batches of square images
     int flags = 0;           // ske_params.flags of the current run
     SweepShape last_shape;   // shape of the last compacting sweep launched
+    SweepShape fixed_shape{0, 0, 0};  // ske_set_sweep_shape (lvl0 0: the autotuner decides)
     uint64_t* d_tune_items = nullptr;  // the autotuner's sample of a work list
     size_t tune_items_cap = 0;
 };
@@ -370,6 +371,10 @@ std::map<std::pair<int, int>, SweepShape> g_tuned;  // (device, max_row / 256) -
 
 int tune_sweep(ske_engine e, const SdemLaunch& base, const std::vector<uint64_t>& items, SweepShape* out) {
     *out = SweepShape();
+    if (e->fixed_shape.lvl0 > 0) {
+        *out = e->fixed_shape;
+        return SKE_OK;
+    }
     if (e->flags & SKE_FLAG_NO_TUNE) return SKE_OK;
     const auto key = std::make_pair(e->device, (base.max_row + 255) / 256);
     std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -678,10 +683,12 @@ struct GridGeo {
     int dimx = 0, dimy = 0;
     Geometry geo;
     std::vector<int32_t> rowoff;  // per skewed row: start within its sector's compact rows
+    std::vector<int4> rowtab;     // per skewed row: {first, last, rowoff, 0}
     std::vector<int64_t> cells;   // per angle: valid cells (compact size)
     SectorDesc* d_desc = nullptr;
     int32_t *d_target = nullptr, *d_first = nullptr, *d_last = nullptr, *d_rowoff = nullptr;
     float* d_weight = nullptr;
+    int4* d_rowtab = nullptr;
 };
 
 struct BatchWave {
@@ -689,12 +696,13 @@ struct BatchWave {
     std::vector<BatchGrid> h_grids; // host copies of the wave's grid table (in/out set per call)
     BatchGrid* d_grids = nullptr;
     BatchSector* d_sectors = nullptr;
-    int* d_order = nullptr;
+    SectorRef* d_refs = nullptr;
     int64_t* d_prep = nullptr;
     int64_t* d_tiles = nullptr;
+    int64_t* d_skew = nullptr;
     uint64_t* d_items = nullptr;
     std::vector<uint64_t> items;
-    int64_t n_items = 0, prep_blocks = 0, tiles = 0, cells = 0;
+    int64_t n_items = 0, prep_blocks = 0, tiles = 0, cells = 0, skew_blocks = 0;
     int max_row = 0;
     BatchTables tables{};
     cudaGraphExec_t graph = nullptr;
@@ -719,7 +727,7 @@ struct BatchPlan {
 
 void free_wave(BatchWave& w) {
     if (w.graph) cudaGraphExecDestroy(w.graph);
-    void* bufs[] = {w.d_grids, w.d_sectors, w.d_order, w.d_prep, w.d_tiles, w.d_items};
+    void* bufs[] = {w.d_grids, w.d_sectors, w.d_refs, w.d_prep, w.d_tiles, w.d_skew, w.d_items};
     for (void* b : bufs) cudaFree(b);
     w = BatchWave();
 }
@@ -729,7 +737,7 @@ void destroy_batch_plan(BatchPlan* p) {
     for (BatchWave& w : p->waves) free_wave(w);
     for (auto& kv : p->geos) {
         GridGeo* g = kv.second;
-        void* bufs[] = {g->d_desc, g->d_target, g->d_first, g->d_last, g->d_rowoff, g->d_weight};
+        void* bufs[] = {g->d_desc, g->d_target, g->d_first, g->d_last, g->d_rowoff, g->d_weight, g->d_rowtab};
         for (void* b : bufs) cudaFree(b);
         delete g;
     }
@@ -754,6 +762,7 @@ int make_grid_geo(int dimx, int dimy, GridGeo** out) {
     g->dimy = dimy;
     build_geometry(dimx, dimy, g->geo);
     g->rowoff.assign(g->geo.first.size(), 0);
+    g->rowtab.assign(g->geo.first.size(), make_int4(0, 0, 0, 0));
     g->cells.assign(g->geo.desc.size(), 0);
     for (size_t a = 0; a < g->geo.desc.size(); a++) {
         SectorDesc& d = g->geo.desc[a];
@@ -762,6 +771,7 @@ int make_grid_geo(int dimx, int dimy, GridGeo** out) {
         for (int r = 0; r < d.H; r++) {
             const int64_t k = d.row_off + r;
             g->rowoff[k] = (int32_t)c;
+            g->rowtab[k] = make_int4(g->geo.first[k], g->geo.last[k], (int)c, 0);
             const int L = g->geo.last[k] - g->geo.first[k];
             if (L > 0) c += L;
             if (g->geo.last[k] > d.dim_i) d.in_width = 0;
@@ -774,6 +784,7 @@ int make_grid_geo(int dimx, int dimy, GridGeo** out) {
     SKE_TRY(upload_vec(&g->d_first, g->geo.first));
     SKE_TRY(upload_vec(&g->d_last, g->geo.last));
     SKE_TRY(upload_vec(&g->d_rowoff, g->rowoff));
+    SKE_TRY(upload_vec(&g->d_rowtab, g->rowtab));
     return SKE_OK;
 }
 
@@ -782,8 +793,8 @@ int make_grid_geo(int dimx, int dimy, GridGeo** out) {
 // work list (every valid row, longest first).
 int build_wave(BatchPlan* p, BatchWave& w) {
     std::vector<BatchSector> secs;
-    std::vector<int> order;
-    std::vector<int64_t> prep(1, 0), tiles(1, 0);
+    std::vector<SectorRef> refs;
+    std::vector<int64_t> prep(1, 0), tiles(1, 0), skew(1, 0);
     int64_t cells = 0;
     int lmax = 0;
     w.h_grids.clear();
@@ -804,19 +815,23 @@ int build_wave(BatchPlan* p, BatchWave& w) {
         G.first = gg->d_first;
         G.last = gg->d_last;
         G.rowoff = gg->d_rowoff;
+        G.rowtab = gg->d_rowtab;
         const int s0 = (int)secs.size();
         for (int a : p->angles) {
             secs.push_back(BatchSector{(int)li, a, cells});
             cells += gg->cells[a];
             const SectorDesc& d = gg->geo.desc[a];
+            skew.push_back(skew.back() + batch_skew_blocks(d.dim_i, d.H));
             for (int r = 0; r < d.H; r++)
                 lmax = std::max(lmax, gg->geo.last[d.row_off + r] - gg->geo.first[d.row_off + r]);
         }
         for (int t = 0; t < 4; t++) {
-            G.ts_start[t] = (int)order.size();
-            for (int s = s0; s < (int)secs.size(); s++)
-                if (gg->geo.desc[secs[s].angle].type == t) order.push_back(s);
-            G.ts_count[t] = (int)order.size() - G.ts_start[t];
+            G.ts_start[t] = (int)refs.size();
+            for (int s = s0; s < (int)secs.size(); s++) {
+                const SectorDesc& d = gg->geo.desc[secs[s].angle];
+                if (d.type == t) refs.push_back(SectorRef{secs[s].cells, d.col_off, d.row_off, d.H, d.angle});
+            }
+            G.ts_count[t] = (int)refs.size() - G.ts_start[t];
             if (G.ts_count[t] > 0) G.used |= 1u << t;
             tiles.push_back(tiles.back() + (G.ts_count[t] > 0 ? batch_deskew_tiles(G.dimx, G.dimy, t) : 0));
         }
@@ -853,13 +868,16 @@ int build_wave(BatchPlan* p, BatchWave& w) {
     w.cells = cells;
     w.prep_blocks = prep.back();
     w.tiles = tiles.back();
+    w.skew_blocks = skew.back();
     SKE_TRY(upload_vec(&w.d_grids, w.h_grids));
     SKE_TRY(upload_vec(&w.d_sectors, secs));
-    SKE_TRY(upload_vec(&w.d_order, order));
+    SKE_TRY(upload_vec(&w.d_refs, refs));
     SKE_TRY(upload_vec(&w.d_prep, prep));
     SKE_TRY(upload_vec(&w.d_tiles, tiles));
+    SKE_TRY(upload_vec(&w.d_skew, skew));
     SKE_TRY(upload_vec(&w.d_items, w.items));
-    w.tables = BatchTables{w.d_grids, w.d_sectors, w.d_order, w.d_prep, w.d_tiles, (int)w.grids.size()};
+    w.tables = BatchTables{w.d_grids, w.d_sectors, w.d_refs,  w.d_prep, w.d_tiles,
+                           w.d_skew,  (int)w.grids.size(), (int)secs.size()};
     return SKE_OK;
 }
 
@@ -963,7 +981,7 @@ int launch_wave(ske_engine e, BatchPlan* p, BatchWave& w, float povh) {
     }
     {
         LaunchScope ls(e, "skew", 1);
-        SKE_TRY(ls.done(launch_skew_batch(t, w.d_items, w.n_items, p->d_SI, e->num_sms, e->stream)));
+        SKE_TRY(ls.done(launch_skew_batch(t, w.skew_blocks, p->d_SI, e->stream)));
     }
     SdemLaunch a;
     memset(&a.g, 0, sizeof(a.g));
@@ -1054,7 +1072,7 @@ int run_wave(ske_engine e, BatchPlan* p, BatchWave& w, float povh, const float* 
         }
         {
             LaunchScope ls(e, "skew", 1);
-            SKE_TRY(ls.done(launch_skew_batch(t, w.d_items, w.n_items, p->d_SI, e->num_sms, e->stream)));
+            SKE_TRY(ls.done(launch_skew_batch(t, w.skew_blocks, p->d_SI, e->stream)));
         }
         SKE_TRY(tune_batch(e, p, w, povh));
         SKE_TRY(launch_wave(e, p, w, povh));  // again from the orientations (the tuner wrote parts of SO)
@@ -1115,7 +1133,7 @@ void destroy_image_plan(ImagePlan* p) {
     if (!p) return;
     if (p->geo) {
         GridGeo* g = p->geo;
-        void* bufs[] = {g->d_desc, g->d_target, g->d_first, g->d_last, g->d_rowoff, g->d_weight};
+        void* bufs[] = {g->d_desc, g->d_target, g->d_first, g->d_last, g->d_rowoff, g->d_weight, g->d_rowtab};
         for (void* b : bufs) cudaFree(b);
         delete g;
     }
@@ -1200,7 +1218,7 @@ int run_images_f32(ske_engine e, int count, int dim, const float* const* inputs,
         }
         SKE_CK(cudaMemcpyAsync(p->d_grids, p->h_grids.data(), sizeof(BatchGrid) * nw, cudaMemcpyHostToDevice,
                                e->stream));
-        const BatchTables t{p->d_grids, nullptr, nullptr, p->d_prep, nullptr, nw};
+        const BatchTables t{p->d_grids, nullptr, nullptr, p->d_prep, nullptr, nullptr, nw, 0};
         const int64_t blocks = (int64_t)nw * batch_prep_blocks(dim, dim);
         {
             LaunchScope ls(e, "prepare", 1);
@@ -1587,6 +1605,22 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
         if (sub != e) e->launches += sub->launches - before;
         if (rc != SKE_OK) return rc;
     }
+    return SKE_OK;
+}
+
+int ske_set_sweep_shape(ske_engine e, int lvl0, int lvl1, int ctas_per_sm) {
+    if (!e) return fail(SKE_ERR_INVALID, "null engine");
+    auto ok = [](int v) { return v == 16 || v == 32 || v == 48 || v == 64; };
+    if (lvl0 != 0 && (!ok(lvl0) || (lvl1 != 0 && !ok(lvl1)) || ctas_per_sm < 0))
+        return fail(SKE_ERR_INVALID, "sweep shape: levels of 16, 32, 48 or 64 steps (lvl1 also 0), CTAs >= 0");
+    e->fixed_shape = lvl0 == 0 ? SweepShape{0, 0, 0} : SweepShape{lvl0, lvl1, ctas_per_sm};
+    if (e->batch_plan) e->batch_plan->tuned = false;  // the next batch call applies it (and captures again)
+    if (e->batch_plan)
+        for (BatchWave& w : e->batch_plan->waves)
+            if (w.graph) {
+                cudaGraphExecDestroy(w.graph);
+                w.graph = nullptr;
+            }
     return SKE_OK;
 }
 

@@ -19,8 +19,7 @@ namespace ske {
 namespace {
 
 constexpr int kTile = 32;
-constexpr int kRows = 64;              // deskew tile rows
-constexpr int kBand = kRows + 34;      // rows + 1 + max column drift over 32 columns (+1)
+constexpr int kRows = 32;              // deskew tile rows (8 warps x 4 rows)
 enum { kAdd = 0, kKahan = 1 };
 
 // Largest k in [0, n) with start[k] <= b (start[n] is the total, above b).
@@ -85,47 +84,67 @@ __global__ void __launch_bounds__(256) k_prepare_batch(BatchTables T) {
     }
 }
 
-// Compact skewed rows: a warp per work item (sector, row) writes the row's
-// valid cells, each the reference scatter's two contributions gathered
-// (skew_gather, skewEngine.cuh:615-620).
-__global__ void __launch_bounds__(256) k_skew_batch(BatchTables T, const uint64_t* __restrict__ items,
-                                                    int64_t n_items, float* __restrict__ SI) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n_items; w += nwarps) {
-        const uint64_t it = items[w];
-        const int sidx = (int)(it >> 32), row = (int)(it & 0xffffffffu);
-        const BatchSector bs = T.sectors[sidx];
-        const BatchGrid& G = T.grids[bs.grid];
-        const SectorDesc d = G.desc[bs.angle];
-        const int f = G.first[d.row_off + row];
-        const int L = G.last[d.row_off + row] - f;
-        const int32_t* tg = G.target + d.col_off;
-        const float* wg = G.weight + d.col_off;
-        const float* src = G.orient + (int64_t)d.type * G.n;
-        float* o = SI + bs.cells + G.rowoff[d.row_off + row];
-        for (int x = lane; x < L; x += 32) o[x] = skew_gather(d, tg, wg, src, row, f + x);
+// Compact skewed rows, streamed by column as k_skew does: a thread owns column
+// c of kSkewRows consecutive skewed rows of one sector.  Cell (r, c) is the
+// reference scatter's two contributions gathered (skew_gather,
+// skewEngine.cuh:615-620): w*x[r-t-1][c] + (1-w)*x[r-t][c] onto 0; the
+// column's target and weight stay in registers and row r's second source value
+// is row r+1's first, so a cell costs one load.  Row r's valid cells
+// [first, last) go to the row's compact segment, so a block's stores to one row
+// are consecutive.
+constexpr int kSkewRows = 32;
+constexpr int kSkewCols = 256;
+
+__global__ void __launch_bounds__(kSkewCols) k_skew_batch(BatchTables T, float* __restrict__ SI) {
+    __shared__ int4 meta[kSkewRows];
+    const int sidx = find_entry(T.skew_start, T.n_sectors, blockIdx.x);
+    const BatchSector bs = T.sectors[sidx];
+    const BatchGrid& G = T.grids[bs.grid];
+    const SectorDesc& d = G.desc[bs.angle];
+    const int dim_i = d.dim_i, dim_o = d.dim_o, H = d.H;
+    const int64_t lb = blockIdx.x - T.skew_start[sidx];
+    const int bx_n = (dim_i + kSkewCols - 1) / kSkewCols;
+    const int c = (int)(lb % bx_n) * kSkewCols + threadIdx.x;
+    const int r0 = (int)(lb / bx_n) * kSkewRows;
+    const int r1 = min(r0 + kSkewRows, H);
+    if (threadIdx.x < r1 - r0) meta[threadIdx.x] = G.rowtab[d.row_off + r0 + threadIdx.x];
+    __syncthreads();
+    if (c >= dim_i) return;
+    const float* src = G.orient + (int64_t)d.type * G.n;
+    const int t = G.target[d.col_off + c];
+    const float w = G.weight[d.col_off + c], w1 = __fsub_rn(1.0f, w);
+    int i0 = r0 - t - 1;  // source row of the w term
+    const float* p = src + ((int64_t)i0 * dim_i + c);
+    float a = (unsigned)i0 < (unsigned)dim_o ? p[0] : 0.0f;
+    float* out = SI + bs.cells;
+    for (int r = r0; r < r1; r++) {
+        const bool v0 = (unsigned)i0 < (unsigned)dim_o, v1 = (unsigned)(i0 + 1) < (unsigned)dim_o;
+        const float bv = v1 ? p[dim_i] : 0.0f;
+        const int4 m = meta[r - r0];
+        if (c >= m.x && c < m.y) {
+            float acc = 0.0f;
+            acc = v0 ? __fadd_rn(acc, __fmul_rn(w, a)) : acc;
+            acc = v1 ? __fadd_rn(acc, __fmul_rn(w1, bv)) : acc;
+            out[m.z + (c - m.x)] = acc;
+        }
+        a = bv;
+        i0++;
+        p += dim_i;
     }
 }
 
-// Skewed output cell (r, c) of a sector in compact rows; zero outside the rows.
-__device__ __forceinline__ float compact_cell(const SectorDesc& d, const int32_t* __restrict__ first,
-                                              const int32_t* __restrict__ last, const int32_t* __restrict__ rowoff,
-                                              const float* __restrict__ so, int r, int c) {
-    if (r >= d.H) return 0.0f;
-    const int f = first[r];
-    return (c >= f && c < last[r]) ? so[rowoff[r] + (c - f)] : 0.0f;
-}
-
-// Deskew + accumulate (skewEngine.cuh:772-792) of one 64 x 32 accumulator tile
-// of one orientation of one grid over that type's sectors in accumulation
-// order, as k_deskew: the tile's accumulators stay in registers; per sector the
-// band of skewed rows it needs is staged in shared memory (zeros outside the
-// rows), and every thread combines its two cells exactly as the reference.
+// Deskew + accumulate (skewEngine.cuh:772-792) of one kRows x 32 accumulator
+// tile of one orientation of one grid over that type's sectors in accumulation
+// order.  A thread owns kPer consecutive accumulator rows of one column, keeps
+// them in registers, and per sector gathers the kPer+1 skewed cells they need
+// (rows i+t_j .. i+t_j+kPer of column j; a cell outside its row's valid range
+// is zero) straight from the compact rows: one row-table load and one value
+// load per cell, lanes of a warp on consecutive columns.  There are no
+// barriers, so warps advance independently and hide each other's latency; the
+// next sector's descriptor, target and weight are loaded a sector ahead.  The
+// arithmetic is the reference's, in its order.
 template <int kMode>
-__global__ void __launch_bounds__(256, kMode == kKahan ? 2 : 4)
-    k_deskew_batch(BatchTables T, const float* __restrict__ SO) {
-    __shared__ float band[kBand][kTile];
+__global__ void __launch_bounds__(256) k_deskew_batch(BatchTables T, const float* __restrict__ SO) {
     constexpr int kPer = kRows / 8;
     const int k = find_entry(T.tile_start, 4 * T.n_grids, blockIdx.x);
     const int gi = k >> 2, t = k & 3;
@@ -137,68 +156,48 @@ __global__ void __launch_bounds__(256, kMode == kKahan ? 2 : 4)
     const int dim_o = (t == 1 || t == 2) ? G.dimx : G.dimy;
     const int64_t lt = blockIdx.x - T.tile_start[k];
     const int tiles_x = (dim_i + kTile - 1) / kTile;
-    const int j0 = (int)(lt % tiles_x) * kTile, i0 = (int)(lt / tiles_x) * kRows;
-    if (j0 >= dim_i || i0 >= dim_o) return;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int j = j0 + tx;
-    const bool col_ok = j < dim_i;
-    const int jlast = min(j0 + kTile, dim_i) - 1;
-    const int i_end = min(i0 + kRows, dim_o);
-    const int ib = ty * kPer;
-    const int nv = min(kPer, i_end - i0 - ib);
-    float* A = G.acc + t * n;
-    float* Cc = G.comp + t * n;
+    const int j = (int)(lt % tiles_x) * kTile + (threadIdx.x & 31);
+    const int ib = (int)(lt / tiles_x) * kRows + (threadIdx.x >> 5) * kPer;
+    if (j >= dim_i || ib >= dim_o) return;
+    const int nv = min(kPer, dim_o - ib);
+    float* A = G.acc + t * n + (int64_t)ib * dim_i + j;
+    float* Cc = G.comp + t * n + (int64_t)ib * dim_i + j;
     float s[kPer], c[kPer];
 #pragma unroll
     for (int q = 0; q < kPer; q++) {
-        const int i = i0 + ib + q;
-        s[q] = (col_ok && i < i_end) ? A[(int64_t)i * dim_i + j] : 0.0f;
-        c[q] = (kMode == kKahan && col_ok && i < i_end) ? Cc[(int64_t)i * dim_i + j] : 0.0f;
+        s[q] = q < nv ? A[(int64_t)q * dim_i] : 0.0f;
+        c[q] = (kMode == kKahan && q < nv) ? Cc[(int64_t)q * dim_i] : 0.0f;
     }
-    const int* ord = T.order + G.ts_start[t];
+    const SectorRef* refs = T.refs + G.ts_start[t];
+    SectorRef nx = refs[0];
+    int ntj = G.target[nx.col_off + j];
+    float nw = G.weight[nx.col_off + j];
     for (int q = 0; q < cnt; q++) {
-        const BatchSector bs = T.sectors[ord[q]];
-        const SectorDesc& d = G.desc[bs.angle];
-        const int32_t* tg = G.target + d.col_off;
-        const int32_t* rfirst = G.first + d.row_off;
-        const int32_t* rlast = G.last + d.row_off;
-        const int32_t* roff = G.rowoff + d.row_off;
-        const float* so = SO + bs.cells;
-        const int tmin = tg[j0], tmax = tg[jlast];
-        const int tj = col_ok ? tg[j] : tmin;
-        const float w = col_ok ? G.weight[d.col_off + j] : 0.0f;
-        const int r0 = i0 + tmin;
-        const int nrows = (i_end - i0) + 1 + (tmax - tmin);
-        const bool staged = nrows <= kBand;  // always for square grids (drift <= 32 over 32 columns)
-        if (staged) {
-            constexpr int kLoads = (kBand + 7) / 8;
-            float v[kLoads];
-#pragma unroll
-            for (int u = 0; u < kLoads; u++) {
-                const int rr = ty + 8 * u;
-                v[u] = (rr < nrows && j0 + tx <= jlast) ? compact_cell(d, rfirst, rlast, roff, so, r0 + rr, j0 + tx)
-                                                        : 0.0f;
-            }
-            __syncthreads();  // previous sector's band fully consumed
-#pragma unroll
-            for (int u = 0; u < kLoads; u++)
-                if (ty + 8 * u < nrows) band[ty + 8 * u][tx] = v[u];
-            __syncthreads();
+        const SectorRef cur = nx;
+        const int tj = ntj;
+        const float w = nw;
+        if (q + 1 < cnt) {  // the next sector's descriptor, target and weight, a sector ahead
+            nx = refs[q + 1];
+            ntj = G.target[nx.col_off + j];
+            nw = G.weight[nx.col_off + j];
         }
-        if (!col_ok || nv <= 0) continue;
-        const int off = tj - tmin;
+        const int4* rt = G.rowtab + cur.row_off;
+        const float* so = SO + cur.cells;
         float cell[kPer + 1];
 #pragma unroll
         for (int kk = 0; kk <= kPer; kk++) {
+            const int r = ib + kk + tj;
             cell[kk] = 0.0f;
-            if (kk > nv) continue;
-            cell[kk] = staged ? band[ib + kk + off][tx]
-                              : compact_cell(d, rfirst, rlast, roff, so, i0 + ib + kk + tj, j);
+            if (kk <= nv && r < cur.H) {
+                const int4 m = rt[r];
+                if (j >= m.x && j < m.y) cell[kk] = so[m.z + (j - m.x)];
+            }
         }
+        const float w1 = __fsub_rn(1.0f, w);
 #pragma unroll
         for (int q2 = 0; q2 < kPer; q2++) {
             if (q2 >= nv) continue;
-            const float v = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, w), cell[q2]), __fmul_rn(w, cell[q2 + 1]));
+            const float v = __fadd_rn(__fmul_rn(w1, cell[q2]), __fmul_rn(w, cell[q2 + 1]));
             if (kMode == kKahan) {
                 const float y = __fsub_rn(v, c[q2]);
                 const float ts = __fadd_rn(s[q2], y);
@@ -209,13 +208,11 @@ __global__ void __launch_bounds__(256, kMode == kKahan ? 2 : 4)
             }
         }
     }
-    if (!col_ok) return;
 #pragma unroll
     for (int q = 0; q < kPer; q++) {
-        const int i = i0 + ib + q;
-        if (i >= i_end) continue;
-        A[(int64_t)i * dim_i + j] = s[q];
-        if (kMode == kKahan) Cc[(int64_t)i * dim_i + j] = c[q];
+        if (q >= nv) continue;
+        A[(int64_t)q * dim_i] = s[q];
+        if (kMode == kKahan) Cc[(int64_t)q * dim_i] = c[q];
     }
 }
 
@@ -278,12 +275,14 @@ cudaError_t launch_prepare_batch(const BatchTables& t, int64_t blocks, cudaStrea
     return cudaGetLastError();
 }
 
-cudaError_t launch_skew_batch(const BatchTables& t, const uint64_t* items, int64_t n_items, float* SI, int num_sms,
-                              cudaStream_t st) {
-    if (n_items <= 0) return cudaSuccess;
-    int64_t blocks = (n_items + 7) / 8;
-    if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
-    k_skew_batch<<<(unsigned)blocks, 256, 0, st>>>(t, items, n_items, SI);
+int64_t batch_skew_blocks(int dim_i, int H) {
+    return (int64_t)((dim_i + kSkewCols - 1) / kSkewCols) * ((H + kSkewRows - 1) / kSkewRows);
+}
+
+cudaError_t launch_skew_batch(const BatchTables& t, int64_t blocks, float* SI, cudaStream_t st) {
+    if (blocks <= 0) return cudaSuccess;
+    if (blocks > 0x7fffffff) return cudaErrorInvalidValue;
+    k_skew_batch<<<(unsigned)blocks, kSkewCols, 0, st>>>(t, SI);
     return cudaGetLastError();
 }
 
@@ -291,8 +290,8 @@ cudaError_t launch_deskew_batch(const BatchTables& t, int64_t tiles, const float
                                 cudaStream_t st) {
     if (tiles <= 0) return cudaSuccess;
     if (tiles > 0x7fffffff) return cudaErrorInvalidValue;
-    if (accum_mode == kAccumKahan) k_deskew_batch<kKahan><<<(unsigned)tiles, dim3(kTile, 8), 0, st>>>(t, SO);
-    else k_deskew_batch<kAdd><<<(unsigned)tiles, dim3(kTile, 8), 0, st>>>(t, SO);
+    if (accum_mode == kAccumKahan) k_deskew_batch<kKahan><<<(unsigned)tiles, 256, 0, st>>>(t, SO);
+    else k_deskew_batch<kAdd><<<(unsigned)tiles, 256, 0, st>>>(t, SO);
     return cudaGetLastError();
 }
 

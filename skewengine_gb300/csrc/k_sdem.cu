@@ -466,13 +466,13 @@ __device__ __forceinline__ void visit(Slots& s, int q, float sl, float ring) {
 // An observer that ends inside the level reads at most kLevel-1 cells of the
 // row's NaN padding (see visit).  The level runs as a loop over blocks of
 // kUnroll steps: fully unrolled levels overflow the instruction cache.
-template <bool kF0, bool kF1>
-__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0, int len) {
+template <bool kF0, bool kF1, int kLen>
+__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0) {
     const float* p0 = A + (kF0 ? s.x[0] + d0 : s.x[0] - d0);
     const float* p1 = A + (kF1 ? s.x[1] + d0 : s.x[1] - d0);
     const f2 hh = pk(s.h[0], s.h[1]);
 #pragma unroll 1
-    for (int k0 = 0; k0 < len; k0 += kUnroll) {
+    for (int k0 = 0; k0 < kLen; k0 += kUnroll) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const int d = d0 + k0 + k;
@@ -622,12 +622,12 @@ struct RowLists {
 
 // One batch of a level: slot q takes entry used[dir] + lane + 32*qi of its
 // direction's list, where qi counts the batch's earlier slots of that direction.
-template <bool kF0, bool kF1>
+template <bool kF0, bool kF1, int kLen>
 __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const RowMax& rm, int L, float povh,
-                                            RowLists& rl, int d0, int len, int lane) {
+                                            RowLists& rl, int d0, int lane) {
     constexpr bool kDir[kSlots] = {kF0, kF1};
     const unsigned below = (1u << lane) - 1u;
-    const int dc = d0 + len - 1;  // last step of the level
+    const int dc = d0 + kLen - 1;  // last step of the level
     Slots s;
 #pragma unroll
     for (int q = 0; q < kSlots; q++) {
@@ -659,7 +659,7 @@ __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const R
     }
     if (kF0 == kF1) rl.used[kF0 ? 0 : 1] += 64;
     else rl.used[0] += 32, rl.used[1] += 32;
-    level_steps<kF0, kF1>(s, A, d0, len);
+    level_steps<kF0, kF1, kLen>(s, A, d0);
 
     // Retire finished observers, keep the others for the next level.
 #pragma unroll
@@ -690,8 +690,18 @@ __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const R
 // in slot 0, a backward one in slot 1), so short lists share batches.
 // lists: four lists of L_max entries (forward in/out, backward in/out);
 // cvf, cvb: the two directions' counts, added and scaled at the end.
-// Level lengths: lvl0, then lvl1 (skipped when 0), then kLevel each; all
-// multiples of kUnroll in [kUnroll, kLevel] (lvl1 may be 0).
+// One level of kLen steps over the current lists: full batches of one
+// direction, then the remainders paired.
+template <int kLen>
+__device__ __forceinline__ void run_level(const float* __restrict__ A, const RowMax& rm, int L, float povh,
+                                          RowLists& rl, int d0, int lane) {
+    while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true, kLen>(A, rm, L, povh, rl, d0, lane);
+    while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false, kLen>(A, rm, L, povh, rl, d0, lane);
+    while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1]) sweep_batch<true, false, kLen>(A, rm, L, povh, rl, d0, lane);
+}
+
+// Level lengths: lvl0, then lvl1 (skipped when 0), then kLevel each; each one
+// of 16, 32, 48 or 64 steps (compile-time loop bounds).
 __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, float povh, int4* lists,
                           int max_row, float* cvf, float* cvb, const RowOut& o, int lane, int lvl0, int lvl1) {
     RowLists rl;
@@ -706,10 +716,10 @@ __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, 
         len = level == 0 ? lvl0 : (level == 1 && lvl1 > 0) ? lvl1 : kLevel;
         rl.used[0] = rl.used[1] = 0;
         rl.made[0] = rl.made[1] = 0;
-        while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true>(A, rm, L, povh, rl, d0, len, lane);
-        while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false>(A, rm, L, povh, rl, d0, len, lane);
-        while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1])
-            sweep_batch<true, false>(A, rm, L, povh, rl, d0, len, lane);
+        if (len == kLevel) run_level<kLevel>(A, rm, L, povh, rl, d0, lane);
+        else if (len == 32) run_level<32>(A, rm, L, povh, rl, d0, lane);
+        else if (len == 16) run_level<16>(A, rm, L, povh, rl, d0, lane);
+        else run_level<48>(A, rm, L, povh, rl, d0, lane);
         __syncwarp();  // this level's lists and counts are visible to every lane
 #pragma unroll
         for (int dir = 0; dir < 2; dir++) {
@@ -749,8 +759,8 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if ((int64_t)idx >= a.n_items) break;
         const SectorDesc* dp;
-        const int32_t *first, *last;
-        int row;
+        const int32_t *first = nullptr, *last = nullptr;
+        int row, f, L;
         int64_t slot_off = 0;  // the sector's slot in SI/SO (per-engine runs)
         RowOut o;
         if (kBatch) {
@@ -759,23 +769,24 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
             const BatchGrid& G = a.bt.grids[bs.grid];
             row = (int)(raw & 0xffffffffu);
             dp = &G.desc[bs.angle];
-            first = G.first + dp->row_off;
-            last = G.last + dp->row_off;
+            const int4 m = G.rowtab[dp->row_off + row];  // {first, last, rowoff}
+            f = m.x;
+            L = m.y - m.x;
             o.out = a.SO;
-            o.rowbase = bs.cells + G.rowoff[dp->row_off + row];
+            o.rowbase = bs.cells + m.z;
         } else {
             const Item it = decode(a.items[idx]);
             row = it.row;
             dp = &a.g.desc[a.b.angle[it.slot]];
             first = a.g.first + dp->row_off;
             last = a.g.last + dp->row_off;
+            f = first[row];
+            L = last[row] - f;
             slot_off = it.slot * a.stride;
             o.out = a.SO + slot_off;
-            o.rowbase = (int64_t)row * dp->dim_i + first[row];
+            o.rowbase = (int64_t)row * dp->dim_i + f;
         }
         const SectorDesc& d = *dp;
-        const int f = first[row];
-        const int L = last[row] - f;
         if (L > a.max_row || L <= 0) {
             if (lane == 0) atomicExch(a.status, 1);
             continue;
@@ -950,7 +961,7 @@ int sdem_max_ctas_per_sm(const SdemLaunch& a) {
 
 cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (a.n_items == 0) return cudaSuccess;
-    auto level_ok = [](int v) { return v >= kUnroll && v <= kLevel && v % kUnroll == 0; };
+    auto level_ok = [](int v) { return v == 16 || v == 32 || v == 48 || v == 64; };
     if (!level_ok(a.lvl0) || (a.lvl1 != 0 && !level_ok(a.lvl1)) || a.ctas_per_sm < 0) return cudaErrorInvalidValue;
     const size_t smem = sizeof(float) * (size_t)LLayout(a.max_row).total * kLWarps;
     auto kern = a.batched ? k_sdem<true> : k_sdem<false>;

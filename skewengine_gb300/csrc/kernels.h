@@ -93,22 +93,32 @@ struct BatchGrid {
     const int32_t* first;
     const int32_t* last;
     const int32_t* rowoff;     // per angle, row r's start within the sector's compact rows
+    const int4* rowtab;        // per row (rowoff's layout): {first, last, rowoff, 0}
     unsigned used;             // types that receive a sector
-    int ts_start[4];           // sectors of type t: order[ts_start[t] .. + ts_count[t]]
+    int ts_start[4];           // sectors of type t: refs[ts_start[t] .. + ts_count[t]]
     int ts_count[4];
 };
 struct BatchSector {
     int grid, angle;
     int64_t cells;  // start of the sector's compact rows in the skewed pools
 };
+// What the deskew needs of a sector, in the (grid, type) accumulation order.
+struct SectorRef {
+    int64_t cells;    // start of its compact rows
+    int64_t col_off;  // its target/weight entries
+    int64_t row_off;  // its rows in the grid's row tables
+    int32_t H, angle;
+};
 // Tables of one wave of a batched run (device pointers).
 struct BatchTables {
     const BatchGrid* grids;
     const BatchSector* sectors;
-    const int* order;            // sector indices grouped by (grid, type), accumulation order inside
+    const SectorRef* refs;       // sectors grouped by (grid, type), accumulation order inside
     const int64_t* prep_start;   // per grid, its first block of the prepare and fold launches (+ total)
     const int64_t* tile_start;   // per (grid, type), its first deskew tile (+ total)
+    const int64_t* skew_start;   // per sector, its first skew block (+ total)
     int n_grids;
+    int n_sectors;
 };
 // Work items of a batch's skew and sweep: (sector index << 32) | row, longest
 // row first.
@@ -119,9 +129,10 @@ __host__ __device__ inline uint64_t batch_item(int sector, int row) {
 // Orientations of every grid of the wave, zeroing their accumulators (and
 // compensations, where comp is set).  blocks: prep_start[n_grids].
 cudaError_t launch_prepare_batch(const BatchTables& t, int64_t blocks, cudaStream_t st);
-// Compact skewed rows of every item.
-cudaError_t launch_skew_batch(const BatchTables& t, const uint64_t* items, int64_t n_items, float* SI, int num_sms,
-                              cudaStream_t st);
+// Compact skewed rows of every sector.  blocks: skew_start[n_sectors].
+cudaError_t launch_skew_batch(const BatchTables& t, int64_t blocks, float* SI, cudaStream_t st);
+// Blocks of the skew launch for one sector of dim_i columns and H rows.
+int64_t batch_skew_blocks(int dim_i, int H);
 // Deskew + accumulate of every sector of the wave in (grid, type) order;
 // tiles: tile_start[4 * n_grids].
 cudaError_t launch_deskew_batch(const BatchTables& t, int64_t tiles, const float* SO, int accum_mode,
@@ -153,7 +164,7 @@ struct SdemLaunch {
     int4* lists;        // survivor-list scratch (compacting sweep only)
     size_t list_bytes;  // its size; at least sdem_list_bytes(max_row, num_sms)
     // Compacting sweep's level lengths: lvl0 steps, then lvl1 (none when 0),
-    // then 64 each; multiples of 8 in [8, 64] (lvl1 also 0).
+    // then 64 each; each 16, 32, 48 or 64 (lvl1 also 0).
     int lvl0 = 64, lvl1 = 0;
     int ctas_per_sm = 0;  // compacting sweep: resident CTAs per SM (0 = as many as fit)
     // Batched runs (compacting sweep only): items are batch_item()s whose rows

@@ -301,6 +301,10 @@ class SkewEngine:
         check(self._lib.ske_sweep_shape(self._h, *[C.byref(x) for x in v]))
         return tuple(x.value for x in v)
 
+    def set_sweep_shape(self, lvl0: int = 0, lvl1: int = 0, ctas_per_sm: int = 0) -> None:
+        """Fix the sweep's shape (ske_set_sweep_shape); lvl0 = 0 hands it back to the autotuner."""
+        check(self._lib.ske_set_sweep_shape(self._h, int(lvl0), int(lvl1), int(ctas_per_sm)))
+
     def launch_count(self) -> int:
         n = C.c_int64()
         check(self._lib.ske_launch_count(self._h, C.byref(n)))
