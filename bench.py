@@ -335,7 +335,9 @@ def batch_workload(args):
     import skewengine_gb300 as ske
     from skewengine_gb300 import build, synthetic
     build.build()
-    spec = synthetic.uneven_dem_batch(64, 3000)
+    # SKE_BATCH_COUNT / SKE_BATCH_MAX_SIDE shrink the batch for profiler captures.
+    spec = synthetic.uneven_dem_batch(_env_int("SKE_BATCH_COUNT", 64), 3000,
+                                      hi=_env_int("SKE_BATCH_MAX_SIDE", 2000))
     grids = [torch.from_numpy(synthetic.fractal_dem(s, seed, roughness=h)).cuda() for s, h, seed in spec]
     outs = [torch.empty_like(g) for g in grids]
     cells = sum(g.numel() for g in grids)

@@ -405,6 +405,12 @@ int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, c
  * cout a multiple of 8. */
 int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
                            int cout, void* stream);
+/* Forward-convolution kernel choice for later calls: 0 (default) = the
+ * halo-staged kernel wherever it applies (Cin, Cout and C1 multiples of 16,
+ * Cout <= 256, an image row of at most about 2600 pixels), else the im2col
+ * kernel; 1 = always the im2col kernel.  No reference counterpart. */
+int ske_conv_select(int path);
+
 /* Synchronises `stream`, then sets *failed to 1 if a forward convolution since
  * the previous call gave up waiting for its tensor-core operations (its output
  * is then not written), else 0, and clears the flag. */

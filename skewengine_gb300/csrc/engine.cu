@@ -482,7 +482,7 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             return ls.done(launch_sdem(a, e->num_sms, e->stream));
         }
         case SKE_KERNEL_RADON: {
-            LaunchScope ls(e, "radon", rows_only ? 2 : 3);
+            LaunchScope ls(e, "radon", radon_launches(rows_only, e->max_H2));
             return ls.done(launch_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_P, e->pstride, e->d_tw,
                                         e->d_tw_off, e->max_H2, e->stream, !rows_only,
                                         rows_only ? e->d_orient : nullptr, e->N));

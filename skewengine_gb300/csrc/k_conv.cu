@@ -358,6 +358,207 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
     }
 }
 
+// ---- halo-staged forward convolution on the tensor cores ---------------------
+//
+// Output pixels are numbered as slots of rows with one extra slot each: slot
+// s of an image is pixel (s / (W+1), s % (W+1)), and column W is a junk slot
+// whose output is discarded (1/(W+1) of the work).  A CTA computes nb blocks
+// of 128 consecutive slots (nb = 4, or 2 when Cout > 128; its accumulators are
+// nb x Cout tensor-memory columns) for all Cout channels, with Cin and Cout
+// multiples of 16 and Cout <= 256.  K advances in groups of 16 input channels,
+// each staged once in shared memory as
+//   halo:    two planes of 8 channels holding the input rows the tile's slots
+//            touch, in the same slot layout (row pitch W+1, the extra slot and
+//            a leading slot zero, zeros outside the image): a pixel's 8
+//            channels are one 16-byte row of a core matrix;
+//   weights: for each of the 9 taps, the 16 channels' Cout x 16 slice in the
+//            canonical K-major layout (8-row x 16-byte core matrices).
+// With that layout the input of output slot s for tap (ky, kx) sits at plane
+// slot s - R0*(W+1) + ky*(W+1) + kx (R0 the tile's first row), so the MMA of
+// block j and tap (ky, kx) reads its A operand in place: 128 consecutive plane
+// slots, core matrices 128 bytes apart (stride byte offset), the second 8
+// channels one plane further (leading byte offset).  The zero slot between
+// rows is what the left tap of column 0 and the right tap of column W-1 read,
+// the zero padding.  Each input pixel leaves L2 once per CTA (plus the two
+// halo rows) instead of once per tap as in the im2col gather above.
+// kHaloStages groups are in flight; thread 0 issues a group's MMAs (nb blocks x
+// 9 taps, K = 16 each) and commits them to the stage's mbarrier, which frees
+// the stage for the group kHaloStages later.  Waits are bounded as in
+// k_conv3x3.
+constexpr int kHaloStages = 2;
+constexpr int kSlotBlock = 128;
+
+// Plane slots of a tile of nb blocks: the leading zero slot, then enough rows of
+// W+1 slots for every tap of every output slot.
+__host__ __device__ constexpr int halo_slots(int W, int nb) { return 3 * (W + 1) + nb * kSlotBlock + 1; }
+__host__ __device__ constexpr int halo_plane(int W, int nb) { return halo_slots(W, nb) * 16; }
+__host__ __device__ constexpr int halo_wbytes(int cout) { return 9 * 2 * cout * 16; }
+__host__ __device__ constexpr int halo_stage_bytes(int W, int nb, int cout) {
+    return (2 * halo_plane(W, nb) + halo_wbytes(cout) + 1023) / 1024 * 1024;
+}
+__host__ __device__ constexpr int halo_smem_bytes(int W, int nb, int cout) {
+    return kHaloStages * halo_stage_bytes(W, nb, cout) + 1024 + 64;
+}
+
+// Descriptor with explicit byte offsets (16-byte units): no swizzle, version 1.
+__device__ __forceinline__ uint64_t tc_desc2(unsigned saddr, unsigned lbo, unsigned sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+template <bool kUpCat>
+__global__ void __launch_bounds__(kThreads) k_conv3x3_halo(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
+                                                           const float* __restrict__ bias, bf16* __restrict__ Y,
+                                                           int H, int W, int Cin, int Cout, int Kpad, int relu,
+                                                           const bf16* __restrict__ X2, int C1, int nb,
+                                                           int tiles_per_img) {
+    extern __shared__ __align__(1024) unsigned char hsm_raw[];
+    unsigned char* hsm = hsm_raw + ((1024 - (smem_u32(hsm_raw) & 1023)) & 1023);  // 1024-byte aligned stages
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int W1 = W + 1;
+    const int hslots = halo_slots(W, nb);
+    const int plane = hslots * 16;
+    const int sbytes = halo_stage_bytes(W, nb, Cout);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(hsm + kHaloStages * sbytes);
+    unsigned* tslot = reinterpret_cast<unsigned*>(bar + kHaloStages);
+    const int n = blockIdx.x / tiles_per_img;
+    const int S0 = (blockIdx.x - n * tiles_per_img) * nb * kSlotBlock;  // first output slot of the tile
+    const int R0 = S0 / W1;                                              // its row
+    const int soff = S0 - R0 * W1;                                       // its column (plane slot base)
+    unsigned ncols = 32;
+    while (ncols < (unsigned)(nb * Cout)) ncols <<= 1;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kHaloStages; s++) tc_mbar_init(&bar[s]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+
+    const int groups = Cin / 16;
+    const int64_t img = (int64_t)n * H * W;
+    // Stage group g into stage st: plane slot p >= 1 is input (R0 - 1 + t / W1,
+    // t % W1), t = p - 1; slot 0 and column W are zero.
+    auto load = [&](int st, int g) {
+        unsigned char* base = hsm + st * sbytes;
+        const int c0 = 16 * g;
+        for (int q = tid; q < 2 * hslots; q += kThreads) {
+            const int pl = q >= hslots;
+            const int p = q - pl * hslots;
+            const int t = p - 1;
+            const int iy = R0 - 1 + (t >= 0 ? t / W1 : -1), ix = t >= 0 ? t - (t / W1) * W1 : W;
+            const int ci = c0 + 8 * pl;
+            const bool ok = t >= 0 && iy >= 0 && iy < H && ix < W;
+            const bf16* src = X;
+            if (ok) {
+                if (!kUpCat)
+                    src = X + ((img + (int64_t)iy * W + ix) * Cin + ci);
+                else if (ci < C1)
+                    src = X + (((int64_t)n * (H >> 1) + (iy >> 1)) * (W >> 1) + (ix >> 1)) * C1 + ci;
+                else
+                    src = X2 + ((img + (int64_t)iy * W + ix) * (Cin - C1) + (ci - C1));
+            }
+            cp_async16_ca(base + pl * plane + p * 16, src, ok ? 16 : 0);
+        }
+        unsigned char* wb = base + 2 * plane;
+        for (int q = tid; q < 9 * 2 * Cout; q += kThreads) {
+            const int co = q % Cout, tk = q / Cout;  // tk = tap * 2 + kc
+            const int tap = tk >> 1, kc = tk & 1;
+            cp_async16_ca(wb + (tk * Cout + co) * 16, Wt + (int64_t)co * Kpad + tap * Cin + c0 + 8 * kc, 16);
+        }
+    };
+
+    const uint32_t idesc = tc_idesc(Cout);
+    for (int s = 0; s < kHaloStages - 1; s++) {
+        if (s < groups) load(s, s);
+        cp_commit();
+    }
+    bool fail = false;
+    int last_commit = -1;
+    for (int g = 0; g < groups; g++) {
+        const int nxt = g + kHaloStages - 1;
+        if (nxt < groups) {
+            // Stage nxt % kHaloStages last held group nxt - kHaloStages: its MMAs
+            // must be done reading it.
+            const int st = nxt % kHaloStages, prev = nxt - kHaloStages;
+            if (prev >= 0 && !fail) fail = !tc_mbar_wait(&bar[st], (prev / kHaloStages) & 1);
+            load(st, nxt);
+        }
+        cp_commit();
+        cp_wait<kHaloStages - 1>();  // this thread's copies of group g have landed
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (__syncthreads_or(fail)) {
+            fail = true;
+            break;
+        }
+        if (tid == 0) {
+            tc_fence_after();
+            const int st = g % kHaloStages;
+            const unsigned hb = smem_u32(hsm + st * sbytes), wb = hb + 2 * plane;
+            for (int j = 0; j < nb; j++)
+#pragma unroll
+                for (int tap = 0; tap < 9; tap++) {
+                    const int ky = tap / 3, kx = tap - 3 * (tap / 3);
+                    const int p0 = soff + j * kSlotBlock + ky * W1 + kx;
+                    const uint64_t da = tc_desc2(hb + (unsigned)(p0 * 16), (unsigned)plane, 128);
+                    const uint64_t db = tc_desc2(wb + (unsigned)(tap * 2 * Cout * 16), (unsigned)(Cout * 16), 128);
+                    tc_mma(tmem + (unsigned)(j * Cout), da, db, idesc, (g | tap) != 0);
+                }
+            tc_commit(&bar[st]);
+            last_commit = g;
+        }
+    }
+    cp_wait<0>();
+    if (!fail && groups > 0) fail = !tc_mbar_wait(&bar[(groups - 1) % kHaloStages], ((groups - 1) / kHaloStages) & 1);
+    fail = __syncthreads_or(fail);
+    if (fail && tid == 0 && last_commit >= 0)
+        tc_mbar_wait(&bar[last_commit % kHaloStages], (last_commit / kHaloStages) & 1);
+    tc_fence_after();
+    if (!fail) {
+        for (int j = 0; j < nb; j++) {
+            const int s = S0 + j * kSlotBlock + warp * 32 + lane;  // this thread's slot (TMEM lane)
+            const int r = s / W1, c = s - (s / W1) * W1;
+            const bool store = r < H && c < W;
+            bf16* dst = Y + ((img + (int64_t)r * W + c) * Cout);
+            for (int c0 = 0; c0 < Cout; c0 += 16) {
+                float v[16];
+                tc_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(j * Cout + c0), v);
+                if (!store) continue;
+                __nv_bfloat162 h[8];
+#pragma unroll
+                for (int e = 0; e < 16; e += 2) {
+                    float o0 = __fadd_rn(v[e], bias ? bias[c0 + e] : 0.0f);
+                    float o1 = __fadd_rn(v[e + 1], bias ? bias[c0 + e + 1] : 0.0f);
+                    if (relu) {
+                        o0 = fmaxf(o0, 0.0f);
+                        o1 = fmaxf(o1, 0.0f);
+                    }
+                    h[e / 2] = __floats2bfloat162_rn(o0, o1);
+                }
+                uint4* d4 = reinterpret_cast<uint4*>(dst + c0);
+                d4[0] = *reinterpret_cast<const uint4*>(&h[0]);
+                d4[1] = *reinterpret_cast<const uint4*>(&h[4]);
+            }
+        }
+    } else if (tid == 0) {
+        atomicExch(&g_conv_status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+}
+
 // Weight gradient: a CTA owns a 64 (co) x 64 (k) tile of dW and a chunk of
 // kWgChunk pixels; per slice of 32 pixels it stages dY[m][co] and A[m][k]
 // (rows m) and reads both with transposing ldmatrix: dY^T as the row-major
@@ -443,14 +644,56 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_wgrad(const bf16* __restri
 // 4 bytes, for the bf16 pairs of the epilogue).
 bool aligned(const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
 
+// Forward-convolution kernel choice (ske_conv_select): 0 = halo-staged where it
+// applies, 1 = always the im2col kernel.
+int g_conv_path = 0;
+
 // Launch of the tensor-core forward convolution: BN = Cout rounded up to 16,
 // at most kTcMaxBN, and Cout / BN column tiles.  With 4 stages a CTA holds
 // 36-64 KB of shared memory, so at most 6 (BN 16) down to 3 (BN 128) CTAs share
 // an SM and their tensor-memory columns (32, 64 or 128 each) stay within the
 // SM's 512.
+// The halo-staged kernel applies when Cin, Cout (<= 256) and, for the upsampled
+// concatenation, C1 are multiples of 16 and its stages fit shared memory.  Its
+// shared memory is padded so that the CTAs an SM holds never ask for more than
+// its 512 tensor-memory columns.
+int halo_blocks(int cout) { return cout > 128 ? 2 : 4; }
+
+bool halo_applies(int w_, int cin, int cout, int c1) {
+    return cin % 16 == 0 && cout % 16 == 0 && cout >= 16 && cout <= 256 && c1 % 16 == 0 &&
+           halo_smem_bytes(w_, halo_blocks(cout), cout) <= 227 * 1024;
+}
+
+template <bool kUpCat>
+int launch_conv_halo(const bf16* x, const bf16* w, const float* bias, bf16* y, int n, int h, int w_, int cin,
+                     int cout, int relu, const bf16* x2, int c1, cudaStream_t st) {
+    const int kpad = (9 * cin + kTcBK - 1) / kTcBK * kTcBK;
+    const int nb = halo_blocks(cout);
+    unsigned ncols = 32;
+    while (ncols < (unsigned)(nb * cout)) ncols <<= 1;
+    int smem = halo_smem_bytes(w_, nb, cout);
+    const int max_ctas = 512 / (int)ncols;  // CTAs whose columns fit the SM's tensor memory
+    const int floor_smem = 228 * 1024 / (max_ctas + 1) + 1;
+    if (smem < floor_smem) smem = floor_smem;
+    if (smem > 227 * 1024) return SKE_ERR_UNSUPPORTED;
+    if (cudaFuncSetAttribute(k_conv3x3_halo<kUpCat>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+        cudaSuccess)
+        return SKE_ERR_CUDA;
+    const int64_t slots = (int64_t)h * (w_ + 1);
+    const int64_t tiles = (slots + (int64_t)nb * kSlotBlock - 1) / ((int64_t)nb * kSlotBlock);
+    const int64_t blocks = (int64_t)n * tiles;
+    if (blocks > 0x7fffffff || slots > 0x7fffffff / 2) return SKE_ERR_INVALID;
+    k_conv3x3_halo<kUpCat><<<(unsigned)blocks, kThreads, smem, st>>>(x, w, bias, y, h, w_, cin, cout, kpad, relu, x2,
+                                                                     c1, nb, (int)tiles);
+    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
 template <bool kUpCat>
 int launch_conv_tc(const bf16* x, const bf16* w, const float* bias, bf16* y, int64_t m, int h, int w_, int cin,
                    int cout, int relu, const bf16* x2, int c1, cudaStream_t st) {
+    if (halo_applies(w_, cin, cout, kUpCat ? c1 : 0) && aligned(y, 16) && g_conv_path != 1)
+        return launch_conv_halo<kUpCat>(x, w, bias, y, (int)(m / ((int64_t)h * w_)), h, w_, cin, cout, relu, x2, c1,
+                                        st);
     const int kpad = (9 * cin + kTcBK - 1) / kTcBK * kTcBK;
     const int bn = std::min(kTcMaxBN, (cout + 15) / 16 * 16);
     const int smem = tc_smem_bytes(bn);
@@ -489,6 +732,12 @@ extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const
     if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
     return launch_conv_tc<true>((const bf16*)xlow, (const bf16*)w, bias, (bf16*)y, m, h, w_, cin, cout, relu,
                                 (const bf16*)xskip, c1, (cudaStream_t)stream);
+}
+
+extern "C" int ske_conv_select(int path) {
+    if (path != 0 && path != 1) return SKE_ERR_INVALID;
+    g_conv_path = path;
+    return SKE_OK;
 }
 
 extern "C" int ske_conv_status(int* failed, void* stream) {

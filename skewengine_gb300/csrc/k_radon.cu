@@ -12,8 +12,11 @@
 // sector), back-projection (one thread per cell).  For sectors whose rows stay
 // within their width the engine skips the back-projection (its deskew reads the
 // filtered row values) and the skew (the row sums gather the skewed cells from
-// the oriented input themselves).
+// the oriented input themselves), and runs sums and transform as one fused
+// sector kernel (k_radon_sector, a thread-block cluster per sector).
 #include <climits>
+
+#include <cooperative_groups.h>
 
 #include "kernels.h"
 
@@ -237,6 +240,90 @@ __global__ void __launch_bounds__(kTransformThreads)
     for (int i = threadIdx.x; i < H; i += blockDim.x) p[i].re = __dmul_rn(x[i].re, inv);
 }
 
+// The whole Radon operator of a sector whose rows stay within its width, in
+// one launch: a cluster of kClusterCtas CTAs per sector.  Every CTA of the
+// cluster forms exact row sums (as k_radon_sums, gathering the skewed cells
+// from the oriented input) for its share of the rows and stores them straight
+// into the leader CTA's shared memory (distributed shared memory); after the
+// cluster barrier the leader applies the transform, ramp filter and inverse
+// transform in place (as k_radon_transform) and writes the filtered row values
+// q to P, which the deskew reads.  The other CTAs exit at the barrier, so
+// their SM slots take other sectors' sums while the leaders run the binary64
+// transforms.  Bit-identical to the three-launch path.
+constexpr int kClusterCtas = 8;
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kTransformThreads)
+    k_radon_sector(DevGeometry g, Batch b, const float* __restrict__ orient, int64_t n_cells, cd* __restrict__ P,
+                   int64_t pstride, const double* __restrict__ twiddles, const int64_t* __restrict__ tw_off) {
+    namespace cg = cooperative_groups;
+    extern __shared__ cd xs[];
+    cg::cluster_group cluster = cg::this_cluster();
+    const unsigned rank = cluster.block_rank();
+    const int lane = threadIdx.x & 31;
+    const int slot = blockIdx.y;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const int H = d.H;
+    const int H2 = pow2_at_least(H);
+    const float* src = orient + (int64_t)d.type * n_cells;
+    const int32_t* tgt = g.target + d.col_off;
+    const float* wgt = g.weight + d.col_off;
+    cd* x0 = cluster.map_shared_rank(xs, 0);  // the leader's buffer
+    constexpr int kWarps = kTransformThreads / 32;
+    for (int r = rank * kWarps + (threadIdx.x >> 5); r < H2; r += kClusterCtas * kWarps) {
+        if (r >= H) {
+            if (lane == 0) x0[r] = {0.0, 0.0};
+            continue;
+        }
+        const int f = g.first[d.row_off + r], l = g.last[d.row_off + r];
+        ExactPart a;
+#pragma unroll 2
+        for (int j = f + lane; j < l; j += 32) a.add(skew_gather(d, tgt, wgt, src, r, j));
+        const bool lane_bad = a.bad();
+        int gmin = a.emin, gmax = a.emax;
+        for (int o = 16; o > 0; o >>= 1) {
+            gmin = min(gmin, __shfl_xor_sync(0xffffffffu, gmin, o));
+            gmax = max(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+        }
+        bool bad = __any_sync(0xffffffffu, lane_bad) || l - f > kMaxExactRow ||
+                   (gmin != INT_MAX && gmax - gmin > kMaxSpread);
+        double s = 0.0;
+        if (!bad && gmin != INT_MAX) {
+            const int sh = a.emin == INT_MAX ? 0 : a.emin - gmin;
+            unsigned long long pos = shl64(a.pos, sh), neg = shl64(a.neg, sh);
+            for (int o = 16; o > 0; o >>= 1) {
+                pos += __shfl_xor_sync(0xffffffffu, pos, o);
+                neg += __shfl_xor_sync(0xffffffffu, neg, o);
+            }
+            if (pos + neg < (1ull << 53)) {
+                const double scale = __longlong_as_double((long long)(gmin - 150 + 1023) << 52);
+                s = __dmul_rn(__ll2double_rn((long long)(pos - neg)), scale);
+            } else {
+                bad = true;
+            }
+        }
+        if (bad && lane == 0)
+            for (int j = f; j < l; j++) s = __dadd_rn(s, (double)skew_gather(d, tgt, wgt, src, r, j));
+        if (lane == 0) x0[r] = {s, 0.0};
+    }
+    cluster.sync();  // every row sum is in the leader's shared memory
+    if (rank != 0) return;
+    const double* tw = twiddles + tw_off[31 - __clz(H2)];
+    int bad = 0;
+    for (int i = threadIdx.x; i < H2; i += blockDim.x) bad |= !isfinite(xs[i].re);
+    if (!__syncthreads_or(bad)) {
+        cta_fft<true, true>(xs, H2, tw);
+        ramp_filter(xs, H, H2);
+        cta_fft<true, false>(xs, H2, tw);
+    } else {
+        cta_fft<false, false>(xs, H2, tw);
+        ramp_filter(xs, H, H2);
+        cta_fft<false, false>(xs, H2, tw);
+    }
+    cd* p = P + slot * pstride;
+    const double inv = 1.0 / (double)H2;
+    for (int i = threadIdx.x; i < H; i += blockDim.x) p[i].re = __dmul_rn(xs[i].re, inv);
+}
+
 __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict__ P, int64_t pstride,
                                     float* __restrict__ SO, int64_t stride, int64_t len) {
     const int slot = blockIdx.y;
@@ -262,11 +349,22 @@ __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict
 
 }  // namespace
 
+int radon_launches(bool rows_only, int max_H2) { return rows_only ? (max_H2 <= kSmemH2 ? 1 : 2) : 3; }
+
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
                          int64_t len, double* P, int64_t pstride, const double* twiddles, const int64_t* tw_off,
                          int max_H2, cudaStream_t st, bool backproject, const float* orient, int64_t n_cells) {
     if (orient && backproject) return cudaErrorInvalidValue;  // the gathered cells are not kept for SO
     cd* Pc = reinterpret_cast<cd*>(P);
+    if (orient && max_H2 <= kSmemH2) {  // one fused launch: a cluster per sector
+        const int smem = max_H2 * (int)sizeof(cd);
+        cudaError_t e = cudaSuccess;
+        if (smem > 48 * 1024) e = cudaFuncSetAttribute(k_radon_sector, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_radon_sector<<<dim3(kClusterCtas, b.count), kTransformThreads, smem, st>>>(g, b, orient, n_cells, Pc, pstride,
+                                                                                   twiddles, tw_off);
+        return cudaGetLastError();
+    }
     dim3 g1((max_H2 + kSumWarps - 1) / kSumWarps, b.count);
     if (orient)
         k_radon_sums<true><<<g1, kSumWarps * 32, 0, st>>>(g, b, SI, stride, orient, n_cells, Pc, pstride);

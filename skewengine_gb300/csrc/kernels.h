@@ -198,6 +198,9 @@ cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, 
                          const int64_t* tw_off, int max_H2, cudaStream_t st, bool backproject = true,
                          const float* orient = nullptr, int64_t n_cells = 0);
 
+// Kernel launches launch_radon makes (rows_only: gathered sums, no back-projection).
+int radon_launches(bool rows_only, int max_H2);
+
 // Local Radon transform (k_lradon.cu): tiles of every sector up to max_H rows
 // and max_cols columns; gauss: 180 x 64 weights, taper: the kept bins' factors.
 cudaError_t launch_local_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,

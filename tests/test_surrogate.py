@@ -170,3 +170,60 @@ def test_trained_network_beats_the_untrained_method(sur):
     constant = np.median(sur.tile_area_error(torch.full_like(y, float(y.mean())), y))
     untrained = np.median(sur.tile_area_error(raw, y))
     assert trained < 0.5 * constant and trained < 0.5 * untrained, (trained, constant, untrained)
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout,relu", [(1, 8, 128, 32, 32, True), (2, 4, 256, 16, 48, False),
+                                                  (1, 8, 256, 64, 128, True), (1, 4, 128, 192, 64, True)])
+def test_halo_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
+    """Widths that are multiples of 128 take the halo-staged tensor-core kernel."""
+    import torch
+    rng = np.random.default_rng(cin * 5 + cout + w)
+    xb = _bf16(rng.normal(0, 1, (n, h, w, cin)))
+    wb = _bf16(rng.normal(0, 0.2, (cout, 9 * cin)))
+    b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32)
+    wpad = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
+    wpad[:, : 9 * cin] = wb
+    y = sur.conv3x3(xb.cuda().contiguous(), wpad.cuda(), b.cuda(), relu)
+    sur.conv_check()
+    y = y.float().cpu().numpy()
+    ref, _, _ = _conv_ref(xb.double().numpy(), wb.double().numpy(), b.double().numpy(), relu)
+    assert np.all(np.abs(y - ref) <= 2 ** -7 * np.abs(ref) + 1e-3), np.abs(y - ref).max()
+
+
+def test_halo_upcat_equals_halo_conv_of_the_concatenation(sur):
+    import torch
+    import torch.nn.functional as F
+    rng = np.random.default_rng(4)
+    low = _bf16(rng.normal(0, 1, (2, 4, 64, 64))).cuda().contiguous()
+    skip = _bf16(rng.normal(0, 1, (2, 8, 128, 32))).cuda().contiguous()
+    w = torch.zeros((32, sur.kpad(96)), dtype=torch.bfloat16)
+    w[:, : 9 * 96] = _bf16(rng.normal(0, 0.1, (32, 9 * 96)))
+    w = w.cuda()
+    b = torch.as_tensor(rng.normal(0, 0.5, 32), dtype=torch.float32).cuda()
+    up = F.interpolate(low.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
+    want = sur.conv3x3(torch.cat([up, skip], 3).contiguous(), w, b, True)
+    got = sur.conv3x3_upcat(low, skip, w, b, True)
+    sur.conv_check()
+    assert torch.equal(got.view(torch.int16), want.view(torch.int16))
+
+
+def test_network_forward_halo_and_im2col_kernels_agree(sur):
+    """The whole U-Net forward with the halo-staged kernel (where it applies)
+    and with the im2col kernel only: same function, float32 accumulation in
+    different orders, so equal to bfloat16 rounding."""
+    import torch
+    from skewengine_gb300 import _lib
+    net = sur.make_net(seed=5)
+    x = sur.encode_tiles(np.stack([synthetic.fractal_dem(256, 80 + i) for i in range(2)]))
+    lib = _lib.load()
+    try:
+        with torch.no_grad():
+            assert lib.ske_conv_select(1) == 0
+            ref = net(x)
+            assert lib.ske_conv_select(0) == 0
+            got = net(x)
+        sur.conv_check()
+    finally:
+        lib.ske_conv_select(0)
+    err = (got - ref).abs().max().item()
+    assert err <= 0.05 * ref.abs().max().item(), err
