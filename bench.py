@@ -514,6 +514,13 @@ def surrogate_workload(args):
             eng.run(0, tdev[i], truth[i])
         torch.cuda.synchronize()
 
+    beng = ske.SkewEngine(sur.TILE, sur.TILE)
+    truth_b = torch.empty_like(tdev)
+
+    def plain_batched():  # every tile in one batched engine call (five launches, graph replay)
+        ske.run_batch(0, [tdev[i] for i in range(len(tiles))], engine=beng, outs=[truth_b[i] for i in range(len(tiles))])
+        torch.cuda.synchronize()
+
     dem_dev = torch.as_tensor(np.ascontiguousarray(dem, np.float32), device="cuda")
 
     def surrogate():  # device-resident like the plain arm: DEM in HBM, area map left in HBM
@@ -532,6 +539,9 @@ def surrogate_workload(args):
         surrogate()
     plain()
     plain_s, _ = timed(plain, max(1, args.steps // 2))
+    plain_batched()
+    plain_b_s, _ = timed(plain_batched, max(1, args.steps))
+    assert torch.equal(truth, truth_b), "batched engine run differs from per-tile runs"
     sur_s, (_, stats) = timed(surrogate, args.steps)
     # accuracy of the network alone on every tile, against the engine
     x = sur.encode_tiles(tiles)
@@ -559,7 +569,8 @@ def surrogate_workload(args):
             "ms_per_step": sur_s * 1e3, "higher_is_better": True, "dtype": "bf16 (f32 accumulation)",
             "data": "synthetic (seeded diamond-square DEM; network trained on 20000 seeded fractal tiles)",
             "config": {"workload": "4000x4000 DEM, 256x256 tiles, 5% engine spot checks, 2% fallback bound",
-                       "plain_ms": plain_s * 1e3, "surrogate_ms": sur_s * 1e3,
+                       "plain_ms": plain_s * 1e3, "plain_batched_ms": plain_b_s * 1e3,
+                       "speedup_vs_batched_plain": plain_b_s / sur_s, "surrogate_ms": sur_s * 1e3,
                        "surrogate_mpoint_sectors_s": side * side * DIR_SECTORS / sur_s / 1e6,
                        "plain_mpoint_sectors_s": len(tiles) * sur.TILE ** 2 * DIR_SECTORS / plain_s / 1e6,
                        "checked_tiles": len(stats["checked"]), "fell_back": len(stats["fell_back"]),

@@ -1624,6 +1624,11 @@ int ske_set_sweep_shape(ske_engine e, int lvl0, int lvl1, int ctas_per_sm) {
     return SKE_OK;
 }
 
+int ske_radon_select(int path) {
+    if (radon_select(path) != 0) return fail(SKE_ERR_INVALID, "radon path %d: 0 (fused) or 1 (two launches)", path);
+    return SKE_OK;
+}
+
 int ske_sweep_shape(ske_engine e, int* lvl0, int* lvl1, int* ctas_per_sm) {
     if (!e || !lvl0 || !lvl1 || !ctas_per_sm) return fail(SKE_ERR_INVALID, "null argument");
     *lvl0 = e->last_shape.lvl0;

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kTransformThreads)
 // transforms.  Bit-identical to the three-launch path.
 constexpr int kClusterCtas = 8;
 
-__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kTransformThreads)
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kTransformThreads, 6)
     k_radon_sector(DevGeometry g, Batch b, const float* __restrict__ orient, int64_t n_cells, cd* __restrict__ P,
                    int64_t pstride, const double* __restrict__ twiddles, const int64_t* __restrict__ tw_off) {
     namespace cg = cooperative_groups;
@@ -349,14 +349,26 @@ __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict
 
 }  // namespace
 
-int radon_launches(bool rows_only, int max_H2) { return rows_only ? (max_H2 <= kSmemH2 ? 1 : 2) : 3; }
+// 0: the fused sector kernel where it applies; 1: row sums and transform as two
+// launches (radon_select).
+int g_radon_path = 0;
+
+int radon_launches(bool rows_only, int max_H2) {
+    return rows_only ? (max_H2 <= kSmemH2 && g_radon_path == 0 ? 1 : 2) : 3;
+}
+
+int radon_select(int path) {
+    if (path != 0 && path != 1) return -1;
+    g_radon_path = path;
+    return 0;
+}
 
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
                          int64_t len, double* P, int64_t pstride, const double* twiddles, const int64_t* tw_off,
                          int max_H2, cudaStream_t st, bool backproject, const float* orient, int64_t n_cells) {
     if (orient && backproject) return cudaErrorInvalidValue;  // the gathered cells are not kept for SO
     cd* Pc = reinterpret_cast<cd*>(P);
-    if (orient && max_H2 <= kSmemH2) {  // one fused launch: a cluster per sector
+    if (orient && max_H2 <= kSmemH2 && g_radon_path == 0) {  // one fused launch: a cluster per sector
         const int smem = max_H2 * (int)sizeof(cd);
         cudaError_t e = cudaSuccess;
         if (smem > 48 * 1024) e = cudaFuncSetAttribute(k_radon_sector, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -466,13 +466,15 @@ __device__ __forceinline__ void visit(Slots& s, int q, float sl, float ring) {
 // An observer that ends inside the level reads at most kLevel-1 cells of the
 // row's NaN padding (see visit).  The level runs as a loop over blocks of
 // kUnroll steps: fully unrolled levels overflow the instruction cache.
+// kLen > 0: a compile-time level length; kLen = 0: the run-time length len.
 template <bool kF0, bool kF1, int kLen>
-__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0) {
+__device__ __forceinline__ void level_steps(Slots& s, const float* __restrict__ A, int d0, int len) {
     const float* p0 = A + (kF0 ? s.x[0] + d0 : s.x[0] - d0);
     const float* p1 = A + (kF1 ? s.x[1] + d0 : s.x[1] - d0);
     const f2 hh = pk(s.h[0], s.h[1]);
+    const int steps = kLen > 0 ? kLen : len;
 #pragma unroll 1
-    for (int k0 = 0; k0 < kLen; k0 += kUnroll) {
+    for (int k0 = 0; k0 < steps; k0 += kUnroll) {
 #pragma unroll
         for (int k = 0; k < kUnroll; k++) {
             const int d = d0 + k0 + k;
@@ -624,10 +626,10 @@ struct RowLists {
 // direction's list, where qi counts the batch's earlier slots of that direction.
 template <bool kF0, bool kF1, int kLen>
 __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const RowMax& rm, int L, float povh,
-                                            RowLists& rl, int d0, int lane) {
+                                            RowLists& rl, int d0, int len, int lane) {
     constexpr bool kDir[kSlots] = {kF0, kF1};
     const unsigned below = (1u << lane) - 1u;
-    const int dc = d0 + kLen - 1;  // last step of the level
+    const int dc = d0 + (kLen > 0 ? kLen : len) - 1;  // last step of the level
     Slots s;
 #pragma unroll
     for (int q = 0; q < kSlots; q++) {
@@ -659,7 +661,7 @@ __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const R
     }
     if (kF0 == kF1) rl.used[kF0 ? 0 : 1] += 64;
     else rl.used[0] += 32, rl.used[1] += 32;
-    level_steps<kF0, kF1, kLen>(s, A, d0);
+    level_steps<kF0, kF1, kLen>(s, A, d0, len);
 
     // Retire finished observers, keep the others for the next level.
 #pragma unroll
@@ -690,18 +692,23 @@ __device__ __forceinline__ void sweep_batch(const float* __restrict__ A, const R
 // in slot 0, a backward one in slot 1), so short lists share batches.
 // lists: four lists of L_max entries (forward in/out, backward in/out);
 // cvf, cvb: the two directions' counts, added and scaled at the end.
-// One level of kLen steps over the current lists: full batches of one
-// direction, then the remainders paired.
+// One level over the current lists: full batches of one direction, then the
+// remainders paired.  kLen > 0: every level kLen steps (compile time); kLen = 0:
+// len steps.
 template <int kLen>
 __device__ __forceinline__ void run_level(const float* __restrict__ A, const RowMax& rm, int L, float povh,
-                                          RowLists& rl, int d0, int lane) {
-    while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true, kLen>(A, rm, L, povh, rl, d0, lane);
-    while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false, kLen>(A, rm, L, povh, rl, d0, lane);
-    while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1]) sweep_batch<true, false, kLen>(A, rm, L, povh, rl, d0, lane);
+                                          RowLists& rl, int d0, int len, int lane) {
+    while (rl.n[0] - rl.used[0] >= 64) sweep_batch<true, true, kLen>(A, rm, L, povh, rl, d0, len, lane);
+    while (rl.n[1] - rl.used[1] >= 64) sweep_batch<false, false, kLen>(A, rm, L, povh, rl, d0, len, lane);
+    while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1])
+        sweep_batch<true, false, kLen>(A, rm, L, povh, rl, d0, len, lane);
 }
 
 // Level lengths: lvl0, then lvl1 (skipped when 0), then kLevel each; each one
-// of 16, 32, 48 or 64 steps (compile-time loop bounds).
+// of 16, 32, 48 or 64 steps.  The built-in schedule (all kLevel) runs with a
+// compile-time level length; any other runs one loop with run-time lengths.
+// Two code paths, not one per length: a sweep that mixed several compiled
+// lengths in one row measured much slower (instruction-cache misses).
 __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, float povh, int4* lists,
                           int max_row, float* cvf, float* cvb, const RowOut& o, int lane, int lvl0, int lvl1) {
     RowLists rl;
@@ -716,10 +723,8 @@ __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, 
         len = level == 0 ? lvl0 : (level == 1 && lvl1 > 0) ? lvl1 : kLevel;
         rl.used[0] = rl.used[1] = 0;
         rl.made[0] = rl.made[1] = 0;
-        if (len == kLevel) run_level<kLevel>(A, rm, L, povh, rl, d0, lane);
-        else if (len == 32) run_level<32>(A, rm, L, povh, rl, d0, lane);
-        else if (len == 16) run_level<16>(A, rm, L, povh, rl, d0, lane);
-        else run_level<48>(A, rm, L, povh, rl, d0, lane);
+        if (lvl0 == kLevel && lvl1 == 0) run_level<kLevel>(A, rm, L, povh, rl, d0, len, lane);
+        else run_level<0>(A, rm, L, povh, rl, d0, len, lane);
         __syncwarp();  // this level's lists and counts are visible to every lane
 #pragma unroll
         for (int dir = 0; dir < 2; dir++) {

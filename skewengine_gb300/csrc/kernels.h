@@ -200,6 +200,9 @@ cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, 
 
 // Kernel launches launch_radon makes (rows_only: gathered sums, no back-projection).
 int radon_launches(bool rows_only, int max_H2);
+// Radon path for later launches: 0 = fused sector kernel where it applies, 1 =
+// separate sums and transform; -1 for another value.
+int radon_select(int path);
 
 // Local Radon transform (k_lradon.cu): tiles of every sector up to max_H rows
 // and max_cols columns; gauss: 180 x 64 weights, taper: the kept bins' factors.

@@ -33,6 +33,7 @@ from ._lib import SkeError, check, load
 TILE = 256
 IN_CH = 8
 BASE = 32
+CTX = 64  # width of the tile-context MLP
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "surrogate_unet32.npz")
 
 
@@ -176,6 +177,14 @@ def make_net(seed: int = 0, device="cuda"):
                 self.b[name] = torch.nn.Parameter(torch.zeros(cout))
             self.head_w = torch.nn.Parameter(torch.randn(BASE, 1, generator=g) * math.sqrt(1.0 / BASE))
             self.head_b = torch.nn.Parameter(torch.full((1,), 8.0))
+            # Tile context: the bottleneck's channel means (and maxima) -> MLP
+            # -> the log of the tile's total visible area, which calibrates the
+            # per-cell map (visibility is a property of whole lines of sight).
+            cin = 2 * 8 * BASE
+            self.ctx1_w = torch.nn.Parameter(torch.randn(cin, CTX, generator=g) * math.sqrt(2.0 / cin))
+            self.ctx1_b = torch.nn.Parameter(torch.zeros(CTX))
+            self.ctx2_w = torch.nn.Parameter(torch.randn(CTX, 1, generator=g) * math.sqrt(1.0 / CTX) * 0.1)
+            self.ctx2_b = torch.nn.Parameter(torch.full((1,), 19.0))
 
         def c(self, x, name):
             return conv_op(x, self.w[name], self.b[name], True)
@@ -205,10 +214,24 @@ def make_net(seed: int = 0, device="cuda"):
             d3 = self.c(self.upcat(b4, e3, "d3a"), "d3b")
             d2 = self.c(self.upcat(d3, e2, "d2a"), "d2b")
             d1 = self.c(self.upcat(d2, e1, "d1a"), "d1b")
-            return (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log area
+            cells = (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log(1 + area)
+            f = b4.float()
+            pooled = torch.cat([f.mean((1, 2)), f.amax((1, 2))], 1)
+            t = (torch.relu(pooled @ self.ctx1_w + self.ctx1_b) @ self.ctx2_w)[:, 0] + self.ctx2_b  # log total
+            return calibrate(cells, t)
 
     import torch  # noqa: F811  (used inside forward)
     return UNet().to(device)
+
+
+def calibrate(cells, log_total):
+    """Scale the per-cell areas of each tile (cells: log(1 + area)) so that they
+    sum to exp(log_total); returns log(1 + scaled area)."""
+    import torch
+    area = torch.expm1(cells).clamp_min(0.0)
+    tot = area.sum((1, 2)).clamp_min(1e-6)
+    scale = torch.exp(log_total - torch.log(tot))
+    return torch.log1p(area * scale[:, None, None])
 
 
 def encode_tiles(tiles):
@@ -224,15 +247,16 @@ def encode_tiles(tiles):
     return x
 
 
-def label_tiles(tiles: np.ndarray, engine=None):
-    """The engine's total visible area of every cell of each tile (180 angles), as log(1 + area)."""
+def label_tiles(tiles: np.ndarray, engine=None, chunk: int = 512):
+    """The engine's total visible area of every cell of each tile (180 angles),
+    as log(1 + area): batched engine calls of `chunk` tiles each."""
     import torch
-    from .engine import SkewEngine
+    from .engine import SkewEngine, run_batch
     eng = engine or SkewEngine(tiles.shape[2], tiles.shape[1])
     out = torch.empty(tiles.shape, dtype=torch.float32, device="cuda")
-    for i in range(len(tiles)):
-        x = torch.as_tensor(np.ascontiguousarray(tiles[i], np.float32), device="cuda")
-        eng.run(0, x, out[i])
+    for i in range(0, len(tiles), chunk):
+        x = torch.as_tensor(np.ascontiguousarray(tiles[i:i + chunk], np.float32), device="cuda")
+        run_batch(0, [x[j] for j in range(len(x))], engine=eng, outs=[out[i + j] for j in range(len(x))])
     torch.cuda.synchronize()
     if engine is None:
         eng.close()
@@ -279,7 +303,7 @@ def make_tiles(count: int, seed: int, workers: int | None = None) -> np.ndarray:
 def _log_total(logarea):
     """log of a tile's total visible area from per-cell log(1 + area)."""
     import torch
-    return torch.logsumexp(logarea.flatten(1), 1)
+    return torch.log(torch.expm1(logarea.float()).clamp_min(0.0).sum((1, 2)).clamp_min(1e-6))
 
 
 def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 0, log=None,
@@ -362,7 +386,7 @@ def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float 
     `dem` is a NumPy array or a CUDA tensor; the area map comes back the same way
     (a CUDA tensor stays on the device throughout).  Returns (area map, stats)."""
     import torch
-    from .engine import SkewEngine
+    from .engine import SkewEngine, run_batch
     on_host = not torch.is_tensor(dem)
     d = torch.as_tensor(np.ascontiguousarray(dem, np.float32) if on_host else dem, dtype=torch.float32,
                         device="cuda")
@@ -379,8 +403,10 @@ def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float 
     checked = np.sort(rng.choice(len(tiles), n_check, replace=False))
     eng = engine or SkewEngine(TILE, TILE)
     truth = torch.empty((n_check, TILE, TILE), dtype=torch.float32, device="cuda")
-    for j, t in enumerate(checked):
-        eng.run(0, tiles[int(t)], truth[j])
+    # All checked tiles in one batched engine call (ske_run_batch: the engine
+    # keeps the batch plan and replays it as a CUDA graph on later calls).
+    sel = tiles[torch.as_tensor(checked, device="cuda")].contiguous()
+    run_batch(0, [sel[j] for j in range(n_check)], engine=eng, outs=[truth[j] for j in range(n_check)])
     truth = torch.log1p(truth)
     errs = tile_area_error(out[torch.as_tensor(checked, device="cuda")], truth)
     if force_error:
@@ -413,6 +439,7 @@ def main(argv=None) -> int:
     ap.add_argument("--steps", type=int, default=4000)
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--tile-weight", type=float, default=4.0)
     ap.add_argument("--out", default=WEIGHTS)
     a = ap.parse_args(argv)
     t0 = time.time()
@@ -424,7 +451,10 @@ def main(argv=None) -> int:
     torch.cuda.synchronize()
     t2 = time.time()
     net = make_net(seed=0)
-    losses = train(net, x, y, a.steps, a.batch, a.lr, log=lambda m: print(m, flush=True))
+    with torch.no_grad():  # start the tile-context head at the data's mean log total
+        net.ctx2_b.fill_(float(_log_total(y[:1024]).mean()))
+    losses = train(net, x, y, a.steps, a.batch, a.lr, log=lambda m: print(m, flush=True),
+                   tile_weight=a.tile_weight)
     torch.cuda.synchronize()
     t3 = time.time()
     with torch.no_grad():
