@@ -235,10 +235,10 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
                          int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p);
 
 /* Radon operator's kernels for sectors whose rows stay within their width:
- * 0 (default) = one fused sector kernel (a thread-block cluster per sector:
- * row sums into the leader's shared memory, then the filtered transform), 1 =
- * row sums and transform as two launches.  Same results.  No reference
- * counterpart. */
+ * 0 = one fused sector kernel (a thread-block cluster per sector: row sums into
+ * the leader's shared memory, then the filtered transform), 1 (default) = row
+ * sums and transform as two launches, which measured faster on GB300.  Same
+ * results.  No reference counterpart. */
 int ske_radon_select(int path);
 
 /* Shape of the last viewshed sweep the engine launched: level schedule (lvl0

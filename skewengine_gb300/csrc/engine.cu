@@ -362,10 +362,10 @@ int get_items(ske_engine e, const Batch& b, ItemPlan** out) {
 // The compacting sweep's speed depends on its level schedule (a short first
 // level retires the many observers that see nothing far away sooner, for more
 // retirement tests) and on how many CTAs share an SM (more warps hide latency,
-// fewer leave each warp more L1).  The tuner times a few shapes on a sample of
-// the actual work list (every 8th row, which keeps the longest-first length
-// distribution) the first time a device meets rows of a given length class,
-// and keeps the fastest for the process.  Every shape writes the same bits.
+// fewer leave each warp more L1).  The tuner times a few shapes on the actual
+// work list (a strided sample of it beyond 2^20 rows) the first time a device
+// meets rows of a given length class, and keeps the fastest for the process.
+// Every shape writes the same bits.
 std::mutex g_tune_mutex;
 std::map<std::pair<int, int>, SweepShape> g_tuned;  // (device, max_row / 256) -> shape
 
@@ -383,11 +383,13 @@ int tune_sweep(ske_engine e, const SdemLaunch& base, const std::vector<uint64_t>
         *out = it->second;
         return SKE_OK;
     }
-    constexpr int kStride = 8;
     if (items.size() < (size_t)64 * e->num_sms) return SKE_OK;  // too little work to time; keep the default
+    // The whole list up to 2^20 rows, else every stride-th row (which keeps the
+    // longest-first length distribution).
+    const size_t stride = std::max<size_t>(1, items.size() >> 20);
     std::vector<uint64_t> sample;
-    sample.reserve(items.size() / kStride + 1);
-    for (size_t i = 0; i < items.size(); i += kStride) sample.push_back(items[i]);
+    sample.reserve(items.size() / stride + 1);
+    for (size_t i = 0; i < items.size(); i += stride) sample.push_back(items[i]);
     if (sample.size() > e->tune_items_cap) {
         cudaFree(e->d_tune_items);
         e->d_tune_items = nullptr;
@@ -398,7 +400,7 @@ int tune_sweep(ske_engine e, const SdemLaunch& base, const std::vector<uint64_t>
     SKE_CK(cudaMemcpyAsync(e->d_tune_items, sample.data(), sizeof(uint64_t) * sample.size(), cudaMemcpyHostToDevice,
                            e->stream));
     const int max_ctas = sdem_max_ctas_per_sm(base);
-    const SweepShape sched[] = {{64, 0, 0}, {32, 0, 0}, {16, 48, 0}, {32, 32, 0}};
+    const SweepShape sched[] = {{64, 0, 0}, {16, 48, 0}, {32, 0, 0}};
     std::vector<SweepShape> cands;
     for (const SweepShape& c : sched) {
         cands.push_back(c);

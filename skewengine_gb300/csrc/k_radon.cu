@@ -349,9 +349,9 @@ __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict
 
 }  // namespace
 
-// 0: the fused sector kernel where it applies; 1: row sums and transform as two
-// launches (radon_select).
-int g_radon_path = 0;
+// 0: the fused sector kernel where it applies; 1 (default): row sums and
+// transform as two launches, measured faster (radon_select).
+int g_radon_path = 1;
 
 int radon_launches(bool rows_only, int max_H2) {
     return rows_only ? (max_H2 <= kSmemH2 && g_radon_path == 0 ? 1 : 2) : 3;

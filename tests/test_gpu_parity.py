@@ -385,3 +385,19 @@ def test_run_batch_uneven(ske, oracle):
     outs = ske.run_batch(0, grids, povh=POVH)
     for g, o in zip(grids, outs):
         assert bits_equal(o, oracle.run(0, g, povh=POVH))
+
+
+def test_radon_fused_sector_kernel_bit_exact(ske, oracle, gpu_lib):
+    """The thread-block-cluster Radon kernel (row sums into the leader CTA's
+    shared memory, then the filtered transform) gives the same bits as the
+    two-launch path and the oracle, including rows with non-finite values."""
+    try:
+        assert gpu_lib.ske_radon_select(0) == 0
+        for x in (synthetic.ellipse_phantom(512, 2024), synthetic.ellipse_phantom(96, 5, side_y=70)):
+            assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
+        x = synthetic.ellipse_phantom(64, 9)
+        x[3, 5] = np.inf
+        x[40, 7] = np.nan
+        assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
+    finally:
+        gpu_lib.ske_radon_select(1)
