@@ -490,6 +490,70 @@ def cepstrum_batch_workload(args):
     return 0
 
 
+def convs_workload(args):
+    """Every 3x3 convolution of the surrogate U-Net, forward, on a batch of
+    SKE_CONV_BATCH (default 16) 256x256 tiles: per-layer time and TFLOP/s for the
+    halo-staged kernel and the im2col kernel (ske_conv_select), CUDA events, and
+    the whole set against the measured bf16 peak."""
+    import torch
+    from skewengine_gb300 import _lib, build
+    build.build()
+    from skewengine_gb300 import surrogate as sur
+    lib = _lib.load()
+    n = _env_int("SKE_CONV_BATCH", 16)
+    res = {"e1": 256, "e2": 128, "e3": 64, "b4": 32, "d3": 64, "d2": 128, "d1": 256}
+    skip_ch = {"d3": 128, "d2": 64, "d1": 32}
+    layers, total = [], {0: 0.0, 1: 0.0}
+    flops_all = 0.0
+    g = torch.Generator(device="cuda").manual_seed(0)
+    for name, cin, cout in sur.LAYERS:
+        r = res[name[:2]]
+        w = (torch.randn(cout, sur.kpad(cin), device="cuda", generator=g) * 0.05).to(torch.bfloat16)
+        b = torch.zeros(cout, device="cuda")
+        if name[0] == "d" and name[2] == "a":
+            c2 = skip_ch[name[:2]]
+            low = torch.randn(n, r // 2, r // 2, cin - c2, device="cuda", generator=g).to(torch.bfloat16)
+            skip = torch.randn(n, r, r, c2, device="cuda", generator=g).to(torch.bfloat16)
+            fn = (lambda lo=low, sk=skip, w=w, b=b: sur.conv3x3_upcat(lo, sk, w, b, True))
+        else:
+            x = torch.randn(n, r, r, cin, device="cuda", generator=g).to(torch.bfloat16)
+            fn = (lambda x=x, w=w, b=b: sur.conv3x3(x, w, b, True))
+        flops = 2.0 * 9 * cin * cout * r * r * n
+        flops_all += flops
+        row = {"layer": name, "cin": cin, "cout": cout, "side": r}
+        for path in (1, 0):
+            lib.ske_conv_select(path)
+            for _ in range(max(1, args.warmup)):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(args.steps):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            us = e0.elapsed_time(e1) / args.steps * 1e3
+            total[path] += us
+            row["halo" if path == 0 else "im2col"] = {"us": round(us, 1), "tflops": round(flops / us / 1e6, 1)}
+        sur.conv_check()
+        layers.append(row)
+    lib.ske_conv_select(0)
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
+    achieved = flops_all / (total[0] / 1e6) / 1e12
+    line = {"metric": f"surrogate U-Net 3x3 convolutions TFLOP/s (batch {n} x 256², forward)", "value": achieved,
+            "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total[0] / 1e3, "higher_is_better": True, "dtype": "bf16 (f32 accumulation)",
+            "data": "synthetic (random activations and weights)",
+            "config": {"workload": "the 14 convolutions of the 4-level, 32-channel U-Net, one forward pass",
+                       "im2col_ms": total[1] / 1e3, "layers": layers},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks.get("bf16_tflops", 1900.0),
+                         "unit": "TFLOP/s", "frac": achieved / peaks.get("bf16_tflops", 1900.0),
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 GEMM burst) of measured"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def surrogate_workload(args):
     """Learned total-viewshed surrogate on a 4000x4000 DEM cut into 256 tiles of
     256x256: the network predicts every tile, the engine checks 5% of them and
@@ -599,7 +663,7 @@ def main():
     ap.add_argument("--side", type=int, default=SIDE,
                     help="DEM side (the metric is quoted at 2000; smaller sides are for profiling)")
     ap.add_argument("--workload", choices=["sdem", "radon", "localradon", "cepstrum", "sdem_batch", "cepstrum_batch",
-                                           "surrogate"],
+                                           "surrogate", "convs"],
                     default="sdem",
                     help="sdem = the headline metric; the others are secondary measurements")
     args = ap.parse_args()
@@ -611,6 +675,8 @@ def main():
         return batch_workload(args)
     if args.workload == "cepstrum_batch":
         return cepstrum_batch_workload(args)
+    if args.workload == "convs":
+        return convs_workload(args)
     if args.workload == "surrogate":
         return surrogate_workload(args)
     if args.workload != "sdem":

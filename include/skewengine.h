@@ -414,7 +414,7 @@ int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int 
                            int cout, void* stream);
 /* Forward-convolution kernel choice for later calls: 0 (default) = the
  * halo-staged kernel wherever it applies (Cin, Cout and C1 multiples of 16,
- * Cout <= 256, an image row of at most about 2600 pixels), else the im2col
+ * Cout <= 128, an image row of at most about 2600 pixels), else the im2col
  * kernel; 1 = always the im2col kernel.  No reference counterpart. */
 int ske_conv_select(int path);
 

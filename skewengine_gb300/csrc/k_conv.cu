@@ -659,8 +659,11 @@ int g_conv_path = 0;
 // its 512 tensor-memory columns.
 int halo_blocks(int cout) { return cout > 128 ? 2 : 4; }
 
+// Cout above 128 (the 32 x 32, 256-channel bottleneck) measured faster on the
+// im2col kernel (155-185 against 201-228 TFLOP/s): two 128-slot blocks per CTA
+// leave too few MMAs per staged group.
 bool halo_applies(int w_, int cin, int cout, int c1) {
-    return cin % 16 == 0 && cout % 16 == 0 && cout >= 16 && cout <= 256 && c1 % 16 == 0 &&
+    return cin % 16 == 0 && cout % 16 == 0 && cout >= 16 && cout <= 128 && c1 % 16 == 0 &&
            halo_smem_bytes(w_, halo_blocks(cout), cout) <= 227 * 1024;
 }
 

@@ -16,8 +16,11 @@ PyTorch operations around them.
 
 Tensors are NHWC.  Input channels: 0 = the tile's heights minus their mean,
 divided by the tile's height range (or 1 for a flat tile), 1 = log(1 + range)
-(the relief amplitude, which visibility depends on), 2-7 = 0 (the kernels need
-a multiple of 8 channels).
+(the relief amplitude, which visibility depends on), 2 = the engine's own total
+viewshed of the tile at 1/4 resolution (4 x 4 cell means, 40 m cells, about 1/64
+of the full-resolution run's work), as log(1 + area per cell in tile cells) /
+16, 3-7 = 0 (the kernels need a multiple of 8 channels).  The tile-context head
+predicts a correction to the log of the coarse run's total area.
 """
 from __future__ import annotations
 
@@ -34,6 +37,8 @@ TILE = 256
 IN_CH = 8
 BASE = 32
 CTX = 64  # width of the tile-context MLP
+COARSE = 4  # the coarse engine run's cell is COARSE x COARSE tile cells
+COARSE_SCALE = 16.0  # input channel 2 = log(1 + coarse area per cell) / COARSE_SCALE
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "surrogate_unet32.npz")
 
 
@@ -180,11 +185,11 @@ def make_net(seed: int = 0, device="cuda"):
             # Tile context: the bottleneck's channel means (and maxima) -> MLP
             # -> the log of the tile's total visible area, which calibrates the
             # per-cell map (visibility is a property of whole lines of sight).
-            cin = 2 * 8 * BASE
+            cin = 2 * 8 * BASE + 1
             self.ctx1_w = torch.nn.Parameter(torch.randn(cin, CTX, generator=g) * math.sqrt(2.0 / cin))
             self.ctx1_b = torch.nn.Parameter(torch.zeros(CTX))
             self.ctx2_w = torch.nn.Parameter(torch.randn(CTX, 1, generator=g) * math.sqrt(1.0 / CTX) * 0.1)
-            self.ctx2_b = torch.nn.Parameter(torch.full((1,), 19.0))
+            self.ctx2_b = torch.nn.Parameter(torch.zeros(1))
 
         def c(self, x, name):
             return conv_op(x, self.w[name], self.b[name], True)
@@ -216,8 +221,10 @@ def make_net(seed: int = 0, device="cuda"):
             d1 = self.c(self.upcat(d2, e1, "d1a"), "d1b")
             cells = (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log(1 + area)
             f = b4.float()
-            pooled = torch.cat([f.mean((1, 2)), f.amax((1, 2))], 1)
-            t = (torch.relu(pooled @ self.ctx1_w + self.ctx1_b) @ self.ctx2_w)[:, 0] + self.ctx2_b  # log total
+            # log total area of the coarse engine run (input channel 2)
+            lct = torch.log(torch.expm1(x[..., 2].float() * COARSE_SCALE).clamp_min(0).sum((1, 2)).clamp_min(1.0))
+            pooled = torch.cat([f.mean((1, 2)), f.amax((1, 2)), (lct / 20.0)[:, None]], 1)
+            t = lct + (torch.relu(pooled @ self.ctx1_w + self.ctx1_b) @ self.ctx2_w)[:, 0] + self.ctx2_b
             return calibrate(cells, t)
 
     import torch  # noqa: F811  (used inside forward)
@@ -234,9 +241,37 @@ def calibrate(cells, log_total):
     return torch.log1p(area * scale[:, None, None])
 
 
-def encode_tiles(tiles):
+_COARSE_ENGINES = {}
+
+
+def coarse_area(tiles, engine=None, chunk: int = 4096):
+    """The engine's total viewshed (180 angles) of each tile at 1/COARSE
+    resolution, per tile cell in tile-cell units: (N, 256, 256) float32 (CUDA).
+    The coarse grid averages COARSE x COARSE cells; its heights, observer height
+    and areas are rescaled to its COARSE-times larger cells."""
+    import torch
+    from .engine import SkewEngine, run_batch
+    t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda")
+    n, side = t.shape[0], TILE // COARSE
+    c = (t.reshape(n, side, COARSE, side, COARSE).mean((2, 4)) / COARSE).contiguous()
+    out = torch.empty_like(c)
+    if engine is None:  # one engine per device for the process: it keeps the batch plan
+        dev = torch.cuda.current_device()
+        if dev not in _COARSE_ENGINES:
+            _COARSE_ENGINES[dev] = SkewEngine(side, side, device=dev)
+        engine = _COARSE_ENGINES[dev]
+    povh = float(synthetic.POVH) / COARSE
+    for i in range(0, n, chunk):
+        run_batch(0, [c[j] for j in range(i, min(n, i + chunk))], povh=povh, engine=engine,
+                  outs=[out[j] for j in range(i, min(n, i + chunk))])
+    area = out * float(COARSE * COARSE)
+    return area.repeat_interleave(COARSE, 1).repeat_interleave(COARSE, 2)
+
+
+def encode_tiles(tiles, coarse=None):
     """(N, 256, 256) float32 heights (NumPy or CUDA tensor) -> (N, 256, 256, 8)
-    bfloat16 network input (CUDA)."""
+    bfloat16 network input (CUDA).  coarse: coarse_area(tiles), computed here
+    when not given."""
     import torch
     t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda")
     mean = t.mean((1, 2), keepdim=True)
@@ -244,6 +279,9 @@ def encode_tiles(tiles):
     x = torch.zeros(t.shape + (IN_CH,), dtype=torch.bfloat16, device="cuda")
     x[..., 0] = ((t - mean) / torch.where(rng > 0, rng, torch.ones_like(rng))).to(torch.bfloat16)
     x[..., 1] = torch.log1p(rng).expand_as(t).to(torch.bfloat16)
+    if coarse is None:
+        coarse = coarse_area(t)
+    x[..., 2] = (torch.log1p(coarse) / COARSE_SCALE).to(torch.bfloat16)
     return x
 
 
@@ -451,8 +489,6 @@ def main(argv=None) -> int:
     torch.cuda.synchronize()
     t2 = time.time()
     net = make_net(seed=0)
-    with torch.no_grad():  # start the tile-context head at the data's mean log total
-        net.ctx2_b.fill_(float(_log_total(y[:1024]).mean()))
     losses = train(net, x, y, a.steps, a.batch, a.lr, log=lambda m: print(m, flush=True),
                    tile_weight=a.tile_weight)
     torch.cuda.synchronize()
