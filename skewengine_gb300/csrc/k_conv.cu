@@ -360,27 +360,29 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
 
 // ---- halo-staged forward convolution on the tensor cores ---------------------
 //
-// Output pixels are numbered as slots of rows with one extra slot each: slot
-// s of an image is pixel (s / (W+1), s % (W+1)), and column W is a junk slot
-// whose output is discarded (1/(W+1) of the work).  A CTA computes nb blocks
-// of 128 consecutive slots (nb = 4, or 2 when Cout > 128; its accumulators are
-// nb x Cout tensor-memory columns) for all Cout channels, with Cin and Cout
-// multiples of 16 and Cout <= 256.  K advances in groups of 16 input channels,
+// An image is cut into column segments of Ws pixels (128 when the width is a
+// multiple of 128 above it, else the whole width), and a segment's output
+// pixels are numbered as slots of rows of pitch P = Ws + 2: slot s is pixel
+// (s / P, x0 + s % P), and the two last slots of a row are junk whose outputs
+// are discarded (2/P of the work).  A CTA computes nb blocks of 128
+// consecutive slots of one segment (nb = 8 for Cout <= 32, 4 for Cout <= 128;
+// its accumulators are nb x Cout tensor-memory columns) for all Cout channels,
+// Cin and Cout multiples of 16.  K advances in groups of 16 input channels,
 // each staged once in shared memory as
 //   halo:    two planes of 8 channels holding the input rows the tile's slots
-//            touch, in the same slot layout (row pitch W+1, the extra slot and
-//            a leading slot zero, zeros outside the image): a pixel's 8
-//            channels are one 16-byte row of a core matrix;
+//            touch in the same pitch: plane slot (hr, hc) is input pixel
+//            (R0 - 1 + hr, x0 - 1 + hc), the segment plus one column on each
+//            side, zero outside the image; a pixel's 8 channels are one
+//            16-byte row of a core matrix;
 //   weights: for each of the 9 taps, the 16 channels' Cout x 16 slice in the
 //            canonical K-major layout (8-row x 16-byte core matrices).
-// With that layout the input of output slot s for tap (ky, kx) sits at plane
-// slot s - R0*(W+1) + ky*(W+1) + kx (R0 the tile's first row), so the MMA of
-// block j and tap (ky, kx) reads its A operand in place: 128 consecutive plane
-// slots, core matrices 128 bytes apart (stride byte offset), the second 8
-// channels one plane further (leading byte offset).  The zero slot between
-// rows is what the left tap of column 0 and the right tap of column W-1 read,
-// the zero padding.  Each input pixel leaves L2 once per CTA (plus the two
-// halo rows) instead of once per tap as in the im2col gather above.
+// The input of output slot s for tap (ky, kx) then sits at plane slot
+// s - R0*P + ky*P + kx (R0 the tile's first row), so the MMA of block j and tap
+// (ky, kx) reads its A operand in place: 128 consecutive plane slots, core
+// matrices 128 bytes apart (stride byte offset), the second 8 channels one
+// plane further (leading byte offset).  Each input pixel leaves L2 once per CTA
+// (plus the two halo rows and columns) instead of once per tap as in the
+// im2col gather above.
 // kHaloStages groups are in flight; thread 0 issues a group's MMAs (nb blocks x
 // 9 taps, K = 16 each) and commits them to the stage's mbarrier, which frees
 // the stage for the group kHaloStages later.  Waits are bounded as in
@@ -388,16 +390,17 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X
 constexpr int kHaloStages = 2;
 constexpr int kSlotBlock = 128;
 
-// Plane slots of a tile of nb blocks: the leading zero slot, then enough rows of
-// W+1 slots for every tap of every output slot.
-__host__ __device__ constexpr int halo_slots(int W, int nb) { return 3 * (W + 1) + nb * kSlotBlock + 1; }
-__host__ __device__ constexpr int halo_plane(int W, int nb) { return halo_slots(W, nb) * 16; }
+// Column segment width of an image width, and plane slots of a tile of nb
+// blocks at row pitch P = Ws + 2: enough rows for every tap of every output slot.
+__host__ __device__ constexpr int halo_seg(int W) { return (W > 128 && W % 128 == 0) ? 128 : W; }
+__host__ __device__ constexpr int halo_slots(int P, int nb) { return 3 * P + nb * kSlotBlock; }
+__host__ __device__ constexpr int halo_plane(int P, int nb) { return halo_slots(P, nb) * 16; }
 __host__ __device__ constexpr int halo_wbytes(int cout) { return 9 * 2 * cout * 16; }
-__host__ __device__ constexpr int halo_stage_bytes(int W, int nb, int cout) {
-    return (2 * halo_plane(W, nb) + halo_wbytes(cout) + 1023) / 1024 * 1024;
+__host__ __device__ constexpr int halo_stage_bytes(int P, int nb, int cout) {
+    return (2 * halo_plane(P, nb) + halo_wbytes(cout) + 1023) / 1024 * 1024;
 }
-__host__ __device__ constexpr int halo_smem_bytes(int W, int nb, int cout) {
-    return kHaloStages * halo_stage_bytes(W, nb, cout) + 1024 + 64;
+__host__ __device__ constexpr int halo_smem_bytes(int P, int nb, int cout) {
+    return kHaloStages * halo_stage_bytes(P, nb, cout) + 1024 + 64;
 }
 
 // Descriptor with explicit byte offsets (16-byte units): no swizzle, version 1.
@@ -411,20 +414,25 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_halo(const bf16* __restric
                                                            const float* __restrict__ bias, bf16* __restrict__ Y,
                                                            int H, int W, int Cin, int Cout, int Kpad, int relu,
                                                            const bf16* __restrict__ X2, int C1, int nb,
-                                                           int tiles_per_img) {
+                                                           int tiles_per_seg) {
     extern __shared__ __align__(1024) unsigned char hsm_raw[];
     unsigned char* hsm = hsm_raw + ((1024 - (smem_u32(hsm_raw) & 1023)) & 1023);  // 1024-byte aligned stages
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int W1 = W + 1;
-    const int hslots = halo_slots(W, nb);
+    const int Ws = halo_seg(W), P = Ws + 2, segs = W / Ws;
+    const int hslots = halo_slots(P, nb);
     const int plane = hslots * 16;
-    const int sbytes = halo_stage_bytes(W, nb, Cout);
+    const int sbytes = halo_stage_bytes(P, nb, Cout);
     uint64_t* bar = reinterpret_cast<uint64_t*>(hsm + kHaloStages * sbytes);
     unsigned* tslot = reinterpret_cast<unsigned*>(bar + kHaloStages);
-    const int n = blockIdx.x / tiles_per_img;
-    const int S0 = (blockIdx.x - n * tiles_per_img) * nb * kSlotBlock;  // first output slot of the tile
-    const int R0 = S0 / W1;                                              // its row
-    const int soff = S0 - R0 * W1;                                       // its column (plane slot base)
+    int bi = blockIdx.x;
+    const int tile = bi % tiles_per_seg;
+    bi /= tiles_per_seg;
+    const int seg = bi % segs;
+    const int n = bi / segs;
+    const int x0 = seg * Ws;                     // the segment's first column
+    const int S0 = tile * nb * kSlotBlock;       // first output slot of the tile
+    const int R0 = S0 / P;                       // its row
+    const int soff = S0 - R0 * P;                // its column (plane slot base)
     unsigned ncols = 32;
     while (ncols < (unsigned)(nb * Cout)) ncols <<= 1;
 
@@ -445,18 +453,18 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_halo(const bf16* __restric
 
     const int groups = Cin / 16;
     const int64_t img = (int64_t)n * H * W;
-    // Stage group g into stage st: plane slot p >= 1 is input (R0 - 1 + t / W1,
-    // t % W1), t = p - 1; slot 0 and column W are zero.
+    // Stage group g into stage st: plane slot p is input (R0 - 1 + p / P,
+    // x0 - 1 + p % P), zero outside the image.
     auto load = [&](int st, int g) {
         unsigned char* base = hsm + st * sbytes;
         const int c0 = 16 * g;
         for (int q = tid; q < 2 * hslots; q += kThreads) {
             const int pl = q >= hslots;
             const int p = q - pl * hslots;
-            const int t = p - 1;
-            const int iy = R0 - 1 + (t >= 0 ? t / W1 : -1), ix = t >= 0 ? t - (t / W1) * W1 : W;
+            const int hr = p / P;
+            const int iy = R0 - 1 + hr, ix = x0 - 1 + (p - hr * P);
             const int ci = c0 + 8 * pl;
-            const bool ok = t >= 0 && iy >= 0 && iy < H && ix < W;
+            const bool ok = iy >= 0 && iy < H && ix >= 0 && ix < W;
             const bf16* src = X;
             if (ok) {
                 if (!kUpCat)
@@ -507,7 +515,7 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_halo(const bf16* __restric
 #pragma unroll
                 for (int tap = 0; tap < 9; tap++) {
                     const int ky = tap / 3, kx = tap - 3 * (tap / 3);
-                    const int p0 = soff + j * kSlotBlock + ky * W1 + kx;
+                    const int p0 = soff + j * kSlotBlock + ky * P + kx;
                     const uint64_t da = tc_desc2(hb + (unsigned)(p0 * 16), (unsigned)plane, 128);
                     const uint64_t db = tc_desc2(wb + (unsigned)(tap * 2 * Cout * 16), (unsigned)(Cout * 16), 128);
                     tc_mma(tmem + (unsigned)(j * Cout), da, db, idesc, (g | tap) != 0);
@@ -525,9 +533,9 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_halo(const bf16* __restric
     if (!fail) {
         for (int j = 0; j < nb; j++) {
             const int s = S0 + j * kSlotBlock + warp * 32 + lane;  // this thread's slot (TMEM lane)
-            const int r = s / W1, c = s - (s / W1) * W1;
-            const bool store = r < H && c < W;
-            bf16* dst = Y + ((img + (int64_t)r * W + c) * Cout);
+            const int r = s / P, c = s - (s / P) * P;
+            const bool store = r < H && c < Ws;
+            bf16* dst = Y + ((img + (int64_t)r * W + x0 + c) * Cout);
             for (int c0 = 0; c0 < Cout; c0 += 16) {
                 float v[16];
                 tc_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(j * Cout + c0), v);
@@ -657,14 +665,14 @@ int g_conv_path = 0;
 // concatenation, C1 are multiples of 16 and its stages fit shared memory.  Its
 // shared memory is padded so that the CTAs an SM holds never ask for more than
 // its 512 tensor-memory columns.
-int halo_blocks(int cout) { return cout > 128 ? 2 : 4; }
+int halo_blocks(int cout) { return cout <= 32 ? 8 : cout <= 128 ? 4 : 2; }
 
 // Cout above 128 (the 32 x 32, 256-channel bottleneck) measured faster on the
 // im2col kernel (155-185 against 201-228 TFLOP/s): two 128-slot blocks per CTA
 // leave too few MMAs per staged group.
 bool halo_applies(int w_, int cin, int cout, int c1) {
     return cin % 16 == 0 && cout % 16 == 0 && cout >= 16 && cout <= 128 && c1 % 16 == 0 &&
-           halo_smem_bytes(w_, halo_blocks(cout), cout) <= 227 * 1024;
+           halo_smem_bytes(halo_seg(w_) + 2, halo_blocks(cout), cout) <= 227 * 1024;
 }
 
 template <bool kUpCat>
@@ -674,7 +682,8 @@ int launch_conv_halo(const bf16* x, const bf16* w, const float* bias, bf16* y, i
     const int nb = halo_blocks(cout);
     unsigned ncols = 32;
     while (ncols < (unsigned)(nb * cout)) ncols <<= 1;
-    int smem = halo_smem_bytes(w_, nb, cout);
+    const int ws = halo_seg(w_), pitch = ws + 2;
+    int smem = halo_smem_bytes(pitch, nb, cout);
     const int max_ctas = 512 / (int)ncols;  // CTAs whose columns fit the SM's tensor memory
     const int floor_smem = 228 * 1024 / (max_ctas + 1) + 1;
     if (smem < floor_smem) smem = floor_smem;
@@ -682,9 +691,9 @@ int launch_conv_halo(const bf16* x, const bf16* w, const float* bias, bf16* y, i
     if (cudaFuncSetAttribute(k_conv3x3_halo<kUpCat>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
         cudaSuccess)
         return SKE_ERR_CUDA;
-    const int64_t slots = (int64_t)h * (w_ + 1);
+    const int64_t slots = (int64_t)h * pitch;  // of one segment
     const int64_t tiles = (slots + (int64_t)nb * kSlotBlock - 1) / ((int64_t)nb * kSlotBlock);
-    const int64_t blocks = (int64_t)n * tiles;
+    const int64_t blocks = (int64_t)n * (w_ / ws) * tiles;
     if (blocks > 0x7fffffff || slots > 0x7fffffff / 2) return SKE_ERR_INVALID;
     k_conv3x3_halo<kUpCat><<<(unsigned)blocks, kThreads, smem, st>>>(x, w, bias, y, h, w_, cin, cout, kpad, relu, x2,
                                                                      c1, nb, (int)tiles);
