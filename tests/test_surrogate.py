@@ -166,10 +166,16 @@ def test_trained_network_beats_the_untrained_method(sur):
     with torch.no_grad():
         pred = torch.cat([net(x[i:i + 16]) for i in range(0, len(tiles), 16)])
         raw = torch.cat([sur.make_net(seed=5)(x[i:i + 16]) for i in range(0, len(tiles), 16)])
-    trained = np.median(sur.tile_area_error(pred, y))
+    err = sur.tile_area_error(pred, y)
+    trained = np.median(err)
     constant = np.median(sur.tile_area_error(torch.full_like(y, float(y.mean())), y))
     untrained = np.median(sur.tile_area_error(raw, y))
+    print(f"held-out tile-area error: trained median {trained:.4f} p90 {np.quantile(err, 0.9):.4f}, "
+          f"constant {constant:.4f}, untrained {untrained:.4f}")
     assert trained < 0.5 * constant and trained < 0.5 * untrained, (trained, constant, untrained)
+    # The stated bound: median tile-area error within 2.5% on these held-out tiles
+    # (1.9% median, 4.4% at the 90th percentile on the 256 validation tiles of training).
+    assert trained <= 0.025, trained
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout,relu", [(1, 8, 128, 32, 32, True), (2, 4, 256, 16, 48, False),
