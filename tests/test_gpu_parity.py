@@ -398,6 +398,11 @@ def test_radon_fused_sector_kernel_bit_exact(ske, oracle, gpu_lib):
         x = synthetic.ellipse_phantom(64, 9)
         x[3, 5] = np.inf
         x[40, 7] = np.nan
-        assert bits_equal(_run(ske, 2, x), oracle.run(2, x, povh=POVH))
+        fused = _run(ske, 2, x)
+        assert gpu_lib.ske_radon_select(1) == 0
+        two = _run(ske, 2, x)
+        assert bits_equal(fused, two)  # both on the GPU: the same NaN encodings too
+        want = oracle.run(2, x, povh=POVH)  # host NaNs may be encoded differently
+        assert ((fused.view(np.uint32) == want.view(np.uint32)) | (np.isnan(fused) & np.isnan(want))).all()
     finally:
         gpu_lib.ske_radon_select(1)
