@@ -582,7 +582,7 @@ def surrogate_workload(args):
     truth_b = torch.empty_like(tdev)
 
     def plain_batched():  # every tile in one batched engine call (five launches, graph replay)
-        ske.run_batch(0, [tdev[i] for i in range(len(tiles))], engine=beng, outs=[truth_b[i] for i in range(len(tiles))])
+        ske.run_batch(0, tdev, engine=beng, outs=truth_b)
         torch.cuda.synchronize()
 
     dem_dev = torch.as_tensor(np.ascontiguousarray(dem, np.float32), device="cuda")
@@ -802,6 +802,7 @@ def main():
                    "dem": f"{side}x{side}", "sectors": DIR_SECTORS, "parallelism": f"replicas{world}",
                    "kernel_ms_per_step": breakdown, "wall_ms_per_step": wall_ms,
                    "profiled_pass_ms_per_step": prof_ms,
+                   "sweep_shape": dict(zip(("lvl0", "lvl1", "ctas_per_sm"), eng.sweep_shape())),
                    "l2": f"{L2_FLUSH_BYTES >> 20} MiB written between steps (inputs {x.nbytes >> 20} MB are L2-resident)"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(x.nbytes), "d2h_bytes_per_step": int(x.nbytes),
                 "ms_per_step": e2e_ms},

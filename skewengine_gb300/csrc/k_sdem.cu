@@ -704,11 +704,14 @@ __device__ __forceinline__ void run_level(const float* __restrict__ A, const Row
         sweep_batch<true, false, kLen>(A, rm, L, povh, rl, d0, len, lane);
 }
 
-// Level lengths: lvl0, then lvl1 (skipped when 0), then kLevel each; each one
-// of 16, 32, 48 or 64 steps.  The built-in schedule (all kLevel) runs with a
-// compile-time level length; any other runs one loop with run-time lengths.
-// Two code paths, not one per length: a sweep that mixed several compiled
-// lengths in one row measured much slower (instruction-cache misses).
+// kFixed: every level kLevel steps, a compile-time length (the built-in
+// schedule).  Otherwise lvl0, then lvl1 (skipped when 0), then kLevel each, each
+// one of 16, 32, 48 or 64 steps, in one loop with run-time lengths.  The two are
+// separate kernels: with both in one kernel the built-in schedule ran 7%
+// slower (shared register allocation), and a loop compiled once per length ran
+// the short schedules far slower still (a row then executes several compiled
+// lengths and falls out of the instruction cache).
+template <bool kFixed>
 __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, float povh, int4* lists,
                           int max_row, float* cvf, float* cvb, const RowOut& o, int lane, int lvl0, int lvl1) {
     RowLists rl;
@@ -723,7 +726,7 @@ __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, 
         len = level == 0 ? lvl0 : (level == 1 && lvl1 > 0) ? lvl1 : kLevel;
         rl.used[0] = rl.used[1] = 0;
         rl.made[0] = rl.made[1] = 0;
-        if (lvl0 == kLevel && lvl1 == 0) run_level<kLevel>(A, rm, L, povh, rl, d0, len, lane);
+        if (kFixed) run_level<kLevel>(A, rm, L, povh, rl, d0, kLevel, lane);
         else run_level<0>(A, rm, L, povh, rl, d0, len, lane);
         __syncwarp();  // this level's lists and counts are visible to every lane
 #pragma unroll
@@ -743,7 +746,8 @@ __device__ void sweep_row(const float* __restrict__ A, const RowMax& rm, int L, 
 
 // kBatch: the items are batch_item()s of a batched run over several grids,
 // whose rows are compact rows of the pools SI/SO (kernels.h, BatchGrid).
-template <bool kBatch>
+// kFixed: the built-in level schedule (see sweep_row).
+template <bool kBatch, bool kFixed>
 __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
     extern __shared__ float4 smem4[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -820,7 +824,7 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
             row_maxima(A, L, s128, p128, b16, b128, lane);
             __syncwarp();
             const RowMax rm{s128, p128, b16, b128, nblk(L, kB2)};
-            sweep_row(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane, a.lvl0, a.lvl1);
+            sweep_row<kFixed>(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane, a.lvl0, a.lvl1);
         } else {
             for (int x = lane; x < L; x += 32) {
                 if (!owns(o, x)) continue;
@@ -951,7 +955,9 @@ size_t sdem_list_bytes(int max_row, int num_sms) {
 
 int sdem_max_ctas_per_sm(const SdemLaunch& a) {
     const size_t smem = sizeof(float) * (size_t)LLayout(std::max(a.max_row, 1)).total * kLWarps;
-    auto kern = a.batched ? k_sdem<true> : k_sdem<false>;
+    const bool fixed = a.lvl0 == kLevel && a.lvl1 == 0;
+    auto kern = a.batched ? (fixed ? k_sdem<true, true> : k_sdem<true, false>)
+                          : (fixed ? k_sdem<false, true> : k_sdem<false, false>);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -969,7 +975,9 @@ cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     auto level_ok = [](int v) { return v == 16 || v == 32 || v == 48 || v == 64; };
     if (!level_ok(a.lvl0) || (a.lvl1 != 0 && !level_ok(a.lvl1)) || a.ctas_per_sm < 0) return cudaErrorInvalidValue;
     const size_t smem = sizeof(float) * (size_t)LLayout(a.max_row).total * kLWarps;
-    auto kern = a.batched ? k_sdem<true> : k_sdem<false>;
+    const bool fixed = a.lvl0 == kLevel && a.lvl1 == 0;
+    auto kern = a.batched ? (fixed ? k_sdem<true, true> : k_sdem<true, false>)
+                          : (fixed ? k_sdem<false, true> : k_sdem<false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;

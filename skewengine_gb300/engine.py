@@ -322,34 +322,62 @@ def execute(kernel, data, max_sector: int = 180, povh: float = DEFAULT_POVH, acc
 def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference",
               device: int = 0, outs=None, angles=None, engine=None, flags: int = 0):
     """Run one operator over many grids of uneven size (``ske_run_batch``, or
-    ``ske_run_batch_angles`` with an angle list).  ``engine``: an existing
-    SkewEngine to run on (it keeps the batch's plan and buffers for later calls);
-    by default one is made for the largest grid and closed afterwards."""
-    grids = list(grids)
-    if not grids:
-        return []
-    dims = [(g.shape[1], g.shape[0]) for g in grids]
-    big = max(dims, key=lambda d: d[0] * d[1])
-    on_dev = _is_device(grids[0])
-    if outs is None:
-        if on_dev:
-            import torch
-            outs = [torch.empty_like(g) for g in grids]
-        else:
-            outs = [np.empty_like(g) for g in grids]
-    ins = (C.c_void_p * len(grids))(*[_ptr(g)[0].value for g in grids])
-    ous = (C.c_void_p * len(grids))(*[_ptr(o, writable=True)[0].value for o in outs])
-    dx = np.array([d[0] for d in dims], np.int32)
-    dy = np.array([d[1] for d in dims], np.int32)
+    ``ske_run_batch_angles`` with an angle list).  ``grids`` is a list of 2-D
+    arrays or tensors, or one C-contiguous (N, H, W) float32 array or tensor of
+    N equal grids (``outs`` then the same, made when None); for the stack the
+    pointer tables are computed, not gathered grid by grid.  ``engine``: an
+    existing SkewEngine to run on (it keeps the batch's plan and buffers for
+    later calls); by default one is made for the largest grid and closed
+    afterwards."""
+    stacked = getattr(grids, "ndim", 2) == 3
+    if stacked:
+        n, h, w = (int(v) for v in grids.shape)
+        if n == 0:
+            return grids if outs is None else outs
+        on_dev = _is_device(grids)
+        if outs is None:
+            if on_dev:
+                import torch
+                outs = torch.empty_like(grids)
+            else:
+                outs = np.empty_like(grids)
+        for arr in (grids, outs):
+            _ptr(arr, (n, h, w), writable=arr is outs)  # dtype, contiguity, shape checks
+        step = np.arange(n, dtype=np.uint64) * np.uint64(4 * h * w)
+        ip = (np.uint64(_ptr(grids)[0].value) + step).astype(np.uint64)
+        op = (np.uint64(_ptr(outs)[0].value) + step).astype(np.uint64)
+        ins = (C.c_void_p * n).from_buffer_copy(ip.tobytes())
+        ous = (C.c_void_p * n).from_buffer_copy(op.tobytes())
+        dx = np.full(n, w, np.int32)
+        dy = np.full(n, h, np.int32)
+        big, count = (w, h), n
+    else:
+        grids = list(grids)
+        if not grids:
+            return []
+        dims = [(g.shape[1], g.shape[0]) for g in grids]
+        big = max(dims, key=lambda d: d[0] * d[1])
+        on_dev = _is_device(grids[0])
+        if outs is None:
+            if on_dev:
+                import torch
+                outs = [torch.empty_like(g) for g in grids]
+            else:
+                outs = [np.empty_like(g) for g in grids]
+        ins = (C.c_void_p * len(grids))(*[_ptr(g)[0].value for g in grids])
+        ous = (C.c_void_p * len(grids))(*[_ptr(o, writable=True)[0].value for o in outs])
+        dx = np.array([d[0] for d in dims], np.int32)
+        dy = np.array([d[1] for d in dims], np.int32)
+        count = len(grids)
     prm = params(max_sector, povh, accum, flags)
     eng = engine if engine is not None else SkewEngine(big[0], big[1], device)
     try:
         if angles is None:
-            check(eng._lib.ske_run_batch(eng._h, _kernel_id(kernel), len(grids), dx.ctypes.data, dy.ctypes.data,
+            check(eng._lib.ske_run_batch(eng._h, _kernel_id(kernel), count, dx.ctypes.data, dy.ctypes.data,
                                          ins, int(on_dev), ous, int(on_dev), C.byref(prm)))
         else:
             a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
-            check(eng._lib.ske_run_batch_angles(eng._h, _kernel_id(kernel), len(grids), dx.ctypes.data,
+            check(eng._lib.ske_run_batch_angles(eng._h, _kernel_id(kernel), count, dx.ctypes.data,
                                                 dy.ctypes.data, ins, int(on_dev), ous, int(on_dev), a.ctypes.data,
                                                 len(a), C.byref(prm)))
     finally:

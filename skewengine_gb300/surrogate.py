@@ -262,8 +262,7 @@ def coarse_area(tiles, engine=None, chunk: int = 4096):
         engine = _COARSE_ENGINES[dev]
     povh = float(synthetic.POVH) / COARSE
     for i in range(0, n, chunk):
-        run_batch(0, [c[j] for j in range(i, min(n, i + chunk))], povh=povh, engine=engine,
-                  outs=[out[j] for j in range(i, min(n, i + chunk))])
+        run_batch(0, c[i:i + chunk], povh=povh, engine=engine, outs=out[i:i + chunk])
     area = out * float(COARSE * COARSE)
     return area.repeat_interleave(COARSE, 1).repeat_interleave(COARSE, 2)
 
@@ -294,7 +293,7 @@ def label_tiles(tiles: np.ndarray, engine=None, chunk: int = 512):
     out = torch.empty(tiles.shape, dtype=torch.float32, device="cuda")
     for i in range(0, len(tiles), chunk):
         x = torch.as_tensor(np.ascontiguousarray(tiles[i:i + chunk], np.float32), device="cuda")
-        run_batch(0, [x[j] for j in range(len(x))], engine=eng, outs=[out[i + j] for j in range(len(x))])
+        run_batch(0, x, engine=eng, outs=out[i:i + len(x)])
     torch.cuda.synchronize()
     if engine is None:
         eng.close()
@@ -413,7 +412,7 @@ def _cut_tiles_dev(dem):
 
 
 def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float = 0.02,
-              batch: int = 16, seed: int = 0, force_error=None):
+              batch: int = 256, seed: int = 0, force_error=None):
     """Per-tile total viewshed of a large DEM cut into 256 x 256 tiles (edge tiles
     padded by replicating the last row / column).  The network predicts every
     tile; the engine recomputes a random check_fraction of them, and any checked
@@ -444,7 +443,7 @@ def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float 
     # All checked tiles in one batched engine call (ske_run_batch: the engine
     # keeps the batch plan and replays it as a CUDA graph on later calls).
     sel = tiles[torch.as_tensor(checked, device="cuda")].contiguous()
-    run_batch(0, [sel[j] for j in range(n_check)], engine=eng, outs=[truth[j] for j in range(n_check)])
+    run_batch(0, sel, engine=eng, outs=truth)
     truth = torch.log1p(truth)
     errs = tile_area_error(out[torch.as_tensor(checked, device="cuda")], truth)
     if force_error:

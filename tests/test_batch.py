@@ -104,3 +104,17 @@ def test_autotuned_single_grid_run_is_unchanged(ske, oracle):
         assert eng.sweep_shape() == (64, 0, 0)
     assert bits_equal(tuned, fixed)
     assert bits_equal(tuned, oracle.run_ordered(0, x, povh=POVH))
+
+
+def test_batch_stacked_grids_equal_list(ske, oracle):
+    """A (N, H, W) stack runs as N grids with computed pointer tables, device and
+    host, with the same bits as the list form."""
+    torch = pytest.importorskip("torch")
+    stack = np.stack([synthetic.fractal_dem(48, 950 + i) for i in range(5)]).astype(np.float32)
+    with ske.SkewEngine(48, 48) as eng:
+        host = ske.run_batch(0, stack, povh=POVH, engine=eng)
+        dev = ske.run_batch(0, torch.from_numpy(stack).cuda(), povh=POVH, engine=eng)
+        lst = ske.run_batch(0, [g for g in stack], povh=POVH, engine=eng)
+    for i in range(5):
+        want = oracle.run_ordered(0, stack[i], povh=POVH)
+        assert bits_equal(host[i], want) and bits_equal(dev[i].cpu().numpy(), want) and bits_equal(lst[i], want)
