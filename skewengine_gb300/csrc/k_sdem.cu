@@ -836,6 +836,279 @@ __global__ void __launch_bounds__(kLWarps * 32) k_sdem(SdemLaunch a) {
     }
 }
 
+// ---- the built-in schedule, per-engine runs ---------------------------------
+// The same sweep as k_sdem<false, true>, kept as its own copy: the built-in
+// schedule's kernel ran 7% slower once the level-length and batch variants
+// shared its source functions (the compiler allocates and schedules this hot
+// loop differently; with a larger register budget it ran slower still), so the
+// engine's per-grid runs launch this copy, whose code is the one measured in
+// the sweep's tuning record.
+__device__ __forceinline__ bool owns64(const RowOut& o, int x) {
+    return o.first + x < o.sd->dim_i || owner_row(*o.sd, o.rfirst, o.rlast, o.rowbase + x) == o.row;
+}
+
+template <bool kF0, bool kF1>
+__device__ __forceinline__ void level_steps64(Slots& s, const float* __restrict__ A, int d0) {
+    const float* p0 = A + (kF0 ? s.x[0] + d0 : s.x[0] - d0);
+    const float* p1 = A + (kF1 ? s.x[1] + d0 : s.x[1] - d0);
+    const f2 hh = pk(s.h[0], s.h[1]);
+#pragma unroll 1
+    for (int k0 = 0; k0 < kLevel; k0 += kUnroll) {
+#pragma unroll
+        for (int k = 0; k < kUnroll; k++) {
+            const int d = d0 + k0 + k;
+            const float4 st = c_step[d];
+            const float z0 = kF0 ? p0[k] : p0[-k];
+            const float z1 = kF1 ? p1[k] : p1[-k];
+            float q0, q1;
+            upk(div2(sub2(pk(z0, z1), hh), pk(st.x, st.x), pk(st.y, st.y)), q0, q1);
+            visit(s, 0, q0, st.z);
+            visit(s, 1, q1, st.z);
+        }
+        p0 += kF0 ? kUnroll : -kUnroll;
+        p1 += kF1 ? kUnroll : -kUnroll;
+    }
+}
+
+// One batch of a level: slot q takes entry used[dir] + lane + 32*qi of its
+// direction's list, where qi counts the batch's earlier slots of that direction.
+template <bool kF0, bool kF1>
+__device__ __forceinline__ void sweep_batch64(const float* __restrict__ A, const RowMax& rm, int L, float povh,
+                                            RowLists& rl, int d0, int lane) {
+    constexpr bool kDir[kSlots] = {kF0, kF1};
+    const unsigned below = (1u << lane) - 1u;
+    const int dc = d0 + kLevel - 1;  // last step of the level
+    Slots s;
+#pragma unroll
+    for (int q = 0; q < kSlots; q++) {
+        const int dir = kDir[q] ? 0 : 1;
+        const int idx = rl.used[dir] + lane + (q == 1 && kF0 == kF1 ? 32 : 0);
+        if (idx < rl.n[dir]) {
+            if (rl.in[dir]) {
+                const int4 e = rl.in[dir][idx];
+                s.x[q] = e.x;
+                s.mx[q] = __int_as_float(e.y);
+                s.acc[q] = __int_as_float(e.z);
+                s.cl[q] = __int_as_float(e.w);
+            } else {
+                s.x[q] = idx;
+                s.mx[q] = -2000.0f;
+                s.acc[q] = 0.0f;
+                s.cl[q] = -1.0f;
+            }
+            s.n[q] = kDir[q] ? L - 1 - s.x[q] : s.x[q];
+            s.valid[q] = true;
+            s.h[q] = __fadd_rn(A[s.x[q]], povh);
+        } else {
+            // Empty: its reads stay in A[-(kLevel-1) .. kLevel-1].
+            s.x[q] = kDir[q] ? -d0 : d0;
+            s.n[q] = dc;
+            s.valid[q] = false;
+            s.h[q] = s.mx[q] = s.acc[q] = s.cl[q] = 0.0f;
+        }
+    }
+    if (kF0 == kF1) rl.used[kF0 ? 0 : 1] += 64;
+    else rl.used[0] += 32, rl.used[1] += 32;
+    level_steps64<kF0, kF1>(s, A, d0);
+
+    // Retire finished observers, keep the others for the next level.
+#pragma unroll
+    for (int q = 0; q < kSlots; q++) {
+        const int dir = kDir[q] ? 0 : 1;
+        bool keep = false;
+        if (s.valid[q]) {
+            bool done = false;
+            if (s.n[q] > dc) {
+                done = kDir[q] ? retire<true>(rm, s.x[q], s.n[q], dc, s.h[q], s.mx[q])
+                               : retire<false>(rm, s.x[q], s.n[q], dc, s.h[q], s.mx[q]);
+                keep = !done;
+            }
+            if (!keep) rl.cv[dir][s.x[q]] = __fadd_rn(1.0f, done ? s.acc[q] : s.cl[q]);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep)
+            rl.out[dir][rl.made[dir] + __popc(m & below)] =
+                make_int4(s.x[q], __float_as_int(s.mx[q]), __float_as_int(s.acc[q]), __float_as_int(s.cl[q]));
+        rl.made[dir] += __popc(m);
+    }
+}
+
+// Both scan directions of the row, level by level.  Level 0 takes every
+// observer 0..L-1 in each direction; each later level takes the previous
+// level's survivors.  A level runs full batches of one direction while a list
+// has 64 entries left, then pairs what remains of the two (a forward observer
+// in slot 0, a backward one in slot 1), so short lists share batches.
+// lists: four lists of L_max entries (forward in/out, backward in/out);
+// cvf, cvb: the two directions' counts, added and scaled at the end.
+__device__ void sweep_row64(const float* __restrict__ A, const RowMax& rm, int L, float povh, int4* lists,
+                          int max_row, float* cvf, float* cvb, const RowOut& o, int lane) {
+    RowLists rl;
+    rl.in[0] = rl.in[1] = nullptr;
+    rl.out[0] = lists;
+    rl.out[1] = lists + 2 * (int64_t)max_row;
+    rl.n[0] = rl.n[1] = L;
+    rl.cv[0] = cvf;
+    rl.cv[1] = cvb;
+    for (int d0 = 1; rl.n[0] > 0 || rl.n[1] > 0; d0 += kLevel) {
+        rl.used[0] = rl.used[1] = 0;
+        rl.made[0] = rl.made[1] = 0;
+        while (rl.n[0] - rl.used[0] >= 64) sweep_batch64<true, true>(A, rm, L, povh, rl, d0, lane);
+        while (rl.n[1] - rl.used[1] >= 64) sweep_batch64<false, false>(A, rm, L, povh, rl, d0, lane);
+        while (rl.used[0] < rl.n[0] || rl.used[1] < rl.n[1]) sweep_batch64<true, false>(A, rm, L, povh, rl, d0, lane);
+        __syncwarp();  // this level's lists and counts are visible to every lane
+#pragma unroll
+        for (int dir = 0; dir < 2; dir++) {
+            int4* base = lists + 2 * (int64_t)max_row * dir;
+            rl.in[dir] = rl.out[dir];
+            rl.out[dir] = rl.out[dir] == base ? base + max_row : base;
+            rl.n[dir] = rl.made[dir];
+        }
+    }
+    for (int x = lane; x < L; x += 32) {
+        if (!owns64(o, x)) continue;
+        const float t = __fadd_rn(cvf[x], cvb[x]);  // forward count, then backward
+        o.out[o.rowbase + x] = o.counts_only ? t : __fmul_rn(t, o.sd->r2);
+    }
+}
+
+__global__ void __launch_bounds__(kLWarps * 32) k_sdem_fixed(SdemLaunch a) {
+    extern __shared__ float4 smem4[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const LLayout lay(a.max_row);
+    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * lay.total;
+    float* A = buf + kLPad;
+    float* s128 = buf + lay.s128;
+    float* p128 = buf + lay.p128;
+    float* b16 = buf + lay.b16;
+    float* b128 = buf + lay.b128;
+    const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    int4* lists = a.lists + gwarp * kListsPerWarp * (int64_t)a.max_row;
+    float* cvf = reinterpret_cast<float*>(lists + 4 * (int64_t)a.max_row);
+    float* cvb = cvf + a.max_row;
+    for (;;) {
+        unsigned idx = 0;
+        if (lane == 0) idx = atomicAdd(a.counter, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if ((int64_t)idx >= a.n_items) break;
+        const Item it = decode(a.items[idx]);
+        const SectorDesc& d = a.g.desc[a.b.angle[it.slot]];
+        const int32_t* first = a.g.first + d.row_off;
+        const int32_t* last = a.g.last + d.row_off;
+        const int f = first[it.row];
+        const int L = last[it.row] - f;
+        if (L > a.max_row || L <= 0) {
+            if (lane == 0) atomicExch(a.status, 1);
+            continue;
+        }
+        RowOut o;
+        o.out = a.SO + it.slot * a.stride;
+        o.rowbase = (int64_t)it.row * d.dim_i + f;
+        o.first = f;
+        o.row = it.row;
+        o.sd = &d;
+        o.rfirst = first;
+        o.rlast = last;
+        o.counts_only = a.counts_only;
+        const float* src = a.SI + it.slot * a.stride + o.rowbase;
+        bool ok = true;
+        for (int x = lane; x < L; x += 32) {
+            const float v = src[x];
+            A[x] = v;
+            ok = ok && div_safe(v) && div_safe(__fadd_rn(v, a.povh));
+        }
+        const float pad = __int_as_float(0x7fc00000);  // NaN (see visit)
+        for (int x = lane; x < kLPad; x += 32) buf[x] = pad;
+        const int tail_end = ((L + 3) & ~3) + kLPad;
+        for (int x = L + lane; x < tail_end; x += 32) A[x] = pad;
+        const bool fast = __all_sync(0xffffffffu, ok) && L <= kLFastMaxRow && div_safe(a.povh);
+        __syncwarp();
+        if (fast) {
+            row_maxima(A, L, s128, p128, b16, b128, lane);
+            __syncwarp();
+            const RowMax rm{s128, p128, b16, b128, nblk(L, kB2)};
+            sweep_row64(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane);
+        } else {
+            for (int x = lane; x < L; x += 32) {
+                if (!owns64(o, x)) continue;
+                const float cv = scan_reference(A, x, L, a.povh);
+                o.out[o.rowbase + x] = a.counts_only ? cv : __fmul_rn(cv, d.r2);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// The built-in schedule for batched runs: the same sweep over compact rows
+// (kernels.h, BatchGrid); only the work item's decode differs.
+__global__ void __launch_bounds__(kLWarps * 32) k_sdem_fixed_batch(SdemLaunch a) {
+    extern __shared__ float4 smem4[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const LLayout lay(a.max_row);
+    float* buf = reinterpret_cast<float*>(smem4) + (size_t)warp * lay.total;
+    float* A = buf + kLPad;
+    float* s128 = buf + lay.s128;
+    float* p128 = buf + lay.p128;
+    float* b16 = buf + lay.b16;
+    float* b128 = buf + lay.b128;
+    const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + warp;
+    int4* lists = a.lists + gwarp * kListsPerWarp * (int64_t)a.max_row;
+    float* cvf = reinterpret_cast<float*>(lists + 4 * (int64_t)a.max_row);
+    float* cvb = cvf + a.max_row;
+    for (;;) {
+        unsigned idx = 0;
+        if (lane == 0) idx = atomicAdd(a.counter, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if ((int64_t)idx >= a.n_items) break;
+        const uint64_t raw = a.items[idx];
+        const BatchSector bs = a.bt.sectors[(int)(raw >> 32)];
+        const BatchGrid& G = a.bt.grids[bs.grid];
+        const int row = (int)(raw & 0xffffffffu);
+        const SectorDesc& d = G.desc[bs.angle];
+        const int4 m = G.rowtab[d.row_off + row];  // {first, last, rowoff}
+        const int f = m.x;
+        const int L = m.y - m.x;
+        if (L > a.max_row || L <= 0) {
+            if (lane == 0) atomicExch(a.status, 1);
+            continue;
+        }
+        RowOut o;  // a compact row: its cells are its own (first + x < last <= dim_i)
+        o.out = a.SO;
+        o.rowbase = bs.cells + m.z;
+        o.first = f;
+        o.row = row;
+        o.sd = &d;
+        o.rfirst = nullptr;
+        o.rlast = nullptr;
+        o.counts_only = a.counts_only;
+        const float* src = a.SI + o.rowbase;
+        bool ok = true;
+        for (int x = lane; x < L; x += 32) {
+            const float v = src[x];
+            A[x] = v;
+            ok = ok && div_safe(v) && div_safe(__fadd_rn(v, a.povh));
+        }
+        const float pad = __int_as_float(0x7fc00000);  // NaN (see visit)
+        for (int x = lane; x < kLPad; x += 32) buf[x] = pad;
+        const int tail_end = ((L + 3) & ~3) + kLPad;
+        for (int x = L + lane; x < tail_end; x += 32) A[x] = pad;
+        const bool fast = __all_sync(0xffffffffu, ok) && L <= kLFastMaxRow && div_safe(a.povh);
+        __syncwarp();
+        if (fast) {
+            row_maxima(A, L, s128, p128, b16, b128, lane);
+            __syncwarp();
+            const RowMax rm{s128, p128, b16, b128, nblk(L, kB2)};
+            sweep_row64(A, rm, L, a.povh, lists, a.max_row, cvf, cvb, o, lane);
+        } else {
+            for (int x = lane; x < L; x += 32) {
+                if (!owns64(o, x)) continue;
+                const float cv = scan_reference(A, x, L, a.povh);
+                o.out[o.rowbase + x] = a.counts_only ? cv : __fmul_rn(cv, d.r2);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Exhaustive check of div_fast against IEEE division: every float bit pattern a
 // with div_safe-compatible magnitude (zero or |a| in [2^-103, 2^91], the range
 // of S[k]-h when both operands pass div_safe) and every d in [1, dmax].
@@ -956,8 +1229,8 @@ size_t sdem_list_bytes(int max_row, int num_sms) {
 int sdem_max_ctas_per_sm(const SdemLaunch& a) {
     const size_t smem = sizeof(float) * (size_t)LLayout(std::max(a.max_row, 1)).total * kLWarps;
     const bool fixed = a.lvl0 == kLevel && a.lvl1 == 0;
-    auto kern = a.batched ? (fixed ? k_sdem<true, true> : k_sdem<true, false>)
-                          : (fixed ? k_sdem<false, true> : k_sdem<false, false>);
+    auto kern = a.batched ? (fixed ? k_sdem_fixed_batch : k_sdem<true, false>)
+                          : (fixed ? k_sdem_fixed : k_sdem<false, false>);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
@@ -976,8 +1249,8 @@ cudaError_t launch_sdem(const SdemLaunch& a, int num_sms, cudaStream_t st) {
     if (!level_ok(a.lvl0) || (a.lvl1 != 0 && !level_ok(a.lvl1)) || a.ctas_per_sm < 0) return cudaErrorInvalidValue;
     const size_t smem = sizeof(float) * (size_t)LLayout(a.max_row).total * kLWarps;
     const bool fixed = a.lvl0 == kLevel && a.lvl1 == 0;
-    auto kern = a.batched ? (fixed ? k_sdem<true, true> : k_sdem<true, false>)
-                          : (fixed ? k_sdem<false, true> : k_sdem<false, false>);
+    auto kern = a.batched ? (fixed ? k_sdem_fixed_batch : k_sdem<true, false>)
+                          : (fixed ? k_sdem_fixed : k_sdem<false, false>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;

@@ -196,8 +196,9 @@ def make_net(seed: int = 0, device="cuda"):
 
         @staticmethod
         def pool(x):
-            import torch.nn.functional as F
-            return F.max_pool2d(x.permute(0, 3, 1, 2), 2).permute(0, 2, 3, 1).contiguous()
+            # 2 x 2 max pooling of an NHWC tensor in place of layout (no NCHW round trip).
+            n, h, w, c = x.shape
+            return x.view(n, h // 2, 2, w // 2, 2, c).amax((2, 4))
 
         @staticmethod
         def up(x):
