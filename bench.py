@@ -388,11 +388,12 @@ def batch_workload(args):
     e2e_ms = (time.perf_counter() - c0) * 1e3 / args.steps
     assert all(torch.equal(o.cpu(), h) for o, h in zip(outs, h_out)), "host-buffer batch differs from device batch"
     lvl0, lvl1, ctas = eng.sweep_shape()
-    line = {"metric": "Batched viewshed Mpoint·sectors/s (64 uneven DEMs 256-2000², 360 sect)",
+    hi = _env_int("SKE_BATCH_MAX_SIDE", 2000)
+    line = {"metric": f"Batched viewshed Mpoint·sectors/s ({len(grids)} uneven DEMs 256-{hi}², 360 sect)",
             "value": cells * DIR_SECTORS / (ms / 1e3) / 1e6, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "dtype": "f32",
-            "data": "synthetic (64 seeded diamond-square DEMs)",
-            "config": {"workload": "64 DEMs, sides uniform 256-2000, roughness 0.6-0.9, Kahan accumulation",
+            "data": f"synthetic ({len(grids)} seeded diamond-square DEMs)",
+            "config": {"workload": f"{len(grids)} DEMs, sides uniform 256-{hi}, roughness 0.6-0.9, Kahan accumulation",
                        "cells": cells, "sides": [int(s) for s, _, _ in spec],
                        "sweep_shape": {"lvl0": lvl0, "lvl1": lvl1, "ctas_per_sm": ctas},
                        "timed": "graph replay of the batch plan (captured on the first call)"},
