@@ -494,20 +494,31 @@ def cepstrum_batch_workload(args):
 def convs_workload(args):
     """Every 3x3 convolution of the surrogate U-Net, forward, on a batch of
     SKE_CONV_BATCH (default 16) 256x256 tiles: per-layer time and TFLOP/s for the
-    halo-staged kernel and the im2col kernel (ske_conv_select), CUDA events, and
-    the whole set against the measured bf16 peak."""
+    default kernel choice (warp-specialised where it applies), the halo-staged
+    kernel and the im2col kernel (ske_conv_select), CUDA events, and the whole
+    set on the default choice against the measured bf16 peak."""
     import torch
     from skewengine_gb300 import _lib, build
     build.build()
     from skewengine_gb300 import surrogate as sur
     lib = _lib.load()
     n = _env_int("SKE_CONV_BATCH", 16)
+    # SKE_CONV_STAGE: input channels per pipeline step of the warp-specialised kernel (0 = its own choice).
+    stage = _env_int("SKE_CONV_STAGE", 0)
+    assert lib.ske_conv_stage_channels(stage) == 0
     res = {"e1": 256, "e2": 128, "e3": 64, "b4": 32, "d3": 64, "d2": 128, "d1": 256}
     skip_ch = {"d3": 128, "d2": 64, "d1": 32}
-    layers, total = [], {0: 0.0, 1: 0.0}
+    layers, total = [], {0: 0.0, 1: 0.0, 2: 0.0}
+    names = {0: "ws", 1: "im2col", 2: "halo"}
     flops_all = 0.0
     g = torch.Generator(device="cuda").manual_seed(0)
+    # SKE_CONV_LAYERS: comma-separated layer names to run (profiler captures); default all.
+    only = [x for x in os.environ.get("SKE_CONV_LAYERS", "").split(",") if x]
+    # SKE_CONV_GRAPH=0 times the eager calls (host launch work included) instead of graph replays.
+    graphs = _env_int("SKE_CONV_GRAPH", 1) != 0
     for name, cin, cout in sur.LAYERS:
+        if only and name not in only:
+            continue
         r = res[name[:2]]
         w = (torch.randn(cout, sur.kpad(cin), device="cuda", generator=g) * 0.05).to(torch.bfloat16)
         b = torch.zeros(cout, device="cuda")
@@ -522,20 +533,30 @@ def convs_workload(args):
         flops = 2.0 * 9 * cin * cout * r * r * n
         flops_all += flops
         row = {"layer": name, "cin": cin, "cout": cout, "side": r}
-        for path in (1, 0):
+        for path in (1, 2, 0):
             lib.ske_conv_select(path)
             for _ in range(max(1, args.warmup)):
                 fn()
             torch.cuda.synchronize()
+            run = fn
+            if graphs:
+                # One call captured as a CUDA graph and replayed: the layer's kernels
+                # back to back without the host's per-call launch work.
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+                    fn()
+                run = graph.replay
+                run()
+                torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(args.steps):
-                fn()
+                run()
             e1.record()
             torch.cuda.synchronize()
             us = e0.elapsed_time(e1) / args.steps * 1e3
             total[path] += us
-            row["halo" if path == 0 else "im2col"] = {"us": round(us, 1), "tflops": round(flops / us / 1e6, 1)}
+            row[names[path]] = {"us": round(us, 1), "tflops": round(flops / us / 1e6, 1)}
         sur.conv_check()
         layers.append(row)
     lib.ske_conv_select(0)
@@ -547,7 +568,10 @@ def convs_workload(args):
             "ms_per_step": total[0] / 1e3, "higher_is_better": True, "dtype": "bf16 (f32 accumulation)",
             "data": "synthetic (random activations and weights)",
             "config": {"workload": "the 14 convolutions of the 4-level, 32-channel U-Net, one forward pass",
-                       "im2col_ms": total[1] / 1e3, "layers": layers},
+                       "stage_channels": stage or "auto",
+                       "timing": "CUDA graph replay of each layer's call" if graphs else "eager calls",
+                       "im2col_ms": total[1] / 1e3,
+                       "halo_ms": total[2] / 1e3, "layers": layers},
             "roofline": {"bound": "tensor", "achieved": achieved, "peak": peaks.get("bf16_tflops", 1900.0),
                          "unit": "TFLOP/s", "frac": achieved / peaks.get("bf16_tflops", 1900.0),
                          "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 GEMM burst) of measured"}}

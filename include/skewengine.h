@@ -413,10 +413,20 @@ int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, c
 int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
                            int cout, void* stream);
 /* Forward-convolution kernel choice for later calls: 0 (default) = the
- * halo-staged kernel wherever it applies (Cin, Cout and C1 multiples of 16,
- * Cout <= 128, an image row of at most about 2600 pixels), else the im2col
- * kernel; 1 = always the im2col kernel.  No reference counterpart. */
+ * warp-specialised persistent kernel wherever it applies (Cin a multiple of 8,
+ * Cout a multiple of 16 up to 256, C1 a multiple of 16, two pipeline stages
+ * within shared memory), else the halo-staged kernel where it applies (Cin,
+ * Cout and C1 multiples of 16, Cout <= 128), else the im2col kernel; 1 = always
+ * the im2col kernel; 2 = the halo-staged kernel where it applies, else im2col.
+ * No reference counterpart. */
 int ske_conv_select(int path);
+
+/* Input channels the warp-specialised forward kernel stages per pipeline step
+ * for later calls: 16, 32 or 64 (wider steps copy longer contiguous runs of
+ * each pixel but fit fewer steps in shared memory), or 0 (default) = the most
+ * of 64, 32, 16 that divides Cin and C1 with two steps fitting.  A tuning
+ * knob; no reference counterpart. */
+int ske_conv_stage_channels(int channels);
 
 /* Synchronises `stream`, then sets *failed to 1 if a forward convolution since
  * the previous call gave up waiting for its tensor-core operations (its output

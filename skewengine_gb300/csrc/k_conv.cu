@@ -18,6 +18,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "../../include/skewengine.h"
@@ -44,6 +45,7 @@ template <int kN>
 __device__ __forceinline__ void cp_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(kN));
 }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ void ldsm_x4_t(unsigned& r0, unsigned& r1, unsigned& r2, unsigned& r3, const void* p) {
     asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
@@ -190,6 +192,23 @@ __device__ __forceinline__ void tc_ld16(unsigned taddr, float* v) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// 32 consecutive f32 columns of this warp's 32 lanes from tensor memory.
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float* v) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
 template <bool kUpCat>
@@ -391,9 +410,12 @@ constexpr int kHaloStages = 2;
 constexpr int kSlotBlock = 128;
 
 // Column segment width of an image width, and plane slots of a tile of nb
-// blocks at row pitch P = Ws + 2: enough rows for every tap of every output slot.
+// blocks at row pitch P = Ws + 2: output slot s - S0 < nb*128 of a tile whose
+// first slot sits at column soff <= P - 1 reads plane slot
+// (s - S0) + soff + ky*P + kx <= 3P + nb*128 for tap (ky, kx), so the plane
+// holds 3P + nb*128 + 1 slots.
 __host__ __device__ constexpr int halo_seg(int W) { return (W > 128 && W % 128 == 0) ? 128 : W; }
-__host__ __device__ constexpr int halo_slots(int P, int nb) { return 3 * P + nb * kSlotBlock; }
+__host__ __device__ constexpr int halo_slots(int P, int nb) { return 3 * P + nb * kSlotBlock + 1; }
 __host__ __device__ constexpr int halo_plane(int P, int nb) { return halo_slots(P, nb) * 16; }
 __host__ __device__ constexpr int halo_wbytes(int cout) { return 9 * 2 * cout * 16; }
 __host__ __device__ constexpr int halo_stage_bytes(int P, int nb, int cout) {
@@ -652,8 +674,10 @@ __global__ void __launch_bounds__(kThreads) k_conv3x3_wgrad(const bf16* __restri
 // 4 bytes, for the bf16 pairs of the epilogue).
 bool aligned(const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; }
 
-// Forward-convolution kernel choice (ske_conv_select): 0 = halo-staged where it
-// applies, 1 = always the im2col kernel.
+// Forward-convolution kernel choice (ske_conv_select): 0 = the warp-specialised
+// kernel where it applies, else the halo-staged one where it applies, else
+// im2col; 1 = always the im2col kernel; 2 = halo-staged where it applies, else
+// im2col.
 int g_conv_path = 0;
 
 // Launch of the tensor-core forward convolution: BN = Cout rounded up to 16,
@@ -700,9 +724,410 @@ int launch_conv_halo(const bf16* x, const bf16* w, const float* bias, bf16* y, i
     return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
 }
 
+// ---- warp-specialised persistent forward convolution -------------------------
+//
+// The halo-staged scheme above with the roles split across warps and each CTA
+// resident for the whole launch (one CTA per SM, tiles taken round-robin).  A
+// work item is one tile and one stage of 16*gs input channels (gs = 1, 2 or 4
+// groups of 16), staged as 2*gs halo planes of 8 channels plus the groups'
+// weights:
+//   warps 4-7  producers: copy an item into a ring of S stages with 16-byte
+//              cp.async.  Consecutive threads take consecutive 16-byte chunks
+//              of one pixel's 16*gs channels (contiguous in NHWC), so a warp's
+//              copies cover whole 32*gs-byte runs; the weights come from a copy
+//              packed per call in the stage's own order (one contiguous block
+//              per item).  Each producer thread's copies of an item arrive on
+//              the stage's `full` barrier when they land
+//              (cp.async.mbarrier.arrive.noinc, 128 arrivals), so the
+//              producers never wait for their copies and all S stages can be
+//              in flight.
+//   warp 8     lane 0 waits for a stage's barrier, fences the producers' writes
+//              for the async proxy and issues the item's gs x nb x 9 MMAs
+//              (M 128, N Cout, K 16) into one of two tensor-memory
+//              accumulators (columns 0 and 256),
+//              commits them to the stage's `empty` barrier and, after a tile's
+//              last item, to the accumulator's `acc_full` barrier.
+//   warps 0-3  epilogue: warp w reads lanes 32w..32w+31 of the finished
+//              accumulator (tcgen05.ld, 32 columns at a time), adds the bias,
+//              applies ReLU, stores
+//              bfloat16 and arrives on `acc_empty`, while the MMAs of the next
+//              tile run into the other accumulator.
+// Per output the MMAs run group by group and tap by tap, the order of the
+// halo-staged kernel, so both give the same bits.  nb = 256 / Cout blocks of
+// 128 slots (at most 8) so that the two accumulators fill the SM's 512
+// tensor-memory columns.  Input channels past Cin (Cin a multiple of 8) read as
+// zero, as do their weights.  kUpCat reads the channels below C1 (a multiple of
+// 16*gs) from the half-resolution X at (y/2, x/2) and the others from X2.  Every
+// wait is bounded and also gives up once another role has given up (the CTA's
+// abort word); a producer then drains its own copies, the MMA thread waits for
+// its last commit, and the CTA releases its tensor memory after a block
+// barrier.  g_conv_status reports a give-up.
+constexpr int kWsEpiWarps = 4, kWsProdWarps = 4;
+constexpr int kWsProd = kWsProdWarps * 32;
+constexpr int kWsThreads = (kWsEpiWarps + kWsProdWarps + 1) * 32;
+constexpr int kWsMaxStages = 4;
+constexpr int kWsExtra = 128 + 2 * kWsMaxStages * 8 + 4 * 8 + 16 + 256 * 4;  // alignment, barriers, words, bias
+constexpr int kWsMinSmem = 116 * 1024;  // more than half an SM's shared memory: one CTA per SM
+constexpr int kWsDevices = 64;          // devices whose SM count is cached
+
+struct WsGeom {
+    int H, W, Cin, Cout, C1, relu;
+    int Ws, P, segs, tps, nb, hslots;
+    int gs, lgs;      // 16-channel groups per item and log2(2 * gs)
+    int items;        // items per tile
+    int S;            // stages
+    int plane, wbytes, sbytes;  // bytes: one 8-channel plane, an item's weights, one stage
+    int total;        // tiles
+};
+
+__host__ __device__ constexpr int ws_blocks(int cout) { return 256 / cout > 8 ? 8 : 256 / cout; }
+
+__device__ __forceinline__ void ws_bar_init(uint64_t* bar, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void ws_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool ws_try(uint64_t* bar, int parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait that also returns (false) once the CTA's abort word is set; a
+// wait that runs out sets it.
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, int parity, volatile int* abort_word) {
+    for (long long i = 0; i < kTcWaitLimit; i++) {
+        if (ws_try(bar, parity)) return true;
+        if ((i & 63) == 63 && *abort_word) return false;
+    }
+    *abort_word = 1;
+    return false;
+}
+
+// Weights packed in the staged order: for each 16-channel group g, tap and
+// 8-channel half, the Cout rows of 8 channels: Wp[((g*9 + tap)*2 + half)*Cout + co][0..7]
+// = Wt[co][tap*Cin + 16g + 8half + 0..7], zero past Cin.  One thread per row.
+__global__ void k_pack_weights(const bf16* __restrict__ Wt, bf16* __restrict__ Wp, int Cin, int Cout, int Kpad,
+                               int rows) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= rows) return;
+    const int co = e % Cout, r = e / Cout, half = r & 1, tap = (r >> 1) % 9, g = (r >> 1) / 9;
+    const int ci = 16 * g + 8 * half;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (ci < Cin) v = *reinterpret_cast<const uint4*>(Wt + (int64_t)co * Kpad + tap * Cin + ci);
+    reinterpret_cast<uint4*>(Wp)[e] = v;
+}
+
+template <bool kUpCat>
+__global__ void __launch_bounds__(kWsThreads, 1)
+    k_conv3x3_ws(const bf16* __restrict__ X, const bf16* __restrict__ Wp, const float* __restrict__ bias,
+                 bf16* __restrict__ Y, const bf16* __restrict__ X2, const WsGeom g) {
+    extern __shared__ __align__(128) unsigned char ws_raw[];
+    unsigned char* sm = ws_raw + ((128 - (smem_u32(ws_raw) & 127)) & 127);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + g.S * g.sbytes);
+    uint64_t* empty = full + kWsMaxStages;
+    uint64_t* accf = empty + kWsMaxStages;
+    uint64_t* acce = accf + 2;
+    unsigned* tslot = reinterpret_cast<unsigned*>(acce + 2);
+    volatile int* abort_word = reinterpret_cast<volatile int*>(tslot + 1);
+    float* sbias = reinterpret_cast<float*>(tslot + 4);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        for (int s = 0; s < g.S; s++) {
+            ws_bar_init(&full[s], kWsProd);
+            ws_bar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; b++) {
+            ws_bar_init(&accf[b], 1);
+            ws_bar_init(&acce[b], kWsEpiWarps * 32);
+        }
+        *abort_word = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int c = tid; c < g.Cout; c += kWsThreads) sbias[c] = bias ? bias[c] : 0.0f;
+    if (warp == 8) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+    const int64_t HW = (int64_t)g.H * g.W;
+    const int tslots = g.nb * kSlotBlock;
+
+    if (warp >= kWsEpiWarps && warp < kWsEpiWarps + kWsProdWarps) {
+        // ---- producers ----
+        const int pt = tid - kWsEpiWarps * 32;
+        const int chunk = pt & ((1 << g.lgs) - 1);  // this thread's 8-channel plane of every item
+        const int step = kWsProd >> g.lgs;          // slots per pass of all producer threads
+        const int dq = step / g.P, dr = step - dq * g.P;
+        const int slot0 = pt >> g.lgs, hr0 = slot0 / g.P, hc0 = slot0 - hr0 * g.P;
+        const int c2 = g.Cin - g.C1;  // channels of X2 (kUpCat)
+        const int wchunks = g.wbytes / 16;
+        int k = 0;
+        bool fail = false;
+        for (int t = blockIdx.x; t < g.total && !fail; t += gridDim.x) {
+            const int tile = t % g.tps, rest = t / g.tps, seg = rest % g.segs, n = rest / g.segs;
+            const int x0 = seg * g.Ws, R0 = tile * tslots / g.P;
+            for (int it = 0; it < g.items; it++, k++) {
+                const int s = k % g.S, u = k / g.S;
+                if (u > 0 && !ws_wait(&empty[s], (u - 1) & 1, abort_word)) {
+                    fail = true;
+                    break;
+                }
+                unsigned char* base = sm + s * g.sbytes;
+                const int ci0 = 16 * g.gs * it, ci = ci0 + 8 * chunk;
+                // Source of this thread's chunk: low-resolution X, X2 (kUpCat) or X,
+                // its channel offset and channel count, or none past Cin.
+                const bf16* src = X;
+                int cs = g.Cin, cl = ci;
+                bool lo = false;
+                if (kUpCat) {
+                    if (ci0 < g.C1) {
+                        cs = g.C1;
+                        lo = true;
+                    } else {
+                        src = X2;
+                        cs = c2;
+                        cl = ci - g.C1;
+                    }
+                }
+                const bool chan_ok = cl < cs;
+                unsigned char* dst = base + chunk * g.plane;
+                int hr = hr0, hc = hc0;
+                for (int p = slot0; p < g.hslots; p += step) {
+                    const int iy = R0 - 1 + hr, ix = x0 - 1 + hc;
+                    const bool ok = chan_ok && iy >= 0 && iy < g.H && ix >= 0 && ix < g.W;
+                    const bf16* a = X;
+                    if (ok) {
+                        if (kUpCat && lo)
+                            a = src + (((int64_t)n * (g.H >> 1) + (iy >> 1)) * (g.W >> 1) + (ix >> 1)) * cs + cl;
+                        else
+                            a = src + ((int64_t)n * HW + (int64_t)iy * g.W + ix) * cs + cl;
+                    }
+                    cp_async16(dst + p * 16, a, ok ? 16 : 0);
+                    hc += dr;
+                    hr += dq;
+                    if (hc >= g.P) {
+                        hc -= g.P;
+                        hr++;
+                    }
+                }
+                unsigned char* wb = base + 2 * g.gs * g.plane;
+                const bf16* wsrc = Wp + (int64_t)it * (g.wbytes / 2);
+                for (int q = pt; q < wchunks; q += kWsProd) cp_async16(wb + q * 16, wsrc + q * 8, 16);
+                // The stage's barrier receives this thread's arrival once its copies have landed.
+                asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&full[s]))
+                             : "memory");
+            }
+        }
+        cp_wait_all();
+    } else if (warp == kWsEpiWarps + kWsProdWarps) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            const uint32_t idesc = tc_idesc(g.Cout);
+            uint64_t* last = nullptr;
+            int last_par = 0, k = 0, i = 0;
+            bool fail = false;
+            for (int t = blockIdx.x; t < g.total && !fail; t += gridDim.x, i++) {
+                const int b = i & 1, v = i >> 1;
+                if (v > 0 && !ws_wait(&acce[b], (v - 1) & 1, abort_word)) break;
+                tc_fence_after();
+                const int S0 = (t % g.tps) * tslots, soff = S0 - (S0 / g.P) * g.P;
+                const unsigned dcol = tmem + (unsigned)(b * 256);
+                for (int it = 0; it < g.items; it++, k++) {
+                    const int s = k % g.S, u = k / g.S;
+                    if (!ws_wait(&full[s], u & 1, abort_word)) {
+                        fail = true;
+                        break;
+                    }
+                    // The producers' cp.async writes, now visible to this thread, before
+                    // the tensor cores read them through the async proxy.
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                    tc_fence_after();
+                    const unsigned hb = smem_u32(sm + s * g.sbytes);
+                    const unsigned wbs = hb + 2u * g.gs * g.plane;
+                    for (int kk = 0; kk < g.gs; kk++) {
+                        const uint64_t da0 = tc_desc2(hb + 2u * kk * g.plane, (unsigned)g.plane, 128);
+                        const uint64_t db0 = tc_desc2(wbs + (unsigned)(kk * 18 * g.Cout * 16), (unsigned)(g.Cout * 16), 128);
+                        for (int j = 0; j < g.nb; j++)
+#pragma unroll
+                            for (int tap = 0; tap < 9; tap++) {
+                                const int ky = tap / 3, kx = tap - 3 * (tap / 3);
+                                // start addresses advance in 16-byte units in the descriptors' low field
+                                const uint64_t da = da0 + (uint64_t)(soff + j * kSlotBlock + ky * g.P + kx);
+                                const uint64_t db = db0 + (uint64_t)(tap * 2 * g.Cout);
+                                tc_mma(dcol + (unsigned)(j * g.Cout), da, db, idesc, (it | kk | tap) != 0);
+                            }
+                    }
+                    tc_commit(&empty[s]);
+                    last = &empty[s];
+                    last_par = u & 1;
+                }
+                if (fail) break;
+                tc_commit(&accf[b]);
+                last = &accf[b];
+                last_par = v & 1;
+            }
+            // Issued MMAs finish before the tensor memory is released.
+            if (*abort_word && last) tc_mbar_wait(last, last_par);
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue ----
+        int i = 0;
+        for (int t = blockIdx.x; t < g.total; t += gridDim.x, i++) {
+            const int b = i & 1, v = i >> 1;
+            if (!ws_wait(&accf[b], v & 1, abort_word)) break;
+            tc_fence_after();
+            const int tile = t % g.tps, rest = t / g.tps, seg = rest % g.segs, n = rest / g.segs;
+            const int x0 = seg * g.Ws, S0 = tile * tslots;
+            for (int j = 0; j < g.nb; j++) {
+                const int s = S0 + j * kSlotBlock + warp * 32 + lane;  // this thread's slot (lane)
+                const int r = s / g.P, c = s - (s / g.P) * g.P;
+                const bool store = r < g.H && c < g.Ws;
+                bf16* dst = Y + ((int64_t)n * HW + (int64_t)r * g.W + x0 + c) * g.Cout;
+                const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(b * 256 + j * g.Cout);
+                for (int c0 = 0; c0 < g.Cout; c0 += 32) {
+                    float v[32];
+                    const int nc = g.Cout - c0 >= 32 ? 32 : 16;
+                    if (nc == 32)
+                        tc_ld32(taddr + (unsigned)c0, v);
+                    else
+                        tc_ld16(taddr + (unsigned)c0, v);
+                    if (!store) continue;
+                    for (int e0 = 0; e0 < nc; e0 += 16) {
+                        __nv_bfloat162 h[8];
+#pragma unroll
+                        for (int e = 0; e < 16; e += 2) {
+                            float o0 = __fadd_rn(v[e0 + e], sbias[c0 + e0 + e]);
+                            float o1 = __fadd_rn(v[e0 + e + 1], sbias[c0 + e0 + e + 1]);
+                            if (g.relu) {
+                                o0 = fmaxf(o0, 0.0f);
+                                o1 = fmaxf(o1, 0.0f);
+                            }
+                            h[e / 2] = __floats2bfloat162_rn(o0, o1);
+                        }
+                        uint4* d4 = reinterpret_cast<uint4*>(dst + c0 + e0);
+                        d4[0] = *reinterpret_cast<const uint4*>(&h[0]);
+                        d4[1] = *reinterpret_cast<const uint4*>(&h[4]);
+                    }
+                }
+            }
+            tc_fence_before();
+            ws_arrive(&acce[b]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && *abort_word) atomicExch(&g_conv_status, 1);
+    if (warp == kWsEpiWarps + kWsProdWarps) {
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
+}
+
+// Channels per item for later launches (ske_conv_stage_channels): 0 = the most
+// of 64, 32, 16 whose stages fit twice in shared memory.
+int g_ws_stage = 0;
+
+// The warp-specialised kernel applies for Cin a multiple of 8, Cout a multiple
+// of 16 up to 256, C1 (upsampled channels) a multiple of 16, and at least two
+// stages in shared memory.
+bool ws_geometry(WsGeom* g, int n, int h, int w_, int cin, int cout, int c1, int relu) {
+    if (cin % 8 || cout % 16 || cout < 16 || cout > 256 || c1 % 16) return false;
+    g->H = h;
+    g->W = w_;
+    g->Cin = cin;
+    g->Cout = cout;
+    g->C1 = c1;
+    g->relu = relu;
+    g->Ws = halo_seg(w_);
+    g->P = g->Ws + 2;
+    g->segs = w_ / g->Ws;
+    g->nb = ws_blocks(cout);
+    g->hslots = halo_slots(g->P, g->nb);
+    g->plane = (g->hslots * 16 + 127) / 128 * 128;
+    const int groups = (cin + 15) / 16;
+    g->S = 0;
+    for (int gs = 4; gs >= 1; gs >>= 1) {
+        if (g_ws_stage && g_ws_stage != 16 * gs) continue;
+        if (gs > 1 && (cin % (16 * gs) || c1 % (16 * gs))) continue;
+        const int wbytes = gs * 18 * cout * 16;
+        const int sbytes = 2 * gs * g->plane + (wbytes + 127) / 128 * 128;
+        const int stages = std::min(kWsMaxStages, (227 * 1024 - kWsExtra) / sbytes);
+        if (stages < 2) continue;
+        g->gs = gs;
+        g->lgs = gs == 4 ? 3 : gs == 2 ? 2 : 1;
+        g->items = groups / gs;
+        g->wbytes = wbytes;
+        g->sbytes = sbytes;
+        g->S = stages;
+        break;
+    }
+    if (g->S < 2) return false;
+    const int64_t slots = (int64_t)h * g->P;
+    const int64_t tps = (slots + g->nb * kSlotBlock - 1) / (g->nb * kSlotBlock);
+    const int64_t total = (int64_t)n * g->segs * tps;
+    if (total > 0x7fffffff || slots + 4 * g->P > 0x7fffffff / 2) return false;
+    g->tps = (int)tps;
+    g->total = (int)total;
+    return true;
+}
+
+// Packs the weights into a stream-ordered temporary (freed after the launch)
+// and launches one CTA per SM.  SKE_ERR_UNSUPPORTED if the temporary cannot be
+// had (the caller then takes another kernel).
+template <bool kUpCat>
+int launch_conv_ws(const WsGeom& g, const bf16* x, const bf16* w, const float* bias, bf16* y, const bf16* x2,
+                   cudaStream_t st) {
+    const int smem = std::max(kWsMinSmem, g.S * g.sbytes + kWsExtra);
+    // Per device, once: the SM count and the kernel's shared-memory limit.
+    static std::atomic<int> sm_count[kWsDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return SKE_ERR_CUDA;
+    int sms = dev < kWsDevices ? sm_count[dev].load(std::memory_order_relaxed) : 0;
+    if (sms < 1) {
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1 ||
+            cudaFuncSetAttribute(k_conv3x3_ws<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_conv3x3_ws<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+                cudaSuccess)
+            return SKE_ERR_CUDA;
+        if (dev < kWsDevices) sm_count[dev].store(sms, std::memory_order_relaxed);
+    }
+    const int kpad = (9 * g.Cin + kTcBK - 1) / kTcBK * kTcBK;
+    const int rows = g.items * g.gs * 18 * g.Cout;  // 16-byte rows of the packed weights
+    bf16* wp = nullptr;
+    if (cudaMallocAsync(reinterpret_cast<void**>(&wp), (size_t)rows * 16, st) != cudaSuccess) {
+        cudaGetLastError();
+        return SKE_ERR_UNSUPPORTED;
+    }
+    k_pack_weights<<<(rows + 255) / 256, 256, 0, st>>>(w, wp, g.Cin, g.Cout, kpad, rows);
+    const int grid = std::min(g.total, sms);
+    k_conv3x3_ws<kUpCat><<<grid, kWsThreads, smem, st>>>(x, wp, bias, y, x2, g);
+    const cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(wp, st);
+    return e == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
 template <bool kUpCat>
 int launch_conv_tc(const bf16* x, const bf16* w, const float* bias, bf16* y, int64_t m, int h, int w_, int cin,
                    int cout, int relu, const bf16* x2, int c1, cudaStream_t st) {
+    const int n = (int)(m / ((int64_t)h * w_));
+    WsGeom geo;
+    if (g_conv_path == 0 && aligned(y, 16) && ws_geometry(&geo, n, h, w_, cin, cout, kUpCat ? c1 : 0, relu)) {
+        const int r = launch_conv_ws<kUpCat>(geo, x, w, bias, y, x2, st);
+        if (r != SKE_ERR_UNSUPPORTED) return r;
+    }
     if (halo_applies(w_, cin, cout, kUpCat ? c1 : 0) && aligned(y, 16) && g_conv_path != 1)
         return launch_conv_halo<kUpCat>(x, w, bias, y, (int)(m / ((int64_t)h * w_)), h, w_, cin, cout, relu, x2, c1,
                                         st);
@@ -747,8 +1172,14 @@ extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const
 }
 
 extern "C" int ske_conv_select(int path) {
-    if (path != 0 && path != 1) return SKE_ERR_INVALID;
+    if (path < 0 || path > 2) return SKE_ERR_INVALID;
     g_conv_path = path;
+    return SKE_OK;
+}
+
+extern "C" int ske_conv_stage_channels(int channels) {
+    if (channels != 0 && channels != 16 && channels != 32 && channels != 64) return SKE_ERR_INVALID;
+    g_ws_stage = channels;
     return SKE_OK;
 }
 

@@ -3,6 +3,8 @@ NumPy convolution (forward, data and weight gradients), training, and the
 engine-checked tiled inference with fallback."""
 from __future__ import annotations
 
+import contextlib
+
 import numpy as np
 import pytest
 
@@ -178,10 +180,28 @@ def test_trained_network_beats_the_untrained_method(sur):
     assert trained <= 0.025, trained
 
 
+@contextlib.contextmanager
+def _conv_path(path):
+    """Forward-convolution kernel choice (ske_conv_select) for the block."""
+    from skewengine_gb300 import _lib
+    lib = _lib.load()
+    assert lib.ske_conv_select(path) == 0
+    try:
+        yield
+    finally:
+        lib.ske_conv_select(0)
+
+
+# 0: warp-specialised persistent kernel, 2: halo-staged kernel (both stage the
+# input once per 16-channel group; odd widths give an odd row pitch).
+@pytest.mark.parametrize("path", [0, 2])
 @pytest.mark.parametrize("n,h,w,cin,cout,relu", [(1, 8, 128, 32, 32, True), (2, 4, 256, 16, 48, False),
-                                                  (1, 8, 256, 64, 128, True), (1, 4, 128, 192, 64, True)])
-def test_halo_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
-    """Widths that are multiples of 128 take the halo-staged tensor-core kernel."""
+                                                  (1, 8, 256, 64, 128, True), (1, 4, 128, 192, 64, True),
+                                                  (1, 760, 45, 16, 32, True), (3, 33, 30, 48, 16, False)])
+def test_halo_conv_forward_matches_numpy(sur, path, n, h, w, cin, cout, relu):
+    """The staged kernels against float64 NumPy.  760 x 45 (row pitch 47) has a
+    tile whose first slot sits in the last column of its row, so the last
+    output slot's tap (2, 2) reads the last staged plane slot."""
     import torch
     rng = np.random.default_rng(cin * 5 + cout + w)
     xb = _bf16(rng.normal(0, 1, (n, h, w, cin)))
@@ -189,14 +209,16 @@ def test_halo_conv_forward_matches_numpy(sur, n, h, w, cin, cout, relu):
     b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32)
     wpad = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
     wpad[:, : 9 * cin] = wb
-    y = sur.conv3x3(xb.cuda().contiguous(), wpad.cuda(), b.cuda(), relu)
-    sur.conv_check()
+    with _conv_path(path):
+        y = sur.conv3x3(xb.cuda().contiguous(), wpad.cuda(), b.cuda(), relu)
+        sur.conv_check()
     y = y.float().cpu().numpy()
     ref, _, _ = _conv_ref(xb.double().numpy(), wb.double().numpy(), b.double().numpy(), relu)
     assert np.all(np.abs(y - ref) <= 2 ** -7 * np.abs(ref) + 1e-3), np.abs(y - ref).max()
 
 
-def test_halo_upcat_equals_halo_conv_of_the_concatenation(sur):
+@pytest.mark.parametrize("path", [0, 2])
+def test_halo_upcat_equals_halo_conv_of_the_concatenation(sur, path):
     import torch
     import torch.nn.functional as F
     rng = np.random.default_rng(4)
@@ -207,29 +229,46 @@ def test_halo_upcat_equals_halo_conv_of_the_concatenation(sur):
     w = w.cuda()
     b = torch.as_tensor(rng.normal(0, 0.5, 32), dtype=torch.float32).cuda()
     up = F.interpolate(low.permute(0, 3, 1, 2), scale_factor=2, mode="nearest").permute(0, 2, 3, 1)
-    want = sur.conv3x3(torch.cat([up, skip], 3).contiguous(), w, b, True)
-    got = sur.conv3x3_upcat(low, skip, w, b, True)
-    sur.conv_check()
+    with _conv_path(path):
+        want = sur.conv3x3(torch.cat([up, skip], 3).contiguous(), w, b, True)
+        got = sur.conv3x3_upcat(low, skip, w, b, True)
+        sur.conv_check()
     assert torch.equal(got.view(torch.int16), want.view(torch.int16))
 
 
-def test_network_forward_halo_and_im2col_kernels_agree(sur):
-    """The whole U-Net forward with the halo-staged kernel (where it applies)
-    and with the im2col kernel only: same function, float32 accumulation in
-    different orders, so equal to bfloat16 rounding."""
+@pytest.mark.parametrize("path", [0, 2])
+def test_network_forward_halo_and_im2col_kernels_agree(sur, path):
+    """The whole U-Net forward with a staged kernel (where it applies) and with
+    the im2col kernel only: same function, float32 accumulation in different
+    orders, so equal to bfloat16 rounding."""
     import torch
-    from skewengine_gb300 import _lib
     net = sur.make_net(seed=5)
     x = sur.encode_tiles(np.stack([synthetic.fractal_dem(256, 80 + i) for i in range(2)]))
-    lib = _lib.load()
-    try:
-        with torch.no_grad():
-            assert lib.ske_conv_select(1) == 0
+    with torch.no_grad():
+        with _conv_path(1):
             ref = net(x)
-            assert lib.ske_conv_select(0) == 0
+        with _conv_path(path):
             got = net(x)
-        sur.conv_check()
-    finally:
-        lib.ske_conv_select(0)
+            sur.conv_check()
     err = (got - ref).abs().max().item()
     assert err <= 0.05 * ref.abs().max().item(), err
+
+
+def test_ws_conv_equals_halo_conv_bits(sur):
+    """The warp-specialised and halo-staged kernels issue the same MMAs in the
+    same order per output (taps within a group, groups in order), so their
+    outputs are the same bits."""
+    import torch
+    rng = np.random.default_rng(11)
+    for (n, h, w, cin, cout) in ((2, 16, 256, 32, 32), (1, 20, 64, 128, 128), (2, 9, 128, 64, 64)):
+        x = _bf16(rng.normal(0, 1, (n, h, w, cin))).cuda().contiguous()
+        wt = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
+        wt[:, : 9 * cin] = _bf16(rng.normal(0, 0.1, (cout, 9 * cin)))
+        wt = wt.cuda()
+        b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32).cuda()
+        with _conv_path(2):
+            want = sur.conv3x3(x, wt, b, True)
+        with _conv_path(0):
+            got = sur.conv3x3(x, wt, b, True)
+            sur.conv_check()
+        assert torch.equal(got.view(torch.int16), want.view(torch.int16)), (n, h, w, cin, cout)
