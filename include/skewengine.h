@@ -21,6 +21,11 @@
  *  - An engine is bound to one device and one CUDA stream; calls on one engine
  *    are not thread-safe (as one reference skewEngine object per OpenMP thread,
  *    src/main.cu:91).  Different engines may be used from different threads.
+ *  - Device buffers are read and written in the engine's stream order: a caller
+ *    that produces an input (or still reads an output buffer) on another stream
+ *    makes the engine's stream wait for that work first (an event, or the
+ *    engine created on the caller's stream).  A call that runs sectors has
+ *    finished its device work when it returns.
  */
 #ifndef SKEWENGINE_H
 #define SKEWENGINE_H

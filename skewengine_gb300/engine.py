@@ -119,6 +119,8 @@ class SkewEngine:
                                    C.c_void_p(stream) if stream else None))
         self._h = h
         self._keep = []
+        self.device = int(device)
+        self._ext = None  # torch's handle on the engine's stream, made on first device call
 
     # lifetime -------------------------------------------------------------
     def close(self) -> None:
@@ -144,6 +146,20 @@ class SkewEngine:
         check(self._lib.ske_stream(self._h, C.byref(s)))
         return s.value or 0
 
+    def _after_torch(self, *arrays) -> None:
+        """CUDA tensors handed to the engine may still be written (inputs) or
+        read (outputs) by work queued on torch's current stream: the engine's
+        stream waits for that work first (an event, no host synchronisation).
+        Every engine call has finished its own work when it returns."""
+        if not any(_is_device(a) for a in arrays if a is not None):
+            return
+        import torch
+        cur = torch.cuda.current_stream(self.device)
+        if self._ext is None:
+            self._ext = torch.cuda.ExternalStream(self.stream, device=self.device)
+        if cur.cuda_stream != self._ext.cuda_stream:
+            self._ext.wait_stream(cur)
+
     # whole run ------------------------------------------------------------
     def run(self, kernel, data, out=None, max_sector: int = 180, povh: float = DEFAULT_POVH,
             accum="reference", angles=None, flags: int = 0):
@@ -157,6 +173,7 @@ class SkewEngine:
             else:
                 out = np.empty(shape, np.float32)
         pout, out_dev = _ptr(out, shape, writable=True)
+        self._after_torch(data, out)
         prm = params(max_sector, povh, accum, flags)
         if angles is None:
             check(self._lib.ske_run(self._h, _kernel_id(kernel), pin, in_dev, pout, out_dev, C.byref(prm)))
@@ -169,6 +186,7 @@ class SkewEngine:
     def accumulate(self, kernel, data, angles, povh: float = DEFAULT_POVH, accum="reference"):
         """Run the listed sectors and return (4 x N per-type accumulators, used-type mask)."""
         pin, in_dev = _ptr(data, (self.dimy, self.dimx))
+        self._after_torch(data)
         a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
         acc = np.empty((4, self.N), np.float32)
         used = C.c_uint32(0)
@@ -183,6 +201,7 @@ class SkewEngine:
         with ``acc``, ``comp`` (4 x N float32) and ``used``; None = zero) and
         return the new state."""
         pin, in_dev = _ptr(data, (self.dimy, self.dimx))
+        self._after_torch(data)
         a = np.ascontiguousarray(np.asarray(angles, dtype=np.int32))
         if state is None:
             state = {"acc": np.zeros((4, self.N), np.float32), "comp": np.zeros((4, self.N), np.float32), "used": 0}
@@ -201,6 +220,7 @@ class SkewEngine:
         if out is None:
             out = np.empty(shape, np.float32)
         p, dev = _ptr(out, shape, writable=True)
+        self._after_torch(out)
         acc = np.ascontiguousarray(state["acc"], np.float32)
         comp = np.ascontiguousarray(state["comp"], np.float32)
         check(self._lib.ske_fold(self._h, _kernel_id(kernel), acc.ctypes.data, comp.ctypes.data, 0,
@@ -242,6 +262,7 @@ class SkewEngine:
     # per-sector API (main.cu:147-164) -------------------------------------
     def prepare(self, data) -> None:
         p, dev = _ptr(data, (self.dimy, self.dimx))
+        self._after_torch(data)
         check(self._lib.ske_prepare(self._h, p, dev))
 
     def skew(self, angle: int) -> None:
@@ -264,6 +285,7 @@ class SkewEngine:
         if out is None:
             out = np.empty(shape, np.float32)
         p, dev = _ptr(out, shape, writable=True)
+        self._after_torch(out)
         check(self._lib.ske_reduce(self._h, p, dev, int(is_max)))
         return out
 
@@ -372,6 +394,8 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
     prm = params(max_sector, povh, accum, flags)
     eng = engine if engine is not None else SkewEngine(big[0], big[1], device)
     try:
+        if on_dev:
+            eng._after_torch(grids if stacked else grids[0], outs if stacked else outs[0])
         if angles is None:
             check(eng._lib.ske_run_batch(eng._h, _kernel_id(kernel), count, dx.ctypes.data, dy.ctypes.data,
                                          ins, int(on_dev), ous, int(on_dev), C.byref(prm)))

@@ -118,3 +118,31 @@ def test_batch_stacked_grids_equal_list(ske, oracle):
     for i in range(5):
         want = oracle.run_ordered(0, stack[i], povh=POVH)
         assert bits_equal(host[i], want) and bits_equal(dev[i].cpu().numpy(), want) and bits_equal(lst[i], want)
+
+
+def test_device_inputs_written_late_on_torch_stream(ske, oracle):
+    """An engine on its own stream, given CUDA tensors that torch's stream is
+    still writing: torch's stream spins on the GPU, then copies the input in.
+    The engine's work waits for the copy (first call and graph replays alike)
+    instead of reading the buffer early."""
+    import torch
+    grids = np.stack([synthetic.fractal_dem(64, 700 + i) for i in range(6)])
+    want = [oracle.run(0, g, povh=synthetic.POVH) for g in grids]
+    src = torch.as_tensor(grids, device="cuda")
+    eng = ske.SkewEngine(64, 64)  # its own non-blocking stream
+    try:
+        for rep in range(4):
+            dst = torch.full_like(src, float("nan"))
+            torch.cuda._sleep(20_000_000)  # about 10 ms of GPU time queued before the copy
+            dst.copy_(src)
+            out = ske.run_batch(0, dst, engine=eng)
+            single = torch.full_like(src[0], float("nan"))
+            torch.cuda._sleep(20_000_000)
+            single.copy_(src[rep])
+            one = eng.run(0, single)
+            torch.cuda.synchronize()
+            for g in range(len(grids)):
+                assert bits_equal(out[g].cpu().numpy(), want[g]), (rep, g)
+            assert bits_equal(one.cpu().numpy(), want[rep]), rep
+    finally:
+        eng.close()

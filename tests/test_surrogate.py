@@ -217,6 +217,26 @@ def test_halo_conv_forward_matches_numpy(sur, path, n, h, w, cin, cout, relu):
     assert np.all(np.abs(y - ref) <= 2 ** -7 * np.abs(ref) + 1e-3), np.abs(y - ref).max()
 
 
+def test_ws_upcat_many_tiles_equals_halo_bits(sur):
+    """The fused upsample + concatenate convolution with several tiles per CTA:
+    the warp-specialised kernel gives the halo-staged kernel's bits."""
+    import torch
+    rng = np.random.default_rng(12)
+    for (n, r, c1, c2, cout) in ((32, 256, 64, 32, 32), (32, 64, 256, 128, 128)):
+        low = _bf16(rng.normal(0, 1, (n, r // 2, r // 2, c1))).cuda().contiguous()
+        skip = _bf16(rng.normal(0, 1, (n, r, r, c2))).cuda().contiguous()
+        w = torch.zeros((cout, sur.kpad(c1 + c2)), dtype=torch.bfloat16)
+        w[:, : 9 * (c1 + c2)] = _bf16(rng.normal(0, 0.05, (cout, 9 * (c1 + c2))))
+        w = w.cuda()
+        b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32).cuda()
+        with _conv_path(2):
+            want = sur.conv3x3_upcat(low, skip, w, b, True)
+        with _conv_path(0):
+            got = sur.conv3x3_upcat(low, skip, w, b, True)
+            sur.conv_check()
+        assert torch.equal(got.view(torch.int16), want.view(torch.int16)), (n, r, c1, c2, cout)
+
+
 @pytest.mark.parametrize("path", [0, 2])
 def test_halo_upcat_equals_halo_conv_of_the_concatenation(sur, path):
     import torch
@@ -257,10 +277,13 @@ def test_network_forward_halo_and_im2col_kernels_agree(sur, path):
 def test_ws_conv_equals_halo_conv_bits(sur):
     """The warp-specialised and halo-staged kernels issue the same MMAs in the
     same order per output (taps within a group, groups in order), so their
-    outputs are the same bits."""
+    outputs are the same bits.  The larger cases give every persistent CTA
+    several tiles (2112, 1056 and 544 tiles on 152 SMs), so both tensor-memory
+    accumulators and every pipeline stage are reused."""
     import torch
     rng = np.random.default_rng(11)
-    for (n, h, w, cin, cout) in ((2, 16, 256, 32, 32), (1, 20, 64, 128, 128), (2, 9, 128, 64, 64)):
+    for (n, h, w, cin, cout) in ((2, 16, 256, 32, 32), (1, 20, 64, 128, 128), (2, 9, 128, 64, 64),
+                                 (32, 256, 256, 32, 32), (32, 128, 128, 64, 64), (32, 64, 64, 128, 128)):
         x = _bf16(rng.normal(0, 1, (n, h, w, cin))).cuda().contiguous()
         wt = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
         wt[:, : 9 * cin] = _bf16(rng.normal(0, 0.1, (cout, 9 * cin)))
