@@ -417,6 +417,22 @@ int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, c
  * cout a multiple of 8. */
 int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
                            int cout, void* stream);
+/* The same 3x3 convolution (+ bias, ReLU when relu != 0) followed by a 1x1
+ * convolution to one channel, fused: y[pixel] = head_b + sum over c in order of
+ * bf16(act[pixel][c]) * head_w[c] in float32, y float32 (n x h x w), head_w
+ * (cout floats) and head_b (one float) on the device.  The activations are not
+ * written.  Cout a multiple of 16; SKE_ERR_UNSUPPORTED where the
+ * warp-specialised kernel does not apply (or another kernel is selected).  No
+ * reference counterpart. */
+int ske_conv3x3_head_bf16(const void* x, const void* w, const float* bias, const float* head_w,
+                          const float* head_b, float* y, int n, int h, int w_, int cin, int cout, int relu,
+                          void* stream);
+
+/* 2 x 2 max pooling of an NHWC bfloat16 tensor on the device (h, w even, c a
+ * multiple of 8): y[n][i][j][c] = max of x[n][2i..2i+1][2j..2j+1][c], NaN
+ * propagated.  No reference counterpart. */
+int ske_maxpool2_bf16(const void* x, void* y, int n, int h, int w_, int c, void* stream);
+
 /* Forward-convolution kernel choice for later calls: 0 (default) = the
  * warp-specialised persistent kernel wherever it applies (Cin a multiple of 8,
  * Cout a multiple of 16 up to 256, C1 a multiple of 16, two pipeline stages

@@ -766,7 +766,8 @@ constexpr int kWsEpiWarps = 4, kWsProdWarps = 4;
 constexpr int kWsProd = kWsProdWarps * 32;
 constexpr int kWsThreads = (kWsEpiWarps + kWsProdWarps + 1) * 32;
 constexpr int kWsMaxStages = 4;
-constexpr int kWsExtra = 128 + 2 * kWsMaxStages * 8 + 4 * 8 + 16 + 256 * 4;  // alignment, barriers, words, bias
+constexpr int kWsExtra = 128 + 2 * kWsMaxStages * 8 + 4 * 8 + 16 + (2 * 256 + 4) * 4;  // alignment, barriers,
+                                                                                        // words, bias, head
 constexpr int kWsMinSmem = 116 * 1024;  // more than half an SM's shared memory: one CTA per SM
 constexpr int kWsDevices = 64;          // devices whose SM count is cached
 
@@ -825,7 +826,8 @@ __global__ void k_pack_weights(const bf16* __restrict__ Wt, bf16* __restrict__ W
 template <bool kUpCat>
 __global__ void __launch_bounds__(kWsThreads, 1)
     k_conv3x3_ws(const bf16* __restrict__ X, const bf16* __restrict__ Wp, const float* __restrict__ bias,
-                 bf16* __restrict__ Y, const bf16* __restrict__ X2, const WsGeom g) {
+                 bf16* __restrict__ Y, const bf16* __restrict__ X2, const float* __restrict__ head_w,
+                 const float* __restrict__ head_b, float* __restrict__ Yh, const WsGeom g) {
     extern __shared__ __align__(128) unsigned char ws_raw[];
     unsigned char* sm = ws_raw + ((128 - (smem_u32(ws_raw) & 127)) & 127);
     uint64_t* full = reinterpret_cast<uint64_t*>(sm + g.S * g.sbytes);
@@ -835,6 +837,7 @@ __global__ void __launch_bounds__(kWsThreads, 1)
     unsigned* tslot = reinterpret_cast<unsigned*>(acce + 2);
     volatile int* abort_word = reinterpret_cast<volatile int*>(tslot + 1);
     float* sbias = reinterpret_cast<float*>(tslot + 4);
+    float* shead = sbias + 256;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
@@ -849,7 +852,11 @@ __global__ void __launch_bounds__(kWsThreads, 1)
         *abort_word = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int c = tid; c < g.Cout; c += kWsThreads) sbias[c] = bias ? bias[c] : 0.0f;
+    for (int c = tid; c < g.Cout; c += kWsThreads) {
+        sbias[c] = bias ? bias[c] : 0.0f;
+        shead[c] = head_w ? head_w[c] : 0.0f;
+    }
+    if (tid == 0) shead[256] = head_b ? *head_b : 0.0f;
     if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
                      : "memory");
@@ -993,8 +1000,10 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                 const int s = S0 + j * kSlotBlock + warp * 32 + lane;  // this thread's slot (lane)
                 const int r = s / g.P, c = s - (s / g.P) * g.P;
                 const bool store = r < g.H && c < g.Ws;
-                bf16* dst = Y + ((int64_t)n * HW + (int64_t)r * g.W + x0 + c) * g.Cout;
+                const int64_t pix = (int64_t)n * HW + (int64_t)r * g.W + x0 + c;
+                bf16* dst = Y + pix * g.Cout;
                 const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(b * 256 + j * g.Cout);
+                float hsum = 0.0f;  // head: sum over channels of bf16(activation) * head_w, in channel order
                 for (int c0 = 0; c0 < g.Cout; c0 += 32) {
                     float v[32];
                     const int nc = g.Cout - c0 >= 32 ? 32 : 16;
@@ -1015,11 +1024,21 @@ __global__ void __launch_bounds__(kWsThreads, 1)
                             }
                             h[e / 2] = __floats2bfloat162_rn(o0, o1);
                         }
-                        uint4* d4 = reinterpret_cast<uint4*>(dst + c0 + e0);
-                        d4[0] = *reinterpret_cast<const uint4*>(&h[0]);
-                        d4[1] = *reinterpret_cast<const uint4*>(&h[4]);
+                        if (Yh) {
+#pragma unroll
+                            for (int e = 0; e < 16; e += 2) {
+                                const float2 f = __bfloat1622float2(h[e / 2]);
+                                hsum = __fmaf_rn(f.x, shead[c0 + e0 + e], hsum);
+                                hsum = __fmaf_rn(f.y, shead[c0 + e0 + e + 1], hsum);
+                            }
+                        } else {
+                            uint4* d4 = reinterpret_cast<uint4*>(dst + c0 + e0);
+                            d4[0] = *reinterpret_cast<const uint4*>(&h[0]);
+                            d4[1] = *reinterpret_cast<const uint4*>(&h[4]);
+                        }
                     }
                 }
+                if (Yh && store) Yh[pix] = __fadd_rn(hsum, shead[256]);
             }
             tc_fence_before();
             ws_arrive(&acce[b]);
@@ -1088,7 +1107,8 @@ bool ws_geometry(WsGeom* g, int n, int h, int w_, int cin, int cout, int c1, int
 // had (the caller then takes another kernel).
 template <bool kUpCat>
 int launch_conv_ws(const WsGeom& g, const bf16* x, const bf16* w, const float* bias, bf16* y, const bf16* x2,
-                   cudaStream_t st) {
+                   cudaStream_t st, const float* head_w = nullptr, const float* head_b = nullptr,
+                   float* yh = nullptr) {
     const int smem = std::max(kWsMinSmem, g.S * g.sbytes + kWsExtra);
     // Per device, once: the SM count and the kernel's shared-memory limit.
     static std::atomic<int> sm_count[kWsDevices];
@@ -1113,7 +1133,7 @@ int launch_conv_ws(const WsGeom& g, const bf16* x, const bf16* w, const float* b
     }
     k_pack_weights<<<(rows + 255) / 256, 256, 0, st>>>(w, wp, g.Cin, g.Cout, kpad, rows);
     const int grid = std::min(g.total, sms);
-    k_conv3x3_ws<kUpCat><<<grid, kWsThreads, smem, st>>>(x, wp, bias, y, x2, g);
+    k_conv3x3_ws<kUpCat><<<grid, kWsThreads, smem, st>>>(x, wp, bias, y, x2, head_w, head_b, yh, g);
     const cudaError_t e = cudaGetLastError();
     cudaFreeAsync(wp, st);
     return e == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
@@ -1169,6 +1189,61 @@ extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const
     if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
     return launch_conv_tc<true>((const bf16*)xlow, (const bf16*)w, bias, (bf16*)y, m, h, w_, cin, cout, relu,
                                 (const bf16*)xskip, c1, (cudaStream_t)stream);
+}
+
+extern "C" int ske_conv3x3_head_bf16(const void* x, const void* w, const float* bias, const float* head_w,
+                                     const float* head_b, float* y, int n, int h, int w_, int cin, int cout,
+                                     int relu, void* stream) {
+    if (!x || !w || !head_w || !head_b || !y || n < 1 || h < 1 || w_ < 1 || cin < 8 || cin % 8 || cout < 16 || cout % 16)
+        return SKE_ERR_INVALID;
+    if (!aligned(x, 16) || !aligned(w, 16) || !aligned(y, 4) || !aligned(bias, 4) || !aligned(head_w, 4) ||
+        !aligned(head_b, 4))
+        return SKE_ERR_INVALID;
+    const int64_t m = (int64_t)n * h * w_;
+    if (m > 0x7fffffff / 2 || (int64_t)cin * 9 > 0x7fffffff / 2) return SKE_ERR_INVALID;
+    WsGeom geo;
+    if (g_conv_path != 0 || !ws_geometry(&geo, n, h, w_, cin, cout, 0, relu)) return SKE_ERR_UNSUPPORTED;
+    return launch_conv_ws<false>(geo, (const bf16*)x, (const bf16*)w, bias, nullptr, nullptr, (cudaStream_t)stream,
+                                 head_w, head_b, y);
+}
+
+// 2 x 2 max pooling of NHWC bfloat16 (H, W even, C a multiple of 8): one
+// thread per output pixel and 8 channels, four 16-byte loads, NaN propagated
+// (as torch.amax).
+static __global__ void k_maxpool2(const bf16* __restrict__ X, bf16* __restrict__ Y, int64_t total, int H2, int W2,
+                           int C8) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int c8 = (int)(i % C8);
+    int64_t rest = i / C8;
+    const int x = (int)(rest % W2);
+    rest /= W2;
+    const int y = (int)(rest % H2);
+    const int64_t n = rest / H2;
+    const int64_t W = 2 * (int64_t)W2, C = 8 * (int64_t)C8;
+    const bf16* p = X + ((n * 2 * H2 + 2 * y) * W + 2 * x) * C + 8 * c8;
+    const uint4 q[4] = {*reinterpret_cast<const uint4*>(p), *reinterpret_cast<const uint4*>(p + C),
+                        *reinterpret_cast<const uint4*>(p + W * C), *reinterpret_cast<const uint4*>(p + W * C + C)};
+    uint4 o;
+    const __nv_bfloat162* a = reinterpret_cast<const __nv_bfloat162*>(&q[0]);
+    const __nv_bfloat162* b = reinterpret_cast<const __nv_bfloat162*>(&q[1]);
+    const __nv_bfloat162* c = reinterpret_cast<const __nv_bfloat162*>(&q[2]);
+    const __nv_bfloat162* d = reinterpret_cast<const __nv_bfloat162*>(&q[3]);
+    __nv_bfloat162* r = reinterpret_cast<__nv_bfloat162*>(&o);
+#pragma unroll
+    for (int k = 0; k < 4; k++) r[k] = __hmax2_nan(__hmax2_nan(a[k], b[k]), __hmax2_nan(c[k], d[k]));
+    reinterpret_cast<uint4*>(Y)[i] = o;
+}
+
+extern "C" int ske_maxpool2_bf16(const void* x, void* y, int n, int h, int w_, int c, void* stream) {
+    if (!x || !y || n < 1 || h < 2 || w_ < 2 || h % 2 || w_ % 2 || c < 8 || c % 8) return SKE_ERR_INVALID;
+    if (!aligned(x, 16) || !aligned(y, 16)) return SKE_ERR_INVALID;
+    const int64_t total = (int64_t)n * (h / 2) * (w_ / 2) * (c / 8);
+    const int64_t blocks = (total + 255) / 256;
+    if (blocks > 0x7fffffff) return SKE_ERR_INVALID;
+    k_maxpool2<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)y, total, h / 2, w_ / 2,
+                                                                   c / 8);
+    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
 }
 
 extern "C" int ske_conv_select(int path) {

@@ -10,16 +10,20 @@ a sample of tiles and recomputes every tile whose error exceeds the bound.
 The convolutions are the engine's hand-written implicit-GEMM kernels
 (``ske_conv3x3_bf16`` forward and data gradient on tcgen05 with the accumulator
 in tensor memory, ``ske_conv3x3_wgrad_bf16`` weight gradient on mma.sync, both
-with bfloat16 operands and float32 accumulation); pooling,
-upsampling, concatenation, the 1x1 output layer, the loss and the optimiser are
-PyTorch operations around them.
+with bfloat16 operands and float32 accumulation).  At inference the decoder's
+upsampling and concatenation are read in place by the convolution
+(``ske_conv3x3_upcat_bf16``), the last convolution and the 1x1 output layer are
+one kernel (``ske_conv3x3_head_bf16``) and pooling is a kernel of its own
+(``ske_maxpool2_bf16``); in training those, the loss and the optimiser are
+PyTorch operations around the convolutions.
 
 Tensors are NHWC.  Input channels: 0 = the tile's heights minus their mean,
 divided by the tile's height range (or 1 for a flat tile), 1 = log(1 + range)
 (the relief amplitude, which visibility depends on), 2 = the engine's own total
-viewshed of the tile at 1/4 resolution (4 x 4 cell means, 40 m cells, about 1/64
-of the full-resolution run's work), as log(1 + area per cell in tile cells) /
-16, 3-7 = 0 (the kernels need a multiple of 8 channels).  The tile-context head
+viewshed of the tile at 1/4 resolution (4 x 4 cell means, 40 m cells) from every
+4th angle, scaled by 4 (about 1/256 of the full-resolution run's work), as
+log(1 + area per cell in tile cells) / 16, 3-7 = 0 (the kernels need a multiple
+of 8 channels).  The tile-context head
 predicts a correction to the log of the coarse run's total area.
 """
 from __future__ import annotations
@@ -39,6 +43,7 @@ BASE = 32
 CTX = 64  # width of the tile-context MLP
 COARSE = 4  # the coarse engine run's cell is COARSE x COARSE tile cells
 COARSE_SCALE = 16.0  # input channel 2 = log(1 + coarse area per cell) / COARSE_SCALE
+COARSE_ANGLE_STEP = 4  # the coarse run takes every 4th of the 180 angles
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "surrogate_unet32.npz")
 
 
@@ -80,6 +85,40 @@ def conv3x3_upcat(xlow, skip, w, bias=None, relu: bool = False):
                                         C.c_void_p(w.data_ptr()),
                                         C.c_void_p(bias.data_ptr()) if bias is not None else None,
                                         C.c_void_p(y.data_ptr()), n, h, wd, c1, c2, cout, int(relu), _stream(skip)))
+    return y
+
+
+def conv3x3_head(x, w, bias, head_w, head_b, relu: bool = True):
+    """head_b + sum_c bf16(relu?(conv3x3(x, w) + bias))[..., c] * head_w[c]: the
+    3x3 convolution and a 1x1 convolution to one channel in one kernel
+    (ske_conv3x3_head_bf16), float32 (N, H, W); the activations are not stored.
+    None where that kernel does not apply."""
+    import torch
+    n, h, wd, cin = x.shape
+    cout = w.shape[0]
+    assert x.is_contiguous() and w.is_contiguous() and x.dtype == torch.bfloat16 and w.dtype == torch.bfloat16
+    assert w.shape[1] == kpad(cin)
+    hw = head_w.reshape(-1).float().contiguous()
+    hb = head_b.reshape(-1).float().contiguous()
+    assert hw.numel() == cout and hb.numel() == 1
+    y = torch.empty((n, h, wd), dtype=torch.float32, device=x.device)
+    rc = load().ske_conv3x3_head_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
+                                      C.c_void_p(bias.data_ptr()) if bias is not None else None,
+                                      C.c_void_p(hw.data_ptr()), C.c_void_p(hb.data_ptr()), C.c_void_p(y.data_ptr()),
+                                      n, h, wd, cin, cout, int(relu), _stream(x))
+    if rc == 5:  # SKE_ERR_UNSUPPORTED
+        return None
+    check(rc)
+    return y
+
+
+def maxpool2(x):
+    """2 x 2 max pooling of a contiguous NHWC bfloat16 tensor (ske_maxpool2_bf16)."""
+    import torch
+    n, h, wd, c = x.shape
+    assert x.is_contiguous() and x.dtype == torch.bfloat16
+    y = torch.empty((n, h // 2, wd // 2, c), dtype=torch.bfloat16, device=x.device)
+    check(load().ske_maxpool2_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), n, h, wd, c, _stream(x)))
     return y
 
 
@@ -196,8 +235,11 @@ def make_net(seed: int = 0, device="cuda"):
 
         @staticmethod
         def pool(x):
-            # 2 x 2 max pooling of an NHWC tensor in place of layout (no NCHW round trip).
+            # 2 x 2 max pooling of an NHWC tensor in place of layout (no NCHW round
+            # trip); without gradients one kernel (the same values).
             n, h, w, c = x.shape
+            if not torch.is_grad_enabled() and x.is_contiguous() and h % 2 == 0 and w % 2 == 0 and c % 8 == 0:
+                return maxpool2(x)
             return x.view(n, h // 2, 2, w // 2, 2, c).amax((2, 4))
 
         @staticmethod
@@ -219,8 +261,14 @@ def make_net(seed: int = 0, device="cuda"):
             b4 = self.c(self.c(self.pool(e3), "b4a"), "b4b")
             d3 = self.c(self.upcat(b4, e3, "d3a"), "d3b")
             d2 = self.c(self.upcat(d3, e2, "d2a"), "d2b")
-            d1 = self.c(self.upcat(d2, e1, "d1a"), "d1b")
-            cells = (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log(1 + area)
+            d1a = self.upcat(d2, e1, "d1a")
+            cells = None
+            if not torch.is_grad_enabled():  # the last convolution and the 1x1 head in one kernel
+                cells = conv3x3_head(d1a, self.w["d1b"].to(torch.bfloat16), self.b["d1b"], self.head_w,
+                                     self.head_b, True)
+            if cells is None:
+                d1 = self.c(d1a, "d1b")
+                cells = (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log(1 + area)
             f = b4.float()
             # log total area of the coarse engine run (input channel 2)
             lct = torch.log(torch.expm1(x[..., 2].float() * COARSE_SCALE).clamp_min(0).sum((1, 2)).clamp_min(1.0))
@@ -246,10 +294,11 @@ _COARSE_ENGINES = {}
 
 
 def coarse_area(tiles, engine=None, chunk: int = 4096):
-    """The engine's total viewshed (180 angles) of each tile at 1/COARSE
-    resolution, per tile cell in tile-cell units: (N, 256, 256) float32 (CUDA).
-    The coarse grid averages COARSE x COARSE cells; its heights, observer height
-    and areas are rescaled to its COARSE-times larger cells."""
+    """The engine's total viewshed of each tile at 1/COARSE resolution from
+    every COARSE_ANGLE_STEP-th of the 180 angles (scaled by the step), per tile
+    cell in tile-cell units: (N, 256, 256) float32 (CUDA).  The coarse grid
+    averages COARSE x COARSE cells; its heights, observer height and areas are
+    rescaled to its COARSE-times larger cells."""
     import torch
     from .engine import SkewEngine, run_batch
     t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda")
@@ -262,9 +311,10 @@ def coarse_area(tiles, engine=None, chunk: int = 4096):
             _COARSE_ENGINES[dev] = SkewEngine(side, side, device=dev)
         engine = _COARSE_ENGINES[dev]
     povh = float(synthetic.POVH) / COARSE
+    angles = list(range(0, 180, COARSE_ANGLE_STEP))
     for i in range(0, n, chunk):
-        run_batch(0, c[i:i + chunk], povh=povh, engine=engine, outs=out[i:i + chunk])
-    area = out * float(COARSE * COARSE)
+        run_batch(0, c[i:i + chunk], povh=povh, engine=engine, outs=out[i:i + chunk], angles=angles)
+    area = out * float(COARSE * COARSE * COARSE_ANGLE_STEP)
     return area.repeat_interleave(COARSE, 1).repeat_interleave(COARSE, 2)
 
 

@@ -295,3 +295,37 @@ def test_ws_conv_equals_halo_conv_bits(sur):
             got = sur.conv3x3(x, wt, b, True)
             sur.conv_check()
         assert torch.equal(got.view(torch.int16), want.view(torch.int16)), (n, h, w, cin, cout)
+
+
+def test_conv_head_equals_conv_then_1x1(sur):
+    """The fused last convolution + 1x1 head against the two steps: bfloat16
+    activations, then their float32 dot product with the head weights (orders
+    of the float32 sums differ, so equal to float32 rounding).  16 tiles of
+    64 x 256 give every persistent CTA two tiles."""
+    import torch
+    rng = np.random.default_rng(21)
+    n, h, w, cin, cout = 16, 64, 256, 96, 32
+    x = _bf16(rng.normal(0, 1, (n, h, w, cin))).cuda().contiguous()
+    wt = torch.zeros((cout, sur.kpad(cin)), dtype=torch.bfloat16)
+    wt[:, : 9 * cin] = _bf16(rng.normal(0, 0.05, (cout, 9 * cin)))
+    wt = wt.cuda()
+    b = torch.as_tensor(rng.normal(0, 0.5, cout), dtype=torch.float32).cuda()
+    hw = torch.as_tensor(rng.normal(0, 0.3, (cout, 1)), dtype=torch.float32).cuda()
+    hb = torch.tensor([8.0], device="cuda")
+    got = sur.conv3x3_head(x, wt, b, hw, hb, True)
+    sur.conv_check()
+    assert got is not None and got.shape == (n, h, w)
+    want = (sur.conv3x3(x, wt, b, True).float() @ hw)[..., 0] + hb
+    err = (got - want).abs().max().item()
+    assert err <= 1e-5 * want.abs().max().item(), err
+
+
+def test_maxpool2_equals_torch_amax_bits(sur):
+    import torch
+    rng = np.random.default_rng(22)
+    x = _bf16(rng.normal(0, 1, (3, 34, 18, 48))).cuda().contiguous()
+    x.view(-1)[::977] = float("nan")
+    want = x.view(3, 17, 2, 9, 2, 48).amax((2, 4))
+    got = sur.maxpool2(x)
+    assert torch.equal(torch.isnan(got), torch.isnan(want))
+    assert torch.equal(got.nan_to_num(0).view(torch.int16), want.nan_to_num(0).view(torch.int16))
