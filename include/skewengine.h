@@ -428,6 +428,15 @@ int ske_conv3x3_head_bf16(const void* x, const void* w, const float* bias, const
                           const float* head_b, float* y, int n, int h, int w_, int cin, int cout, int relu,
                           void* stream);
 
+/* The surrogate's network input on the device: x (n x side x side x 8,
+ * bfloat16) from float32 tiles (n x side x side), their per-tile mean and
+ * height range (n floats each) and coarse areas (n x side/f x side/f, f =
+ * coarse_factor): x[...,0] = (h - mean) / (range, or 1 for 0), x[...,1] =
+ * log1p(range), x[...,2] = log1p(coarse area of the cell's coarse cell) /
+ * coarse_scale, channels 3-7 zero.  No reference counterpart. */
+int ske_surrogate_encode_bf16(const float* tiles, const float* mean, const float* range, const float* coarse,
+                              int coarse_factor, float coarse_scale, void* x, int n, int side, void* stream);
+
 /* 2 x 2 max pooling of an NHWC bfloat16 tensor on the device (h, w even, c a
  * multiple of 8): y[n][i][j][c] = max of x[n][2i..2i+1][2j..2j+1][c], NaN
  * propagated.  No reference counterpart. */

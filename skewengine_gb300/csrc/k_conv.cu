@@ -1246,6 +1246,43 @@ extern "C" int ske_maxpool2_bf16(const void* x, void* y, int n, int h, int w_, i
     return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
 }
 
+// Surrogate network input, one thread per cell: channel 0 = (h - mean) /
+// (range, or 1 when 0), 1 = log1p(range), 2 = log1p(coarse area of the cell's
+// coarse cell) / coarse_scale, 3..7 = 0, each rounded to bfloat16 (the same
+// float32 operations as the element-wise tensor expressions).
+static __global__ void k_encode(const float* __restrict__ T, const float* __restrict__ mean,
+                                const float* __restrict__ range, const float* __restrict__ coarse, int factor,
+                                float coarse_scale, bf16* __restrict__ X, int64_t total, int side) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int64_t n = i / ((int64_t)side * side);
+    const int rem = (int)(i - n * side * side), y = rem / side, x = rem - (rem / side) * side;
+    const float r = range[n];
+    const int cs = side / factor;
+    const float c = coarse[(n * cs + y / factor) * cs + x / factor];
+    __nv_bfloat162 v[4];
+    v[0] = __halves2bfloat162(__float2bfloat16_rn(__fdiv_rn(__fsub_rn(T[i], mean[n]), r > 0.0f ? r : 1.0f)),
+                              __float2bfloat16_rn(log1pf(r)));
+    v[1] = __halves2bfloat162(__float2bfloat16_rn(__fdiv_rn(log1pf(c), coarse_scale)), __float2bfloat16_rn(0.0f));
+    v[2] = v[3] = __halves2bfloat162(__float2bfloat16_rn(0.0f), __float2bfloat16_rn(0.0f));
+    reinterpret_cast<uint4*>(X)[i] = *reinterpret_cast<const uint4*>(v);
+}
+
+extern "C" int ske_surrogate_encode_bf16(const float* tiles, const float* mean, const float* range,
+                                         const float* coarse, int coarse_factor, float coarse_scale, void* x, int n,
+                                         int side, void* stream) {
+    if (!tiles || !mean || !range || !coarse || !x || n < 1 || side < 1 || coarse_factor < 1 ||
+        side % coarse_factor || !(coarse_scale > 0.0f))
+        return SKE_ERR_INVALID;
+    if (!aligned(x, 16) || !aligned(tiles, 4) || !aligned(coarse, 4)) return SKE_ERR_INVALID;
+    const int64_t total = (int64_t)n * side * side;
+    const int64_t blocks = (total + 255) / 256;
+    if (blocks > 0x7fffffff) return SKE_ERR_INVALID;
+    k_encode<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(tiles, mean, range, coarse, coarse_factor,
+                                                                 coarse_scale, (bf16*)x, total, side);
+    return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
 extern "C" int ske_conv_select(int path) {
     if (path < 0 || path > 2) return SKE_ERR_INVALID;
     g_conv_path = path;

@@ -31,6 +31,7 @@ from __future__ import annotations
 import ctypes as C
 import math
 import os
+import threading
 
 import numpy as np
 
@@ -229,9 +230,22 @@ def make_net(seed: int = 0, device="cuda"):
             self.ctx1_b = torch.nn.Parameter(torch.zeros(CTX))
             self.ctx2_w = torch.nn.Parameter(torch.randn(CTX, 1, generator=g) * math.sqrt(1.0 / CTX) * 0.1)
             self.ctx2_b = torch.nn.Parameter(torch.zeros(1))
+            self._wb = {}
 
         def c(self, x, name):
+            if not torch.is_grad_enabled():
+                return conv3x3(x, self.wb(name), self.b[name], True)
             return conv_op(x, self.w[name], self.b[name], True)
+
+        def wb(self, name):
+            # bfloat16 copy of a layer's weights for inference, made again only
+            # when the float32 parameter has changed (its version counter).
+            p = self.w[name]
+            hit = self._wb.get(name)
+            if hit is None or hit[0] != p._version or hit[1].device != p.device:
+                hit = (p._version, p.detach().to(torch.bfloat16).contiguous())
+                self._wb[name] = hit
+            return hit[1]
 
         @staticmethod
         def pool(x):
@@ -251,7 +265,7 @@ def make_net(seed: int = 0, device="cuda"):
             # Without gradients the decoder reads the upsampled low-resolution
             # input and the skip connection in place (same values).
             if not torch.is_grad_enabled():
-                return conv3x3_upcat(low, skip, self.w[name].to(torch.bfloat16), self.b[name], True)
+                return conv3x3_upcat(low, skip, self.wb(name), self.b[name], True)
             return self.c(torch.cat([self.up(low), skip], 3).contiguous(), name)
 
         def forward(self, x):
@@ -264,15 +278,15 @@ def make_net(seed: int = 0, device="cuda"):
             d1a = self.upcat(d2, e1, "d1a")
             cells = None
             if not torch.is_grad_enabled():  # the last convolution and the 1x1 head in one kernel
-                cells = conv3x3_head(d1a, self.w["d1b"].to(torch.bfloat16), self.b["d1b"], self.head_w,
-                                     self.head_b, True)
+                cells = conv3x3_head(d1a, self.wb("d1b"), self.b["d1b"], self.head_w, self.head_b, True)
             if cells is None:
                 d1 = self.c(d1a, "d1b")
                 cells = (d1.float() @ self.head_w)[..., 0] + self.head_b  # (N, H, W) log(1 + area)
-            f = b4.float()
             # log total area of the coarse engine run (input channel 2)
             lct = torch.log(torch.expm1(x[..., 2].float() * COARSE_SCALE).clamp_min(0).sum((1, 2)).clamp_min(1.0))
-            pooled = torch.cat([f.mean((1, 2)), f.amax((1, 2)), (lct / 20.0)[:, None]], 1)
+            # the bottleneck's channel means (float32 sums) and maxima
+            pooled = torch.cat([b4.mean((1, 2), dtype=torch.float32), b4.amax((1, 2)).float(),
+                                (lct / 20.0)[:, None]], 1)
             t = lct + (torch.relu(pooled @ self.ctx1_w + self.ctx1_b) @ self.ctx2_w)[:, 0] + self.ctx2_b
             return calibrate(cells, t)
 
@@ -295,10 +309,11 @@ _COARSE_ENGINES = {}
 
 def coarse_area(tiles, engine=None, chunk: int = 4096):
     """The engine's total viewshed of each tile at 1/COARSE resolution from
-    every COARSE_ANGLE_STEP-th of the 180 angles (scaled by the step), per tile
-    cell in tile-cell units: (N, 256, 256) float32 (CUDA).  The coarse grid
-    averages COARSE x COARSE cells; its heights, observer height and areas are
-    rescaled to its COARSE-times larger cells."""
+    every COARSE_ANGLE_STEP-th of the 180 angles (scaled by the step), per
+    coarse cell in tile-cell units: (N, 256/COARSE, 256/COARSE) float32 (CUDA);
+    every tile cell takes its coarse cell's value.  The coarse grid averages
+    COARSE x COARSE cells; its heights, observer height and areas are rescaled
+    to its COARSE-times larger cells."""
     import torch
     from .engine import SkewEngine, run_batch
     t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda")
@@ -314,24 +329,27 @@ def coarse_area(tiles, engine=None, chunk: int = 4096):
     angles = list(range(0, 180, COARSE_ANGLE_STEP))
     for i in range(0, n, chunk):
         run_batch(0, c[i:i + chunk], povh=povh, engine=engine, outs=out[i:i + chunk], angles=angles)
-    area = out * float(COARSE * COARSE * COARSE_ANGLE_STEP)
-    return area.repeat_interleave(COARSE, 1).repeat_interleave(COARSE, 2)
+    return out * float(COARSE * COARSE * COARSE_ANGLE_STEP)
 
 
 def encode_tiles(tiles, coarse=None):
     """(N, 256, 256) float32 heights (NumPy or CUDA tensor) -> (N, 256, 256, 8)
-    bfloat16 network input (CUDA).  coarse: coarse_area(tiles), computed here
+    bfloat16 network input (CUDA), written by one kernel
+    (ske_surrogate_encode_bf16).  coarse: coarse_area(tiles), computed here
     when not given."""
     import torch
-    t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda")
-    mean = t.mean((1, 2), keepdim=True)
-    rng = (t.amax((1, 2), keepdim=True) - t.amin((1, 2), keepdim=True))
-    x = torch.zeros(t.shape + (IN_CH,), dtype=torch.bfloat16, device="cuda")
-    x[..., 0] = ((t - mean) / torch.where(rng > 0, rng, torch.ones_like(rng))).to(torch.bfloat16)
-    x[..., 1] = torch.log1p(rng).expand_as(t).to(torch.bfloat16)
+    t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda").contiguous()
+    n, side = t.shape[0], t.shape[1]
+    mean = t.mean((1, 2)).contiguous()
+    rng = (t.amax((1, 2)) - t.amin((1, 2))).contiguous()
     if coarse is None:
         coarse = coarse_area(t)
-    x[..., 2] = (torch.log1p(coarse) / COARSE_SCALE).to(torch.bfloat16)
+    coarse = coarse.contiguous()
+    x = torch.empty(t.shape + (IN_CH,), dtype=torch.bfloat16, device="cuda")
+    check(load().ske_surrogate_encode_bf16(C.c_void_p(t.data_ptr()), C.c_void_p(mean.data_ptr()),
+                                           C.c_void_p(rng.data_ptr()), C.c_void_p(coarse.data_ptr()),
+                                           side // coarse.shape[1], COARSE_SCALE, C.c_void_p(x.data_ptr()), n, side,
+                                           _stream(t)))
     return x
 
 
@@ -480,21 +498,42 @@ def infer_dem(net, dem, engine=None, check_fraction: float = 0.05, bound: float 
                         device="cuda")
     H, W = d.shape
     tiles, (ty, tx) = _cut_tiles_dev(d)
-    x = encode_tiles(tiles)
-    out = torch.empty((len(tiles), TILE, TILE), dtype=torch.float32, device="cuda")
-    with torch.no_grad():
-        for i in range(0, len(tiles), batch):
-            out[i:i + batch] = net(x[i:i + batch])
-    conv_check()
     rng = np.random.default_rng(seed)
     n_check = max(1, int(round(check_fraction * len(tiles))))
     checked = np.sort(rng.choice(len(tiles), n_check, replace=False))
     eng = engine or SkewEngine(TILE, TILE)
     truth = torch.empty((n_check, TILE, TILE), dtype=torch.float32, device="cuda")
-    # All checked tiles in one batched engine call (ske_run_batch: the engine
-    # keeps the batch plan and replays it as a CUDA graph on later calls).
     sel = tiles[torch.as_tensor(checked, device="cuda")].contiguous()
-    run_batch(0, sel, engine=eng, outs=truth)
+    # The checked tiles do not depend on the network: their batched engine call
+    # (ske_run_batch on the engine's own stream, a CUDA graph replay after the
+    # first call) runs from a host thread while this thread computes the coarse
+    # channel and the network on torch's stream.
+    # The engine's stream waits here for the gather of `sel` (torch's stream of
+    # this thread); the worker makes the engine's stream its current one, so it
+    # adds no wait on other work.
+    eng._after_torch(sel, truth)
+    failure = []
+
+    def checks():
+        try:
+            with torch.cuda.stream(eng._ext):
+                run_batch(0, sel, engine=eng, outs=truth)
+        except BaseException as exc:  # re-raised below
+            failure.append(exc)
+
+    worker = threading.Thread(target=checks)
+    worker.start()
+    try:
+        x = encode_tiles(tiles)
+        out = torch.empty((len(tiles), TILE, TILE), dtype=torch.float32, device="cuda")
+        with torch.no_grad():
+            for i in range(0, len(tiles), batch):
+                out[i:i + batch] = net(x[i:i + batch])
+        conv_check()
+    finally:
+        worker.join()
+    if failure:
+        raise failure[0]
     truth = torch.log1p(truth)
     errs = tile_area_error(out[torch.as_tensor(checked, device="cuda")], truth)
     if force_error:

@@ -329,3 +329,23 @@ def test_maxpool2_equals_torch_amax_bits(sur):
     got = sur.maxpool2(x)
     assert torch.equal(torch.isnan(got), torch.isnan(want))
     assert torch.equal(got.nan_to_num(0).view(torch.int16), want.nan_to_num(0).view(torch.int16))
+
+
+def test_encode_kernel_equals_tensor_expressions(sur):
+    """The input-encoding kernel writes the bits of the element-wise tensor
+    expressions it replaces (coarse areas repeated over their 4 x 4 cells)."""
+    import torch
+    tiles = torch.as_tensor(np.stack([synthetic.fractal_dem(256, 90 + i) for i in range(3)] +
+                                     [np.full((256, 256), 7.0, np.float32)]), device="cuda")
+    coarse = sur.coarse_area(tiles)
+    assert coarse.shape == (4, 64, 64)
+    got = sur.encode_tiles(tiles, coarse)
+    t = tiles
+    mean = t.mean((1, 2), keepdim=True)
+    rng = t.amax((1, 2), keepdim=True) - t.amin((1, 2), keepdim=True)
+    want = torch.zeros(t.shape + (8,), dtype=torch.bfloat16, device="cuda")
+    want[..., 0] = ((t - mean) / torch.where(rng > 0, rng, torch.ones_like(rng))).to(torch.bfloat16)
+    want[..., 1] = torch.log1p(rng).expand_as(t).to(torch.bfloat16)
+    full = coarse.repeat_interleave(4, 1).repeat_interleave(4, 2)
+    want[..., 2] = (torch.log1p(full) / sur.COARSE_SCALE).to(torch.bfloat16)
+    assert torch.equal(got.view(torch.int16), want.view(torch.int16))
