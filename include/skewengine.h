@@ -246,6 +246,15 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
  * results.  No reference counterpart. */
 int ske_radon_select(int path);
 
+/* Skew kernel for later runs of every engine: 0 (default) = column gather (each
+ * thread streams one skewed column from the L2-resident orientations), 1 = each
+ * 32-column x 64-row block's source rows staged by one TMA box load (grids whose
+ * sides are multiples of 4 and at least 129 cells; others keep the gather).
+ * Both give the same bits; the gather measured faster (0.94 against 1.31 ms per
+ * 2000x2000 step of 180 sectors).  Replaces no reference call (cudaSkew,
+ * skewEngine.cuh:56-88, is one kernel). */
+int ske_skew_select(int path);
+
 /* Shape of the last viewshed sweep the engine launched: level schedule (lvl0
  * steps, then lvl1 when non-zero, then 64-step levels) and resident CTAs per SM
  * (0 = as many as fit), as chosen by the autotuner.  No reference counterpart. */

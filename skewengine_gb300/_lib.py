@@ -63,6 +63,7 @@ SIGNATURES = [
     ("ske_run_batch_angles", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                        C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(Params)]),
     ("ske_radon_select", C.c_int, [C.c_int]),
+    ("ske_skew_select", C.c_int, [C.c_int]),
     ("ske_sweep_shape", C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("ske_set_sweep_shape", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     ("ske_prepare", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),

@@ -140,6 +140,8 @@ struct ske_engine_s {
     DeskewMaps maps;
     const float* maps_so = nullptr;
     int maps_slots = 0;
+    // Tensor maps of d_orient for the TMA-staged skew (encoded with the buffer).
+    SkewMaps skew_maps;
     int4* d_lists = nullptr;  // survivor lists of the viewshed sweep
     size_t list_bytes = 0;
     float* h_pin = nullptr;
@@ -512,8 +514,9 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
 // the slot past H*dim_i unwritten, since no operator of the batch reads it.
 int run_skew(ske_engine e, const Batch& b, bool zero_tail = true) {
     LaunchScope ls(e, "skew", 1);
-    return ls.done(launch_skew(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len, std::max(e->dimx, e->dimy),
-                               e->geo.max_H, e->stream, zero_tail));
+    return ls.done(launch_skew_staged(e->dg, b, e->d_orient, e->N, e->d_SI, e->stride, e->len,
+                                      std::max(e->dimx, e->dimy), e->geo.max_H, e->stream, zero_tail, &e->skew_maps,
+                                      e->d_status));
 }
 
 // rows_from_p: the batch is Radon sectors whose back-projection was skipped;
@@ -1398,6 +1401,7 @@ int init_engine(ske_engine e, int dimx, int dimy, int device, void* stream, ske_
     // Grids and accumulators.
     SKE_TRY(dev_alloc(&e->d_in, e->N));
     SKE_TRY(dev_alloc(&e->d_orient, 4 * e->N));
+    encode_skew_maps(&e->skew_maps, e->d_orient, e->dimx, e->dimy);  // ok = false: the gather kernel runs
     SKE_TRY(dev_alloc(&e->d_acc, 4 * e->N));
     SKE_TRY(dev_alloc(&e->d_comp, 4 * e->N));
     SKE_TRY(dev_alloc(&e->d_out, e->N));
@@ -1607,6 +1611,11 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
         if (sub != e) e->launches += sub->launches - before;
         if (rc != SKE_OK) return rc;
     }
+    return SKE_OK;
+}
+
+int ske_skew_select(int path) {
+    if (skew_select(path) != 0) return fail(SKE_ERR_INVALID, "skew path must be 0 or 1");
     return SKE_OK;
 }
 

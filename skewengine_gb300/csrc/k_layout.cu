@@ -489,6 +489,103 @@ __global__ void __launch_bounds__(256, kMode == kDeskewKahan ? 2 : 4)
     }
 }
 
+// ---- TMA-staged skew -------------------------------------------------------
+// A block of 256 threads owns kSkTmaCols skewed columns c0.. and kSkTmaRows
+// skewed rows r0.. of one sector.  Column c of row r reads orientation rows
+// r - t_c - 1 and r - t_c (skew_gather), so the block needs rows
+// [r0 - max t - 1, r0 + kSkTmaRows - min t] of its 32 columns: thread 0 loads
+// them as one kSkTmaBox x 32 TMA box (128-byte rows, zero outside the grid) and
+// every thread then reads its column from shared memory (one bank per column)
+// and writes its rows coalesced.  The same operations and validity tests as
+// k_skew, so the same bits.  Where the columns' shifts span more than
+// kSkTmaSpan rows (strongly non-square grids) the block reads global memory
+// directly.  The wait for the box is bounded: one that runs out sets the
+// engine's status word (7), skips the block's rows and waits once more for the
+// copy before the block exits.
+constexpr int kSkTmaCols = 32, kSkTmaRows = 64, kSkTmaSpan = 64;
+constexpr int kSkTmaBox = kSkTmaRows + kSkTmaSpan + 1;
+constexpr int kSkTmaBytes = kSkTmaBox * kSkTmaCols * 4;
+
+__global__ void __launch_bounds__(256) k_skew_tma(const __grid_constant__ SkewMaps maps, DevGeometry g, Batch b,
+                                                  const float* __restrict__ orient, int64_t n_cells,
+                                                  float* __restrict__ SI, int64_t stride, int64_t len,
+                                                  bool zero_tail, int* __restrict__ status) {
+    __shared__ __align__(128) float box[kSkTmaBox][kSkTmaCols];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_tmax, s_tmin;
+    const int slot = blockIdx.z;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    float* out = SI + slot * stride;
+    const int c0 = blockIdx.x * kSkTmaCols, r0 = blockIdx.y * kSkTmaRows;
+    const int x = threadIdx.x & 31, y = threadIdx.x >> 5;
+    if (r0 < d.H && c0 < d.dim_i) {  // uniform over the block
+        const int c = c0 + x;
+        const int cc = min(c, d.dim_i - 1);
+        const int t = g.target[d.col_off + cc];
+        if (y == 0) {
+            int hi = t, lo = t;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+                lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            }
+            if (x == 0) {
+                s_tmax = hi;
+                s_tmin = lo;
+                mbar_init(&bar);
+                asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            }
+        }
+        __syncthreads();
+        const int tmax = s_tmax, rbase = r0 - tmax - 1;
+        const bool staged = tmax - s_tmin <= kSkTmaSpan;
+        bool ok = true;
+        if (staged) {
+            if (threadIdx.x == 0) {
+                mbar_expect(&bar, kSkTmaBytes);
+                asm volatile(
+                    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+                    "[%4];" ::"r"(smem_addr(&box[0][0])),
+                    "l"(reinterpret_cast<uint64_t>(&maps.t[d.type])), "r"(c0), "r"(rbase), "r"(smem_addr(&bar))
+                    : "memory");
+            }
+            ok = mbar_wait(&bar, 0);
+        }
+        if (!ok) {
+            if (threadIdx.x == 0) {
+                atomicExch(status, 7);
+                mbar_wait(&bar, 0);  // the copy lands before the block's shared memory is released
+            }
+        } else if (c < d.dim_i) {
+            const float* src = orient + (int64_t)d.type * n_cells;
+            const float w = g.weight[d.col_off + c], w1 = __fsub_rn(1.0f, w);
+            const int r1 = min(r0 + kSkTmaRows, d.H);
+            for (int r = r0 + y; r < r1; r += 8) {
+                const int i0 = r - t - 1;
+                const bool v0 = (unsigned)i0 < (unsigned)d.dim_o, v1 = (unsigned)(i0 + 1) < (unsigned)d.dim_o;
+                float a, bv;
+                if (staged) {
+                    a = box[i0 - rbase][x];
+                    bv = box[i0 + 1 - rbase][x];
+                } else {
+                    a = v0 ? src[(int64_t)i0 * d.dim_i + c] : 0.0f;
+                    bv = v1 ? src[(int64_t)(i0 + 1) * d.dim_i + c] : 0.0f;
+                }
+                float acc = 0.0f;
+                acc = v0 ? __fadd_rn(acc, __fmul_rn(w, a)) : acc;
+                acc = v1 ? __fadd_rn(acc, __fmul_rn(w1, bv)) : acc;
+                out[(int64_t)r * d.dim_i + c] = acc;
+            }
+        }
+    }
+    if (!zero_tail && d.in_width) return;  // nothing reads past H*dim_i
+    const int64_t z0 = (int64_t)d.H * d.dim_i;
+    const int64_t nthreads = (int64_t)gridDim.x * gridDim.y * blockDim.x;
+    for (int64_t q = z0 + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x; q < len;
+         q += nthreads)
+        out[q] = 0.0f;
+}
+
 __global__ void k_reduce(const float* __restrict__ acc, const float* __restrict__ comp, unsigned used,
                          float* __restrict__ out, int dimx, int dimy, int is_max, int kahan) {
     const int64_t n = (int64_t)dimx * dimy;
@@ -533,6 +630,24 @@ cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orien
                         int64_t stride, int64_t len, int max_cols, int max_rows, cudaStream_t st, bool zero_tail) {
     dim3 grid((max_cols + kSkewCols - 1) / kSkewCols, (max_rows + kSkewRows - 1) / kSkewRows, b.count);
     k_skew<<<grid, kSkewCols, 0, st>>>(g, b, orient, n_cells, SI, stride, len, zero_tail);
+    return cudaGetLastError();
+}
+
+int g_skew_path = 0;
+
+int skew_select(int path) {
+    if (path != 0 && path != 1) return -1;
+    g_skew_path = path;
+    return 0;
+}
+
+cudaError_t launch_skew_staged(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells,
+                               float* SI, int64_t stride, int64_t len, int max_cols, int max_rows, cudaStream_t st,
+                               bool zero_tail, const SkewMaps* maps, int* status) {
+    if (g_skew_path != 1 || !maps || !maps->ok || !status)
+        return launch_skew(g, b, orient, n_cells, SI, stride, len, max_cols, max_rows, st, zero_tail);
+    dim3 grid((max_cols + kSkTmaCols - 1) / kSkTmaCols, (max_rows + kSkTmaRows - 1) / kSkTmaRows, b.count);
+    k_skew_tma<<<grid, 256, 0, st>>>(*maps, g, b, orient, n_cells, SI, stride, len, zero_tail, status);
     return cudaGetLastError();
 }
 
@@ -582,6 +697,31 @@ bool encode_band_maps(DeskewMaps* m, const float* SO, int64_t stride, int slots,
         const cuuint32_t box[3] = {(cuuint32_t)kTile, (cuuint32_t)kDeskewBand, 1};
         const cuuint32_t estr[3] = {1, 1, 1};
         if (fn(k == 0 ? &m->x : &m->y, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)SO, dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    m->ok = true;
+    return true;
+}
+
+bool encode_skew_maps(SkewMaps* m, const float* orient, int dimx, int dimy) {
+    m->ok = false;
+    const EncodeTiledFn fn = encode_fn();
+    // Row pitch and orientation offsets multiples of 16 bytes; the box (32 x
+    // kSkTmaBox) no wider or taller than an orientation.
+    if (!fn || !orient || dimx % 4 || dimy % 4 || dimx < kSkTmaBox || dimy < kSkTmaBox ||
+        ((uintptr_t)orient & 15))
+        return false;
+    const int64_t n = (int64_t)dimx * dimy;
+    for (int t = 0; t < 4; t++) {
+        const bool tr = t == 1 || t == 2;  // transposed orientations: rows of dimy cells
+        const int di = tr ? dimy : dimx, dout = tr ? dimx : dimy;
+        const cuuint64_t dims[2] = {(cuuint64_t)di, (cuuint64_t)dout};
+        const cuuint64_t strides[1] = {(cuuint64_t)di * 4};
+        const cuuint32_t box[2] = {(cuuint32_t)kSkTmaCols, (cuuint32_t)kSkTmaBox};
+        const cuuint32_t estr[2] = {1, 1};
+        if (fn(&m->t[t], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)(orient + t * n), dims, strides, box, estr,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return false;

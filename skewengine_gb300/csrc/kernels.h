@@ -35,6 +35,25 @@ cudaError_t launch_skew(const DevGeometry& g, const Batch& b, const float* orien
                         float* SI, int64_t stride, int64_t len, int max_cols, int max_rows, cudaStream_t st,
                         bool zero_tail = true);
 
+// Tensor maps of the four input orientations for the TMA-staged skew: 2-D
+// float32 views (dim_i columns, dim_o rows) of orient + t*N.
+struct SkewMaps {
+    CUtensorMap t[4];
+    bool ok = false;
+};
+// Encodes the four maps; false (maps unusable, the gather kernel runs) unless
+// both sides are multiples of 4 and at least 129 cells.
+bool encode_skew_maps(SkewMaps* m, const float* orient, int dimx, int dimy);
+// The same skew as launch_skew with each block's input rows staged by one TMA
+// box load when that path is selected (skew_select(1)) and `maps` is usable
+// (status: the engine's status word, set when a bounded wait gives up).  The
+// column-gather kernel is the default: it measured faster (0.94 against 1.31 ms
+// per 2000x2000 step of 180 sectors).
+int skew_select(int path);  // 0 = column gather, 1 = TMA-staged; -1 for another value
+cudaError_t launch_skew_staged(const DevGeometry& g, const Batch& b, const float* orient, int64_t n_cells,
+                               float* SI, int64_t stride, int64_t len, int max_cols, int max_rows, cudaStream_t st,
+                               bool zero_tail, const SkewMaps* maps, int* status);
+
 // Identity operator (kernelUNIT.h:16-23): SO = SI on covered cells, 0 elsewhere.
 cudaError_t launch_identity(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
                             int64_t stride, int64_t len, cudaStream_t st);

@@ -417,10 +417,15 @@ def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 
     """Adam on the mean squared error of per-cell log area plus `tile_weight`
     times the squared error of the log of each tile's total area (per-cell log
     errors alone leave tile totals biased low: the totals are dominated by the
-    few cells that see far).  Returns the per-step losses."""
+    few cells that see far).  The learning rate warms up linearly over the first
+    5% of the steps and then follows a cosine to zero; gradients are clipped to
+    norm 1 (without both, runs at this rate could diverge part-way).  Returns
+    the per-step losses."""
     import torch
     opt = torch.optim.Adam(net.parameters(), lr=lr)
-    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, max(steps, 1))
+    warm = max(1, steps // 20)
+    sched = torch.optim.lr_scheduler.LambdaLR(
+        opt, lambda s: min(1.0, (s + 1) / warm) * 0.5 * (1.0 + math.cos(math.pi * min(s, steps) / max(steps, 1))))
     g = torch.Generator(device="cpu").manual_seed(seed)
     losses = []
     for step in range(steps):
@@ -430,6 +435,7 @@ def train(net, x, y, steps: int, batch: int = 16, lr: float = 2e-3, seed: int = 
         loss = torch.mean((pred - yt) ** 2) + tile_weight * torch.mean((_log_total(pred) - _log_total(yt)) ** 2)
         opt.zero_grad(set_to_none=True)
         loss.backward()
+        torch.nn.utils.clip_grad_norm_(net.parameters(), 1.0)
         opt.step()
         sched.step()
         losses.append(float(loss.detach()))

@@ -406,3 +406,34 @@ def test_radon_fused_sector_kernel_bit_exact(ske, oracle, gpu_lib):
         assert ((fused.view(np.uint32) == want.view(np.uint32)) | (np.isnan(fused) & np.isnan(want))).all()
     finally:
         gpu_lib.ske_radon_select(1)
+
+
+@pytest.mark.parametrize("side,side_y", [(640, 480), (1024, 160), (200, 200)])
+def test_staged_skew_matches_oracle(ske, oracle, side, side_y):
+    """The TMA-staged skew (ske_skew_select(1); sides multiples of 4, >= 129).
+    On 1024 x 160 the columns of a 32-wide block shift by more than 64 rows at
+    angles 9-25 and 155-171 (those blocks read global memory directly); the
+    other angles stage their rows.  Output bit for bit against the oracle, and
+    the skewed input of every sector equal to the gather kernel's."""
+    x = synthetic.fractal_dem(side, 17, side_y=side_y)
+    angles = [0, 5, 9, 12, 20, 33, 45, 80, 90, 100, 135, 160, 170, 179]
+    lib = ske.engine.load()
+    try:
+        assert lib.ske_skew_select(1) == 0
+        with ske.SkewEngine(side, side_y) as eng:
+            got = eng.run(0, x, povh=synthetic.POVH, angles=angles)
+            eng.prepare(x)
+            staged = []
+            for a in angles:
+                eng.skew(a)
+                staged.append(eng.skewed()[0])
+        assert lib.ske_skew_select(0) == 0
+        with ske.SkewEngine(side, side_y) as eng:
+            eng.prepare(x)
+            for a, si in zip(angles, staged):
+                eng.skew(a)
+                assert bits_equal(si, eng.skewed()[0]), a
+    finally:
+        lib.ske_skew_select(0)
+    want = oracle.run_ordered(0, x, angles, povh=synthetic.POVH)
+    assert bits_equal(got, want)
