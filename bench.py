@@ -493,7 +493,7 @@ def cepstrum_batch_workload(args):
 
 def convs_workload(args):
     """Every 3x3 convolution of the surrogate U-Net, forward, on a batch of
-    SKE_CONV_BATCH (default 16) 256x256 tiles: per-layer time and TFLOP/s for the
+    SKE_CONV_BATCH (default 256, the inference batch) 256x256 tiles: per-layer time and TFLOP/s for the
     default kernel choice (warp-specialised where it applies), the halo-staged
     kernel and the im2col kernel (ske_conv_select), CUDA events, and the whole
     set on the default choice against the measured bf16 peak."""
@@ -502,7 +502,7 @@ def convs_workload(args):
     build.build()
     from skewengine_gb300 import surrogate as sur
     lib = _lib.load()
-    n = _env_int("SKE_CONV_BATCH", 16)
+    n = _env_int("SKE_CONV_BATCH", 256)
     # SKE_CONV_STAGE: input channels per pipeline step of the warp-specialised kernel (0 = its own choice).
     stage = _env_int("SKE_CONV_STAGE", 0)
     assert lib.ske_conv_stage_channels(stage) == 0

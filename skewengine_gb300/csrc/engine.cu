@@ -402,12 +402,13 @@ int tune_sweep(ske_engine e, const SdemLaunch& base, const std::vector<uint64_t>
     SKE_CK(cudaMemcpyAsync(e->d_tune_items, sample.data(), sizeof(uint64_t) * sample.size(), cudaMemcpyHostToDevice,
                            e->stream));
     const int max_ctas = sdem_max_ctas_per_sm(base);
-    const SweepShape sched[] = {{64, 0, 0}, {16, 48, 0}, {32, 0, 0}};
+    const SweepShape sched[] = {{64, 0, 0}, {16, 48, 0}, {32, 0, 0}, {48, 0, 0}};
     std::vector<SweepShape> cands;
     for (const SweepShape& c : sched) {
         cands.push_back(c);
         if (max_ctas > 1) cands.push_back({c.lvl0, c.lvl1, max_ctas - 1});
     }
+    if (max_ctas > 2) cands.push_back({32, 0, max_ctas - 2});
     cudaEvent_t ev[2];
     SKE_CK(cudaEventCreate(&ev[0]));
     SKE_CK(cudaEventCreate(&ev[1]));

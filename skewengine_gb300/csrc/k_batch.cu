@@ -133,6 +133,24 @@ __global__ void __launch_bounds__(kSkewCols) k_skew_batch(BatchTables T, float* 
     }
 }
 
+// A sector's kPer + 1 staged cells of this thread's column (zero outside the
+// sector's rows and outside a row's valid range).
+template <int kPer>
+__device__ __forceinline__ void deskew_cells(const BatchGrid& G, const SectorRef& d, int tj, int ib, int j, int nv,
+                                             const float* __restrict__ SO, float* cell) {
+    const int4* rt = G.rowtab + d.row_off;
+    const float* so = SO + d.cells;
+#pragma unroll
+    for (int kk = 0; kk <= kPer; kk++) {
+        const int r = ib + kk + tj;
+        cell[kk] = 0.0f;
+        if (kk <= nv && r < d.H) {
+            const int4 m = rt[r];
+            if (j >= m.x && j < m.y) cell[kk] = so[m.z + (j - m.x)];
+        }
+    }
+}
+
 // Deskew + accumulate (skewEngine.cuh:772-792) of one kRows x 32 accumulator
 // tile of one orientation of one grid over that type's sectors in accumulation
 // order.  A thread owns kPer consecutive accumulator rows of one column, keeps
@@ -141,10 +159,11 @@ __global__ void __launch_bounds__(kSkewCols) k_skew_batch(BatchTables T, float* 
 // is zero) straight from the compact rows: one row-table load and one value
 // load per cell, lanes of a warp on consecutive columns.  There are no
 // barriers, so warps advance independently and hide each other's latency; the
-// next sector's descriptor, target and weight are loaded a sector ahead.  The
-// arithmetic is the reference's, in its order.
+// next sector's cells are loaded before the current one is accumulated, and
+// descriptors, targets and weights two sectors ahead.  The arithmetic is the
+// reference's, in its order.
 template <int kMode>
-__global__ void __launch_bounds__(256) k_deskew_batch(BatchTables T, const float* __restrict__ SO) {
+__global__ void __launch_bounds__(256, 4) k_deskew_batch(BatchTables T, const float* __restrict__ SO) {
     constexpr int kPer = kRows / 8;
     const int k = find_entry(T.tile_start, 4 * T.n_grids, blockIdx.x);
     const int gi = k >> 2, t = k & 3;
@@ -168,30 +187,30 @@ __global__ void __launch_bounds__(256) k_deskew_batch(BatchTables T, const float
         s[q] = q < nv ? A[(int64_t)q * dim_i] : 0.0f;
         c[q] = (kMode == kKahan && q < nv) ? Cc[(int64_t)q * dim_i] : 0.0f;
     }
+    // Software pipeline: the cells of sector q + 1 are loaded before sector q is
+    // accumulated, and descriptors, targets and weights two sectors ahead.
     const SectorRef* refs = T.refs + G.ts_start[t];
-    SectorRef nx = refs[0];
-    int ntj = G.target[nx.col_off + j];
-    float nw = G.weight[nx.col_off + j];
+    const SectorRef d0 = refs[0];
+    float cell[kPer + 1], nxt[kPer + 1];
+    deskew_cells<kPer>(G, d0, G.target[d0.col_off + j], ib, j, nv, SO, cell);
+    float w = G.weight[d0.col_off + j];
+    SectorRef d1 = d0;
+    int t1 = 0;
+    float w_1 = 0.0f;
+    if (cnt > 1) {
+        d1 = refs[1];
+        t1 = G.target[d1.col_off + j];
+        w_1 = G.weight[d1.col_off + j];
+    }
     for (int q = 0; q < cnt; q++) {
-        const SectorRef cur = nx;
-        const int tj = ntj;
-        const float w = nw;
-        if (q + 1 < cnt) {  // the next sector's descriptor, target and weight, a sector ahead
-            nx = refs[q + 1];
-            ntj = G.target[nx.col_off + j];
-            nw = G.weight[nx.col_off + j];
-        }
-        const int4* rt = G.rowtab + cur.row_off;
-        const float* so = SO + cur.cells;
-        float cell[kPer + 1];
-#pragma unroll
-        for (int kk = 0; kk <= kPer; kk++) {
-            const int r = ib + kk + tj;
-            cell[kk] = 0.0f;
-            if (kk <= nv && r < cur.H) {
-                const int4 m = rt[r];
-                if (j >= m.x && j < m.y) cell[kk] = so[m.z + (j - m.x)];
-            }
+        if (q + 1 < cnt) deskew_cells<kPer>(G, d1, t1, ib, j, nv, SO, nxt);
+        SectorRef d2 = d1;
+        int t2 = 0;
+        float w_2 = 0.0f;
+        if (q + 2 < cnt) {
+            d2 = refs[q + 2];
+            t2 = G.target[d2.col_off + j];
+            w_2 = G.weight[d2.col_off + j];
         }
         const float w1 = __fsub_rn(1.0f, w);
 #pragma unroll
@@ -207,6 +226,12 @@ __global__ void __launch_bounds__(256) k_deskew_batch(BatchTables T, const float
                 s[q2] = __fadd_rn(s[q2], v);
             }
         }
+#pragma unroll
+        for (int kk = 0; kk <= kPer; kk++) cell[kk] = nxt[kk];
+        w = w_1;
+        d1 = d2;
+        t1 = t2;
+        w_1 = w_2;
     }
 #pragma unroll
     for (int q = 0; q < kPer; q++) {
