@@ -644,6 +644,20 @@ def surrogate_workload(args):
         t1.record()
         torch.cuda.synchronize()
     fwd_ms = t0.elapsed_time(t1) / 3
+    # The plain engine's headline throughput on this machine (2000x2000 DEM, 360
+    # directional sectors, device-resident), the reference point of the target
+    # "surrogate throughput >= 10x the plain engine's".
+    d2k = torch.as_tensor(synthetic.fractal_dem(SIDE, 1000, roughness=0.8), device="cuda")
+    o2k = torch.empty_like(d2k)
+    with ske.SkewEngine(SIDE, SIDE) as e2k:
+        e2k.run(0, d2k, o2k)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(3):
+            e2k.run(0, d2k, o2k)
+        torch.cuda.synchronize()
+        head_s = (time.perf_counter() - t) / 3
+    head_tput = SIDE * SIDE * DIR_SECTORS / head_s / 1e6
     err = sur.tile_area_error(pred, torch.log1p(truth))
     # the whole DEM's visible area (the sum over its tiles), network alone
     net_total = float(torch.expm1(pred).clamp_min(0).sum())
@@ -661,6 +675,8 @@ def surrogate_workload(args):
                        "plain_ms": plain_s * 1e3, "plain_batched_ms": plain_b_s * 1e3,
                        "speedup_vs_batched_plain": plain_b_s / sur_s, "surrogate_ms": sur_s * 1e3,
                        "surrogate_mpoint_sectors_s": side * side * DIR_SECTORS / sur_s / 1e6,
+                       "plain_2000_mpoint_sectors_s": head_tput,
+                       "throughput_vs_plain_2000": side * side * DIR_SECTORS / sur_s / 1e6 / head_tput,
                        "plain_mpoint_sectors_s": len(tiles) * sur.TILE ** 2 * DIR_SECTORS / plain_s / 1e6,
                        "checked_tiles": len(stats["checked"]), "fell_back": len(stats["fell_back"]),
                        "tile_area_error_median": float(np.median(err)),

@@ -140,6 +140,23 @@ def test_convolutions_validate_arguments_before_launching(lib):
     assert wgrad(a, a, a, 1, 8, 8, 16, 12, s) == 1  # cout not a multiple of 8
     assert wgrad(a, a, odd, 1, 8, 8, 16, 16, s) == 1  # misaligned float32 gradient
     assert lib.ske_conv_status(None, s) == 1
+    head = lib.ske_conv3x3_head_bf16
+    assert head(a, a, None, a, a, a, 1, 8, 8, 16, 24, 1, s) == 1  # cout not a multiple of 16
+    assert head(a, a, None, None, a, a, 1, 8, 8, 16, 32, 1, s) == 1  # no head weights
+    assert head(a, a, None, a, None, a, 1, 8, 8, 16, 32, 1, s) == 1  # no head bias
+    assert head(a, a, None, a, a, C.c_void_p(0x10001), 1, 8, 8, 16, 32, 1, s) == 1  # misaligned output
+    pool = lib.ske_maxpool2_bf16
+    assert pool(a, a, 1, 7, 8, 16, s) == 1  # odd height
+    assert pool(a, a, 1, 8, 8, 12, s) == 1  # channels not a multiple of 8
+    assert pool(a, C.c_void_p(0x10008), 1, 8, 8, 16, s) == 1  # output not 16-byte aligned
+    enc = lib.ske_surrogate_encode_bf16
+    assert enc(a, a, a, a, 3, 16.0, a, 1, 256, s) == 1  # side not a multiple of the coarse factor
+    assert enc(a, a, a, a, 4, 0.0, a, 1, 256, s) == 1  # scale not positive
+    assert enc(a, None, a, a, 4, 16.0, a, 1, 256, s) == 1  # no means
+    # kernel choices: valid values are taken, others refused and the choice kept
+    assert lib.ske_conv_select(3) == 1 and lib.ske_conv_select(0) == 0
+    assert lib.ske_conv_stage_channels(24) == 1 and lib.ske_conv_stage_channels(0) == 0
+    assert lib.ske_skew_select(2) == 1 and lib.ske_skew_select(0) == 0
 
 
 def test_cli_usage_errors():
