@@ -88,6 +88,13 @@ typedef struct ske_params {
                                value sits at a bin edge (a measured, stated rate);
                                without the flag the cepstrum is the reference's,
                                bit for bit                                         */
+#define SKE_FLAG_LOCAL_RADON_F32 8 /* local Radon transform in float32 on the
+                               FP32 pipes (direct sums over the transform bins the
+                               reference reads); values differ in their last bits
+                               and, where two successive |Z|^2 nearly tie, the
+                               first ascent can fall on another bin (a measured,
+                               stated rate); without the flag it is the
+                               reference's binary64, bit for bit                   */
 
 /* Geometry of one sector, computeParams + skewShape (skewEngine.cuh:504-596). */
 typedef struct ske_sector_geometry {

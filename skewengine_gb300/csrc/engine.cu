@@ -51,6 +51,7 @@ int ensure_device_tables(int device) {
     if (g_tables_ready[device]) return SKE_OK;
     SKE_CK(sdem_init_tables());
     SKE_CK(cepstrum_f32_init_tables());
+    if (lradon_f32_init_tables() != 0) return fail(SKE_ERR_CUDA, "local Radon float32 tables");
     g_tables_ready[device] = 1;
     return SKE_OK;
 }
@@ -495,6 +496,10 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
         case SKE_KERNEL_LOCAL_RADON: {
             SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));
             LaunchScope ls(e, "local_radon", 1);
+            if (e->flags & SKE_FLAG_LOCAL_RADON_F32)
+                return ls.done(launch_local_radon_f32(e->dg, b, e->d_SI, e->d_SO, e->stride, e->geo.max_H,
+                                                      std::max(e->dimx, e->dimy), e->d_tw + e->lr_gauss_off,
+                                                      e->d_tw + e->lr_taper_off, e->stream));
             return ls.done(launch_local_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->geo.max_H,
                                               std::max(e->dimx, e->dimy), e->d_tw + e->lr_gauss_off,
                                               e->d_tw + e->lr_taper_off, e->d_tw + e->tw_off_host[6], e->stream));

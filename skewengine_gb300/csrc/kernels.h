@@ -236,6 +236,12 @@ cudaError_t launch_local_radon(const DevGeometry& g, const Batch& b, const float
 cudaError_t launch_cepstrum_f32(const BatchTables& t, int images, const DevGeometry& g, const TypeLists& tl, int dim,
                                 cudaStream_t st);
 cudaError_t cepstrum_f32_init_tables();
+// Local Radon in float32 (SKE_FLAG_LOCAL_RADON_F32, k_lradon_f32.cu): the
+// twiddle tables (once per device) and the launch (same grid as k_lradon).
+int lradon_f32_init_tables();
+cudaError_t launch_local_radon_f32(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
+                                   int max_H, int max_cols, const double* gauss, const double* taper,
+                                   cudaStream_t st);
 
 // Cepstrum blur estimation (k_cepstrum.cu).
 cudaError_t launch_cepstrum(const DevGeometry& g, const Batch& b, const float* SI, float* SO,

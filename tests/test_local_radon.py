@@ -47,3 +47,29 @@ def test_local_radon_angle_subset_and_name(gpu_lib, oracle):
     with ske.SkewEngine(64, 64) as eng:
         got = eng.run("localradon", x, povh=POVH, angles=angles)
     assert bits_equal(got, oracle.run_angles(5, x, angles, povh=POVH))
+
+
+# Stated float32-mode bound: share of output cells that differ from the
+# reference's binary64 result by more than 1e-3 relative.
+F32_MAX_OFF = 1e-3  # measured: 3.8e-6 at 512 x 512, 0 on the small grids
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("side,side_y,angles", [(512, 512, list(range(0, 180, 15)) + [44, 45, 46, 90]),
+                                                 (64, 48, None), (97, 80, [0, 33, 45, 90, 120, 179])])
+def test_local_radon_float32_mode_rate(gpu_lib, oracle, side, side_y, angles):
+    """SKE_FLAG_LOCAL_RADON_F32 against the binary64 operator (itself bit-equal
+    to the oracle): the rate of cells off by more than 1e-3 relative, printed
+    and bounded by F32_MAX_OFF; the rest agree to float32 rounding."""
+    import skewengine_gb300 as ske
+    x = np.ascontiguousarray(synthetic.ellipse_phantom(side, 21, side_y=side_y), np.float32)
+    with ske.SkewEngine(side, side_y) as eng:
+        exact = eng.run(ske.KERNEL_LOCAL_RADON, x, povh=POVH, angles=angles)
+        fast = eng.run(ske.KERNEL_LOCAL_RADON, x, povh=POVH, angles=angles, flags=ske.FLAG_LOCAL_RADON_F32)
+    want = oracle.run_ordered(5, x, angles, povh=POVH) if angles else oracle.run_ordered(5, x, povh=POVH)
+    assert bits_equal(exact, want)
+    rel = np.abs(fast.astype(np.float64) - exact) / np.maximum(np.abs(exact.astype(np.float64)), 1e-30)
+    off = float((rel > 1e-3).mean())
+    print(f"float32 local Radon {side}x{side_y}: {off:.2e} of cells off by > 1e-3 relative, "
+          f"median relative difference {np.median(rel):.1e}")
+    assert off <= F32_MAX_OFF, off
