@@ -211,6 +211,31 @@ __device__ __forceinline__ void tc_ld32(unsigned taddr, float* v) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// The same load without its wait (tc_ld32_wait completes it).
+__device__ __forceinline__ void tc_ld32_issue(unsigned taddr, unsigned* r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+}
+// Waits for this thread's tensor-memory loads; the registers of the last one
+// pass through the statement, so their uses stay after it.
+__device__ __forceinline__ void tc_ld32_wait(unsigned* r) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+}
+
 template <bool kUpCat>
 __global__ void __launch_bounds__(kThreads) k_conv3x3(const bf16* __restrict__ X, const bf16* __restrict__ Wt,
                                                       const float* __restrict__ bias, bf16* __restrict__ Y, int M,
@@ -823,6 +848,50 @@ __global__ void k_pack_weights(const bf16* __restrict__ Wt, bf16* __restrict__ W
     reinterpret_cast<uint4*>(Wp)[e] = v;
 }
 
+// One 32-column chunk q of a finished accumulator (block q / cpb, columns
+// 32 (q % cpb) ..): bias, ReLU, bfloat16; stored, or with a head folded into
+// hsum (in channel order) and written at the block's last chunk.
+__device__ __forceinline__ void ws_epi_chunk(int q, int cpb, const unsigned* r, int S0, int x0, int n, int64_t HW,
+                                             int warp, int lane, const WsGeom& g, const float* sbias,
+                                             const float* shead, bf16* __restrict__ Y, float* __restrict__ Yh,
+                                             float& hsum) {
+    const int j = q / cpb, c0 = (q - j * cpb) * 32;
+    const int s = S0 + j * kSlotBlock + warp * 32 + lane;  // this thread's slot (lane)
+    const int rr = s / g.P, c = s - rr * g.P;
+    const bool store = rr < g.H && c < g.Ws;
+    const int64_t pix = (int64_t)n * HW + (int64_t)rr * g.W + x0 + c;
+    if (c0 == 0) hsum = 0.0f;
+    if (store) {
+#pragma unroll
+        for (int e0 = 0; e0 < 32; e0 += 16) {
+            __nv_bfloat162 h[8];
+#pragma unroll
+            for (int e = 0; e < 16; e += 2) {
+                float o0 = __fadd_rn(__uint_as_float(r[e0 + e]), sbias[c0 + e0 + e]);
+                float o1 = __fadd_rn(__uint_as_float(r[e0 + e + 1]), sbias[c0 + e0 + e + 1]);
+                if (g.relu) {
+                    o0 = fmaxf(o0, 0.0f);
+                    o1 = fmaxf(o1, 0.0f);
+                }
+                h[e / 2] = __floats2bfloat162_rn(o0, o1);
+            }
+            if (Yh) {
+#pragma unroll
+                for (int e = 0; e < 16; e += 2) {
+                    const float2 f = __bfloat1622float2(h[e / 2]);
+                    hsum = __fmaf_rn(f.x, shead[c0 + e0 + e], hsum);
+                    hsum = __fmaf_rn(f.y, shead[c0 + e0 + e + 1], hsum);
+                }
+            } else {
+                uint4* d4 = reinterpret_cast<uint4*>(Y + pix * g.Cout + c0 + e0);
+                d4[0] = *reinterpret_cast<const uint4*>(&h[0]);
+                d4[1] = *reinterpret_cast<const uint4*>(&h[4]);
+            }
+        }
+        if (Yh && c0 + 32 == g.Cout) Yh[pix] = __fadd_rn(hsum, shead[256]);
+    }
+}
+
 template <bool kUpCat>
 __global__ void __launch_bounds__(kWsThreads, 1)
     k_conv3x3_ws(const bf16* __restrict__ X, const bf16* __restrict__ Wp, const float* __restrict__ bias,
@@ -996,6 +1065,26 @@ __global__ void __launch_bounds__(kWsThreads, 1)
             tc_fence_after();
             const int tile = t % g.tps, rest = t / g.tps, seg = rest % g.segs, n = rest / g.segs;
             const int x0 = seg * g.Ws, S0 = tile * tslots;
+            const unsigned tbase = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(b * 256);
+            if (g.Cout % 32 == 0) {
+                // Chunks of 32 columns, double-buffered: the next chunk's load is in
+                // flight while this one is converted and stored.
+                const int cpb = g.Cout / 32, nq = g.nb * cpb;
+                unsigned ra[32], rb[32];
+                float hsum = 0.0f;
+                tc_ld32_issue(tbase, ra);
+                tc_ld32_wait(ra);
+                for (int q = 0; q < nq; q += 2) {
+                    if (q + 1 < nq) tc_ld32_issue(tbase + (unsigned)((q + 1) / cpb * g.Cout + (q + 1) % cpb * 32), rb);
+                    ws_epi_chunk(q, cpb, ra, S0, x0, n, HW, warp, lane, g, sbias, shead, Y, Yh, hsum);
+                    tc_ld32_wait(rb);
+                    if (q + 1 < nq) {
+                        if (q + 2 < nq) tc_ld32_issue(tbase + (unsigned)((q + 2) / cpb * g.Cout + (q + 2) % cpb * 32), ra);
+                        ws_epi_chunk(q + 1, cpb, rb, S0, x0, n, HW, warp, lane, g, sbias, shead, Y, Yh, hsum);
+                        tc_ld32_wait(ra);
+                    }
+                }
+            } else
             for (int j = 0; j < g.nb; j++) {
                 const int s = S0 + j * kSlotBlock + warp * 32 + lane;  // this thread's slot (lane)
                 const int r = s / g.P, c = s - (s / g.P) * g.P;
