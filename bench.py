@@ -308,11 +308,12 @@ def secondary_workload(args):
             "roofline": {"bound": "fp64", "kernel": families[2], "achieved": ops / (op_ms / 1e3) / 1e12,
                          "peak": dfma.value / 1e12, "unit": "Tops/s (binary64 lane ops)",
                          "frac": ops / (op_ms / 1e3) / dfma.value, "work": work, "traffic": None}}
-    if args.workload == "localradon":
-        # The float32 mode (SKE_FLAG_LOCAL_RADON_F32): time, and the share of
-        # cells that differ from the binary64 result by more than 1e-3 relative.
+    if args.workload in ("localradon", "radon"):
+        # The float32 mode (SKE_FLAG_LOCAL_RADON_F32 / SKE_FLAG_RADON_F32): time,
+        # the share of cells that differ from the binary64 result by more than
+        # 1e-3 relative, and the largest difference over the output's magnitude.
         exact = out_dev.clone()
-        f32 = ske.FLAG_LOCAL_RADON_F32
+        f32 = ske.FLAG_LOCAL_RADON_F32 if args.workload == "localradon" else ske.FLAG_RADON_F32
         out32 = torch.empty_like(x_dev)
         for _ in range(args.warmup):
             eng.run(kernel, x_dev, out32, flags=f32)
@@ -327,7 +328,8 @@ def secondary_workload(args):
         line["config"]["float32_mode"] = {
             "images_per_s": 1e3 / ms32, "ms_per_step": ms32,
             "cells_off_by_more_than_1e-3_relative": float((rel > 1e-3).float().mean()),
-            "median_relative_difference": float(rel.median())}
+            "median_relative_difference": float(rel.median()),
+            "max_difference_over_max_output": float((out32 - exact).abs().max() / exact.abs().max())}
     if not args.no_cpu_baseline:
         fp = np.ctypeslib.ndpointer(np.float32, flags="C")
         ip = np.ctypeslib.ndpointer(np.int32, flags="C")

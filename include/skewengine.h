@@ -88,6 +88,12 @@ typedef struct ske_params {
                                value sits at a bin edge (a measured, stated rate);
                                without the flag the cepstrum is the reference's,
                                bit for bit                                         */
+#define SKE_FLAG_RADON_F32 16 /* Radon ray sums, transform and ramp filter in
+                               float32 on the FP32 pipes (sectors up to 8192
+                               rows); values differ from the reference's binary64
+                               in their low bits (a measured, stated error);
+                               without the flag the operator is the reference's,
+                               bit for bit                                         */
 #define SKE_FLAG_LOCAL_RADON_F32 8 /* local Radon transform in float32 on the
                                FP32 pipes (direct sums over the transform bins the
                                reference reads); values differ in their last bits

@@ -6,7 +6,7 @@ local Radon transform, cepstrum blur estimation, identity), deskews the result a
 compute runs as hand-written sm_103a CUDA kernels behind the C ABI in
 ``include/skewengine.h``; this package is its Python host interface.
 """
-from .engine import (ACCUM_KAHAN, ACCUM_REFERENCE, DEFAULT_POVH, FLAG_CEPSTRUM_F32, FLAG_LOCAL_RADON_F32, FLAG_NO_GRAPH, FLAG_NO_TUNE, KERNEL_CEPSTRUM,
+from .engine import (ACCUM_KAHAN, ACCUM_REFERENCE, DEFAULT_POVH, FLAG_CEPSTRUM_F32, FLAG_LOCAL_RADON_F32, FLAG_NO_GRAPH, FLAG_RADON_F32, FLAG_NO_TUNE, KERNEL_CEPSTRUM,
                      KERNEL_IDENTITYDEM,
                      KERNEL_IDENTITYIMG, KERNEL_LOCAL_RADON, KERNEL_RADON, KERNEL_SDEM, KERNELS, SkewEngine,
                      cli_run, device_count, execute, geometry, params, png_size, read_image, read_png_rgba,
@@ -18,4 +18,4 @@ __all__ = ["SkewEngine", "SkeError", "execute", "run_batch", "geometry", "params
            "KERNEL_SDEM", "KERNEL_IDENTITYDEM", "KERNEL_RADON", "KERNEL_IDENTITYIMG", "KERNEL_CEPSTRUM",
            "KERNEL_LOCAL_RADON",
            "KERNELS", "ACCUM_REFERENCE", "ACCUM_KAHAN", "DEFAULT_POVH", "FLAG_NO_TUNE", "FLAG_NO_GRAPH", "FLAG_CEPSTRUM_F32",
-           "FLAG_LOCAL_RADON_F32"]
+           "FLAG_LOCAL_RADON_F32", "FLAG_RADON_F32"]

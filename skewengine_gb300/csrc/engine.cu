@@ -488,10 +488,11 @@ int run_operator(ske_engine e, int kernel, const Batch& b, float povh, int count
             return ls.done(launch_sdem(a, e->num_sms, e->stream));
         }
         case SKE_KERNEL_RADON: {
-            LaunchScope ls(e, "radon", radon_launches(rows_only, e->max_H2));
+            const bool f32 = (e->flags & SKE_FLAG_RADON_F32) != 0;
+            LaunchScope ls(e, "radon", radon_launches(rows_only, e->max_H2, f32));
             return ls.done(launch_radon(e->dg, b, e->d_SI, e->d_SO, e->stride, e->len, e->d_P, e->pstride, e->d_tw,
                                         e->d_tw_off, e->max_H2, e->stream, !rows_only,
-                                        rows_only ? e->d_orient : nullptr, e->N));
+                                        rows_only ? e->d_orient : nullptr, e->N, f32));
         }
         case SKE_KERNEL_LOCAL_RADON: {
             SKE_CK(cudaMemsetAsync(e->d_SO, 0, sizeof(float) * e->stride * b.count, e->stream));

@@ -324,6 +324,98 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kTransfor
     for (int i = threadIdx.x; i < H; i += blockDim.x) p[i].re = __dmul_rn(xs[i].re, inv);
 }
 
+// ---- float32 mode (SKE_FLAG_RADON_F32) -------------------------------------
+// The same operator on the FP32 pipes: row sums in float (a warp per row,
+// lanes over columns, a shuffle tree), the radix-2 DIF transform, ramp filter
+// and inverse transform in float in shared memory (twiddles rounded from the
+// binary64 table), the filtered row values written to P as doubles for the
+// deskew or back-projection.  Values differ from the reference's binary64 in
+// their low bits (the sums' order and float rounding); the relative error of
+// the output is measured and stated (tests/test_gpu_parity.py).
+template <bool kGather>
+__global__ void __launch_bounds__(kSumWarps * 32)
+    k_radon_sums_f32(DevGeometry g, Batch b, const float* __restrict__ SI, int64_t stride,
+                     const float* __restrict__ orient, int64_t n_cells, cd* __restrict__ P, int64_t pstride) {
+    const int lane = threadIdx.x & 31;
+    const int slot = blockIdx.y;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const int H2 = pow2_at_least(d.H);
+    const float* in = SI + slot * stride;
+    const float* src = orient + (int64_t)d.type * n_cells;
+    const int32_t* tgt = g.target + d.col_off;
+    const float* wgt = g.weight + d.col_off;
+    cd* p = P + slot * pstride;
+    const int nwarps = gridDim.x * kSumWarps;
+    for (int r = blockIdx.x * kSumWarps + (threadIdx.x >> 5); r < H2; r += nwarps) {
+        if (r >= d.H) {
+            if (lane == 0) p[r] = {0.0, 0.0};
+            continue;
+        }
+        const int f = g.first[d.row_off + r], l = g.last[d.row_off + r];
+        const float* row = in + (int64_t)r * d.dim_i;
+        float acc = 0.0f;
+        for (int j = f + lane; j < l; j += 32) acc += kGather ? skew_gather(d, tgt, wgt, src, r, j) : row[j];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) p[r] = {(double)acc, 0.0};
+    }
+}
+
+__device__ void cta_fft_f32(float2* x, int n, const double* __restrict__ tw) {
+    for (int h = n >> 1; h >= 1; h >>= 1) {
+        const double* t = tw + 2 * (size_t)(n - 2 * h);
+        for (int k = threadIdx.x; k < (n >> 1); k += blockDim.x) {
+            const int l = k & (h - 1);
+            const int a = ((k - l) << 1) + l;
+            const int bb = a + h;
+            const float2 xa = x[a], xb = x[bb];
+            const float dr = xa.x - xb.x, di = xa.y - xb.y;
+            const float c = (float)t[2 * l], sn = (float)t[2 * l + 1];
+            x[a] = make_float2(xa.x + xb.x, xa.y + xb.y);
+            x[bb] = make_float2(dr * c - di * sn, dr * sn + di * c);
+        }
+        __syncthreads();
+    }
+    const unsigned bits = 31 - __clz(n);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int j = (int)bitrev((unsigned)i, bits);
+        if (j > i) {
+            const float2 tmp = x[i];
+            x[i] = x[j];
+            x[j] = tmp;
+        }
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTransformThreads)
+    k_radon_transform_f32(DevGeometry g, Batch b, cd* __restrict__ P, int64_t pstride,
+                          const double* __restrict__ twiddles, const int64_t* __restrict__ tw_off) {
+    extern __shared__ float2 xf[];
+    const int slot = blockIdx.x;
+    const SectorDesc d = g.desc[b.angle[slot]];
+    const int H = d.H;
+    const int H2 = pow2_at_least(H);
+    cd* p = P + slot * pstride;
+    const double* tw = twiddles + tw_off[31 - __clz(H2)];
+    for (int i = threadIdx.x; i < H2; i += blockDim.x) xf[i] = make_float2((float)p[i].re, 0.0f);
+    __syncthreads();
+    cta_fft_f32(xf, H2, tw);
+    for (int i = threadIdx.x; i < H2; i += blockDim.x) {  // ramp filter, then the conjugation
+        float2 v = xf[i];
+        if (i > H / 2) {
+            v = make_float2(0.0f, 0.0f);
+        } else {
+            const float sc = __fdiv_rn((float)i, (float)H);
+            v = make_float2(v.x * sc, v.y * sc);
+        }
+        xf[i] = make_float2(v.x, -v.y);
+    }
+    __syncthreads();
+    cta_fft_f32(xf, H2, tw);
+    const float inv = 1.0f / (float)H2;
+    for (int i = threadIdx.x; i < H; i += blockDim.x) p[i].re = (double)(xf[i].x * inv);
+}
+
 __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict__ P, int64_t pstride,
                                     float* __restrict__ SO, int64_t stride, int64_t len) {
     const int slot = blockIdx.y;
@@ -353,7 +445,8 @@ __global__ void k_radon_backproject(DevGeometry g, Batch b, const cd* __restrict
 // transform as two launches, measured faster (radon_select).
 int g_radon_path = 1;
 
-int radon_launches(bool rows_only, int max_H2) {
+int radon_launches(bool rows_only, int max_H2, bool f32) {
+    if (f32 && max_H2 <= kSmemH2) return rows_only ? 2 : 3;
     return rows_only ? (max_H2 <= kSmemH2 && g_radon_path == 0 ? 1 : 2) : 3;
 }
 
@@ -365,9 +458,31 @@ int radon_select(int path) {
 
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO, int64_t stride,
                          int64_t len, double* P, int64_t pstride, const double* twiddles, const int64_t* tw_off,
-                         int max_H2, cudaStream_t st, bool backproject, const float* orient, int64_t n_cells) {
+                         int max_H2, cudaStream_t st, bool backproject, const float* orient, int64_t n_cells,
+                         bool f32) {
     if (orient && backproject) return cudaErrorInvalidValue;  // the gathered cells are not kept for SO
     cd* Pc = reinterpret_cast<cd*>(P);
+    if (f32 && max_H2 <= kSmemH2) {
+        dim3 g1((max_H2 + kSumWarps - 1) / kSumWarps, b.count);
+        if (orient)
+            k_radon_sums_f32<true><<<g1, kSumWarps * 32, 0, st>>>(g, b, SI, stride, orient, n_cells, Pc, pstride);
+        else
+            k_radon_sums_f32<false><<<g1, kSumWarps * 32, 0, st>>>(g, b, SI, stride, orient, n_cells, Pc, pstride);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        const int smem = max_H2 * (int)sizeof(float2);
+        if (smem > 48 * 1024) {
+            e = cudaFuncSetAttribute(k_radon_transform_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+        }
+        k_radon_transform_f32<<<b.count, kTransformThreads, smem, st>>>(g, b, Pc, pstride, twiddles, tw_off);
+        e = cudaGetLastError();
+        if (e != cudaSuccess || !backproject) return e;
+        int64_t blocks = (len + 255) / 256;
+        if (blocks > 4096) blocks = 4096;
+        k_radon_backproject<<<dim3((unsigned)blocks, b.count), 256, 0, st>>>(g, b, Pc, pstride, SO, stride, len);
+        return cudaGetLastError();
+    }
     if (orient && max_H2 <= kSmemH2 && g_radon_path == 0) {  // one fused launch: a cluster per sector
         const int smem = max_H2 * (int)sizeof(cd);
         cudaError_t e = cudaSuccess;

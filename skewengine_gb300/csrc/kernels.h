@@ -215,10 +215,11 @@ int sdem_chunk();
 cudaError_t launch_radon(const DevGeometry& g, const Batch& b, const float* SI, float* SO,
                          int64_t stride, int64_t len, double* P, int64_t pstride, const double* twiddles,
                          const int64_t* tw_off, int max_H2, cudaStream_t st, bool backproject = true,
-                         const float* orient = nullptr, int64_t n_cells = 0);
+                         const float* orient = nullptr, int64_t n_cells = 0, bool f32 = false);
 
-// Kernel launches launch_radon makes (rows_only: gathered sums, no back-projection).
-int radon_launches(bool rows_only, int max_H2);
+// Kernel launches launch_radon makes (rows_only: gathered sums, no back-projection;
+// f32: the float32 mode).
+int radon_launches(bool rows_only, int max_H2, bool f32 = false);
 // Radon path for later launches: 0 = fused sector kernel where it applies, 1 =
 // separate sums and transform; -1 for another value.
 int radon_select(int path);

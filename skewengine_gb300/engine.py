@@ -71,6 +71,7 @@ FLAG_NO_TUNE = 1   # keep the sweep's built-in shape (skip the autotuner)
 FLAG_NO_GRAPH = 2  # batched runs: plain launches, no captured CUDA graph
 FLAG_CEPSTRUM_F32 = 4  # cepstrum in float32, fused sector loop (stated bin-mismatch rate)
 FLAG_LOCAL_RADON_F32 = 8  # local Radon transform in float32 (stated mismatch rate)
+FLAG_RADON_F32 = 16  # Radon ray sums and filter in float32 (stated error)
 
 
 def params(max_sector: int = 180, povh: float = DEFAULT_POVH, accum="reference", flags: int = 0) -> Params:

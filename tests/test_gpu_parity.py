@@ -437,3 +437,26 @@ def test_staged_skew_matches_oracle(ske, oracle, side, side_y):
         lib.ske_skew_select(0)
     want = oracle.run_ordered(0, x, angles, povh=synthetic.POVH)
     assert bits_equal(got, want)
+
+
+# Stated float32 Radon bound: max |float32 - binary64| over max |binary64|.
+RADON_F32_MAX_REL = 1e-5  # measured: 1.2e-6 at 512 x 512, 3-5e-7 on the small grids
+
+
+@pytest.mark.parametrize("side,side_y,angles", [(512, 512, list(range(0, 180, 10)) + [45, 90, 135]),
+                                                 (128, 80, None), (97, 131, [0, 20, 45, 60, 90, 150])])
+def test_radon_float32_mode_error(ske, oracle, side, side_y, angles):
+    """SKE_FLAG_RADON_F32 against the binary64 operator (itself bit-equal to the
+    oracle): square grids take the gathered-sums path, the non-square ones the
+    back-projection path.  The error relative to the output's magnitude is
+    printed and bounded by RADON_F32_MAX_REL."""
+    x = np.ascontiguousarray(synthetic.ellipse_phantom(side, 31, side_y=side_y), np.float32)
+    with ske.SkewEngine(side, side_y) as eng:
+        exact = eng.run(ske.KERNEL_RADON, x, povh=POVH, angles=angles)
+        fast = eng.run(ske.KERNEL_RADON, x, povh=POVH, angles=angles, flags=ske.FLAG_RADON_F32)
+    op = ske.KERNEL_RADON
+    want = oracle.run_ordered(op, x, angles, povh=POVH) if angles else oracle.run_ordered(op, x, povh=POVH)
+    assert bits_equal(exact, want)
+    err = float(np.abs(fast.astype(np.float64) - exact).max() / max(np.abs(exact).max(), 1e-30))
+    print(f"float32 Radon {side}x{side_y}: max error {err:.1e} of the output's magnitude")
+    assert err <= RADON_F32_MAX_REL, err
