@@ -1658,6 +1658,7 @@ int ske_sweep_shape(ske_engine e, int* lvl0, int* lvl1, int* ctas_per_sm) {
 int ske_prepare(ske_engine e, const float* input, int on_device) {
     if (!e || !input) return fail(SKE_ERR_INVALID, "null argument");
     SKE_TRY(set_device(e));
+    e->flags = 0;  // the per-sector calls take no parameters: the reference's operators, no modes
     return run_prepare(e, input, on_device);
 }
 
