@@ -16,9 +16,9 @@
 // twiddles (cosines and sines of 2 pi (k m mod 64) / 64, rounded to float on
 // the host) sit in shared memory as one row per m, read by every thread at the
 // same address (broadcast, 16 bytes per load), with the 26 bins unrolled in
-// registers.  One thread per cell; a CTA of 256 threads owns a 32 x 32 tile of
-// cells, stages the skewed rows it needs (95 rows x 96 columns) and forms each
-// W once.
+// registers.  Two cells per thread (a twiddle row serves both); a CTA of 256
+// threads owns a 32 x 32 tile of cells, stages the skewed rows it needs (95
+// rows x 96 columns) and forms each W once.
 // The order of the float32 sums differs from the reference's binary64 FFT, so
 // values differ in their last bits, and where two successive |Z|^2 nearly tie
 // the first ascent can fall on another bin: the rate of output cells that
@@ -104,18 +104,31 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
 
+    // Two cells per thread, rows ci and ci + kTI/2 of the tile: every twiddle
+    // row and window weight read from shared memory serves both.
     float* out = SO + slot * stride;
-    for (int ci = warp; ci < kTI; ci += kThreads / 32) {
-        const int cj = lane, i = i0 + ci, j = j0 + cj;
-        if (i >= d.H || j < first[i] || j >= last[i]) continue;
-        const int64_t p = (int64_t)i * d.dim_i + j;
-        if (j >= d.dim_i && owner_row(d, first, last, p) != i) continue;
-        float re[kKeep];
+    for (int ca = warp; ca < kTI / 2; ca += kThreads / 32) {
+        const int cj = lane, j = j0 + cj;
+        int64_t p[2];
+        bool valid[2];
 #pragma unroll
-        for (int k = 0; k < kKeep; k++) re[k] = 0.0f;
+        for (int u = 0; u < 2; u++) {
+            const int i = i0 + ca + u * (kTI / 2);
+            valid[u] = i < d.H && j >= first[i] && j < last[i];
+            p[u] = (int64_t)i * d.dim_i + j;
+            if (valid[u] && j >= d.dim_i && owner_row(d, first, last, p[u]) != i) valid[u] = false;
+        }
+        if (!valid[0] && !valid[1]) continue;
+        float re[2][kKeep];
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+            for (int k = 0; k < kKeep; k++) re[u][k] = 0.0f;
 #pragma unroll 2
         for (int m = 0; m < kW; m++) {
-            const float x = __fmul_rn(sm.w[ci + m][cj], sm.gauss[m]);
+            const float gm = sm.gauss[m];
+            const float x0 = __fmul_rn(sm.w[ca + m][cj], gm);
+            const float x1 = __fmul_rn(sm.w[ca + kTI / 2 + m][cj], gm);
             const float4* t4 = reinterpret_cast<const float4*>(sm.tx[m]);
 #pragma unroll
             for (int q = 0; q < kKP / 4; q++) {
@@ -123,16 +136,21 @@ __global__ void __launch_bounds__(kThreads)
                 const float tv[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
                 for (int e = 0; e < 4; e++)
-                    if (4 * q + e < kKeep) re[4 * q + e] = __fmaf_rn(x, tv[e], re[4 * q + e]);
+                    if (4 * q + e < kKeep) {
+                        re[0][4 * q + e] = __fmaf_rn(x0, tv[e], re[0][4 * q + e]);
+                        re[1][4 * q + e] = __fmaf_rn(x1, tv[e], re[1][4 * q + e]);
+                    }
             }
         }
 #pragma unroll
-        for (int k = 0; k < kKeep; k++) re[k] = __fmul_rn(sm.taper[k], __fmul_rn(re[k], 0.125f));
-        float prev = 0.0f, found = 0.0f;
-        bool done = false;
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+            for (int k = 0; k < kKeep; k++) re[u][k] = __fmul_rn(sm.taper[k], __fmul_rn(re[u][k], 0.125f));
+        float prev[2] = {0.0f, 0.0f}, found[2] = {0.0f, 0.0f};
+        bool done[2] = {false, false};
 #pragma unroll 2
         for (int m = kZ0; m < kZ1; m++) {
-            float zr = 0.0f, zi = 0.0f;
+            float zr[2] = {0.0f, 0.0f}, zi[2] = {0.0f, 0.0f};
             const float4* tc4 = reinterpret_cast<const float4*>(sm.tzc[m - kZ0]);
             const float4* ts4 = reinterpret_cast<const float4*>(sm.tzs[m - kZ0]);
 #pragma unroll
@@ -142,20 +160,27 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
                 for (int e = 0; e < 4; e++)
                     if (4 * q + e < kKeep) {
-                        zr = __fmaf_rn(re[4 * q + e], cv[e], zr);
-                        zi = __fmaf_rn(re[4 * q + e], sv[e], zi);
+#pragma unroll
+                        for (int u = 0; u < 2; u++) {
+                            zr[u] = __fmaf_rn(re[u][4 * q + e], cv[e], zr[u]);
+                            zi[u] = __fmaf_rn(re[u][4 * q + e], sv[e], zi[u]);
+                        }
                     }
             }
-            zr = __fmul_rn(zr, 0.125f);
-            zi = __fmul_rn(zi, 0.125f);
-            const float nm = __fadd_rn(__fmul_rn(zr, zr), __fmul_rn(zi, zi));
-            if (m > kZ0 && !done && nm > prev) {
-                found = prev;
-                done = true;
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const float a = __fmul_rn(zr[u], 0.125f), bq = __fmul_rn(zi[u], 0.125f);
+                const float nm = __fadd_rn(__fmul_rn(a, a), __fmul_rn(bq, bq));
+                if (m > kZ0 && !done[u] && nm > prev[u]) {
+                    found[u] = prev[u];
+                    done[u] = true;
+                }
+                prev[u] = nm;
             }
-            prev = nm;
         }
-        out[p] = found;
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+            if (valid[u]) out[p[u]] = found[u];
     }
 }
 
