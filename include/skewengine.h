@@ -480,6 +480,14 @@ int ske_conv_select(int path);
  * knob; no reference counterpart. */
 int ske_conv_stage_channels(int channels);
 
+/* Weight-gradient kernel for later calls of ske_conv3x3_wgrad_bf16: 1 (default)
+ * = ldmatrix + mma.sync; 0 = tcgen05 (dY and X staged once per tile as
+ * 8-channel planes and read in place as MN-major operands, the 9 taps'
+ * accumulators in tensor memory, float32 atomics into dw), measured slower on
+ * the surrogate's layers except the widest.  Same sums in other orders.  No
+ * reference counterpart. */
+int ske_conv_wgrad_select(int path);
+
 /* Synchronises `stream`, then sets *failed to 1 if a forward convolution since
  * the previous call gave up waiting for its tensor-core operations (its output
  * is then not written), else 0, and clears the flag. */

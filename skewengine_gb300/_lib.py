@@ -98,6 +98,7 @@ SIGNATURES = [
                                          C.c_int, C.c_void_p]),
     ("ske_conv_select", C.c_int, [C.c_int]),
     ("ske_conv_stage_channels", C.c_int, [C.c_int]),
+    ("ske_conv_wgrad_select", C.c_int, [C.c_int]),
     ("ske_conv3x3_head_bf16", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("ske_maxpool2_bf16", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),

@@ -1228,6 +1228,212 @@ int launch_conv_ws(const WsGeom& g, const bf16* x, const bf16* w, const float* b
     return e == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
 }
 
+// ---- weight gradient on the tensor cores (tcgen05) ---------------------------
+//
+// dW[co][tap*Cin + ci] = sum over output pixels p of dY[p][co] * X[p + off(tap)][ci].
+// The output pixels of a column segment (kWgSeg wide where the width allows)
+// are numbered as slots of rows of pitch P = Ws + 2 as in the halo-staged
+// forward kernel; a tile is kWgSlots consecutive slots.  Per tile the CTA
+// stages dY as 8-channel planes of the tile's slots (zero for the junk slots
+// and outside the image) and X as 8-channel halo planes (the rows the tile
+// touches, one column on each side, zero outside), and issues for each tap and
+// each K step of 16 slots one MMA
+//   D_tap (M = 128 output channels, N = 16 or 32 input channels) += dY^T X_tap
+// with both operands read in place as MN-major matrices: a core matrix is 8
+// consecutive slots of one plane (128 contiguous bytes), 8 channels along M or
+// N by 8 slots along K.  Without swizzling the leading byte offset steps along
+// K and the stride byte offset along M or N whatever the major-ness, so here
+// the leading byte offset is 128 (the next 8 slots) and the stride byte offset
+// one plane (the next 8 channels) -- the forward kernel's K-major operands have
+// the same two offsets the other way round.  X_tap starts at plane slot
+// k*16 + soff + ky*P + kx, the tap's shift.
+// The 9 taps' accumulators sit side by side in tensor memory (9 N columns
+// each) and sum over all the tiles of the CTA's chunk; the epilogue adds them
+// to dW with float32 atomics (warp w: output channels 32w..32w+31 of the CTA's
+// block of 128).  dY planes past Cout stay zero (zeroed once).  All threads
+// stage a tile with cp.async into a ring of kWgStages stages; thread 0 issues
+// its MMAs and commits them to the stage's mbarrier.  Waits are bounded as in
+// k_conv3x3; a give-up skips the rest, drains the last commit, frees the tensor
+// memory and sets g_conv_status.
+constexpr int kWgSeg = 32;
+constexpr int kWgSlots = 128;
+constexpr int kWgStages = 3;
+constexpr int kWgPlanesA = 16;  // 128 output channels
+
+struct WgGeom {
+    int H, W, Cin, Cout, Kpad;
+    int Ws, P, segs, tps, hslots, total, chunk;
+    int nblk;                  // N: input channels per CTA (16 or 32)
+    int planeA, planeB, sbytes;  // bytes
+};
+
+__host__ __device__ constexpr int wg_seg(int W) { return (W > kWgSeg && W % kWgSeg == 0) ? kWgSeg : W; }
+
+// Instruction descriptor of the weight-gradient MMA: as tc_idesc, with A and B
+// MN-major (bits 15 and 16).
+__host__ __device__ constexpr uint32_t wg_idesc(int n) { return tc_idesc(n) | (1u << 15) | (1u << 16); }
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_conv3x3_wgrad_tc(const bf16* __restrict__ X, const bf16* __restrict__ dY, float* __restrict__ dW,
+                       const WgGeom g) {
+    extern __shared__ __align__(128) unsigned char wg_raw[];
+    unsigned char* sm = wg_raw + ((128 - (smem_u32(wg_raw) & 127)) & 127);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kWgStages * g.sbytes);
+    unsigned* tslot = reinterpret_cast<unsigned*>(bar + kWgStages);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ci0 = blockIdx.x * g.nblk, co0 = blockIdx.y * 128;
+    const int t0 = blockIdx.z * g.chunk, t1 = min(t0 + g.chunk, g.total);
+    if (t0 >= t1) return;  // uniform over the block
+    const int coPl = min(kWgPlanesA, (g.Cout - co0 + 7) / 8);  // dY planes with output channels
+    const int xPl = g.nblk / 8;
+    for (int s = 0; s < kWgStages; s++) {
+        uint4* a = reinterpret_cast<uint4*>(sm + s * g.sbytes);
+        for (int q = tid; q < kWgPlanesA * g.planeA / 16; q += kThreads) a[q] = make_uint4(0, 0, 0, 0);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(tslot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kWgStages; s++) tc_mbar_init(&bar[s]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tmem = *tslot;
+    const int64_t HW = (int64_t)g.H * g.W;
+
+    auto load = [&](int st, int t) {
+        unsigned char* base = sm + st * g.sbytes;
+        const int tile = t % g.tps, rest = t / g.tps, seg = rest % g.segs, n = rest / g.segs;
+        const int x0 = seg * g.Ws, S0 = tile * kWgSlots, R0 = S0 / g.P;
+        for (int q = tid; q < coPl * kWgSlots; q += kThreads) {
+            const int pl = q / kWgSlots, sl = q - pl * kWgSlots;
+            const int s = S0 + sl, r = s / g.P, c = s - r * g.P;
+            const bool ok = r < g.H && c < g.Ws && co0 + 8 * pl < g.Cout;
+            const bf16* src = ok ? dY + ((int64_t)n * HW + (int64_t)r * g.W + x0 + c) * g.Cout + co0 + 8 * pl : dY;
+            cp_async16(base + pl * g.planeA + sl * 16, src, ok ? 16 : 0);
+        }
+        unsigned char* xb = base + kWgPlanesA * g.planeA;
+        for (int q = tid; q < xPl * g.hslots; q += kThreads) {
+            const int pl = q / g.hslots, p = q - pl * g.hslots;
+            const int hr = p / g.P, iy = R0 - 1 + hr, ix = x0 - 1 + (p - hr * g.P);
+            const int ci = ci0 + 8 * pl;
+            const bool ok = iy >= 0 && iy < g.H && ix >= 0 && ix < g.W && ci < g.Cin;
+            const bf16* src = ok ? X + ((int64_t)n * HW + (int64_t)iy * g.W + ix) * g.Cin + ci : X;
+            cp_async16(xb + pl * g.planeB + p * 16, src, ok ? 16 : 0);
+        }
+    };
+
+    const uint32_t idesc = wg_idesc(g.nblk);
+    const int nt = t1 - t0;
+    for (int s = 0; s < kWgStages - 1; s++) {
+        if (s < nt) load(s, t0 + s);
+        cp_commit();
+    }
+    bool fail = false;
+    int last_commit = -1;
+    for (int i = 0; i < nt; i++) {
+        const int nxt = i + kWgStages - 1;
+        if (nxt < nt) {
+            const int st = nxt % kWgStages, prev = nxt - kWgStages;
+            if (prev >= 0 && !fail) fail = !tc_mbar_wait(&bar[st], (prev / kWgStages) & 1);
+            if (!fail) load(st, t0 + nxt);
+        }
+        cp_commit();
+        cp_wait<kWgStages - 1>();
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if (__syncthreads_or(fail)) {
+            fail = true;
+            break;
+        }
+        if (tid == 0) {
+            tc_fence_after();
+            const int st = i % kWgStages;
+            const int S0 = ((t0 + i) % g.tps) * kWgSlots, soff = S0 - (S0 / g.P) * g.P;
+            const unsigned ab = smem_u32(sm + st * g.sbytes), xb = ab + kWgPlanesA * g.planeA;
+            const uint64_t da0 = tc_desc2(ab, 128, (unsigned)g.planeA);
+            const uint64_t db0 = tc_desc2(xb, 128, (unsigned)g.planeB);
+#pragma unroll 1
+            for (int tap = 0; tap < 9; tap++) {
+                const int ky = tap / 3, kx = tap - 3 * (tap / 3);
+#pragma unroll
+                for (int k = 0; k < kWgSlots / 16; k++) {
+                    // start addresses advance in 16-byte units in the descriptors' low field
+                    const uint64_t da = da0 + (uint64_t)(k * 16);
+                    const uint64_t db = db0 + (uint64_t)(k * 16 + soff + ky * g.P + kx);
+                    tc_mma(tmem + (unsigned)(tap * g.nblk), da, db, idesc, (i | k) != 0);
+                }
+            }
+            tc_commit(&bar[st]);
+            last_commit = i;
+        }
+    }
+    cp_wait<0>();
+    if (tid == 0 && last_commit >= 0 && !tc_mbar_wait(&bar[last_commit % kWgStages], (last_commit / kWgStages) & 1))
+        fail = true;
+    fail = __syncthreads_or(fail);
+    tc_fence_after();
+    if (!fail) {
+        const int co = co0 + warp * 32 + lane;
+        for (int tap = 0; tap < 9; tap++)
+            for (int c0 = 0; c0 < g.nblk; c0 += 16) {
+                float v[16];
+                tc_ld16(tmem + ((unsigned)(warp * 32) << 16) + (unsigned)(tap * g.nblk + c0), v);
+                if (co >= g.Cout) continue;
+                float* dst = dW + (int64_t)co * g.Kpad + tap * g.Cin + ci0 + c0;
+#pragma unroll
+                for (int e = 0; e < 16; e++)
+                    if (ci0 + c0 + e < g.Cin) atomicAdd(dst + e, v[e]);
+            }
+    } else if (tid == 0) {
+        atomicExch(&g_conv_status, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+    }
+}
+
+// The tensor-core weight gradient for Cout >= 8 (multiple of 8), Cin a
+// multiple of 8; false where it does not apply.
+bool wg_geometry(WgGeom* g, int n, int h, int w_, int cin, int cout, int sms) {
+    g->H = h;
+    g->W = w_;
+    g->Cin = cin;
+    g->Cout = cout;
+    g->Kpad = (9 * cin + kTcBK - 1) / kTcBK * kTcBK;
+    g->Ws = wg_seg(w_);
+    g->P = g->Ws + 2;
+    g->segs = w_ / g->Ws;
+    g->nblk = cin <= 16 ? 16 : 32;
+    g->hslots = 3 * g->P + kWgSlots + 1;
+    g->planeA = kWgSlots * 16;
+    g->planeB = (g->hslots * 16 + 127) / 128 * 128;
+    g->sbytes = kWgPlanesA * g->planeA + (g->nblk / 8) * g->planeB;
+    if (kWgStages * g->sbytes + 256 > 227 * 1024) return false;
+    const int64_t slots = (int64_t)h * g->P;
+    const int64_t tps = (slots + kWgSlots - 1) / kWgSlots;
+    const int64_t total = (int64_t)n * g->segs * tps;
+    if (total > 0x7fffffff || slots + 4 * g->P > 0x7fffffff / 2) return false;
+    g->tps = (int)tps;
+    g->total = (int)total;
+    const int blocks = ((cin + g->nblk - 1) / g->nblk) * ((cout + 127) / 128);
+    const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>(total, (int64_t)2 * sms / std::max(blocks, 1)));
+    g->chunk = (int)((total + chunks - 1) / chunks);
+    return true;
+}
+
+// Weight-gradient kernel (ske_conv_wgrad_select): 0 = tcgen05 where it applies,
+// 1 (default) = mma.sync, which measured faster for the surrogate's layers
+// (3.22 against 3.75 ms for the 14 layers at batch 16; tcgen05 faster only on
+// the 384-channel decoder input).
+int g_wgrad_path = 1;
+
 template <bool kUpCat>
 int launch_conv_tc(const bf16* x, const bf16* w, const float* bias, bf16* y, int64_t m, int h, int w_, int cin,
                    int cout, int relu, const bf16* x2, int c1, cudaStream_t st) {
@@ -1378,6 +1584,12 @@ extern "C" int ske_conv_select(int path) {
     return SKE_OK;
 }
 
+extern "C" int ske_conv_wgrad_select(int path) {
+    if (path != 0 && path != 1) return SKE_ERR_INVALID;
+    g_wgrad_path = path;
+    return SKE_OK;
+}
+
 extern "C" int ske_conv_stage_channels(int channels) {
     if (channels != 0 && channels != 16 && channels != 32 && channels != 64) return SKE_ERR_INVALID;
     g_ws_stage = channels;
@@ -1405,6 +1617,19 @@ extern "C" int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, 
     const int64_t m = (int64_t)n * h * w_;
     if (m > 0x7fffffff / 2) return SKE_ERR_INVALID;
     const int kpad = (9 * cin + kBK - 1) / kBK * kBK;
+    int dev = 0, sms = 0;
+    WgGeom wg;
+    if (g_wgrad_path == 0 && cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && sms > 0 &&
+        wg_geometry(&wg, n, h, w_, cin, cout, sms)) {
+        const int smem = std::max(kWsMinSmem, kWgStages * wg.sbytes + 256);
+        if (cudaFuncSetAttribute(k_conv3x3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            return SKE_ERR_CUDA;
+        const dim3 g3((unsigned)((cin + wg.nblk - 1) / wg.nblk), (unsigned)((cout + 127) / 128),
+                      (unsigned)((wg.total + wg.chunk - 1) / wg.chunk));
+        k_conv3x3_wgrad_tc<<<g3, kThreads, smem, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)dy, dw, wg);
+        return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+    }
     const dim3 grid((unsigned)((kpad + 63) / 64), (unsigned)((cout + 63) / 64),
                     (unsigned)((m + kWgChunk - 1) / kWgChunk));
     k_conv3x3_wgrad<<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)dy, dw, (int)m, h, w_,

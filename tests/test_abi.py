@@ -157,6 +157,7 @@ def test_convolutions_validate_arguments_before_launching(lib):
     assert lib.ske_conv_select(3) == 1 and lib.ske_conv_select(0) == 0
     assert lib.ske_conv_stage_channels(24) == 1 and lib.ske_conv_stage_channels(0) == 0
     assert lib.ske_skew_select(2) == 1 and lib.ske_skew_select(0) == 0
+    assert lib.ske_conv_wgrad_select(2) == 1 and lib.ske_conv_wgrad_select(1) == 0
 
 
 def test_cli_usage_errors():

@@ -349,3 +349,37 @@ def test_encode_kernel_equals_tensor_expressions(sur):
     full = coarse.repeat_interleave(4, 1).repeat_interleave(4, 2)
     want[..., 2] = (torch.log1p(full) / sur.COARSE_SCALE).to(torch.bfloat16)
     assert torch.equal(got.view(torch.int16), want.view(torch.int16))
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout", [(2, 21, 18, 8, 16), (2, 64, 256, 32, 32), (1, 32, 64, 96, 64),
+                                            (2, 16, 32, 64, 256), (3, 23, 45, 16, 40)])
+def test_wgrad_tcgen05_matches_numpy(sur, n, h, w, cin, cout):
+    """The tcgen05 weight gradient (ske_conv_wgrad_select(0): MN-major operands
+    read in place from staged planes) and the default mma.sync kernel against
+    float64 NumPy on the same bfloat16 inputs: 16- and 32-channel N blocks,
+    several N and M blocks, 32-column segments with several tiles per CTA, an
+    odd width."""
+    import torch
+    from skewengine_gb300 import _lib
+    rng = np.random.default_rng(cin * 3 + cout + w)
+    xb = _bf16(rng.normal(0, 1, (n, h, w, cin)))
+    dyb = _bf16(rng.normal(0, 1, (n, h, w, cout)))
+    xp = np.pad(xb.double().numpy(), ((0, 0), (1, 1), (1, 1), (0, 0)))
+    cols = np.stack([xp[:, ky:ky + h, kx:kx + w, :] for ky in range(3) for kx in range(3)], axis=3)
+    ref = dyb.double().numpy().reshape(-1, cout).T @ cols.reshape(-1, 9 * cin)
+    x, dy = xb.cuda().contiguous(), dyb.cuda().contiguous()
+    lib = _lib.load()
+    try:
+        assert lib.ske_conv_wgrad_select(0) == 0
+        got = sur.conv3x3_wgrad(x, dy, cout)
+    finally:
+        assert lib.ske_conv_wgrad_select(1) == 0
+    dflt = sur.conv3x3_wgrad(x, dy, cout)
+    sur.conv_check()
+    scale = np.abs(ref).max()
+    for name, t in (("tcgen05", got), ("mma.sync", dflt)):
+        v = t.cpu().double().numpy()
+        assert np.all(v[:, 9 * cin:] == 0)
+        err = np.abs(v[:, : 9 * cin] - ref).max() / scale
+        print(f"wgrad {n}x{h}x{w} {cin}->{cout} {name}: {err:.1e} of max |dW|")
+        assert err <= 1e-5, (name, err)
