@@ -455,7 +455,8 @@ int ske_conv3x3_head_bf16(const void* x, const void* w, const float* bias, const
  * height range (n floats each) and coarse areas (n x side/f x side/f, f =
  * coarse_factor): x[...,0] = (h - mean) / (range, or 1 for 0), x[...,1] =
  * log1p(range), x[...,2] = log1p(coarse area of the cell's coarse cell) /
- * coarse_scale, channels 3-7 zero.  No reference counterpart. */
+ * coarse_scale, channels 3-7 zero.  side at most 46340.  No reference
+ * counterpart. */
 int ske_surrogate_encode_bf16(const float* tiles, const float* mean, const float* range, const float* coarse,
                               int coarse_factor, float coarse_scale, void* x, int n, int side, void* stream);
 

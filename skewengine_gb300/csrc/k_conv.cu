@@ -1566,7 +1566,8 @@ static __global__ void k_encode(const float* __restrict__ T, const float* __rest
 extern "C" int ske_surrogate_encode_bf16(const float* tiles, const float* mean, const float* range,
                                          const float* coarse, int coarse_factor, float coarse_scale, void* x, int n,
                                          int side, void* stream) {
-    if (!tiles || !mean || !range || !coarse || !x || n < 1 || side < 1 || coarse_factor < 1 ||
+    // side * side must fit an int (the kernel's cell index within a tile).
+    if (!tiles || !mean || !range || !coarse || !x || n < 1 || side < 1 || side > 46340 || coarse_factor < 1 ||
         side % coarse_factor || !(coarse_scale > 0.0f))
         return SKE_ERR_INVALID;
     if (!aligned(x, 16) || !aligned(tiles, 4) || !aligned(coarse, 4)) return SKE_ERR_INVALID;

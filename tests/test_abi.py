@@ -153,6 +153,7 @@ def test_convolutions_validate_arguments_before_launching(lib):
     assert enc(a, a, a, a, 3, 16.0, a, 1, 256, s) == 1  # side not a multiple of the coarse factor
     assert enc(a, a, a, a, 4, 0.0, a, 1, 256, s) == 1  # scale not positive
     assert enc(a, None, a, a, 4, 16.0, a, 1, 256, s) == 1  # no means
+    assert enc(a, a, a, a, 2, 16.0, a, 1, 46342, s) == 1  # side * side past an int
     # kernel choices: valid values are taken, others refused and the choice kept
     assert lib.ske_conv_select(3) == 1 and lib.ske_conv_select(0) == 0
     assert lib.ske_conv_stage_channels(24) == 1 and lib.ske_conv_stage_channels(0) == 0
