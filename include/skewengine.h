@@ -489,9 +489,11 @@ int ske_conv_stage_channels(int channels);
  * reference counterpart. */
 int ske_conv_wgrad_select(int path);
 
-/* Synchronises `stream`, then sets *failed to 1 if a forward convolution since
- * the previous call gave up waiting for its tensor-core operations (its output
- * is then not written), else 0, and clears the flag. */
+/* Synchronises `stream`, then sets *failed to 1 if a forward convolution or
+ * the tcgen05 weight gradient since the previous call gave up waiting for its
+ * tensor-core operations (a forward convolution's output is then not written;
+ * the weight gradient adds none of its CTA's sums to dw), else 0, and clears
+ * the flag. */
 int ske_conv_status(int* failed, void* stream);
 
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
