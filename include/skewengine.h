@@ -45,7 +45,7 @@ extern "C" {
 #define SKE_ERR_CUDA 2        /* a CUDA runtime call failed                     */
 #define SKE_ERR_NO_DEVICE 3   /* no usable CUDA device                          */
 #define SKE_ERR_STATE 4       /* call out of order (e.g. kernel() before skew())*/
-#define SKE_ERR_UNSUPPORTED 5 /* valid request this build does not support      */
+#define SKE_ERR_UNSUPPORTED 5 /* valid request the library does not support     */
 #define SKE_ERR_DEVICE 6      /* a kernel reported an error through its status  */
 
 /* Operators: values of the reference KERNELS enum (src/global.h:77). */
