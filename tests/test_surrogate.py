@@ -175,9 +175,10 @@ def test_trained_network_beats_the_untrained_method(sur):
     print(f"held-out tile-area error: trained median {trained:.4f} p90 {np.quantile(err, 0.9):.4f}, "
           f"constant {constant:.4f}, untrained {untrained:.4f}")
     assert trained < 0.5 * constant and trained < 0.5 * untrained, (trained, constant, untrained)
-    # The stated bound: median tile-area error within 2.5% on these held-out tiles
-    # (1.9% median, 4.4% at the 90th percentile on the 256 validation tiles of training).
-    assert trained <= 0.025, trained
+    # The stated bound: median tile-area error within 2% on these held-out tiles
+    # (measured 1.89%, 5.9% at the 90th percentile; the tiles are seeded and the
+    # forward pass and the engine's labels are deterministic, so the value repeats).
+    assert trained <= 0.02, trained
 
 
 @contextlib.contextmanager
