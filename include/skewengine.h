@@ -435,8 +435,9 @@ int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, i
 int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
                            int n, int h, int w_, int c1, int c2, int cout, int relu, void* stream);
 /* Weight gradient of ske_conv3x3_bf16, added into dw (cout x kpad float32):
- * dw[co][k] += sum over pixels of dy[pixel][co] * (im2col x)[pixel][k].
- * cout a multiple of 8. */
+ * dw[co][k] += sum over pixels of dy[pixel][co] * (im2col x)[pixel][k],
+ * kpad = 9*cin rounded up to a multiple of 32 (the padding columns are left as
+ * they are).  cin and cout multiples of 8. */
 int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
                            int cout, void* stream);
 /* The same 3x3 convolution (+ bias, ReLU when relu != 0) followed by a 1x1
