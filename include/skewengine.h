@@ -425,7 +425,10 @@ int ske_render_input(const float* image, int count, uint8_t* grey);
  * on the device, ordered on `stream`: y = relu?(conv(x, w) + bias).
  * w: cout x kpad bfloat16, kpad = 9*cin rounded up to a multiple of 32, entry
  * [co][(ky*3 + kx)*cin + ci], zero past 9*cin; bias: cout floats or null.
- * cin a multiple of 8, cout even. */
+ * cin a multiple of 8, cout even.  In every function below the bfloat16
+ * inputs and weights, and the outputs of ske_maxpool2_bf16 and
+ * ske_surrogate_encode_bf16, start on 16-byte boundaries; the other outputs
+ * and the float32 arrays on 4-byte ones (SKE_ERR_INVALID otherwise). */
 int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
                      int cin, int cout, int relu, void* stream);
 /* ske_conv3x3_bf16 of the channel concatenation [nearest-upsampled xlow, xskip]
