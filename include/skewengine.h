@@ -247,7 +247,9 @@ int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, cons
  * src/main.cu:86-168 for every grid at once), replayed as a captured CUDA graph
  * from the second call on (SKE_FLAG_NO_GRAPH: plain launches).  Results are the
  * same as ske_run_angles on each grid, bit for bit in both accumulation modes.
- * Other grids and other operators run one grid at a time. */
+ * Float32 cepstrum (SKE_KERNEL_CEPSTRUM with SKE_FLAG_CEPSTRUM_F32): each run of
+ * consecutive square images of one side shares one launch sequence.  Other
+ * grids and other operators run one grid at a time. */
 int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
                          const float* const* inputs, int inputs_on_device, float* const* outputs,
                          int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p);
