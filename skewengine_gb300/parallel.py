@@ -8,6 +8,10 @@ angles, computes its four accumulators on its GPU, and rank 0 gathers them and
 folds them in rank order: the same arithmetic as the reference run with one
 thread per rank and a static schedule.  The only exchange is that one gather of
 4*N floats per rank.
+
+A batch of independent grids (ske_run_batch) shards by whole grids instead
+(``shard_batch``, ``run_batch_sharded``): each rank runs its grids in one
+batched call and no data crosses ranks until the optional gather of outputs.
 """
 from __future__ import annotations
 
@@ -34,6 +38,36 @@ def shard_angles(n_angles: int, world: int, rank: int, costs=None) -> list[int]:
     cuts.append(n_angles)
     cuts = np.maximum.accumulate(np.clip(cuts, 0, n_angles))
     return list(range(int(cuts[rank]), int(cuts[rank + 1])))
+
+
+def grid_cost(dimx: int, dimy: int) -> float:
+    """A grid's total-viewshed work up to a constant factor: every sector's
+    skewed rows hold about dimx*dimy cells, and each cell's line of sight runs
+    the length of its row (at most max(dimx, dimy)), so cells x longest row."""
+    return float(dimx) * float(dimy) * float(max(dimx, dimy))
+
+
+def shard_batch(shapes, world: int, rank: int) -> list[int]:
+    """Indices (ascending) of the grids of a batch that `rank` runs.
+
+    ``shapes``: one (dimy, dimx) per grid.  The grids are independent, as the
+    reference's one-grid-per-program runs are (src/main.cu:86-168 per grid), so
+    whole grids are dealt out: largest ``grid_cost`` first, each to the rank
+    with the least cost so far (ties to the lower rank), which keeps every
+    rank's share within one grid's cost of the others'.  Every rank computes
+    the same assignment from the shapes alone.
+    """
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("bad world/rank")
+    costs = [grid_cost(int(w), int(h)) for h, w in shapes]
+    load = [0.0] * world
+    mine = []
+    for i in sorted(range(len(costs)), key=lambda k: (-costs[k], k)):
+        r = min(range(world), key=lambda q: (load[q], q))
+        load[r] += costs[i]
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
 
 
 def _orient_index(dimx: int, dimy: int):
@@ -132,3 +166,36 @@ def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, ma
     out = fold_accumulators([results[r][0] for r in range(world)], [results[r][1] for r in range(world)],
                             engine.dimx, engine.dimy, is_max=int(kernel) == KERNEL_CEPSTRUM)
     return out, recovered
+
+
+def run_batch_sharded(run_batch, kernel, grids, group=None, gather: bool = True, **kwargs):
+    """Run a batch of independent grids with whole grids sharded over a
+    torch.distributed group: each rank passes its shard (``shard_batch``) to
+    ``run_batch(kernel, shard, **kwargs)`` — one batched engine call on its GPU,
+    e.g. ``skewengine_gb300.run_batch`` (``ske_run_batch``) — and nothing is
+    exchanged on the data path.  Every rank passes the same list of grids.
+
+    gather=True: rank 0 receives every grid's output (host arrays, in the order
+    of ``grids``) over the group and returns the list; other ranks return None.
+    gather=False: each rank returns ``{index: output}`` for its own grids.
+    """
+    import torch.distributed as dist
+
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    mine = shard_batch([tuple(g.shape[-2:]) for g in grids], world, rank)
+    outs = run_batch(kernel, [grids[i] for i in mine], **kwargs) if mine else []
+    if len(outs) != len(mine):
+        raise RuntimeError(f"run_batch returned {len(outs)} outputs for {len(mine)} grids")
+    local = {i: o for i, o in zip(mine, outs)}
+    if not gather:
+        return local
+    payload = {i: (o.cpu().numpy() if hasattr(o, "cpu") else np.asarray(o)) for i, o in local.items()}
+    gathered = [None] * world if rank == 0 else None
+    dist.gather_object(payload, gathered, dst=0, group=group)
+    if rank != 0:
+        return None
+    merged = {}
+    for part in gathered:
+        merged.update(part)
+    return [merged[i] for i in range(len(grids))]

@@ -163,3 +163,66 @@ def test_resilient_sharding_recovers_failed_ranks(oracle, port, tmp_path, mode):
     assert bits_equal(got, want)
     with open(res + ".json") as f:
         assert json.load(f) == ([1, 2] if mode == "fail" else [])
+
+
+def test_shard_batch_partition():
+    """Whole grids dealt out largest first to the least-loaded rank: every grid
+    on exactly one rank, the same answer on every rank, and every rank's cost
+    within the largest grid's cost of every other's."""
+    shapes = [(s, s) for s, _, _ in synthetic.uneven_dem_batch(64, 3000)] + [(300, 500), (480, 270)]
+    for world in (1, 2, 3, 4, 8):
+        parts = [parallel.shard_batch(shapes, world, r) for r in range(world)]
+        assert sorted(sum(parts, [])) == list(range(len(shapes)))
+        assert parts == [parallel.shard_batch(shapes, world, r) for r in range(world)]
+        loads = [sum(parallel.grid_cost(w, h) for i, (h, w) in enumerate(shapes) if i in p) for p in parts]
+        assert max(loads) - min(loads) <= max(parallel.grid_cost(w, h) for h, w in shapes)
+    assert parallel.shard_batch([], 2, 1) == []
+    with pytest.raises(ValueError):
+        parallel.shard_batch(shapes, 2, 2)
+
+
+def _batch_rank_main(rank, world, port_path, grids, result_path, master_port):
+    import ctypes as C
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(master_port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    lib = C.CDLL(port_path)
+    from tests.conftest import PortOracle
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    lib.port_run.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int]
+    oracle = PortOracle(lib)
+    seen = []
+
+    def batch(kernel, shard, povh):  # stands in for run_batch: one call per rank
+        seen.append(len(shard))
+        return [oracle.run(kernel, g, povh=povh) for g in shard]
+
+    out = parallel.run_batch_sharded(batch, 0, grids, povh=np.float32(0.15))
+    own = parallel.run_batch_sharded(batch, 0, grids, gather=False, povh=np.float32(0.15))
+    assert seen[0] == seen[1] == len(own) and set(own) == set(parallel.shard_batch(
+        [g.shape for g in grids], world, rank))
+    if rank == 0:
+        np.savez(result_path, *out)
+    else:
+        assert out is None
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_batch_sharded(oracle, port, tmp_path):
+    """Independent grids of uneven size split over two gloo ranks, one batched
+    call per rank, gathered on rank 0 in input order: bit-identical to running
+    every grid alone."""
+    import torch.multiprocessing as mp
+    grids = [synthetic.fractal_dem(s, 40 + s, roughness=0.7) for s in (24, 40, 17, 33)]
+    grids.append(synthetic.fractal_dem(30, 7)[:, :21].copy())
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        master_port = s.getsockname()[1]
+    res = str(tmp_path / "outs.npz")
+    mp.start_processes(_batch_rank_main, args=(2, port._name, grids, res, master_port), nprocs=2, join=True,
+                       start_method="spawn")
+    got = np.load(res)
+    assert len(got.files) == len(grids)
+    for k, g in enumerate(grids):
+        assert bits_equal(got[f"arr_{k}"], oracle.run(0, g, povh=np.float32(0.15))), k
