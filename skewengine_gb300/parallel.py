@@ -199,3 +199,63 @@ def run_batch_sharded(run_batch, kernel, grids, group=None, gather: bool = True,
     for part in gathered:
         merged.update(part)
     return [merged[i] for i in range(len(grids))]
+
+
+def run_batch_sharded_resilient(run_batch, kernel, grids, store, rank: int, world: int, timeout: float = 60.0,
+                                poll: float = 0.01, **kwargs):
+    """``run_batch_sharded`` with failure detection and recovery on the host,
+    as ``run_sharded_resilient`` does for sectors.
+
+    Each rank runs its grids (``shard_batch``) in one ``run_batch`` call and
+    posts every output as raw float32 bytes under ``grid/<index>`` of the
+    shared store, then ``done/<rank>``; a rank whose work raises posts its error
+    under ``err/<rank>``.  Rank 0 runs its own grids, then waits for every other
+    rank: one that reports an error or has not finished within ``timeout``
+    seconds is taken over, and rank 0 runs that rank's grids itself (one
+    batched call).  Each grid's output is computed alone, so the results have
+    the same bits as a run without failures.
+
+    Returns (outputs in the order of ``grids``, recovered ranks) on rank 0 and
+    (None, []) elsewhere.
+    """
+    import time
+
+    shapes = [tuple(g.shape[-2:]) for g in grids]
+    shards = [shard_batch(shapes, world, r) for r in range(world)]
+
+    def host(o):
+        return np.ascontiguousarray(o.cpu().numpy() if hasattr(o, "cpu") else o, np.float32)
+
+    def run(idx):
+        outs = run_batch(kernel, [grids[i] for i in idx], **kwargs) if idx else []
+        if len(outs) != len(idx):
+            raise RuntimeError(f"run_batch returned {len(outs)} outputs for {len(idx)} grids")
+        return {i: host(o) for i, o in zip(idx, outs)}
+
+    if rank != 0:
+        try:
+            for i, o in run(shards[rank]).items():
+                store.set(f"grid/{i}", o.tobytes())
+            store.set(f"done/{rank}", b"1")  # set last: every grid of the rank is posted
+        except Exception as exc:
+            store.set(f"err/{rank}", repr(exc).encode())
+            raise
+        return None, []
+    results = run(shards[0])
+    recovered = []
+    deadline = time.monotonic() + timeout
+    for r in range(1, world):
+        while True:
+            if store.check([f"done/{r}"]):
+                for i in shards[r]:
+                    v = np.frombuffer(store.get(f"grid/{i}"), np.float32)
+                    if v.size != shapes[i][0] * shapes[i][1]:
+                        raise ValueError(f"rank {r} posted {v.size} values for grid {i}")
+                    results[i] = v.reshape(shapes[i])
+                break
+            if store.check([f"err/{r}"]) or time.monotonic() > deadline:
+                results.update(run(shards[r]))
+                recovered.append(r)
+                break
+            time.sleep(poll)
+    return [results[i] for i in range(len(grids))], recovered

@@ -226,3 +226,56 @@ def test_two_rank_batch_sharded(oracle, port, tmp_path):
     assert len(got.files) == len(grids)
     for k, g in enumerate(grids):
         assert bits_equal(got[f"arr_{k}"], oracle.run(0, g, povh=np.float32(0.15))), k
+
+
+def _batch_resilient_main(rank, world, port_path, grids, result_path, store_port, mode):
+    import ctypes as C
+    import json
+    from datetime import timedelta
+    import torch.distributed as dist
+    if mode == "fail" and rank == 2:
+        return  # dies before contributing anything
+    store = dist.TCPStore("127.0.0.1", store_port, world, rank == 0, timedelta(seconds=60), wait_for_workers=False)
+    lib = C.CDLL(port_path)
+    from tests.conftest import PortOracle
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    lib.port_run.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int]
+    oracle = PortOracle(lib)
+
+    def batch(kernel, shard, povh):
+        if mode == "fail" and rank == 1:
+            raise RuntimeError("injected failure of this rank's grids")
+        return [oracle.run(kernel, g, povh=povh) for g in shard]
+
+    try:
+        outs, recovered = parallel.run_batch_sharded_resilient(batch, 0, grids, store, rank, world, timeout=5.0,
+                                                               povh=np.float32(0.15))
+    except RuntimeError:
+        assert mode == "fail" and rank == 1
+        return
+    if rank == 0:
+        np.savez(result_path, *outs)
+        with open(result_path + ".json", "w") as f:
+            json.dump(recovered, f)
+
+
+@pytest.mark.parametrize("mode", ["ok", "fail"])
+def test_resilient_batch_sharding_recovers_failed_ranks(oracle, port, tmp_path, mode):
+    """Three CPU ranks share a batch of uneven grids; with mode "fail" rank 1
+    raises inside its batched call and rank 2 exits before contributing.  Rank 0
+    detects both on the host (an error key, a deadline) and runs their grids
+    itself; every output has the same bits as the grid run alone."""
+    import json
+    import torch.multiprocessing as mp
+    grids = [synthetic.fractal_dem(s, 60 + s, roughness=0.75) for s in (20, 31, 26, 18, 35, 23)]
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        store_port = s.getsockname()[1]
+    res = str(tmp_path / "outs.npz")
+    mp.start_processes(_batch_resilient_main, args=(3, port._name, grids, res, store_port, mode), nprocs=3,
+                       join=True, start_method="spawn")
+    got = np.load(res)
+    for k, g in enumerate(grids):
+        assert bits_equal(got[f"arr_{k}"], oracle.run(0, g, povh=np.float32(0.15))), k
+    with open(res + ".json") as f:
+        assert json.load(f) == ([1, 2] if mode == "fail" else [])
