@@ -772,7 +772,8 @@ int make_grid_geo(int dimx, int dimy, GridGeo** out) {
     *out = g;
     g->dimx = dimx;
     g->dimy = dimy;
-    build_geometry(dimx, dimy, g->geo);
+    const std::string why = build_geometry(dimx, dimy, g->geo);
+    if (!why.empty()) return fail(SKE_ERR_INVALID, "sector geometry of %dx%d: %s", dimx, dimy, why.c_str());
     g->rowoff.assign(g->geo.first.size(), 0);
     g->rowtab.assign(g->geo.first.size(), make_int4(0, 0, 0, 0));
     g->cells.assign(g->geo.desc.size(), 0);
@@ -1292,6 +1293,8 @@ int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32
     std::vector<int32_t> f, l, t;
     std::vector<float> w;
     sector_geometry(dimx, dimy, angle, d, f, l, t, w);
+    const std::string why = check_sector(d, f.data(), l.data(), t.data(), dimx, dimy);
+    if (!why.empty()) return fail(SKE_ERR_INVALID, "sector geometry of %dx%d: %s", dimx, dimy, why.c_str());
     geom->angle = d.angle;
     geom->sector_type = d.type;
     geom->new_angle = d.new_angle;
@@ -1358,7 +1361,8 @@ int init_engine(ske_engine e, int dimx, int dimy, int device, void* stream, ske_
     e->N = (int64_t)dimx * dimy;
     e->len = skew_buffer_len(dimx, dimy);
     e->stride = (e->len + 63) & ~(int64_t)63;
-    build_geometry(dimx, dimy, e->geo);
+    const std::string why = build_geometry(dimx, dimy, e->geo);
+    if (!why.empty()) return fail(SKE_ERR_INVALID, "sector geometry of %dx%d: %s", dimx, dimy, why.c_str());
     e->rows_in_width.assign(e->geo.desc.size(), 1);
     for (size_t a = 0; a < e->geo.desc.size(); a++) {
         SectorDesc& d = e->geo.desc[a];

@@ -8,6 +8,7 @@
 //
 // Compiled with -ffp-contract=off so no multiply-add is fused.
 #include <cmath>
+#include <cstdio>
 #include <complex>
 
 #include "ske_internal.h"
@@ -63,7 +64,40 @@ void sector_geometry(int dimx, int dimy, int angle, SectorDesc& d, std::vector<i
     last.assign(l.begin(), l.begin() + d.H);
 }
 
-void build_geometry(int dimx, int dimy, Geometry& g) {
+// The skew, the operators and the deskew index the skewed grid of a sector as
+// rows r < H of stride dim_i whose valid cells are [first[r], last[r]) (a row
+// with first >= last is empty).  They rely on: 0 <= first and last <= dim_l;
+// the farthest cell a row reaches, (H-1)*dim_i + last, inside the skew buffer
+// of 2*dimx*dimy + dim_l floats (skewEngine.cuh:425-426); and every column's
+// source rows target[j] .. target[j] + dim_o inside rows 0 .. H.  The tables
+// follow the reference's formulas, which keep all three; checking them here
+// turns any table that did not into an error before a kernel runs.
+std::string check_sector(const SectorDesc& d, const int32_t* first, const int32_t* last, const int32_t* target,
+                         int dimx, int dimy) {
+    char msg[160];
+    if (d.H < 1 || d.dim_i < 1 || d.dim_o < 1 || d.diml != (dimx > dimy ? dimx : dimy)) {
+        snprintf(msg, sizeof msg, "angle %d: skewed grid %d rows x %d (outer %d)", d.angle, d.H, d.dim_i, d.dim_o);
+        return msg;
+    }
+    const int64_t len = skew_buffer_len(dimx, dimy);
+    for (int r = 0; r < d.H; r++) {
+        if (first[r] < 0 || last[r] > d.diml || (int64_t)r * d.dim_i + last[r] > len) {
+            snprintf(msg, sizeof msg, "angle %d: row %d spans [%d, %d) of %d x %d, buffer %lld", d.angle, r,
+                     first[r], last[r], d.H, d.dim_i, (long long)len);
+            return msg;
+        }
+    }
+    for (int j = 0; j < d.dim_i; j++) {
+        if (target[j] < 0 || target[j] + d.dim_o > d.H) {
+            snprintf(msg, sizeof msg, "angle %d: column %d shifts %d rows in a skewed grid of %d", d.angle, j,
+                     target[j], d.H);
+            return msg;
+        }
+    }
+    return std::string();
+}
+
+std::string build_geometry(int dimx, int dimy, Geometry& g) {
     g.dimx = dimx;
     g.dimy = dimy;
     g.desc.resize(kMaxSectors);
@@ -78,6 +112,8 @@ void build_geometry(int dimx, int dimy, Geometry& g) {
     for (int a = 0; a < kMaxSectors; a++) {
         SectorDesc& d = g.desc[a];
         sector_geometry(dimx, dimy, a, d, f, l, t, w);
+        std::string why = check_sector(d, f.data(), l.data(), t.data(), dimx, dimy);
+        if (!why.empty()) return why;
         d.col_off = (int64_t)g.target.size();
         d.row_off = (int64_t)g.first.size();
         g.target.insert(g.target.end(), t.begin(), t.end());
@@ -88,6 +124,7 @@ void build_geometry(int dimx, int dimy, Geometry& g) {
         if (cells > g.max_cells) g.max_cells = cells;
         if (d.H > g.max_H) g.max_H = d.H;
     }
+    return std::string();
 }
 
 void fft_twiddles(unsigned n, std::vector<double>& re_im) {

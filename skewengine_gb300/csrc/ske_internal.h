@@ -49,7 +49,13 @@ void sector_geometry(int dimx, int dimy, int angle, SectorDesc& d, std::vector<i
                      std::vector<int32_t>& last, std::vector<int32_t>& target, std::vector<float>& weight);
 
 // Geometry of all 180 angles.
-void build_geometry(int dimx, int dimy, Geometry& g);
+// The bounds every kernel relies on (checked on the host once per table build):
+// empty string when they hold, else which one fails.
+std::string check_sector(const SectorDesc& d, const int32_t* first, const int32_t* last, const int32_t* target,
+                         int dimx, int dimy);
+// All 180 sectors' tables; returns check_sector's complaint about the first
+// sector that fails it (empty string: every table is within bounds).
+std::string build_geometry(int dimx, int dimy, Geometry& g);
 
 // Twiddles of the reference radix-2 DIF FFT (helper.h:59-82) for size n (a power
 // of two): the stage with half-span h uses entries [n-2h, n-h), entry l being the

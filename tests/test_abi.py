@@ -166,3 +166,23 @@ def test_cli_usage_errors():
     assert cli_run([]) == 1
     assert cli_run(["nosuchkernel", "x", "1", "1", "y"]) == 1
     assert cli_run(["sdem", "/nonexistent/file.raw", "4", "4", "/tmp/out.raw"]) == 1
+
+
+def test_sector_tables_within_kernel_bounds():
+    """ske_geometry checks every table against the bounds the kernels index
+    with (row spans in [0, dim_l], the farthest cell inside the skew buffer,
+    column shifts inside the skewed rows) and refuses one that breaks them.
+    Every real table passes: all 180 angles of tiny, ragged, strongly
+    non-square and benchmark-sized grids."""
+    from skewengine_gb300 import engine
+    shapes = [(x, y) for x in (1, 2, 3, 7, 33) for y in (1, 2, 3, 7, 33)]
+    shapes += [(1, 500), (500, 1), (17, 4000), (4000, 17), (255, 256), (512, 512), (2000, 2000), (4096, 300)]
+    for dimx, dimy in shapes:
+        n = dimx * dimy
+        for a in range(180):
+            g = engine.geometry(dimx, dimy, a)
+            H, di, dl = g["skew_height"], g["dim_i"], g["dim_l"]
+            f, l = g["first"], g["last"]
+            assert f.min() >= 0 and l.max() <= dl
+            assert int((np.arange(H, dtype=np.int64) * di + l).max()) <= 2 * n + dl
+            assert g["target"].min() >= 0 and int(g["target"].max()) + g["dim_o"] <= H
