@@ -666,7 +666,7 @@ def surrogate_workload(args):
         t1.record()
         torch.cuda.synchronize()
     fwd_ms = t0.elapsed_time(t1) / 3
-    # The plain engine's headline throughput on this machine (2000x2000 DEM, 360
+    # The plain engine's headline throughput on this GPU (2000x2000 DEM, 360
     # directional sectors, device-resident), the reference point of the target
     # "surrogate throughput >= 10x the plain engine's".
     d2k = torch.as_tensor(synthetic.fractal_dem(SIDE, 1000, roughness=0.8), device="cuda")
