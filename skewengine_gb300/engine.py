@@ -365,6 +365,8 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
                 outs = torch.empty_like(grids)
             else:
                 outs = np.empty_like(grids)
+        if _is_device(outs) != on_dev:
+            raise TypeError("the grids and their outputs must both be host arrays or both CUDA tensors")
         for arr in (grids, outs):
             _ptr(arr, (n, h, w), writable=arr is outs)  # dtype, contiguity, shape checks
         step = np.arange(n, dtype=np.uint64) * np.uint64(4 * h * w)
@@ -379,17 +381,31 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
         grids = list(grids)
         if not grids:
             return []
-        dims = [(g.shape[1], g.shape[0]) for g in grids]
+        if any(len(g.shape) != 2 for g in grids):
+            raise ValueError("every grid of a list must be 2-D")
+        dims = [(int(g.shape[1]), int(g.shape[0])) for g in grids]
         big = max(dims, key=lambda d: d[0] * d[1])
+        # One call takes one placement for all inputs and one for all outputs:
+        # a host array passed as a device pointer (or the reverse) would be
+        # read or written at the wrong address, so mixed lists are refused.
         on_dev = _is_device(grids[0])
+        mixed = TypeError("the grids and their outputs must all be host arrays or all CUDA tensors")
+        if any(_is_device(g) != on_dev for g in grids):
+            raise mixed
         if outs is None:
             if on_dev:
                 import torch
                 outs = [torch.empty_like(g) for g in grids]
             else:
                 outs = [np.empty_like(g) for g in grids]
+        outs = list(outs)
+        if len(outs) != len(grids):
+            raise ValueError(f"{len(outs)} outputs for {len(grids)} grids")
+        if any(_is_device(o) != on_dev for o in outs):
+            raise mixed
         ins = (C.c_void_p * len(grids))(*[_ptr(g)[0].value for g in grids])
-        ous = (C.c_void_p * len(grids))(*[_ptr(o, writable=True)[0].value for o in outs])
+        ous = (C.c_void_p * len(grids))(*[_ptr(o, (d[1], d[0]), writable=True)[0].value
+                                          for o, d in zip(outs, dims)])
         dx = np.array([d[0] for d in dims], np.int32)
         dy = np.array([d[1] for d in dims], np.int32)
         count = len(grids)

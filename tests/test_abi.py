@@ -186,3 +186,42 @@ def test_sector_tables_within_kernel_bounds():
             assert f.min() >= 0 and l.max() <= dl
             assert int((np.arange(H, dtype=np.int64) * di + l).max()) <= 2 * n + dl
             assert g["target"].min() >= 0 and int(g["target"].max()) + g["dim_o"] <= H
+
+
+class _FakeCudaGrid:
+    """Stands in for a CUDA tensor in checks that run before any device work."""
+    is_cuda = True
+    dtype = "torch.float32"
+
+    def __init__(self, shape):
+        self.shape = tuple(shape)
+        self.ndim = len(self.shape)
+
+    def is_contiguous(self):
+        return True
+
+    def data_ptr(self):
+        return 16  # never dereferenced: the call is refused first
+
+
+def test_run_batch_refuses_mixed_placements_and_mismatched_outputs(lib):
+    """run_batch passes one placement flag for all inputs and one for all
+    outputs, so a list mixing host arrays and CUDA tensors, outputs placed
+    unlike their grids, outputs of the wrong shape or count, and grids that
+    are not 2-D are refused before an engine is made or a pointer is read."""
+    from skewengine_gb300 import engine
+    h = np.zeros((8, 8), np.float32)
+    with pytest.raises(TypeError):
+        engine.run_batch(0, [h, _FakeCudaGrid((8, 8))])
+    with pytest.raises(TypeError):
+        engine.run_batch(0, [h], outs=[_FakeCudaGrid((8, 8))])
+    with pytest.raises(TypeError):
+        engine.run_batch(0, [_FakeCudaGrid((8, 8))], outs=[np.zeros((8, 8), np.float32)])
+    with pytest.raises(TypeError):
+        engine.run_batch(0, _FakeCudaGrid((2, 8, 8)), outs=np.zeros((2, 8, 8), np.float32))
+    with pytest.raises(ValueError):
+        engine.run_batch(0, [h, h], outs=[np.zeros((8, 8), np.float32)])
+    with pytest.raises(ValueError):
+        engine.run_batch(0, [h], outs=[np.zeros((8, 4), np.float32)])
+    with pytest.raises(ValueError):
+        engine.run_batch(0, [np.zeros((2, 8, 8), np.float32)])
