@@ -58,13 +58,33 @@ def _stream(t):
     return C.c_void_p(torch.cuda.current_stream(t.device).cuda_stream)
 
 
+def _need(t, name: str, dtype, shape=None, device=None) -> None:
+    """Raise unless ``t`` is a contiguous CUDA tensor of ``dtype`` (and
+    ``shape``, on ``device``).  The kernels take raw device pointers and size
+    every read and write from the shape arguments, so a host tensor, another
+    element type or a smaller tensor would be read or written out of place."""
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(t.shape)}, expected {tuple(shape)}")
+    if device is not None and t.device != device:
+        raise ValueError(f"{name} is on {t.device}, the other operands on {device}")
+
+
 def conv3x3(x, w, bias=None, relu: bool = False):
     """y = relu?(conv3x3(x, w) + bias); x (N, H, W, Cin) bf16, w (Cout, kpad(Cin)) bf16."""
     import torch
+    _need(x, "x", torch.bfloat16)
     n, h, wd, cin = x.shape
     cout = w.shape[0]
-    assert x.is_contiguous() and w.is_contiguous() and x.dtype == torch.bfloat16 and w.dtype == torch.bfloat16
-    assert w.shape[1] == kpad(cin)
+    _need(w, "w", torch.bfloat16, (cout, kpad(cin)), x.device)
+    if bias is not None:
+        _need(bias, "bias", torch.float32, (cout,), x.device)
     y = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=x.device)
     check(load().ske_conv3x3_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
                                   C.c_void_p(bias.data_ptr()) if bias is not None else None,
@@ -76,11 +96,15 @@ def conv3x3_upcat(xlow, skip, w, bias=None, relu: bool = False):
     """conv3x3(cat([nearest-upsampled xlow, skip], channels)) without building the
     concatenation; the same values as conv3x3 on it."""
     import torch
+    _need(skip, "skip", torch.bfloat16)
     n, h, wd, c2 = skip.shape
+    _need(xlow, "xlow", torch.bfloat16, None, skip.device)
     c1 = xlow.shape[3]
+    _need(xlow, "xlow", torch.bfloat16, (n, h // 2, wd // 2, c1))
     cout = w.shape[0]
-    assert xlow.shape[:3] == (n, h // 2, wd // 2) and xlow.is_contiguous() and skip.is_contiguous()
-    assert w.shape[1] == kpad(c1 + c2) and w.dtype == torch.bfloat16
+    _need(w, "w", torch.bfloat16, (cout, kpad(c1 + c2)), skip.device)
+    if bias is not None:
+        _need(bias, "bias", torch.float32, (cout,), skip.device)
     y = torch.empty((n, h, wd, cout), dtype=torch.bfloat16, device=skip.device)
     check(load().ske_conv3x3_upcat_bf16(C.c_void_p(xlow.data_ptr()), C.c_void_p(skip.data_ptr()),
                                         C.c_void_p(w.data_ptr()),
@@ -95,13 +119,16 @@ def conv3x3_head(x, w, bias, head_w, head_b, relu: bool = True):
     (ske_conv3x3_head_bf16), float32 (N, H, W); the activations are not stored.
     None where that kernel does not apply."""
     import torch
+    _need(x, "x", torch.bfloat16)
     n, h, wd, cin = x.shape
     cout = w.shape[0]
-    assert x.is_contiguous() and w.is_contiguous() and x.dtype == torch.bfloat16 and w.dtype == torch.bfloat16
-    assert w.shape[1] == kpad(cin)
+    _need(w, "w", torch.bfloat16, (cout, kpad(cin)), x.device)
+    if bias is not None:
+        _need(bias, "bias", torch.float32, (cout,), x.device)
     hw = head_w.reshape(-1).float().contiguous()
     hb = head_b.reshape(-1).float().contiguous()
-    assert hw.numel() == cout and hb.numel() == 1
+    _need(hw, "head_w", torch.float32, (cout,), x.device)
+    _need(hb, "head_b", torch.float32, (1,), x.device)
     y = torch.empty((n, h, wd), dtype=torch.float32, device=x.device)
     rc = load().ske_conv3x3_head_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(w.data_ptr()),
                                       C.c_void_p(bias.data_ptr()) if bias is not None else None,
@@ -116,8 +143,8 @@ def conv3x3_head(x, w, bias, head_w, head_b, relu: bool = True):
 def maxpool2(x):
     """2 x 2 max pooling of a contiguous NHWC bfloat16 tensor (ske_maxpool2_bf16)."""
     import torch
+    _need(x, "x", torch.bfloat16)
     n, h, wd, c = x.shape
-    assert x.is_contiguous() and x.dtype == torch.bfloat16
     y = torch.empty((n, h // 2, wd // 2, c), dtype=torch.bfloat16, device=x.device)
     check(load().ske_maxpool2_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), n, h, wd, c, _stream(x)))
     return y
@@ -136,7 +163,9 @@ def conv_check(device=None) -> None:
 def conv3x3_wgrad(x, dy, cout: int):
     """dW (Cout, kpad(Cin)) float32 of conv3x3 for input x and output gradient dy."""
     import torch
+    _need(x, "x", torch.bfloat16)
     n, h, wd, cin = x.shape
+    _need(dy, "dy", torch.bfloat16, (n, h, wd, cout), x.device)
     dw = torch.zeros((cout, kpad(cin)), dtype=torch.float32, device=x.device)
     check(load().ske_conv3x3_wgrad_bf16(C.c_void_p(x.data_ptr()), C.c_void_p(dy.data_ptr()),
                                         C.c_void_p(dw.data_ptr()), n, h, wd, cin, cout, _stream(x)))

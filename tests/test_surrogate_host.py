@@ -88,3 +88,26 @@ def test_convolution_work_count():
     assert chans["d3a"][0] == chans["b4b"][1] + chans["e3b"][1]
     assert chans["d2a"][0] == chans["d3b"][1] + chans["e2b"][1]
     assert chans["d1a"][0] == chans["d2b"][1] + chans["e1b"][1]
+
+
+def test_kernel_wrappers_refuse_host_tensors_and_wrong_types():
+    """The convolution, pooling and weight-gradient wrappers hand raw device
+    pointers to kernels that size every access from the shape arguments, so
+    each refuses a host tensor (or a non-tensor) before any kernel is called.
+    The element-type, contiguity and shape checks come after this one and
+    need CUDA tensors to reach."""
+    bf = torch.bfloat16
+    x = torch.zeros((1, 8, 8, 8), dtype=bf)
+    w = torch.zeros((16, sur.kpad(8)), dtype=bf)
+    with pytest.raises(TypeError, match="CUDA"):
+        sur.conv3x3(x, w)
+    with pytest.raises(TypeError, match="CUDA"):
+        sur.conv3x3_upcat(torch.zeros((1, 4, 4, 8), dtype=bf), x, torch.zeros((16, sur.kpad(16)), dtype=bf))
+    with pytest.raises(TypeError, match="CUDA"):
+        sur.conv3x3_head(x, w, None, torch.zeros(16), torch.zeros(1))
+    with pytest.raises(TypeError, match="CUDA"):
+        sur.maxpool2(x)
+    with pytest.raises(TypeError, match="CUDA"):
+        sur.conv3x3_wgrad(x, torch.zeros((1, 8, 8, 16), dtype=bf), 16)
+    with pytest.raises(TypeError, match="CUDA"):
+        sur.conv3x3(None, w)
