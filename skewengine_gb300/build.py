@@ -31,7 +31,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["engine.cu", "k_layout.cu", "k_batch.cu", "k_sdem.cu", "k_sdem_noalloc.cu", "k_radon.cu", "k_lradon.cu", "k_lradon_f32.cu", "k_cepstrum.cu", "k_cepstrum_f32.cu",
               "k_peak.cu", "k_conv.cu"]
 CPP_SOURCES = ["geometry.cpp", "cli.cpp", "image_io.cpp"]
-HEADERS = ["ske_internal.h", "ske_device.cuh", "kernels.h"]
+HEADERS = ["ske_internal.h", "ske_device.cuh", "kernels.h", "image_io.h"]
 
 
 def nvcc() -> str:

@@ -26,10 +26,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <string>
 #include <vector>
 
 #include "../../include/skewengine.h"
+#include "image_io.h"
 
 namespace {
 
@@ -77,7 +79,7 @@ long file_size(const char* path) {
 int load_input(const std::string& path, int* dimx, int* dimy, std::vector<float>& out) {
     if (ends_with(path, ".png")) {
         int w = 0, h = 0;
-        int rc = ske_png_size(path.c_str(), &w, &h);
+        const int rc = ske::png_read_grid(path.c_str(), &w, &h, out);
         if (rc != SKE_OK) {
             fprintf(stderr, "run: cannot read image %s\n", path.c_str());
             return rc;
@@ -88,8 +90,7 @@ int load_input(const std::string& path, int* dimx, int* dimy, std::vector<float>
         }
         *dimx = w;
         *dimy = h;
-        out.resize((size_t)w * h);
-        return ske_png_read_image(path.c_str(), out.data(), out.size());
+        return SKE_OK;
     }
     const bool bil = ends_with(path, ".bil");
     const long bytes = file_size(path.c_str());
@@ -126,9 +127,7 @@ int load_input(const std::string& path, int* dimx, int* dimy, std::vector<float>
     return SKE_OK;
 }
 
-}  // namespace
-
-extern "C" int run(int argc, char** argv) {
+int run_main(int argc, char** argv) {
     if (argc < 6) {
         fprintf(stderr, "usage: run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]\n");
         return SKE_ERR_INVALID;
@@ -180,4 +179,15 @@ extern "C" int run(int argc, char** argv) {
     fwrite(out.data(), sizeof(float), out.size(), f);
     fclose(f);
     return SKE_OK;
+}
+
+}  // namespace
+
+extern "C" int run(int argc, char** argv) {
+    try {
+        return run_main(argc, argv);
+    } catch (const std::exception& ex) {  // e.g. a grid too large to allocate: no exception crosses the C ABI
+        fprintf(stderr, "run: %s\n", ex.what());
+        return SKE_ERR_INVALID;
+    }
 }

@@ -26,12 +26,17 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <string>
 #include <vector>
 
 #include "../../include/skewengine.h"
+#include "image_io.h"
 
 namespace {
+
+// Largest image decoded: 2^31 pixels (8 GiB of RGBA).
+constexpr uint64_t kMaxPixels = (uint64_t)1 << 31;
 
 // ---------------------------------------------------------------- checksums
 struct CrcTable {
@@ -416,7 +421,7 @@ int png_decode(const std::vector<uint8_t>& f, PngImage& im, std::vector<uint8_t>
     if (!have_hdr || !have_end || idat.empty()) return SKE_ERR_INVALID;
     if (im.ctype == 3 && im.palette.empty()) return SKE_ERR_INVALID;
     if (!rgba) return SKE_OK;
-    if ((uint64_t)im.w * im.h > ((uint64_t)1 << 31)) return SKE_ERR_INVALID;
+    if ((uint64_t)im.w * im.h > kMaxPixels) return SKE_ERR_INVALID;
 
     const int bits_pp = channels_of(im.ctype) * im.depth;
     const int bpp = bits_pp < 8 ? 1 : bits_pp / 8;
@@ -433,6 +438,9 @@ int png_decode(const std::vector<uint8_t>& f, PngImage& im, std::vector<uint8_t>
     }
     std::vector<uint8_t> raw;
     if (!zlib_decompress(idat, raw, expect)) return SKE_ERR_INVALID;
+    // Short scanline data fails the pass checks below in any case; refusing it
+    // here keeps a damaged file from sizing the RGBA buffer by its header alone.
+    if (raw.size() != expect) return SKE_ERR_INVALID;
     rgba->assign((size_t)im.w * im.h * 4, 0);
     // Adam7 passes (PNG specification 8.2): start and step in x and y.
     static const int ax0[7] = {0, 4, 0, 2, 0, 1, 0}, ay0[7] = {0, 0, 4, 0, 2, 0, 1};
@@ -499,6 +507,25 @@ uint8_t to_u8(float v) { return (uint8_t)(int)v; }
 
 }  // namespace
 
+namespace ske {
+
+int png_read_grid(const char* path, int* width, int* height, std::vector<float>& grid) {
+    PngImage im;
+    std::vector<uint8_t> px;
+    const int rc = png_load(path, im, &px);
+    if (rc != SKE_OK) return rc;
+    if (im.w > 0x7fffffffu || im.h > 0x7fffffffu) return SKE_ERR_INVALID;
+    *width = (int)im.w;
+    *height = (int)im.h;
+    const size_t n = (size_t)im.w * im.h;
+    grid.resize(n);
+    // read_png: pixels[i] = R + G + B (a short); the grid value is that number.
+    for (size_t i = 0; i < n; i++) grid[i] = (float)(short)(px[4 * i] + px[4 * i + 1] + px[4 * i + 2]);
+    return SKE_OK;
+}
+
+}  // namespace ske
+
 extern "C" {
 
 void ske_hsv_to_rgb(float H, float S, float V, uint8_t* rgb) {
@@ -529,37 +556,51 @@ void ske_hsv_to_rgb(float H, float S, float V, uint8_t* rgb) {
 
 int ske_png_size(const char* path, int* width, int* height) {
     if (!width || !height) return SKE_ERR_INVALID;
-    PngImage im;
-    const int rc = png_load(path, im, nullptr);
-    if (rc != SKE_OK) return rc;
-    if (im.w > 0x7fffffffu || im.h > 0x7fffffffu) return SKE_ERR_INVALID;
-    *width = (int)im.w;
-    *height = (int)im.h;
-    return SKE_OK;
+    try {
+        PngImage im;
+        const int rc = png_load(path, im, nullptr);
+        if (rc != SKE_OK) return rc;
+        // The size of an image the decoder takes (at most 2^31 pixels): a
+        // caller sizes its buffers from it.
+        if (im.w > 0x7fffffffu || im.h > 0x7fffffffu || (uint64_t)im.w * im.h > kMaxPixels) return SKE_ERR_INVALID;
+        *width = (int)im.w;
+        *height = (int)im.h;
+        return SKE_OK;
+    } catch (const std::exception&) {  // allocation failure: no exception crosses the C ABI
+        return SKE_ERR_INVALID;
+    }
 }
 
 int ske_png_read_rgba(const char* path, uint8_t* rgba, size_t capacity) {
     if (!rgba) return SKE_ERR_INVALID;
-    PngImage im;
-    std::vector<uint8_t> px;
-    const int rc = png_load(path, im, &px);
-    if (rc != SKE_OK) return rc;
-    if (px.size() > capacity) return SKE_ERR_INVALID;
-    memcpy(rgba, px.data(), px.size());
-    return SKE_OK;
+    try {
+        PngImage im;
+        std::vector<uint8_t> px;
+        const int rc = png_load(path, im, &px);
+        if (rc != SKE_OK) return rc;
+        if (px.size() > capacity) return SKE_ERR_INVALID;
+        memcpy(rgba, px.data(), px.size());
+        return SKE_OK;
+    } catch (const std::exception&) {
+        return SKE_ERR_INVALID;
+    }
 }
 
 int ske_png_read_image(const char* path, float* image, size_t capacity) {
     if (!image) return SKE_ERR_INVALID;
-    PngImage im;
-    std::vector<uint8_t> px;
-    const int rc = png_load(path, im, &px);
-    if (rc != SKE_OK) return rc;
-    const size_t n = (size_t)im.w * im.h;
-    if (n > capacity) return SKE_ERR_INVALID;
-    // read_png: pixels[i] = R + G + B (a short); the grid value is that number.
-    for (size_t i = 0; i < n; i++) image[i] = (float)(short)(px[4 * i] + px[4 * i + 1] + px[4 * i + 2]);
-    return SKE_OK;
+    try {
+        PngImage im;
+        std::vector<uint8_t> px;
+        const int rc = png_load(path, im, &px);
+        if (rc != SKE_OK) return rc;
+        const size_t n = (size_t)im.w * im.h;
+        if (n > capacity) return SKE_ERR_INVALID;
+        // read_png: pixels[i] = R + G + B (a short); the grid value is that number.
+        for (size_t i = 0; i < n; i++) image[i] = (float)(short)(px[4 * i] + px[4 * i + 1] + px[4 * i + 2]);
+        return SKE_OK;
+    } catch (const std::exception&) {
+        return SKE_ERR_INVALID;
+    }
 }
 
 int ske_png_write(const char* path, const uint8_t* pixels, int width, int height, int channels) {

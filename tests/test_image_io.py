@@ -8,7 +8,7 @@ import os
 import numpy as np
 import pytest
 
-from tests.conftest import GOLDEN
+from tests.conftest import GOLDEN, ROOT
 
 
 @pytest.fixture(scope="module")
@@ -139,6 +139,129 @@ def test_render_colourings(ske, images):
         ske.render(0, out)  # the reference writes no image of a viewshed
     grey = ske.render_input(np.array([[0, 3, 765, 382]], np.float32))
     assert list(grey[0]) == [0, 1, 255, 127]
+
+
+def _chunks(png: bytes):
+    import struct
+    i, out = 8, []
+    while i + 8 <= len(png):
+        n = struct.unpack(">I", png[i:i + 4])[0]
+        out.append([png[i + 4:i + 8], bytearray(png[i + 8:i + 8 + n])])
+        i += 12 + n
+    return out
+
+
+def _mutated_pngs(images, count: int, seed: int) -> list[bytes]:
+    """Seeded damaged variants of the reference-encoded fixtures (every colour
+    type and bit depth, plain and interlaced): byte changes inside chunk data
+    with the CRC recomputed, so that the damage gets past the checksums to the
+    header checks, the inflater and the scanline filters; IHDR fields set to
+    extreme values; chunks cut short, dropped or repeated; bytes flipped with
+    the CRC left stale."""
+    import struct
+    import zlib
+    rng = np.random.default_rng(seed)
+    seeds = [images[f"png_{i}"].tobytes() for i in range(int(images["png_meta"].shape[0]))]
+    big = [0, 1, 7, 65535, 1 << 20, 0x7FFFFFFF, 0xFFFFFFFF]
+    out = []
+    for _ in range(count):
+        cs = _chunks(seeds[rng.integers(len(seeds))])
+        for _ in range(int(rng.integers(1, 4))):
+            kind = int(rng.integers(6))
+            c = cs[int(rng.integers(len(cs)))] if cs else None
+            if kind == 0 and c is not None and c[1]:
+                for _ in range(int(rng.integers(1, 4))):
+                    c[1][int(rng.integers(len(c[1])))] = int(rng.integers(256))
+            elif kind == 1 and cs and len(cs[0][1]) == 13:
+                f = int(rng.integers(7))
+                if f < 2:
+                    cs[0][1][4 * f:4 * f + 4] = struct.pack(">I", big[int(rng.integers(len(big)))])
+                else:
+                    cs[0][1][6 + f] = int(rng.choice([0, 1, 2, 3, 4, 6, 8, 16, 255]))
+            elif kind == 2 and c is not None:
+                c[1] = c[1][: int(rng.integers(len(c[1]) + 1))]
+            elif kind == 3 and cs:
+                j = int(rng.integers(len(cs)))
+                cs.insert(j, [cs[j][0], bytearray(cs[j][1])]) if rng.random() < 0.5 else cs.pop(j)
+            elif kind == 4 and c is not None:
+                c[1] += rng.integers(0, 256, int(rng.integers(1, 600)), dtype=np.uint8).tobytes()
+        data = bytearray(b"\x89PNG\r\n\x1a\n" + b"".join(
+            struct.pack(">I", len(d)) + t + bytes(d) + struct.pack(">I", zlib.crc32(t + bytes(d)) & 0xFFFFFFFF)
+            for t, d in cs))
+        if rng.random() < 0.2:
+            for _ in range(int(rng.integers(1, 4))):
+                data[int(rng.integers(len(data)))] = int(rng.integers(256))
+        out.append(bytes(data))
+    return out
+
+
+def test_png_decoder_survives_mutated_files(ske, images, tmp_path):
+    """Two thousand damaged files go through the decoder in a child process (a
+    crash fails the test instead of ending the run): each is either refused
+    with an error or decoded to exactly the size its header declares, never
+    written past its buffer."""
+    import subprocess
+    import sys
+    files = _mutated_pngs(images, 2000, 77)
+    for i, data in enumerate(files):
+        (tmp_path / f"m{i:04d}.png").write_bytes(data)
+    script = (
+        "import sys, glob\n"
+        "import skewengine_gb300 as s\n"
+        "acc = rej = 0\n"
+        "for f in sorted(glob.glob(sys.argv[1] + '/m*.png')):\n"
+        "    try:\n"
+        "        w, h = s.png_size(f)\n"
+        "        if w * h > 1 << 24:\n"
+        "            rej += 1\n"
+        "            continue\n"
+        "        px = s.read_png_rgba(f)\n"
+        "        img = s.read_image(f)\n"
+        "        assert px.shape == (h, w, 4) and img.shape == (h, w)\n"
+        "        acc += 1\n"
+        "    except s.SkeError:\n"
+        "        rej += 1\n"
+        "print(acc, rej)\n")
+    r = subprocess.run([sys.executable, "-c", script, str(tmp_path)], cwd=ROOT, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    acc, rej = (int(v) for v in r.stdout.split())
+    print(f"{acc} decoded, {rej} refused")
+    assert acc + rej == len(files) and acc > 0 and rej > 0, (acc, rej)
+
+
+def test_png_header_alone_sizes_nothing(ske, tmp_path):
+    """A file whose header claims a huge image is refused by png_size beyond
+    the decoder's 2^31-pixel limit, and below it the CLI decodes before it
+    allocates the grid: a damaged 1.6e9-pixel claim with a few bytes of data
+    is refused without the gigabytes its header asks for."""
+    import struct
+    import subprocess
+    import sys
+    import zlib
+    from skewengine_gb300 import SkeError
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xffffffff)
+
+    def png(w, h):
+        return b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 0, 0, 0, 0)) + \
+            chunk(b"IDAT", zlib.compress(b"\0" * 64)) + chunk(b"IEND", b"")
+
+    (tmp_path / "huge.png").write_bytes(png(65536, 65536))
+    with pytest.raises(SkeError):
+        ske.png_size(tmp_path / "huge.png")
+    (tmp_path / "claim.png").write_bytes(png(40000, 40000))
+    assert ske.png_size(tmp_path / "claim.png") == (40000, 40000)
+    script = ("import resource, sys\n"
+              "import skewengine_gb300 as s\n"
+              "rc = s.cli_run(['radon', sys.argv[1], 0, 0, sys.argv[2]])\n"
+              "print(rc, resource.getrusage(resource.RUSAGE_SELF).ru_maxrss)\n")
+    r = subprocess.run([sys.executable, "-c", script, str(tmp_path / "claim.png"), str(tmp_path / "o.png")],
+                       cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rc, peak_kb = (int(v) for v in r.stdout.split()[-2:])
+    assert rc == 1 and peak_kb < 2 << 20, (rc, peak_kb)  # refused, under 2 GB at its peak
 
 
 @pytest.mark.gpu
