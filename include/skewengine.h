@@ -397,7 +397,8 @@ int ske_measure_fp64_peak(int device, double* dfma_ops);
  * Every function returns SKE_OK or SKE_ERR_INVALID (unreadable or malformed
  * file, buffer too small, bad argument). */
 
-/* Width and height of a PNG file. */
+/* Width and height of a PNG file; images of more than 2^31 pixels (the
+ * decoder's limit) are refused. */
 int ske_png_size(const char* path, int* width, int* height);
 /* Decode a PNG (any colour type, bit depth, interlacing) to 8-bit RGBA, as the
  * reference's PNG library does; capacity in bytes (>= 4 * width * height). */
