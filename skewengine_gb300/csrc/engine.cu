@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -29,6 +30,10 @@ int fail(int code, const char* fmt, ...) {
     t_last_error = buf;
     return code;
 }
+
+// A C++ exception from host code (std::bad_alloc when a request is too large
+// for host memory) becomes an error status: none crosses the C ABI.
+int host_failure(const std::exception& ex) { return fail(SKE_ERR_INVALID, "host: %s", ex.what()); }
 
 #define SKE_CK(call)                                                                              \
     do {                                                                                          \
@@ -1207,7 +1212,12 @@ int run_images_f32(ske_engine e, int count, int dim, const float* const* inputs,
         destroy_image_plan(p);
         e->image_plan = nullptr;
         ImagePlan* np = nullptr;
-        const int rc = build_image_plan(dim, count, angles, nangles, &np);
+        int rc;
+        try {
+            rc = build_image_plan(dim, count, angles, nangles, &np);
+        } catch (const std::exception& ex) {
+            rc = host_failure(ex);
+        }
         if (rc != SKE_OK) {
             destroy_image_plan(np);
             return rc;
@@ -1284,7 +1294,7 @@ int ske_device_count(int* count) {
 }
 
 int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32_t* first, int32_t* last,
-                 int32_t* target, float* weight) {
+                 int32_t* target, float* weight) try {
     if (dimx < 1 || dimy < 1 || dimx > 65535 || dimy > 65535)
         return fail(SKE_ERR_INVALID, "grid %dx%d outside [1,65535]", dimx, dimy);
     if (angle < 0 || angle >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angle);
@@ -1310,6 +1320,8 @@ int ske_geometry(int dimx, int dimy, int angle, ske_sector_geometry* geom, int32
     if (target) std::copy(t.begin(), t.end(), target);
     if (weight) std::copy(w.begin(), w.end(), weight);
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 namespace {
@@ -1317,8 +1329,10 @@ int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream,
 int init_engine(ske_engine e, int dimx, int dimy, int device, void* stream, ske_engine parent);
 }
 
-int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) {
+int ske_create(ske_engine* out, int dimx, int dimy, int device, void* stream) try {
     return create_engine(out, dimx, dimy, device, stream, nullptr);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 namespace {
@@ -1336,7 +1350,12 @@ int create_engine(ske_engine* out, int dimx, int dimy, int device, void* stream,
     }
     if (device < 0 || device >= ndev) return fail(SKE_ERR_INVALID, "device %d outside [0,%d)", device, ndev);
     ske_engine e = new ske_engine_s();
-    const int rc = init_engine(e, dimx, dimy, device, stream, parent);
+    int rc;
+    try {
+        rc = init_engine(e, dimx, dimy, device, stream, parent);
+    } catch (const std::exception& ex) {
+        rc = host_failure(ex);
+    }
     if (rc != SKE_OK) {
         ske_destroy(e);  // frees whatever was allocated before the failure
         return rc;
@@ -1464,22 +1483,26 @@ int ske_stream(ske_engine e, void** stream) {
 }
 
 int ske_run(ske_engine e, int kernel, const float* input, int input_on_device, float* output, int output_on_device,
-            const ske_params* p) {
+            const ske_params* p) try {
     ske_params prm;
     SKE_TRY(validate_params(p, &prm));
     std::vector<int32_t> angles(prm.max_sector);
     for (int i = 0; i < prm.max_sector; i++) angles[i] = i;
     return run_angle_list(e, kernel, input, input_on_device, output, output_on_device, angles.data(),
                           prm.max_sector, &prm);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_run_angles(ske_engine e, int kernel, const float* input, int input_on_device, float* output,
-                   int output_on_device, const int32_t* angles, int nangles, const ske_params* p) {
+                   int output_on_device, const int32_t* angles, int nangles, const ske_params* p) try {
     return run_angle_list(e, kernel, input, input_on_device, output, output_on_device, angles, nangles, p);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_accumulate(ske_engine e, int kernel, const float* input, int input_on_device, const int32_t* angles,
-                   int nangles, const ske_params* p, float* acc, int acc_on_device, uint32_t* used_mask) {
+                   int nangles, const ske_params* p, float* acc, int acc_on_device, uint32_t* used_mask) try {
     if (!acc || !used_mask) return fail(SKE_ERR_INVALID, "null output");
     ske_params prm;
     SKE_TRY(accumulate_angles(e, kernel, input, input_on_device, angles, nangles, p, &prm));
@@ -1494,11 +1517,13 @@ int ske_accumulate(ske_engine e, int kernel, const float* input, int input_on_de
     *used_mask = e->used;
     e->prepared = false;
     return check_status(e);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_accumulate_resume(ske_engine e, int kernel, const float* input, int input_on_device, const int32_t* angles,
                           int nangles, const ske_params* p, float* acc, float* comp, int state_on_device,
-                          uint32_t* used_mask) {
+                          uint32_t* used_mask) try {
     if (!acc || !used_mask) return fail(SKE_ERR_INVALID, "null accumulator state");
     const StartState st{acc, comp, *used_mask, state_on_device};
     ske_params prm;
@@ -1520,10 +1545,12 @@ int ske_accumulate_resume(ske_engine e, int kernel, const float* input, int inpu
     *used_mask = e->used;
     e->prepared = false;
     return check_status(e);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_fold(ske_engine e, int kernel, const float* acc, const float* comp, int state_on_device, uint32_t used_mask,
-             int accum, float* output, int output_on_device) {
+             int accum, float* output, int output_on_device) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
     if (accum != SKE_ACCUM_REFERENCE && accum != SKE_ACCUM_KAHAN)
@@ -1534,22 +1561,26 @@ int ske_fold(ske_engine e, int kernel, const float* acc, const float* comp, int 
     SKE_TRY(run_reduce(e, output, output_on_device, kernel == SKE_KERNEL_CEPSTRUM, accum));
     SKE_CK(cudaStreamSynchronize(e->stream));
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_run_batch(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
                   const float* const* inputs, int inputs_on_device, float* const* outputs, int outputs_on_device,
-                  const ske_params* p) {
+                  const ske_params* p) try {
     ske_params prm;
     SKE_TRY(validate_params(p, &prm));
     std::vector<int32_t> angles(prm.max_sector);
     for (int i = 0; i < prm.max_sector; i++) angles[i] = i;
     return ske_run_batch_angles(e, kernel, count, dimx, dimy, inputs, inputs_on_device, outputs, outputs_on_device,
                                 angles.data(), prm.max_sector, &prm);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dimx, const int32_t* dimy,
                          const float* const* inputs, int inputs_on_device, float* const* outputs,
-                         int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p) {
+                         int outputs_on_device, const int32_t* angles, int nangles, const ske_params* p) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
     if (count < 0 || (count > 0 && (!dimx || !dimy || !inputs || !outputs)))
@@ -1587,7 +1618,12 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
             destroy_batch_plan(e->batch_plan);
             e->batch_plan = nullptr;
             BatchPlan* np = nullptr;
-            const int rc = build_batch_plan(e, count, dimx, dimy, angles, nangles, prm.accum, &np);
+            int rc;
+            try {
+                rc = build_batch_plan(e, count, dimx, dimy, angles, nangles, prm.accum, &np);
+            } catch (const std::exception& ex) {
+                rc = host_failure(ex);
+            }
             if (rc != SKE_OK) {
                 destroy_batch_plan(np);
                 return rc;
@@ -1623,6 +1659,8 @@ int ske_run_batch_angles(ske_engine e, int kernel, int count, const int32_t* dim
         if (rc != SKE_OK) return rc;
     }
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_skew_select(int path) {
@@ -1630,7 +1668,7 @@ int ske_skew_select(int path) {
     return SKE_OK;
 }
 
-int ske_set_sweep_shape(ske_engine e, int lvl0, int lvl1, int ctas_per_sm) {
+int ske_set_sweep_shape(ske_engine e, int lvl0, int lvl1, int ctas_per_sm) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     auto ok = [](int v) { return v == 16 || v == 32 || v == 48 || v == 64; };
     if (lvl0 != 0 && (!ok(lvl0) || (lvl1 != 0 && !ok(lvl1)) || ctas_per_sm < 0))
@@ -1644,6 +1682,8 @@ int ske_set_sweep_shape(ske_engine e, int lvl0, int lvl1, int ctas_per_sm) {
                 w.graph = nullptr;
             }
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_radon_select(int path) {
@@ -1659,14 +1699,16 @@ int ske_sweep_shape(ske_engine e, int* lvl0, int* lvl1, int* ctas_per_sm) {
     return SKE_OK;
 }
 
-int ske_prepare(ske_engine e, const float* input, int on_device) {
+int ske_prepare(ske_engine e, const float* input, int on_device) try {
     if (!e || !input) return fail(SKE_ERR_INVALID, "null argument");
     SKE_TRY(set_device(e));
     e->flags = 0;  // the per-sector calls take no parameters: the reference's operators, no modes
     return run_prepare(e, input, on_device);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_skew(ske_engine e, int angle) {
+int ske_skew(ske_engine e, int angle) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (!e->prepared) return fail(SKE_ERR_STATE, "skew() before prepare()");
     if (angle < 0 || angle >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angle);
@@ -1679,9 +1721,11 @@ int ske_skew(ske_engine e, int angle) {
     e->cur_angle = angle;
     e->kernel_ran = false;
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_kernel(ske_engine e, int kernel, float povh) {
+int ske_kernel(ske_engine e, int kernel, float povh) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (!valid_kernel(kernel)) return fail(SKE_ERR_INVALID, "unknown kernel %d", kernel);
     if (e->cur_angle < 0) return fail(SKE_ERR_STATE, "kernel() before skew()");
@@ -1692,6 +1736,8 @@ int ske_kernel(ske_engine e, int kernel, float povh) {
     SKE_TRY(run_operator(e, kernel, b, povh, 0));
     e->kernel_ran = true;
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_sector(ske_engine e, ske_sector_view* v) {
@@ -1732,7 +1778,7 @@ int ske_kernel_custom(ske_engine e, ske_operator_fn fn, void* user, float povh) 
     return SKE_OK;
 }
 
-int ske_deskew(ske_engine e, int is_max, int accum) {
+int ske_deskew(ske_engine e, int is_max, int accum) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (!e->kernel_ran) return fail(SKE_ERR_STATE, "deskew() before kernel()");
     if (accum != SKE_ACCUM_REFERENCE && accum != SKE_ACCUM_KAHAN)
@@ -1743,16 +1789,20 @@ int ske_deskew(ske_engine e, int is_max, int accum) {
     b.angle[0] = e->cur_angle;
     e->accum_mode = accum;
     return run_deskew(e, b, is_max, accum);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_reduce(ske_engine e, float* output, int on_device, int is_max) {
+int ske_reduce(ske_engine e, float* output, int on_device, int is_max) try {
     if (!e || !output) return fail(SKE_ERR_INVALID, "null argument");
     if (!e->prepared) return fail(SKE_ERR_STATE, "reduce() before prepare()");
     SKE_TRY(set_device(e));
     return run_reduce(e, output, on_device, is_max, e->accum_mode);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_copy_skewed(ske_engine e, float* skew_in, float* skew_out, int on_device) {
+int ske_copy_skewed(ske_engine e, float* skew_in, float* skew_out, int on_device) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     if (e->cur_angle < 0) return fail(SKE_ERR_STATE, "no current sector: call skew() first");
     SKE_TRY(set_device(e));
@@ -1766,9 +1816,11 @@ int ske_copy_skewed(ske_engine e, float* skew_in, float* skew_out, int on_device
     if (skew_in) SKE_TRY(download(e, skew_in, e->d_SI, e->len));
     if (skew_out) SKE_TRY(download(e, skew_out, e->d_SO, e->len));
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_device) {
+int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_device) try {
     if (!e || !counts) return fail(SKE_ERR_INVALID, "null argument");
     if (!e->prepared) return fail(SKE_ERR_STATE, "sdem_counts() before prepare()");
     if (angle < 0 || angle >= kMaxSectors) return fail(SKE_ERR_INVALID, "angle %d outside [0,180)", angle);
@@ -1787,18 +1839,22 @@ int ske_sdem_counts(ske_engine e, int angle, float povh, float* counts, int on_d
         SKE_TRY(download(e, counts, e->d_SO, e->len));
     }
     return check_status(e);
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_profile_enable(ske_engine e, int enable) {
+int ske_profile_enable(ske_engine e, int enable) try {
     if (!e) return fail(SKE_ERR_INVALID, "null engine");
     SKE_TRY(set_device(e));
     SKE_TRY(flush_profile(e));
     e->prof = enable != 0;
     e->prof_tot.clear();
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
-int ske_profile_get(ske_engine e, const char* name, double* ms, int64_t* launches) {
+int ske_profile_get(ske_engine e, const char* name, double* ms, int64_t* launches) try {
     if (!e || !name) return fail(SKE_ERR_INVALID, "null argument");
     SKE_TRY(set_device(e));
     SKE_TRY(flush_profile(e));
@@ -1806,6 +1862,8 @@ int ske_profile_get(ske_engine e, const char* name, double* ms, int64_t* launche
     if (ms) *ms = it == e->prof_tot.end() ? 0.0 : it->second.ms;
     if (launches) *launches = it == e->prof_tot.end() ? 0 : it->second.launches;
     return SKE_OK;
+} catch (const std::exception& ex) {
+    return host_failure(ex);
 }
 
 int ske_selftest_division(int device, int dmax, int64_t* checked, int64_t* mismatches, uint32_t* first_bad_bits) {
