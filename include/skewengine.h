@@ -12,7 +12,9 @@
  * Conventions
  *  - Every entry point returns an int status (SKE_OK == 0).  On failure the
  *    message of the calling thread's last error is available from
- *    ske_last_error().  Nothing in the library calls exit() or traps on device.
+ *    ske_last_error().  Nothing in the library calls exit() or traps on device,
+ *    and no C++ exception leaves it: a request too large for host memory
+ *    returns SKE_ERR_INVALID with a "host:" message.
  *  - Arrays are row-major float32, dimy rows of dimx cells, like the reference's
  *    inputD / outD (src/global.cpp:24).
  *  - "on_device" arguments say whether a pointer is a device pointer (1) or a
