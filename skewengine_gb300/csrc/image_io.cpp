@@ -603,7 +603,7 @@ int ske_png_read_image(const char* path, float* image, size_t capacity) {
     }
 }
 
-int ske_png_write(const char* path, const uint8_t* pixels, int width, int height, int channels) {
+int ske_png_write(const char* path, const uint8_t* pixels, int width, int height, int channels) try {
     if (!path || !pixels || width <= 0 || height <= 0 || (channels != 1 && channels != 3)) return SKE_ERR_INVALID;
     const size_t stride = (size_t)width * channels;
     std::vector<uint8_t> raw;
@@ -641,6 +641,8 @@ int ske_png_write(const char* path, const uint8_t* pixels, int width, int height
     const size_t put = fwrite(out.data(), 1, out.size(), f);
     const int closed = fclose(f);
     return (put == out.size() && closed == 0) ? SKE_OK : SKE_ERR_INVALID;
+} catch (const std::exception&) {  // allocation failure: no exception crosses the C ABI
+    return SKE_ERR_INVALID;
 }
 
 int ske_render_input(const float* image, int count, uint8_t* grey) {
