@@ -505,14 +505,29 @@ int ske_conv_wgrad_select(int path);
  * the flag. */
 int ske_conv_status(int* failed, void* stream);
 
+/* The reference's grid input (readBilData, parse_hdr and check_dem,
+ * src/kernelSDEM.h:31-142; read_png, src/helper.h:167-184): an ESRI .bil int16
+ * DEM divided by 10 in binary64 (cell units of a 10 m grid), a raw float32 grid,
+ * or a .png image as R + G + B per pixel.  dimx/dimy give the file's grid; 0
+ * takes the .hdr's NCOLS/NROWS (else a square from the file size) or the
+ * image's size.  crop_x/crop_y drop columns/rows from the right/bottom as
+ * readBilData's crop does: the top-left (dimx - crop_x) x (dimy - crop_y)
+ * window, rows read at the file's pitch.  Writes the window's size to
+ * *out_dimx/*out_dimy and, when `grid` is not NULL, its cells (row-major;
+ * `capacity` in floats).  SKE_OK, or SKE_ERR_INVALID for an unreadable, short
+ * or malformed file, an empty window or a small buffer.  Host only. */
+int ske_read_grid(const char* path, int dimx, int dimy, int crop_x, int crop_y, float* grid, size_t capacity,
+                  int* out_dimx, int* out_dimy);
+
 /* Reference command-line entry point (src/main.cu:200-202): runs one operator on
  * an input file and writes the result.
  *   argv: run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]
+ *         [crop_x] [crop_y]
  *   kernel: sdem | identitydem | radon | identityimg | cepstrum | localradon, or
  *           0..5 (the reference's KERNELS enum, src/global.h:77; 5 = radon with
  *           its local-transform switch set);
  *   input:  raw float32 grid, ESRI .bil int16 DEM (with its .hdr; dimx/dimy 0
- *           take NCOLS/NROWS) or .png image;
+ *           take NCOLS/NROWS) or .png image, read and cropped as ske_read_grid;
  *   output: raw float32 grid (.flt) or, for a name ending in .png, the
  *           reference's coloured result image.
  * Returns 0 or a SKE_* status; messages go to stderr. */

@@ -9,12 +9,12 @@ compute runs as hand-written sm_103a CUDA kernels behind the C ABI in
 from .engine import (ACCUM_KAHAN, ACCUM_REFERENCE, DEFAULT_POVH, FLAG_CEPSTRUM_F32, FLAG_LOCAL_RADON_F32, FLAG_NO_GRAPH, FLAG_RADON_F32, FLAG_NO_TUNE, KERNEL_CEPSTRUM,
                      KERNEL_IDENTITYDEM,
                      KERNEL_IDENTITYIMG, KERNEL_LOCAL_RADON, KERNEL_RADON, KERNEL_SDEM, KERNELS, SkewEngine,
-                     cli_run, device_count, execute, geometry, params, png_size, read_image, read_png_rgba,
+                     cli_run, device_count, execute, geometry, params, png_size, read_grid, read_image, read_png_rgba,
                      render, render_input, run_batch, write_png)
 from ._lib import SkeError
 
 __all__ = ["SkewEngine", "SkeError", "execute", "run_batch", "geometry", "params", "device_count", "cli_run",
-           "png_size", "read_png_rgba", "read_image", "write_png", "render", "render_input",
+           "png_size", "read_grid", "read_png_rgba", "read_image", "write_png", "render", "render_input",
            "KERNEL_SDEM", "KERNEL_IDENTITYDEM", "KERNEL_RADON", "KERNEL_IDENTITYIMG", "KERNEL_CEPSTRUM",
            "KERNEL_LOCAL_RADON",
            "KERNELS", "ACCUM_REFERENCE", "ACCUM_KAHAN", "DEFAULT_POVH", "FLAG_NO_TUNE", "FLAG_NO_GRAPH", "FLAG_CEPSTRUM_F32",

@@ -105,6 +105,8 @@ SIGNATURES = [
     ("ske_surrogate_encode_bf16", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float,
                                             C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
     ("ske_conv_status", C.c_int, [C.POINTER(C.c_int), C.c_void_p]),
+    ("ske_read_grid", C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t,
+                                C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("ske_png_size", C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("ske_png_read_rgba", C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t]),
     ("ske_png_read_image", C.c_int, [C.c_char_p, C.c_void_p, C.c_size_t]),

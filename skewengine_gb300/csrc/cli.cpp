@@ -2,6 +2,7 @@
 // (src/main.cu:200-202), plus the DEM file formats it reads and writes.
 //
 //   run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]
+//       [crop_x] [crop_y]
 //
 //   kernel     sdem | identitydem | radon | identityimg | cepstrum | localradon,
 //              or 0..5 (KERNELS enum, src/global.h:77; 5 = radon with LRT set)
@@ -20,8 +21,12 @@
 //              reference's salida2.png and salida1.png)
 //   max_sector angles 0..max_sector-1 (default 180), povh observer height in cell
 //              units (default 0.15), accum 0 reference order / 1 Kahan.
+//   crop_x/y   columns / rows dropped from the right / bottom of the input grid
+//              (readBilData's crop, src/kernelSDEM.h:31-52): the run takes the
+//              top-left (dimx - crop_x) x (dimy - crop_y) window.
 //
 // Returns 0 on success, a SKE_* status otherwise; messages go to stderr.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -76,60 +81,94 @@ long file_size(const char* path) {
     return n;
 }
 
-int load_input(const std::string& path, int* dimx, int* dimy, std::vector<float>& out) {
+// The input grid of a run: the file's grid (dimx x dimy; 0 = from the .hdr,
+// the image or the file size), then readBilData's crop (src/kernelSDEM.h:31-52):
+// the top-left (dimx - crop_x) x (dimy - crop_y) window, rows at the file's
+// pitch.  On success *dimx/*dimy hold the window's size.
+int load_input(const std::string& path, int* dimx, int* dimy, int crop_x, int crop_y, std::vector<float>& out) {
+    if (crop_x < 0 || crop_y < 0) {
+        fprintf(stderr, "run: negative crop %d, %d\n", crop_x, crop_y);
+        return SKE_ERR_INVALID;
+    }
+    int fdx = *dimx, fdy = *dimy;
+    std::vector<float> full;
     if (ends_with(path, ".png")) {
         int w = 0, h = 0;
-        const int rc = ske::png_read_grid(path.c_str(), &w, &h, out);
+        const int rc = ske::png_read_grid(path.c_str(), &w, &h, full);
         if (rc != SKE_OK) {
             fprintf(stderr, "run: cannot read image %s\n", path.c_str());
             return rc;
         }
-        if ((*dimx > 0 && *dimx != w) || (*dimy > 0 && *dimy != h)) {
-            fprintf(stderr, "run: %s is %dx%d, not %dx%d\n", path.c_str(), w, h, *dimx, *dimy);
+        if ((fdx > 0 && fdx != w) || (fdy > 0 && fdy != h)) {
+            fprintf(stderr, "run: %s is %dx%d, not %dx%d\n", path.c_str(), w, h, fdx, fdy);
             return SKE_ERR_INVALID;
         }
-        *dimx = w;
-        *dimy = h;
-        return SKE_OK;
-    }
-    const bool bil = ends_with(path, ".bil");
-    const long bytes = file_size(path.c_str());
-    if (bytes < 0) {
-        fprintf(stderr, "run: cannot open %s\n", path.c_str());
-        return SKE_ERR_INVALID;
-    }
-    const int cell = bil ? 2 : 4;
-    if (*dimx <= 0 || *dimy <= 0) {
-        int nc = 0, nr = 0;
-        if (bil) read_hdr(path, &nc, &nr);
-        if (nc <= 0 || nr <= 0) nc = nr = (int)std::sqrt((double)(bytes / cell));
-        *dimx = nc;
-        *dimy = nr;
-    }
-    const size_t n = (size_t)*dimx * *dimy;
-    if ((size_t)bytes < n * cell) {
-        fprintf(stderr, "run: %s holds %ld bytes, need %zu\n", path.c_str(), bytes, n * cell);
-        return SKE_ERR_INVALID;
-    }
-    out.resize(n);
-    FILE* f = fopen(path.c_str(), "rb");
-    if (bil) {
-        std::vector<int16_t> raw(n);
-        const size_t got = fread(raw.data(), 2, n, f);
-        fclose(f);
-        if (got != n) return SKE_ERR_INVALID;
-        for (size_t i = 0; i < n; i++) out[i] = (float)(((float)raw[i]) / 10.0);
+        fdx = w;
+        fdy = h;
     } else {
-        const size_t got = fread(out.data(), 4, n, f);
-        fclose(f);
-        if (got != n) return SKE_ERR_INVALID;
+        const bool bil = ends_with(path, ".bil");
+        const long bytes = file_size(path.c_str());
+        if (bytes < 0) {
+            fprintf(stderr, "run: cannot open %s\n", path.c_str());
+            return SKE_ERR_INVALID;
+        }
+        const int cell = bil ? 2 : 4;
+        if (fdx <= 0 || fdy <= 0) {
+            int nc = 0, nr = 0;
+            if (bil) read_hdr(path, &nc, &nr);
+            if (nc <= 0 || nr <= 0) nc = nr = (int)std::sqrt((double)(bytes / cell));
+            fdx = nc;
+            fdy = nr;
+        }
+        if (fdx <= 0 || fdy <= 0 || crop_x >= fdx || crop_y >= fdy) {
+            fprintf(stderr, "run: %s: a %dx%d grid cropped by %d, %d is empty\n", path.c_str(), fdx, fdy, crop_x,
+                    crop_y);
+            return SKE_ERR_INVALID;
+        }
+        // The rows the window reads, at the file's pitch (the last one only up
+        // to the window's width, as readBilData reads it).
+        const size_t rows = (size_t)(fdy - crop_y);
+        const size_t n = (rows - 1) * (size_t)fdx + (size_t)(fdx - crop_x);
+        if ((size_t)bytes < n * cell) {
+            fprintf(stderr, "run: %s holds %ld bytes, need %zu\n", path.c_str(), bytes, n * cell);
+            return SKE_ERR_INVALID;
+        }
+        full.resize(n);
+        FILE* f = fopen(path.c_str(), "rb");
+        if (!f) return SKE_ERR_INVALID;
+        if (bil) {
+            std::vector<int16_t> raw(n);
+            const size_t got = fread(raw.data(), 2, n, f);
+            fclose(f);
+            if (got != n) return SKE_ERR_INVALID;
+            for (size_t i = 0; i < n; i++) full[i] = (float)(((float)raw[i]) / 10.0);
+        } else {
+            const size_t got = fread(full.data(), 4, n, f);
+            fclose(f);
+            if (got != n) return SKE_ERR_INVALID;
+        }
     }
+    if (crop_x >= fdx || crop_y >= fdy) {
+        fprintf(stderr, "run: a %dx%d grid cropped by %d, %d is empty\n", fdx, fdy, crop_x, crop_y);
+        return SKE_ERR_INVALID;
+    }
+    const int wx = fdx - crop_x, wy = fdy - crop_y;
+    if (crop_x == 0 && crop_y == 0 && full.size() == (size_t)wx * wy) {
+        out.swap(full);
+    } else {
+        out.resize((size_t)wx * wy);
+        for (int i = 0; i < wy; i++)
+            std::copy(full.begin() + (size_t)i * fdx, full.begin() + (size_t)i * fdx + wx, out.begin() + (size_t)i * wx);
+    }
+    *dimx = wx;
+    *dimy = wy;
     return SKE_OK;
 }
 
 int run_main(int argc, char** argv) {
     if (argc < 6) {
-        fprintf(stderr, "usage: run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum]\n");
+        fprintf(stderr,
+                "usage: run <kernel> <input> <dimx> <dimy> <output> [max_sector] [povh] [accum] [crop_x] [crop_y]\n");
         return SKE_ERR_INVALID;
     }
     const int kernel = parse_kernel(argv[1]);
@@ -138,8 +177,9 @@ int run_main(int argc, char** argv) {
         return SKE_ERR_INVALID;
     }
     int dimx = atoi(argv[3]), dimy = atoi(argv[4]);
+    const int crop_x = argc > 9 ? atoi(argv[9]) : 0, crop_y = argc > 10 ? atoi(argv[10]) : 0;
     std::vector<float> in;
-    int rc = load_input(argv[2], &dimx, &dimy, in);
+    int rc = load_input(argv[2], &dimx, &dimy, crop_x, crop_y, in);
     if (rc != SKE_OK) return rc;
     ske_params p;
     ske_params_default(&p);
@@ -188,6 +228,25 @@ extern "C" int run(int argc, char** argv) {
         return run_main(argc, argv);
     } catch (const std::exception& ex) {  // e.g. a grid too large to allocate: no exception crosses the C ABI
         fprintf(stderr, "run: %s\n", ex.what());
+        return SKE_ERR_INVALID;
+    }
+}
+
+extern "C" int ske_read_grid(const char* path, int dimx, int dimy, int crop_x, int crop_y, float* grid,
+                             size_t capacity, int* out_dimx, int* out_dimy) {
+    if (!path || !out_dimx || !out_dimy) return SKE_ERR_INVALID;
+    try {
+        std::vector<float> g;
+        int dx = dimx, dy = dimy;
+        const int rc = load_input(path, &dx, &dy, crop_x, crop_y, g);
+        if (rc != SKE_OK) return rc;
+        *out_dimx = dx;
+        *out_dimy = dy;
+        if (!grid) return SKE_OK;
+        if (g.size() > capacity) return SKE_ERR_INVALID;
+        std::copy(g.begin(), g.end(), grid);
+        return SKE_OK;
+    } catch (const std::exception&) {  // allocation failure: no exception crosses the C ABI
         return SKE_ERR_INVALID;
     }
 }

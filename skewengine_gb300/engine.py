@@ -428,6 +428,22 @@ def run_batch(kernel, grids, max_sector: int = 180, povh: float = DEFAULT_POVH, 
     return outs
 
 
+def read_grid(path: str, dimx: int = 0, dimy: int = 0, crop_x: int = 0, crop_y: int = 0) -> np.ndarray:
+    """The input grid of a file as the reference reads it (ske_read_grid): a
+    .bil int16 DEM divided by 10 (size from dimx/dimy, else its .hdr, else a
+    square from the file size), a raw float32 grid, or a .png image as R + G + B
+    per pixel; crop_x/crop_y drop columns/rows from the right/bottom as
+    readBilData's crop does.  float32 (rows, columns)."""
+    lib = load()
+    w, h = C.c_int(), C.c_int()
+    p = str(path).encode()
+    check(lib.ske_read_grid(p, int(dimx), int(dimy), int(crop_x), int(crop_y), None, 0, C.byref(w), C.byref(h)))
+    out = np.empty((h.value, w.value), np.float32)
+    check(lib.ske_read_grid(p, int(dimx), int(dimy), int(crop_x), int(crop_y), out.ctypes.data, out.size,
+                            C.byref(w), C.byref(h)))
+    return out
+
+
 def png_size(path: str) -> tuple[int, int]:
     """(width, height) of a PNG file."""
     w, h = C.c_int(), C.c_int()

@@ -1,6 +1,7 @@
-"""DEM file input and output of run(argc, argv): the ESRI .bil int16 grid with
-its .hdr (readBilData / parse_hdr / check_dem, src/kernelSDEM.h:31-142) and the
-raw float32 .flt result dump (showResultsSDEM, src/kernelSDEM.h:433-439).
+"""DEM file input and output of run(argc, argv) and ske_read_grid: the ESRI .bil
+int16 grid with its .hdr and crop (readBilData / parse_hdr / check_dem,
+src/kernelSDEM.h:31-142) and the raw float32 .flt result dump (showResultsSDEM,
+src/kernelSDEM.h:433-439).
 
 The reference reads a .bil as little-endian int16 metres, row after row, and
 divides each value by 10 in binary64 before storing it as float (cell units of
@@ -42,6 +43,53 @@ def test_bil_reader_rejects_short_files(tmp_path):
     (tmp_path / "dem.bil").write_bytes(raw.tobytes())
     _write_hdr(tmp_path / "dem.hdr", 40, 40)
     assert cli_run(["sdem", str(tmp_path / "dem.bil"), 0, 0, str(tmp_path / "out.flt")]) == 1
+
+
+def test_read_grid_bil_header_and_crop(tmp_path):
+    """ske_read_grid reads a .bil as readBilData does (int16 metres / 10 in
+    binary64), its size from the .hdr, and crops the top-left window at the
+    file's row pitch (readBilData's crop_x/crop_y, src/kernelSDEM.h:31-52).
+    Host only."""
+    from skewengine_gb300 import read_grid
+    raw = _fractal_int16(80, 56, 401)
+    (tmp_path / "dem.bil").write_bytes(raw.tobytes())
+    _write_hdr(tmp_path / "dem.hdr", 80, 56)
+    want = _bil_grid(raw)
+    got = read_grid(tmp_path / "dem.bil")
+    assert got.shape == (56, 80) and np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    got = read_grid(tmp_path / "dem.bil", crop_x=7, crop_y=5)
+    assert got.shape == (51, 73) and np.array_equal(got.view(np.uint32), want[:51, :73].view(np.uint32))
+    # Explicit dims override the header; the crop applies to them.
+    got = read_grid(tmp_path / "dem.bil", 80, 40, crop_x=30)
+    assert np.array_equal(got.view(np.uint32), want[:40, :50].view(np.uint32))
+    # The window's rows alone need be present, as readBilData reads them.
+    cut = raw.tobytes()[: (50 * 80 + 73) * 2]
+    (tmp_path / "cut.bil").write_bytes(cut)
+    got = read_grid(tmp_path / "cut.bil", 80, 56, crop_x=7, crop_y=5)
+    assert np.array_equal(got.view(np.uint32), want[:51, :73].view(np.uint32))
+
+
+def test_read_grid_raw_square_png_and_refusals(tmp_path):
+    import skewengine_gb300 as ske
+    from skewengine_gb300 import SkeError
+    x = synthetic.fractal_dem(33, 402)
+    x.tofile(tmp_path / "g.raw")
+    got = ske.read_grid(tmp_path / "g.raw")  # square from the file size
+    assert np.array_equal(got.view(np.uint32), x.view(np.uint32))
+    got = ske.read_grid(tmp_path / "g.raw", 33, 33, crop_x=1, crop_y=32)
+    assert np.array_equal(got.view(np.uint32), x[:1, :32].view(np.uint32))
+    px = (np.arange(20 * 14 * 3) % 251).astype(np.uint8).reshape(14, 20, 3)
+    ske.write_png(tmp_path / "i.png", px)
+    img = ske.read_image(tmp_path / "i.png")
+    got = ske.read_grid(tmp_path / "i.png", crop_x=3, crop_y=2)
+    assert np.array_equal(got, img[:12, :17])
+    for args in [dict(crop_x=33), dict(crop_y=40), dict(crop_x=-1), dict(dimx=40, dimy=40)]:
+        with pytest.raises(SkeError):
+            ske.read_grid(tmp_path / "g.raw", **args)
+    with pytest.raises(SkeError):
+        ske.read_grid(tmp_path / "missing.bil")
+    with pytest.raises(SkeError):
+        ske.read_grid(tmp_path / "i.png", 21, 14)  # not the image's size
 
 
 @pytest.mark.gpu
