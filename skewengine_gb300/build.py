@@ -93,7 +93,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(out)
             raise RuntimeError("link failed")
         os.replace(tmp, LIB_PATH)
+    _alias_reference_name()
     return LIB_PATH
+
+
+# The reference builds its shared library as `sk_engine` (CMakeLists.txt:83):
+# a link of that name beside the library lets a caller that loads it by that
+# name (its only export, run(argc, argv), is here too) load this one.
+REFERENCE_LIB_NAME = "libsk_engine.so"
+
+
+def _alias_reference_name() -> None:
+    alias = os.path.join(OUT_DIR, REFERENCE_LIB_NAME)
+    try:
+        if os.path.islink(alias) and os.readlink(alias) == LIB_NAME:
+            return
+        if os.path.lexists(alias):
+            os.remove(alias)
+        os.symlink(LIB_NAME, alias)
+    except OSError:
+        pass  # a filesystem without links: the library keeps its own name only
 
 
 def main() -> None:

@@ -225,3 +225,16 @@ def test_run_batch_refuses_mixed_placements_and_mismatched_outputs(lib):
         engine.run_batch(0, [h], outs=[np.zeros((8, 4), np.float32)])
     with pytest.raises(ValueError):
         engine.run_batch(0, [np.zeros((2, 8, 8), np.float32)])
+
+
+def test_reference_library_name_loads_this_library(lib):
+    """The build places libsk_engine.so (the reference's shared-library name,
+    CMakeLists.txt:83) beside libskewengine.so: a caller loading the reference's
+    library by name gets this one, with its run(argc, argv)."""
+    from skewengine_gb300 import _lib
+    alias = os.path.join(os.path.dirname(_lib.LIB_PATH), "libsk_engine.so")
+    assert os.path.realpath(alias) == os.path.realpath(_lib.LIB_PATH)
+    ref = C.CDLL(alias)
+    ref.run.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    argv = (C.c_char_p * 1)(b"run")
+    assert ref.run(1, argv) == 1  # usage: too few arguments
