@@ -513,7 +513,7 @@ int ske_conv_status(int* failed, void* stream);
  * image's size.  crop_x/crop_y drop columns/rows from the right/bottom as
  * readBilData's crop does: the top-left (dimx - crop_x) x (dimy - crop_y)
  * window, rows read at the file's pitch.  Writes the window's size to
- * *out_dimx/*out_dimy and, when `grid` is not NULL, its cells (row-major;
+ * *out_dimx and *out_dimy and, when `grid` is not NULL, its cells (row-major;
  * `capacity` in floats).  SKE_OK, or SKE_ERR_INVALID for an unreadable, short
  * or malformed file, an empty window or a small buffer.  Host only. */
 int ske_read_grid(const char* path, int dimx, int dimy, int crop_x, int crop_y, float* grid, size_t capacity,
