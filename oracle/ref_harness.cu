@@ -24,6 +24,7 @@
 #include <cstring>
 #include <fstream>
 #include <omp.h>
+#include <vector>
 
 #include "helper.h"
 
@@ -175,6 +176,23 @@ int skref_sector(int alg, const float* input, int dx, int dy, int angle, float p
 int skref_set_local_radon(int on) {
     LRT = on != 0;
     return 0;
+}
+
+// The reference's DEM reader readBilData (src/kernelSDEM.h:31-52) on a .bil of
+// file_dx x file_dy int16 cells with its crop: `out` receives the
+// (file_dx - crop_x) x (file_dy - crop_y) grid it builds (int16 / 10.0, rows
+// read at the file's pitch).  Used only to generate golden fixtures.
+int skref_read_bil(const char* path, int file_dx, int file_dy, int crop_x, int crop_y, float* out) {
+    if (crop_x < 0 || crop_y < 0 || file_dx <= crop_x || file_dy <= crop_y) return 1;
+    dimx = file_dx;
+    dimy = file_dy;
+    float* data = new float[(size_t)file_dx * file_dy];
+    std::vector<char> name(path, path + strlen(path) + 1);
+    readBilData<float>(name.data(), data, crop_x, crop_y);
+    const int ok = dimx == file_dx - crop_x && dimy == file_dy - crop_y;
+    if (ok) memcpy(out, data, sizeof(float) * (size_t)dimx * dimy);
+    delete[] data;
+    return ok ? 0 : 2;
 }
 
 // Result rendering and PNG coding as the reference does them: HSVtoRGB from
