@@ -122,3 +122,55 @@ def test_ordered_parallel_oracle_equals_single_thread(oracle, op):
         want = oracle.run_angles(op, x, angles, povh=0.15, threads=1)
         got = oracle.run_ordered(op, x, angles, povh=0.15, threads=5)
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), (op, dx, dy)
+
+
+def _reference_build():
+    """The reference's own CPU path compiled from its sources (oracle/_ref), built
+    here when the sources are present; None where they are not."""
+    import ctypes as C
+    import os
+    import subprocess
+    from tests.conftest import ROOT
+    path = os.path.join(ROOT, "oracle", "_ref", "libskewref.so")
+    if not os.path.exists(path):
+        import __graft_entry__ as entry
+        if not os.path.isdir(os.path.join(entry.REFERENCE, "src")):
+            return None
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={entry.REFERENCE}"],
+                       check=True)
+    lib = C.CDLL(path)
+    fp = np.ctypeslib.ndpointer(np.float32, flags="C")
+    ip = np.ctypeslib.ndpointer(np.int32, flags="C")
+    lib.skref_run_angles.argtypes = [C.c_int, fp, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, C.c_int]
+    lib.skref_set_local_radon.argtypes = [C.c_int]
+    return lib
+
+
+def test_oracle_equals_reference_build_at_workload_sizes(oracle):
+    """The oracle against the reference's own CPU code, run here on the
+    benchmark workloads' inputs and sizes (the fixtures above are small grids):
+    total viewshed of the 500 x 500 fractal DEM, Radon of the 512 x 512 ellipse
+    phantom on all 180 angles, cepstrum and local Radon of the 512 x 512
+    motion-blurred texture, on angle subsets that span the four sector types,
+    reference single-thread order, bit for bit.  Skipped where the reference's
+    sources are absent."""
+    from skewengine_gb300 import synthetic
+    ref = _reference_build()
+    if ref is None:
+        pytest.skip("the reference's sources are not on this machine")
+    dem = synthetic.fractal_dem(500, 1000, roughness=0.8)
+    phantom = synthetic.ellipse_phantom(512, 2024)
+    texture, _, _ = synthetic.blurred_texture(512, 2024)
+    cases = [(0, dem, [0, 1, 17, 44, 45, 46, 63, 89, 90, 91, 112, 135, 158, 179]),
+             (2, phantom, list(range(180))),
+             (4, texture, [0, 30, 45, 60, 90, 120, 135, 170]),
+             (5, texture, [0, 45, 100, 150])]
+    for op, x, angles in cases:
+        ref.skref_set_local_radon(1 if op == 5 else 0)
+        want = np.zeros_like(x)
+        a = np.ascontiguousarray(angles, np.int32)
+        assert ref.skref_run_angles(2 if op == 5 else op, np.ascontiguousarray(x), want, x.shape[1], x.shape[0],
+                                    a, len(a), POVH, 1) == 0
+        ref.skref_set_local_radon(0)
+        got = oracle.run_ordered(op, x, angles, povh=POVH)
+        assert bits_equal(got, want), op
