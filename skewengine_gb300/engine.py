@@ -223,8 +223,9 @@ class SkewEngine:
             out = np.empty(shape, np.float32)
         p, dev = _ptr(out, shape, writable=True)
         self._after_torch(out)
-        acc = np.ascontiguousarray(state["acc"], np.float32)
-        comp = np.ascontiguousarray(state["comp"], np.float32)
+        # 4 x N each: the library reads that many (a smaller array raises here).
+        acc = np.ascontiguousarray(state["acc"], np.float32).reshape(4, self.N)
+        comp = np.ascontiguousarray(state["comp"], np.float32).reshape(4, self.N)
         check(self._lib.ske_fold(self._h, _kernel_id(kernel), acc.ctypes.data, comp.ctypes.data, 0,
                                  int(state["used"]), _accum_id(accum), p, dev))
         return out

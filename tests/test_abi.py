@@ -238,3 +238,18 @@ def test_reference_library_name_loads_this_library(lib):
     ref.run.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
     argv = (C.c_char_p * 1)(b"run")
     assert ref.run(1, argv) == 1  # usage: too few arguments
+
+
+def test_fold_refuses_a_state_of_another_grid(lib):
+    """SkewEngine.fold hands the library 4 x N accumulators and compensations:
+    a saved state of another size raises before the call (checked on an engine
+    object that was never opened, so no device is needed)."""
+    from skewengine_gb300 import engine
+    eng = engine.SkewEngine.__new__(engine.SkewEngine)
+    eng.dimx, eng.dimy, eng.N, eng._h = 4, 3, 12, None
+    small = {"acc": np.zeros((4, 11), np.float32), "comp": np.zeros((4, 12), np.float32), "used": 1}
+    with pytest.raises(ValueError):
+        eng.fold(0, small)
+    small = {"acc": np.zeros((4, 12), np.float32), "comp": np.zeros(5, np.float32), "used": 1}
+    with pytest.raises(ValueError):
+        eng.fold(0, small)
