@@ -368,16 +368,24 @@ def encode_tiles(tiles, coarse=None):
     when not given."""
     import torch
     t = torch.as_tensor(tiles, dtype=torch.float32, device="cuda").contiguous()
+    if t.dim() != 3 or t.shape[1] != t.shape[2]:
+        raise ValueError(f"tiles must be (N, side, side), got {tuple(t.shape)}")
     n, side = t.shape[0], t.shape[1]
     mean = t.mean((1, 2)).contiguous()
     rng = (t.amax((1, 2)) - t.amin((1, 2))).contiguous()
     if coarse is None:
         coarse = coarse_area(t)
     coarse = coarse.contiguous()
+    # The kernel reads N coarse grids of (side / factor)^2 cells, the factor
+    # taken from the coarse grid's side, which must divide the tile's.
+    c = int(coarse.shape[-1]) if coarse.dim() == 3 else 0
+    if c < 1 or side % c:
+        raise ValueError(f"coarse must be (N, c, c) with c dividing {side}, got {tuple(coarse.shape)}")
+    _need(coarse, "coarse", torch.float32, (n, c, c), t.device)
     x = torch.empty(t.shape + (IN_CH,), dtype=torch.bfloat16, device="cuda")
     check(load().ske_surrogate_encode_bf16(C.c_void_p(t.data_ptr()), C.c_void_p(mean.data_ptr()),
                                            C.c_void_p(rng.data_ptr()), C.c_void_p(coarse.data_ptr()),
-                                           side // coarse.shape[1], COARSE_SCALE, C.c_void_p(x.data_ptr()), n, side,
+                                           side // c, COARSE_SCALE, C.c_void_p(x.data_ptr()), n, side,
                                            _stream(t)))
     return x
 
