@@ -185,7 +185,11 @@ int ske_stream(ske_engine e, void** stream);
  * orientations back, and write dimx*dimy floats to `output`.  Replaces
  * skewEngine::allocate + execute() + reduce (skewEngine.cuh:389, main.cu:71-172,
  * skewEngine.cuh:862).  Results equal the reference run on one OpenMP thread
- * (bit for bit for SDEM/identity/Radon in SKE_ACCUM_REFERENCE mode). */
+ * (bit for bit for SDEM/identity/Radon in SKE_ACCUM_REFERENCE mode).
+ * The total-viewshed sweep stages each skewed row in shared memory: rows of up
+ * to 13,224 cells fit a GB300's 227 KB per CTA (grids whose longer side is at
+ * most that); a longer row fails the launch and the call returns
+ * SKE_ERR_CUDA. */
 int ske_run(ske_engine e, int kernel, const float* input, int input_on_device, float* output,
             int output_on_device, const ske_params* p);
 
