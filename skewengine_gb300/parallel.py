@@ -40,6 +40,22 @@ def shard_angles(n_angles: int, world: int, rank: int, costs=None) -> list[int]:
     return list(range(int(cuts[rank]), int(cuts[rank + 1])))
 
 
+def sector_costs(dimx: int, dimy: int, kernel=0, max_sector: int = 180) -> np.ndarray:
+    """Work of each angle 0..max_sector-1 of one operator, from the host
+    geometry (ske_geometry, no device): for the total-viewshed sweep its line of
+    sight steps, the sum over skewed rows of L(L-1) (kernelSDEM.h:180-218); for
+    the other operators the valid skewed cells, the sum of L."""
+    from .engine import KERNEL_SDEM, _kernel_id, geometry
+    sdem = _kernel_id(kernel) == KERNEL_SDEM
+    out = np.zeros(max_sector, np.float64)
+    for a in range(max_sector):
+        g = geometry(dimx, dimy, a)
+        L = (g["last"] - g["first"]).astype(np.float64)
+        L = L[L > 0]
+        out[a] = float(np.sum(L * (L - 1.0))) if sdem else float(L.sum())
+    return out
+
+
 def grid_cost(dimx: int, dimy: int) -> float:
     """A grid's total-viewshed work up to a constant factor: every sector's
     skewed rows hold about dimx*dimy cells, and each cell's line of sight runs
@@ -93,18 +109,25 @@ def fold_accumulators(accs, used_masks, dimx: int, dimy: int, is_max: bool = Fal
     return out.reshape(dimy, dimx)
 
 
-def run_sharded(engine, kernel, data, group=None, max_sector: int = 180, povh=None, accum="reference"):
+def run_sharded(engine, kernel, data, group=None, max_sector: int = 180, povh=None, accum="reference",
+                balance: bool = False):
     """Run one operator with sectors sharded over a torch.distributed group.
 
     Every rank passes the same input; rank 0 returns the folded result, other
-    ranks return None.
+    ranks return None.  balance=False cuts equal-length angle blocks (the
+    reference's static schedule over that many threads); balance=True cuts
+    contiguous blocks of equal work (``sector_costs``), which evens out the
+    ranks' time when the angles' work differs.  Either way the fold is in block
+    order; the blocks differ, so in add mode the two give slightly different
+    sums, as the reference's results differ with its thread count.
     """
     import torch.distributed as dist
     from .engine import DEFAULT_POVH, KERNEL_CEPSTRUM
 
     world = dist.get_world_size(group)
     rank = dist.get_rank(group)
-    angles = shard_angles(max_sector, world, rank)
+    costs = sector_costs(engine.dimx, engine.dimy, kernel, max_sector) if balance else None
+    angles = shard_angles(max_sector, world, rank, costs)
     acc, used = engine.accumulate(kernel, data, angles, povh=DEFAULT_POVH if povh is None else povh, accum=accum)
     payload = {"acc": np.asarray(acc, np.float32), "used": int(used)}
     gathered = [None] * world if rank == 0 else None
@@ -116,7 +139,7 @@ def run_sharded(engine, kernel, data, group=None, max_sector: int = 180, povh=No
 
 
 def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, max_sector: int = 180, povh=None,
-                          accum="reference", timeout: float = 60.0, poll: float = 0.01):
+                          accum="reference", timeout: float = 60.0, poll: float = 0.01, balance: bool = False):
     """Sector sharding with failure detection and recovery on the host.
 
     Each rank accumulates its block of angles and posts the result under
@@ -128,13 +151,16 @@ def run_sharded_resilient(engine, kernel, data, store, rank: int, world: int, ma
     data path, so a lost rank cannot block the others; the fold is in block
     order, so the result has the same bits as a run without failures.
 
+    ``balance`` cuts the blocks as ``run_sharded`` does.
+
     Returns (output, recovered ranks) on rank 0 and (None, []) elsewhere.
     """
     import time
     from .engine import DEFAULT_POVH, KERNEL_CEPSTRUM
 
     pv = DEFAULT_POVH if povh is None else povh
-    blocks = [shard_angles(max_sector, world, r) for r in range(world)]
+    costs = sector_costs(engine.dimx, engine.dimy, kernel, max_sector) if balance else None
+    blocks = [shard_angles(max_sector, world, r, costs) for r in range(world)]
     if rank != 0:
         try:
             acc, used = engine.accumulate(kernel, data, blocks[rank], povh=pv, accum=accum)

@@ -71,7 +71,7 @@ class _OracleEngine:
         return self.oracle.accumulate(kernel, data, angles, povh=povh)
 
 
-def _rank_main(rank, world, port_path, x, port_expect, result_path, master_port):
+def _rank_main(rank, world, port_path, x, port_expect, result_path, master_port, balance=False):
     import ctypes as C
     import torch.distributed as dist
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(master_port))
@@ -82,7 +82,7 @@ def _rank_main(rank, world, port_path, x, port_expect, result_path, master_port)
     ip = np.ctypeslib.ndpointer(np.int32, flags="C")
     lib.port_accumulate.argtypes = [C.c_int, fp, C.c_int, C.c_int, ip, C.c_int, C.c_float, fp, ip]
     eng = _OracleEngine(PortOracle(lib), x.shape[1], x.shape[0])
-    out = parallel.run_sharded(eng, 0, x, povh=np.float32(0.15))
+    out = parallel.run_sharded(eng, 0, x, povh=np.float32(0.15), balance=balance)
     if rank == 0:
         np.save(result_path, out)
     dist.barrier()
@@ -107,6 +107,41 @@ def test_two_rank_sharded_run(oracle, port, tmp_path):
     assert bits_equal(got, want)
     single = oracle.run(0, x, povh=np.float32(0.15))
     np.testing.assert_allclose(got, single, rtol=1e-5)
+
+
+def test_sector_costs_balance_the_shards(port):
+    """sector_costs: each angle's line-of-sight steps from the host geometry
+    (their sum is the oracle's count for the grid); cutting blocks by them
+    evens out a non-square grid's ranks, which equal-length blocks do not."""
+    costs = parallel.sector_costs(200, 120, 0)
+    assert abs(costs.sum() - port.port_los_steps(200, 120, 180)) <= 1e-9 * costs.sum()
+    cells = parallel.sector_costs(200, 120, "radon")
+    assert (cells > 0).all() and cells.sum() < costs.sum()
+    for world in (3, 4, 8):
+        equal = [costs[parallel.shard_angles(180, world, r)].sum() for r in range(world)]
+        blocks = [parallel.shard_angles(180, world, r, costs) for r in range(world)]
+        assert sum(blocks, []) == list(range(180))
+        even = [costs[b].sum() for b in blocks]
+        assert max(even) / np.mean(even) < min(1.1, max(equal) / np.mean(equal)), (world, equal, even)
+
+
+def test_two_rank_sharded_run_balanced(oracle, port, tmp_path):
+    """Two gloo ranks with work-balanced angle blocks: the fold of the two
+    blocks the cost cut gives, bit for bit."""
+    import torch.multiprocessing as mp
+    x = synthetic.fractal_dem(48, 6, side_y=30)
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        master_port = s.getsockname()[1]
+    res = str(tmp_path / "out.npy")
+    mp.start_processes(_rank_main, args=(2, port._name, x, None, res, master_port, True), nprocs=2, join=True,
+                       start_method="spawn")
+    costs = parallel.sector_costs(48, 30, 0)
+    blocks = [parallel.shard_angles(180, 2, r, costs) for r in range(2)]
+    assert blocks[0] != list(range(90))  # the cut moved off the equal split
+    parts = [oracle.accumulate(0, x, b, povh=np.float32(0.15)) for b in blocks]
+    want = parallel.fold_accumulators([p[0] for p in parts], [p[1] for p in parts], 48, 30)
+    assert bits_equal(np.load(res), want)
 
 
 class _FailingEngine(_OracleEngine):
