@@ -169,6 +169,14 @@ public:
                 output[i] = output[i] + fold[i];
         }
     }
+    /* The deprecated row-pointer form reduce(T** output) (src/skewEngine.cuh:
+     * 842-854): the fold added into output[i][j], rows i < dimy. */
+    void reduce(float** output) {
+        std::vector<float> fold((size_t)N);
+        check(ske_reduce(e_, fold.data(), 0, 0));
+        for (int i = 0; i < dimy; i++)
+            for (int j = 0; j < dimx; j++) output[i][j] = output[i][j] + fold[(size_t)i * dimx + j];
+    }
     /* The fold written to a device grid (overwritten, not added). */
     void reduce_device(float* d_output, int isMax = 0) { check(ske_reduce(e_, d_output, 1, isMax)); }
 

@@ -66,6 +66,13 @@ int host_checks() {
     } catch (const ske::error& e) {
         expect(e.status == SKE_ERR_INVALID && std::strlen(e.what()) > 0, "angle 180 is refused with a message");
     }
+    try {
+        std::vector<float> out(64, 0.0f);
+        ske::execute(ske::KERNEL_SDEM, grid.data(), out.data(), 8, 8, 180, 0.15f, 4096);
+        expect(false, "execute on device 4096 is refused");
+    } catch (const ske::error& e) {
+        expect(e.status == SKE_ERR_NO_DEVICE || e.status == SKE_ERR_INVALID, "execute on device 4096 is refused");
+    }
     float* outD = nullptr;
     ske::inputData<float> in2;
     ske::skewEngine<float>::allocate(in2, grid.data(), &outD, 8, 8);
@@ -155,6 +162,21 @@ int gpu_checks() {
     expect(same_bits(loop, whole) && any_nonzero(whole), "per-sector loop equals execute (total viewshed)");
     const int dimx = 48, dimy = 40, n = dimx * dimy;
     const std::vector<float> x = heights(n, 2024u);
+    {
+        // The row-pointer reduce(T**) adds the same fold as reduce(T*).
+        ske::skewEngine<float> eng(dimx, dimy, ske::skewEngine<float>::prepare(x.data(), dimx, dimy));
+        for (int i = 0; i < 180; i += 7) {
+            eng.skew(i);
+            eng.kernel();
+            eng.deskew(0);
+        }
+        std::vector<float> flat((size_t)n, 0.0f), rows((size_t)n, 0.0f);
+        std::vector<float*> ptr((size_t)dimy);
+        for (int i = 0; i < dimy; i++) ptr[(size_t)i] = rows.data() + (size_t)i * dimx;
+        eng.reduce(flat.data(), 0);
+        eng.reduce(ptr.data());
+        expect(same_bits(flat, rows) && any_nonzero(flat), "reduce(T**) equals reduce(T*)");
+    }
     // Cepstrum (max deskew and fold): the facade's loop equals the same calls
     // made on the C ABI directly.
     const std::vector<float> ceps = facade_loop(x, dimx, dimy, ske::KERNEL_CEPSTRUM);
