@@ -174,3 +174,27 @@ def test_oracle_equals_reference_build_at_workload_sizes(oracle):
         ref.skref_set_local_radon(0)
         got = oracle.run_ordered(op, x, angles, povh=POVH)
         assert bits_equal(got, want), op
+
+
+@pytest.mark.parametrize("dims", [(1, 1), (1, 9), (9, 1), (2, 7), (7, 2), (3, 65), (65, 3)])
+def test_oracle_equals_reference_build_on_degenerate_grids(oracle, dims):
+    """Single cells, single rows and columns and strongly non-square grids, every
+    operator over all 180 angles: the oracle against the reference's own CPU
+    code run here, bit for bit (NaNs compared as NaNs).  These are the shapes
+    the GPU's tiny-grid tests compare with the oracle.  Skipped where the
+    reference's sources are absent."""
+    ref = _reference_build()
+    if ref is None:
+        pytest.skip("the reference's sources are not on this machine")
+    dx, dy = dims
+    angles = np.arange(180, dtype=np.int32)
+    for op in (0, 1, 2, 3, 4, 5):
+        rng = np.random.default_rng(dx * 100 + dy + op)
+        x = (rng.random((dy, dx)) * 150).astype(np.float32)
+        ref.skref_set_local_radon(1 if op == 5 else 0)
+        want = np.zeros_like(x)
+        assert ref.skref_run_angles(2 if op == 5 else op, x, want, dx, dy, angles, 180, POVH, 1) == 0
+        ref.skref_set_local_radon(0)
+        got = oracle.run_ordered(op, x, angles, povh=POVH)
+        same = (got.view(np.uint32) == want.view(np.uint32)) | (np.isnan(got) & np.isnan(want))
+        assert same.all(), (dims, op)
