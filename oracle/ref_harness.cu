@@ -24,9 +24,17 @@
 #include <cstring>
 #include <fstream>
 #include <omp.h>
+#include <unistd.h>
 #include <vector>
 
 #include "helper.h"
+
+// The reference writes its result images under the compile-time O_DIR
+// (src/defaults.h:21-28), a directory of its author's machine; the harness
+// renders into the current directory instead (skref_render changes into a
+// directory the caller gives).
+#undef O_DIR
+#define O_DIR ""
 
 // Globals that src/main.cu defines (main.cu:59-60) and the kernel headers use.
 int skewAlgorithm;
@@ -193,6 +201,55 @@ int skref_read_bil(const char* path, int file_dx, int file_dy, int crop_x, int c
     if (ok) memcpy(out, data, sizeof(float) * (size_t)dimx * dimy);
     delete[] data;
     return ok ? 0 : 2;
+}
+
+// The reference's result colourings, run in `dir`: for the Radon operator and
+// the image identity showResultsRADN (src/kernelRADN.h:384-400) with the scale
+// and shift showResults picks (src/main.h:124-141, restated: 255 / (max - min)
+// and min for alg 2, 1/540 for alg 3); for the cepstrum and the DEM identity
+// showResultsCEPS (src/kernelBLUR.h:306-410, after execute()'s sample-point
+// set-up, whose sample dumps it writes too).  `rgb` receives salida2.png, the
+// coloured result, decoded by the reference's PNG library.  Used only to
+// generate golden fixtures.
+int skref_render(int alg, const float* out, int dx, int dy, const char* dir, unsigned char* rgb) {
+    if (dx <= 0 || dy <= 0 || !dir) return 1;
+    dimx = dx;
+    dimy = dy;
+    N = dim = dx * dy;
+    skewAlgorithm = alg;
+    std::vector<float> o(out, out + (size_t)dim);
+    outD = o.data();
+    pixels.assign((size_t)dim, 0);
+    saveSampleData = false;
+    char cwd[4096];
+    if (!getcwd(cwd, sizeof cwd) || chdir(dir) != 0) return 2;
+    if (alg == KERNEL_RADON || alg == KERNEL_IDENTITYIMG) {
+        const pair_t mm = helper::getMinMax(outD);
+        const float autoScale = 255 / (mm.max - mm.min);
+        float escala = (float)(1.0 / 540);
+        if (alg == KERNEL_RADON) escala = autoScale;
+        if (alg == KERNEL_RADON)
+            showResultsRADN(escala, mm.min);
+        else
+            showResultsRADN(escala);
+    } else {
+        if (samplePoints.empty()) {  // execute()'s set-up of the sample points (src/main.cu:79-83)
+            samplePoints.push_back(punto1);
+            samplePoints.push_back(punto2);
+            samplePoints.push_back(punto3);
+        }
+        for (int i = 0; i < 180; i++)
+            if (sampleData1[i].empty()) allocSampleData(i);
+        showResultsCEPS();
+    }
+    std::vector<unsigned char> img;
+    unsigned w = 0, h = 0;
+    const unsigned err = lodepng::decode(img, w, h, "salida2.png", LCT_RGB);
+    const int back = chdir(cwd);
+    outD = nullptr;
+    if (err || back != 0 || w != (unsigned)dx || h != (unsigned)dy) return 3;
+    memcpy(rgb, img.data(), img.size());
+    return 0;
 }
 
 // Result rendering and PNG coding as the reference does them: HSVtoRGB from

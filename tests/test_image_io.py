@@ -118,6 +118,22 @@ def test_min_max_of_renderer_matches_reference(ske, images):
         assert np.array_equal(got[..., 0], want) and np.array_equal(got[..., 1], want)
 
 
+def test_render_matches_reference_colourings(ske):
+    """ske_render against the reference's own result writers run on the same
+    outputs (tests/golden/render.npz from make_render_golden.py): the Radon
+    grey scale with its automatic range (an all-negative grid included), the
+    image identity's 1/540, and the HSV colourings of the cepstrum and the DEM
+    identity, pixel for pixel."""
+    z = np.load(os.path.join(GOLDEN, "render.npz"))
+    n = len([k for k in z.files if k.startswith("alg_")])
+    assert n >= 6
+    for k in range(n):
+        grid, alg = z[f"out_{k}"], int(z[f"alg_{k}"])
+        with np.errstate(all="ignore"):
+            got = ske.render(alg, grid)
+        assert np.array_equal(got, z[f"rgb_{k}"]), (k, alg)
+
+
 def test_render_colourings(ske, images):
     rng = np.random.default_rng(5)
     out = rng.uniform(0, 2e6, (9, 11)).astype(np.float32)
