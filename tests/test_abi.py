@@ -253,3 +253,29 @@ def test_fold_refuses_a_state_of_another_grid(lib):
     small = {"acc": np.zeros((4, 12), np.float32), "comp": np.zeros(5, np.float32), "used": 1}
     with pytest.raises(ValueError):
         eng.fold(0, small)
+
+
+def test_header_serves_plain_c_callers(lib, tmp_path):
+    """include/skewengine.h compiles as C99 with every warning on, and a C
+    program linked against the library runs the whole-run call sequence of
+    the reference's replacement (create, run, destroy); without a device the
+    create call returns SKE_ERR_NO_DEVICE with a message instead of failing."""
+    import subprocess
+    from skewengine_gb300 import _lib
+    src = tmp_path / "caller.c"
+    src.write_text(
+        "#include <stdio.h>\n#include \"skewengine.h\"\n"
+        "int main(void) {\n"
+        "    float in[16] = {0}, out[16];\n    ske_engine e;\n    ske_params p;\n"
+        "    if (ske_params_default(&p) != SKE_OK) return 10;\n"
+        "    int rc = ske_create(&e, 4, 4, 0, NULL);\n"
+        "    if (rc != SKE_OK) { printf(\"create %d %s\\n\", rc, ske_last_error()); return 0; }\n"
+        "    rc = ske_run(e, SKE_KERNEL_SDEM, in, 0, out, 0, &p);\n"
+        "    ske_destroy(e);\n    printf(\"run %d\\n\", rc);\n    return rc;\n}\n")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = str(tmp_path / "caller")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lskewengine", f"-Wl,-rpath,{libdir}", "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("run 0") or r.stdout.startswith("create 3 "), r.stdout
