@@ -111,7 +111,7 @@ def test_min_max_of_renderer_matches_reference(ske, images):
     reports FLT_MIN as its maximum in the reference."""
     for g, n, (lo, hi) in zip(images["minmax_in"], images["minmax_len"], images["minmax_out"]):
         x = g[:n].reshape(1, n)
-        with np.errstate(divide="ignore", invalid="ignore"):  # all-zero grid: 0 * inf, byte 0 as on x86-64
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):  # all-zero grid: 0 * inf, byte 0 as on x86-64
             esc = np.float32(255) / (np.float32(hi) - np.float32(lo))
             want = ((x - np.float32(lo)).astype(np.int32).astype(np.float32) * esc).astype(np.int32).astype(np.uint8)
         got = ske.render(2, x)
