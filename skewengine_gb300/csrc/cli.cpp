@@ -28,6 +28,7 @@
 // Returns 0 on success, a SKE_* status otherwise; messages go to stderr.
 #include <algorithm>
 #include <cmath>
+#include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -39,6 +40,17 @@
 #include "image_io.h"
 
 namespace {
+
+// An input error: the message becomes the calling thread's last error
+// (ske_last_error); run() also prints it.
+int input_error(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    return ske::set_last_error(SKE_ERR_INVALID, buf);
+}
 
 int parse_kernel(const char* s) {
     static const char* names[] = {"sdem", "identitydem", "radon", "identityimg", "cepstrum", "localradon"};
@@ -86,32 +98,21 @@ long file_size(const char* path) {
 // the top-left (dimx - crop_x) x (dimy - crop_y) window, rows at the file's
 // pitch.  On success *dimx/*dimy hold the window's size.
 int load_input(const std::string& path, int* dimx, int* dimy, int crop_x, int crop_y, std::vector<float>& out) {
-    if (crop_x < 0 || crop_y < 0) {
-        fprintf(stderr, "run: negative crop %d, %d\n", crop_x, crop_y);
-        return SKE_ERR_INVALID;
-    }
+    if (crop_x < 0 || crop_y < 0) return input_error("negative crop %d, %d", crop_x, crop_y);
     int fdx = *dimx, fdy = *dimy;
     std::vector<float> full;
     if (ends_with(path, ".png")) {
         int w = 0, h = 0;
         const int rc = ske::png_read_grid(path.c_str(), &w, &h, full);
-        if (rc != SKE_OK) {
-            fprintf(stderr, "run: cannot read image %s\n", path.c_str());
-            return rc;
-        }
-        if ((fdx > 0 && fdx != w) || (fdy > 0 && fdy != h)) {
-            fprintf(stderr, "run: %s is %dx%d, not %dx%d\n", path.c_str(), w, h, fdx, fdy);
-            return SKE_ERR_INVALID;
-        }
+        if (rc != SKE_OK) return input_error("cannot read image %s", path.c_str());
+        if ((fdx > 0 && fdx != w) || (fdy > 0 && fdy != h))
+            return input_error("%s is %dx%d, not %dx%d", path.c_str(), w, h, fdx, fdy);
         fdx = w;
         fdy = h;
     } else {
         const bool bil = ends_with(path, ".bil");
         const long bytes = file_size(path.c_str());
-        if (bytes < 0) {
-            fprintf(stderr, "run: cannot open %s\n", path.c_str());
-            return SKE_ERR_INVALID;
-        }
+        if (bytes < 0) return input_error("cannot open %s", path.c_str());
         const int cell = bil ? 2 : 4;
         if (fdx <= 0 || fdy <= 0) {
             int nc = 0, nr = 0;
@@ -120,38 +121,30 @@ int load_input(const std::string& path, int* dimx, int* dimy, int crop_x, int cr
             fdx = nc;
             fdy = nr;
         }
-        if (fdx <= 0 || fdy <= 0 || crop_x >= fdx || crop_y >= fdy) {
-            fprintf(stderr, "run: %s: a %dx%d grid cropped by %d, %d is empty\n", path.c_str(), fdx, fdy, crop_x,
-                    crop_y);
-            return SKE_ERR_INVALID;
-        }
+        if (fdx <= 0 || fdy <= 0 || crop_x >= fdx || crop_y >= fdy)
+            return input_error("%s: a %dx%d grid cropped by %d, %d is empty", path.c_str(), fdx, fdy, crop_x, crop_y);
         // The rows the window reads, at the file's pitch (the last one only up
         // to the window's width, as readBilData reads it).
         const size_t rows = (size_t)(fdy - crop_y);
         const size_t n = (rows - 1) * (size_t)fdx + (size_t)(fdx - crop_x);
-        if ((size_t)bytes < n * cell) {
-            fprintf(stderr, "run: %s holds %ld bytes, need %zu\n", path.c_str(), bytes, n * cell);
-            return SKE_ERR_INVALID;
-        }
+        if ((size_t)bytes < n * cell) return input_error("%s holds %ld bytes, need %zu", path.c_str(), bytes, n * cell);
         full.resize(n);
         FILE* f = fopen(path.c_str(), "rb");
-        if (!f) return SKE_ERR_INVALID;
+        if (!f) return input_error("cannot open %s", path.c_str());
         if (bil) {
             std::vector<int16_t> raw(n);
             const size_t got = fread(raw.data(), 2, n, f);
             fclose(f);
-            if (got != n) return SKE_ERR_INVALID;
+            if (got != n) return input_error("cannot read %s", path.c_str());
             for (size_t i = 0; i < n; i++) full[i] = (float)(((float)raw[i]) / 10.0);
         } else {
             const size_t got = fread(full.data(), 4, n, f);
             fclose(f);
-            if (got != n) return SKE_ERR_INVALID;
+            if (got != n) return input_error("cannot read %s", path.c_str());
         }
     }
-    if (crop_x >= fdx || crop_y >= fdy) {
-        fprintf(stderr, "run: a %dx%d grid cropped by %d, %d is empty\n", fdx, fdy, crop_x, crop_y);
-        return SKE_ERR_INVALID;
-    }
+    if (crop_x >= fdx || crop_y >= fdy)
+        return input_error("a %dx%d grid cropped by %d, %d is empty", fdx, fdy, crop_x, crop_y);
     const int wx = fdx - crop_x, wy = fdy - crop_y;
     if (crop_x == 0 && crop_y == 0 && full.size() == (size_t)wx * wy) {
         out.swap(full);
@@ -180,7 +173,10 @@ int run_main(int argc, char** argv) {
     const int crop_x = argc > 9 ? atoi(argv[9]) : 0, crop_y = argc > 10 ? atoi(argv[10]) : 0;
     std::vector<float> in;
     int rc = load_input(argv[2], &dimx, &dimy, crop_x, crop_y, in);
-    if (rc != SKE_OK) return rc;
+    if (rc != SKE_OK) {
+        fprintf(stderr, "run: %s\n", ske_last_error());
+        return rc;
+    }
     ske_params p;
     ske_params_default(&p);
     if (argc > 6) p.max_sector = atoi(argv[6]);

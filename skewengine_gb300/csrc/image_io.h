@@ -13,4 +13,8 @@ namespace ske {
 // SKE_ERR_INVALID.
 int png_read_grid(const char* path, int* width, int* height, std::vector<float>& grid);
 
+// Record `msg` as the calling thread's last error (ske_last_error) and return
+// `code` (defined with the engine's entry points).
+int set_last_error(int code, const char* msg);
+
 }  // namespace ske

@@ -105,7 +105,9 @@ def test_read_grid_raw_square_png_and_refusals(tmp_path):
     for args in [dict(crop_x=33), dict(crop_y=40), dict(crop_x=-1), dict(dimx=40, dimy=40)]:
         with pytest.raises(SkeError):
             ske.read_grid(tmp_path / "g.raw", **args)
-    with pytest.raises(SkeError):
+    with pytest.raises(SkeError, match="need"):  # the reason reaches ske_last_error
+        ske.read_grid(tmp_path / "g.raw", 40, 40)
+    with pytest.raises(SkeError, match="cannot open"):
         ske.read_grid(tmp_path / "missing.bil")
     with pytest.raises(SkeError):
         ske.read_grid(tmp_path / "i.png", 21, 14)  # not the image's size
