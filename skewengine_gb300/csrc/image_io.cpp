@@ -35,6 +35,17 @@
 
 namespace {
 
+// An image entry point's failure: the reason (and the file) become the calling
+// thread's last error (ske_last_error).
+int image_error(int code, const char* what, const char* path = nullptr) {
+    std::string m = what;
+    if (path) {
+        m += ": ";
+        m += path;
+    }
+    return ske::set_last_error(code, m.c_str());
+}
+
 // Largest image decoded: 2^31 pixels (8 GiB of RGBA).
 constexpr uint64_t kMaxPixels = (uint64_t)1 << 31;
 
@@ -555,56 +566,58 @@ void ske_hsv_to_rgb(float H, float S, float V, uint8_t* rgb) {
 }
 
 int ske_png_size(const char* path, int* width, int* height) {
-    if (!width || !height) return SKE_ERR_INVALID;
+    if (!width || !height) return image_error(SKE_ERR_INVALID, "png_size: null width or height");
     try {
         PngImage im;
         const int rc = png_load(path, im, nullptr);
-        if (rc != SKE_OK) return rc;
+        if (rc != SKE_OK) return image_error(rc, "png_size: not a readable PNG file", path);
         // The size of an image the decoder takes (at most 2^31 pixels): a
         // caller sizes its buffers from it.
-        if (im.w > 0x7fffffffu || im.h > 0x7fffffffu || (uint64_t)im.w * im.h > kMaxPixels) return SKE_ERR_INVALID;
+        if (im.w > 0x7fffffffu || im.h > 0x7fffffffu || (uint64_t)im.w * im.h > kMaxPixels)
+            return image_error(SKE_ERR_INVALID, "png_size: more than 2^31 pixels", path);
         *width = (int)im.w;
         *height = (int)im.h;
         return SKE_OK;
     } catch (const std::exception&) {  // allocation failure: no exception crosses the C ABI
-        return SKE_ERR_INVALID;
+        return image_error(SKE_ERR_INVALID, "png_size: out of host memory", path);
     }
 }
 
 int ske_png_read_rgba(const char* path, uint8_t* rgba, size_t capacity) {
-    if (!rgba) return SKE_ERR_INVALID;
+    if (!rgba) return image_error(SKE_ERR_INVALID, "png_read_rgba: null buffer");
     try {
         PngImage im;
         std::vector<uint8_t> px;
         const int rc = png_load(path, im, &px);
-        if (rc != SKE_OK) return rc;
-        if (px.size() > capacity) return SKE_ERR_INVALID;
+        if (rc != SKE_OK) return image_error(rc, "png_read_rgba: not a readable PNG file", path);
+        if (px.size() > capacity) return image_error(SKE_ERR_INVALID, "png_read_rgba: buffer smaller than the image", path);
         memcpy(rgba, px.data(), px.size());
         return SKE_OK;
     } catch (const std::exception&) {
-        return SKE_ERR_INVALID;
+        return image_error(SKE_ERR_INVALID, "png_read_rgba: out of host memory", path);
     }
 }
 
 int ske_png_read_image(const char* path, float* image, size_t capacity) {
-    if (!image) return SKE_ERR_INVALID;
+    if (!image) return image_error(SKE_ERR_INVALID, "png_read_image: null buffer");
     try {
         PngImage im;
         std::vector<uint8_t> px;
         const int rc = png_load(path, im, &px);
-        if (rc != SKE_OK) return rc;
+        if (rc != SKE_OK) return image_error(rc, "png_read_image: not a readable PNG file", path);
         const size_t n = (size_t)im.w * im.h;
-        if (n > capacity) return SKE_ERR_INVALID;
+        if (n > capacity) return image_error(SKE_ERR_INVALID, "png_read_image: buffer smaller than the image", path);
         // read_png: pixels[i] = R + G + B (a short); the grid value is that number.
         for (size_t i = 0; i < n; i++) image[i] = (float)(short)(px[4 * i] + px[4 * i + 1] + px[4 * i + 2]);
         return SKE_OK;
     } catch (const std::exception&) {
-        return SKE_ERR_INVALID;
+        return image_error(SKE_ERR_INVALID, "png_read_image: out of host memory", path);
     }
 }
 
 int ske_png_write(const char* path, const uint8_t* pixels, int width, int height, int channels) try {
-    if (!path || !pixels || width <= 0 || height <= 0 || (channels != 1 && channels != 3)) return SKE_ERR_INVALID;
+    if (!path || !pixels || width <= 0 || height <= 0 || (channels != 1 && channels != 3))
+        return image_error(SKE_ERR_INVALID, "png_write: bad argument (null, size, or channels not 1 or 3)");
     const size_t stride = (size_t)width * channels;
     std::vector<uint8_t> raw;
     raw.reserve((stride + 1) * height);
@@ -637,23 +650,23 @@ int ske_png_write(const char* path, const uint8_t* pixels, int width, int height
     put_chunk(out, "IDAT", z);
     put_chunk(out, "IEND", {});
     FILE* f = fopen(path, "wb");
-    if (!f) return SKE_ERR_INVALID;
+    if (!f) return image_error(SKE_ERR_INVALID, "png_write: cannot open", path);
     const size_t put = fwrite(out.data(), 1, out.size(), f);
     const int closed = fclose(f);
-    return (put == out.size() && closed == 0) ? SKE_OK : SKE_ERR_INVALID;
+    return (put == out.size() && closed == 0) ? SKE_OK : image_error(SKE_ERR_INVALID, "png_write: cannot write", path);
 } catch (const std::exception&) {  // allocation failure: no exception crosses the C ABI
-    return SKE_ERR_INVALID;
+    return image_error(SKE_ERR_INVALID, "png_write: out of host memory", path);
 }
 
 int ske_render_input(const float* image, int count, uint8_t* grey) {
-    if (!image || !grey || count < 0) return SKE_ERR_INVALID;
+    if (!image || !grey || count < 0) return image_error(SKE_ERR_INVALID, "render_input: bad argument");
     // grey.push_back(pixels[i] / 3): integer division of the R + G + B sum.
     for (int i = 0; i < count; i++) grey[i] = (uint8_t)((short)image[i] / 3);
     return SKE_OK;
 }
 
 int ske_render(int kernel, const float* out, int dimx, int dimy, uint8_t* rgb) {
-    if (!out || !rgb || dimx <= 0 || dimy <= 0) return SKE_ERR_INVALID;
+    if (!out || !rgb || dimx <= 0 || dimy <= 0) return image_error(SKE_ERR_INVALID, "render: bad argument");
     const size_t n = (size_t)dimx * dimy;
     switch (kernel) {
         case SKE_KERNEL_RADON:
@@ -680,7 +693,8 @@ int ske_render(int kernel, const float* out, int dimx, int dimy, uint8_t* rgb) {
             }
             return SKE_OK;
         }
-        default: return SKE_ERR_INVALID;  // the reference renders no image of a viewshed (it writes floats)
+        default:  // the reference renders no image of a viewshed (it writes floats)
+            return image_error(SKE_ERR_INVALID, "render: no image for this operator (a viewshed is written as floats)");
     }
 }
 

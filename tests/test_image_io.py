@@ -78,9 +78,9 @@ def test_png_rejects_damaged_files(ske, images, tmp_path):
     for name, data in cases.items():
         p = tmp_path / f"{name}.png"
         p.write_bytes(data)
-        with pytest.raises(SkeError):
+        with pytest.raises(SkeError, match="not a readable PNG file"):  # the reason reaches ske_last_error
             ske.read_png_rgba(p)
-    with pytest.raises(SkeError):
+    with pytest.raises(SkeError, match="missing.png"):
         ske.read_png_rgba(tmp_path / "missing.png")
 
 
