@@ -15,6 +15,7 @@
 // pixels per CTA (A and dY staged in shared memory, read with transposing
 // ldmatrix into mma.sync m16n8k16), and the chunks' partial sums are added into
 // a float32 dW with atomics.
+#include <cstdio>
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -1461,7 +1462,25 @@ int launch_conv_tc(const bf16* x, const bf16* w, const float* bias, bf16* y, int
 
 }  // namespace
 
-extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
+namespace ske {
+int set_last_error(int code, const char* msg);  // engine.cu: the thread's ske_last_error
+}  // namespace ske
+
+// A conv entry point's failure: a reason for its status becomes the calling
+// thread's last error (ske_last_error), so no earlier call's message is left.
+static int conv_result(int rc, const char* fn) {
+    if (rc == SKE_OK) return rc;
+    const char* why = rc == SKE_ERR_INVALID       ? "invalid argument (a null pointer, a size outside the kernel's "
+                                                   "limits or a misaligned tensor)"
+                      : rc == SKE_ERR_UNSUPPORTED ? "shape not supported by this kernel"
+                      : rc == SKE_ERR_CUDA        ? "a CUDA launch or call failed"
+                                                  : "failed";
+    char buf[256];
+    snprintf(buf, sizeof buf, "%s: %s", fn, why);
+    return ske::set_last_error(rc, buf);
+}
+
+static int ske_conv3x3_bf16_impl(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
                                 int cin, int cout, int relu, void* stream) {
     if (!x || !w || !y || n < 1 || h < 1 || w_ < 1 || cin < 8 || cin % 8 || cout < 2 || cout % 2)
         return SKE_ERR_INVALID;
@@ -1472,7 +1491,12 @@ extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias,
                                  0, (cudaStream_t)stream);
 }
 
-extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
+extern "C" int ske_conv3x3_bf16(const void* x, const void* w, const float* bias, void* y, int n, int h, int w_,
+                                int cin, int cout, int relu, void* stream) {
+    return conv_result(ske_conv3x3_bf16_impl(x, w, bias, y, n, h, w_, cin, cout, relu, stream), "conv3x3_bf16");
+}
+
+static int ske_conv3x3_upcat_bf16_impl(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
                                       int n, int h, int w_, int c1, int c2, int cout, int relu, void* stream) {
     if (!xlow || !xskip || !w || !y || n < 1 || h < 2 || w_ < 2 || h % 2 || w_ % 2 || c1 < 8 || c1 % 8 ||
         c2 < 8 || c2 % 8 || cout < 2 || cout % 2)
@@ -1486,7 +1510,13 @@ extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const
                                 (const bf16*)xskip, c1, (cudaStream_t)stream);
 }
 
-extern "C" int ske_conv3x3_head_bf16(const void* x, const void* w, const float* bias, const float* head_w,
+extern "C" int ske_conv3x3_upcat_bf16(const void* xlow, const void* xskip, const void* w, const float* bias, void* y,
+                                      int n, int h, int w_, int c1, int c2, int cout, int relu, void* stream) {
+    return conv_result(ske_conv3x3_upcat_bf16_impl(xlow, xskip, w, bias, y, n, h, w_, c1, c2, cout, relu, stream),
+                       "conv3x3_upcat_bf16");
+}
+
+static int ske_conv3x3_head_bf16_impl(const void* x, const void* w, const float* bias, const float* head_w,
                                      const float* head_b, float* y, int n, int h, int w_, int cin, int cout,
                                      int relu, void* stream) {
     if (!x || !w || !head_w || !head_b || !y || n < 1 || h < 1 || w_ < 1 || cin < 8 || cin % 8 || cout < 16 || cout % 16)
@@ -1500,6 +1530,13 @@ extern "C" int ske_conv3x3_head_bf16(const void* x, const void* w, const float* 
     if (g_conv_path != 0 || !ws_geometry(&geo, n, h, w_, cin, cout, 0, relu)) return SKE_ERR_UNSUPPORTED;
     return launch_conv_ws<false>(geo, (const bf16*)x, (const bf16*)w, bias, nullptr, nullptr, (cudaStream_t)stream,
                                  head_w, head_b, y);
+}
+
+extern "C" int ske_conv3x3_head_bf16(const void* x, const void* w, const float* bias, const float* head_w,
+                                     const float* head_b, float* y, int n, int h, int w_, int cin, int cout,
+                                     int relu, void* stream) {
+    return conv_result(ske_conv3x3_head_bf16_impl(x, w, bias, head_w, head_b, y, n, h, w_, cin, cout, relu, stream),
+                       "conv3x3_head_bf16");
 }
 
 // 2 x 2 max pooling of NHWC bfloat16 (H, W even, C a multiple of 8): one
@@ -1530,7 +1567,7 @@ static __global__ void k_maxpool2(const bf16* __restrict__ X, bf16* __restrict__
     reinterpret_cast<uint4*>(Y)[i] = o;
 }
 
-extern "C" int ske_maxpool2_bf16(const void* x, void* y, int n, int h, int w_, int c, void* stream) {
+static int ske_maxpool2_bf16_impl(const void* x, void* y, int n, int h, int w_, int c, void* stream) {
     if (!x || !y || n < 1 || h < 2 || w_ < 2 || h % 2 || w_ % 2 || c < 8 || c % 8) return SKE_ERR_INVALID;
     if (!aligned(x, 16) || !aligned(y, 16)) return SKE_ERR_INVALID;
     const int64_t total = (int64_t)n * (h / 2) * (w_ / 2) * (c / 8);
@@ -1539,6 +1576,10 @@ extern "C" int ske_maxpool2_bf16(const void* x, void* y, int n, int h, int w_, i
     k_maxpool2<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((const bf16*)x, (bf16*)y, total, h / 2, w_ / 2,
                                                                    c / 8);
     return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
+extern "C" int ske_maxpool2_bf16(const void* x, void* y, int n, int h, int w_, int c, void* stream) {
+    return conv_result(ske_maxpool2_bf16_impl(x, y, n, h, w_, c, stream), "maxpool2_bf16");
 }
 
 // Surrogate network input, one thread per cell: channel 0 = (h - mean) /
@@ -1563,7 +1604,7 @@ static __global__ void k_encode(const float* __restrict__ T, const float* __rest
     reinterpret_cast<uint4*>(X)[i] = *reinterpret_cast<const uint4*>(v);
 }
 
-extern "C" int ske_surrogate_encode_bf16(const float* tiles, const float* mean, const float* range,
+static int ske_surrogate_encode_bf16_impl(const float* tiles, const float* mean, const float* range,
                                          const float* coarse, int coarse_factor, float coarse_scale, void* x, int n,
                                          int side, void* stream) {
     // side * side must fit an int (the kernel's cell index within a tile).
@@ -1579,25 +1620,45 @@ extern "C" int ske_surrogate_encode_bf16(const float* tiles, const float* mean, 
     return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
 }
 
-extern "C" int ske_conv_select(int path) {
+extern "C" int ske_surrogate_encode_bf16(const float* tiles, const float* mean, const float* range,
+                                         const float* coarse, int coarse_factor, float coarse_scale, void* x, int n,
+                                         int side, void* stream) {
+    return conv_result(ske_surrogate_encode_bf16_impl(tiles, mean, range, coarse, coarse_factor, coarse_scale, x,
+                                                      n, side, stream),
+                       "surrogate_encode_bf16");
+}
+
+static int ske_conv_select_impl(int path) {
     if (path < 0 || path > 2) return SKE_ERR_INVALID;
     g_conv_path = path;
     return SKE_OK;
 }
 
-extern "C" int ske_conv_wgrad_select(int path) {
+extern "C" int ske_conv_select(int path) {
+    return conv_result(ske_conv_select_impl(path), "conv_select");
+}
+
+static int ske_conv_wgrad_select_impl(int path) {
     if (path != 0 && path != 1) return SKE_ERR_INVALID;
     g_wgrad_path = path;
     return SKE_OK;
 }
 
-extern "C" int ske_conv_stage_channels(int channels) {
+extern "C" int ske_conv_wgrad_select(int path) {
+    return conv_result(ske_conv_wgrad_select_impl(path), "conv_wgrad_select");
+}
+
+static int ske_conv_stage_channels_impl(int channels) {
     if (channels != 0 && channels != 16 && channels != 32 && channels != 64) return SKE_ERR_INVALID;
     g_ws_stage = channels;
     return SKE_OK;
 }
 
-extern "C" int ske_conv_status(int* failed, void* stream) {
+extern "C" int ske_conv_stage_channels(int channels) {
+    return conv_result(ske_conv_stage_channels_impl(channels), "conv_stage_channels");
+}
+
+static int ske_conv_status_impl(int* failed, void* stream) {
     if (!failed) return SKE_ERR_INVALID;
     if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) return SKE_ERR_CUDA;
     int v = 0;
@@ -1610,7 +1671,11 @@ extern "C" int ske_conv_status(int* failed, void* stream) {
     return SKE_OK;
 }
 
-extern "C" int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
+extern "C" int ske_conv_status(int* failed, void* stream) {
+    return conv_result(ske_conv_status_impl(failed, stream), "conv_status");
+}
+
+static int ske_conv3x3_wgrad_bf16_impl(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
                                       int cout, void* stream) {
     if (!x || !dy || !dw || n < 1 || h < 1 || w_ < 1 || cin < 8 || cin % 8 || cout < 8 || cout % 8)
         return SKE_ERR_INVALID;
@@ -1636,4 +1701,9 @@ extern "C" int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, 
     k_conv3x3_wgrad<<<grid, kThreads, 0, (cudaStream_t)stream>>>((const bf16*)x, (const bf16*)dy, dw, (int)m, h, w_,
                                                                  cin, cout, kpad);
     return cudaGetLastError() == cudaSuccess ? SKE_OK : SKE_ERR_CUDA;
+}
+
+extern "C" int ske_conv3x3_wgrad_bf16(const void* x, const void* dy, float* dw, int n, int h, int w_, int cin,
+                                      int cout, void* stream) {
+    return conv_result(ske_conv3x3_wgrad_bf16_impl(x, dy, dw, n, h, w_, cin, cout, stream), "conv3x3_wgrad_bf16");
 }
