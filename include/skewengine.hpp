@@ -49,7 +49,7 @@ enum KERNELS : int {
 /* A failed C ABI call: its status (SKE_ERR_*) and message. */
 class error : public std::runtime_error {
 public:
-    error(int status, const std::string& what) : std::runtime_error(what), status(status) {}
+    error(int code, const std::string& what) : std::runtime_error(what), status(code) {}
     int status;
 };
 
@@ -80,14 +80,13 @@ public:
                                  const int32_t* d_last, const int32_t* d_first, float val, int angle, void* stream);
 
     /* src/skewEngine.cuh:462-477 (+ skewAlloc, :419-456): an engine for
-     * dimx x dimy grids on device deviceId, its orientations built from inData.
+     * dx x dy grids on `device`, its orientations built from inData (the
+     * reference's arguments dimx, dimy, inData, isGPU, deviceId).
      * stream: a cudaStream_t to run on (NULL: the engine makes its own). */
-    skewEngine(int dimx, int dimy, inputData<float> inData, bool isGPU = true, int deviceId = 0,
-               void* stream = nullptr)
-        : dimx(dimx), dimy(dimy), N(dimx * dimy), dim_l(dimx > dimy ? dimx : dimy), isGPU(isGPU),
-          deviceId(deviceId) {
-        if (!isGPU) throw error(SKE_ERR_UNSUPPORTED, "skewEngine: no CPU path, the engine runs on the GPU");
-        check(ske_create(&e_, dimx, dimy, deviceId, stream));
+    skewEngine(int dx, int dy, inputData<float> inData, bool gpu = true, int device = 0, void* stream = nullptr)
+        : dimx(dx), dimy(dy), N(dx * dy), dim_l(dx > dy ? dx : dy), isGPU(gpu), deviceId(device) {
+        if (!gpu) throw error(SKE_ERR_UNSUPPORTED, "skewEngine: no CPU path, the engine runs on the GPU");
+        check(ske_create(&e_, dx, dy, device, stream));
         const int rc = ske_prepare(e_, inData.grid, inData.on_device);
         if (rc != SKE_OK) {
             const std::string msg = ske_last_error();
