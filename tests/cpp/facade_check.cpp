@@ -1,5 +1,5 @@
 // Checks of the C++ facade (include/skewengine.hpp), run by
-// tests/test_cpp_facade.py.
+// tests/test_z_cpp_facade.py.
 //
 //   facade_check host   no device needed: operator ids, host geometry (printed
 //                       for the test to compare with the C ABI through Python),
